@@ -1,0 +1,310 @@
+"""Benchmark of the HEM hot path: Laplace-sample solves/s on the 60 x 60 m,
+12 x 12-mesh grid (1560 segments, 1417 nodes, N = n + 2m = 4537 unknowns),
+Alipio soil (sigma0 = 1 mS/m), lightning current injected at the centre node,
+2048 Laplace samples (nt = 4094, omega_max = 2 pi 10 MHz).
+
+One step = one pass of the whole per-sample path (fill ZL/ZT with images,
+immittance assembly, factorisation, solve/refinement) over one batch of
+samples, cycling through the 2048-sample set. Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|plain]
+  python bench.py --impl reference      # the reference's CPU path on the host cores
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = dict(vertices_x=13, vertices_y=13, length_x=60.0, length_y=60.0, edge_segments_x=5, edge_segments_y=5,
+            radius=7e-3, depth=-0.5)
+NT = 4094
+TMAX = 2047 / 10e6          # omega_max = 2 pi 10 MHz
+SIGMA0 = 1e-3
+H_SOIL = 1.26 * (SIGMA0 * 1e3) ** -0.73
+G_SOIL = 0.54
+EPS_RATIO = 12.0
+# 1.2/50 us double exponential, 1 kA
+I0, K12, ALPHA, BETA = 1000.0, 1.037, 1.0 / 68.2e-6, 1.0 / 0.405e-6
+
+
+def workload(pkg):
+    """Geometry, Laplace samples, soil and injection of the benchmark."""
+    elec, nodes = pkg.electrode_grid(**GRID)
+    img = pkg.images(elec)
+    s = pkg.laplace_samples(NT, TMAX)
+    kappa = np.empty_like(s)
+    for k, sk in enumerate(s):
+        sig, epsr = pkg.alipio_soil(SIGMA0, sk, H_SOIL, G_SOIL, EPS_RATIO)
+        kappa[k] = sig + sk * epsr * pkg.EPS0
+    dt = TMAX / (NT - 1)
+    t = np.arange(NT) * dt
+    i_t = I0 * K12 * (np.exp(-ALPHA * t) - np.exp(-BETA * t))
+    c = math.log(float(NT) ** 2) / TMAX
+    inj = np.fft.rfft(i_t * dt * np.exp(-c * t))   # same transform as laplace_trans (host copy for inputs)
+    centre = int(np.argmin(np.linalg.norm(nodes - [30.0, 30.0, GRID["depth"]], axis=1)))
+    return elec, img, nodes, s, kappa, inj, centre
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+
+        def num(v):
+            try:
+                return float(v)
+            except ValueError:
+                return None
+        sm = [num(r[0]) for r in self.rows if num(r[0]) is not None]
+        mx = [num(r[1]) for r in self.rows if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[j] for r in self.rows for j in range(4) if r[3 + j].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"], "src": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
+
+
+def cpu_baseline(args, elec, img, nodes, s, kappa, inj, centre, nsamp):
+    """The oracle (restatement of the reference's path A) on the host cores:
+    OpenMP over samples, OpenBLAS on 1 thread, the reference's tolerances."""
+    from oracle import oracle as O
+    port = O.get("port")
+    cores = os.cpu_count() or 1
+    idx = np.linspace(0, len(s) - 1, nsamp).astype(int)
+    t0 = time.perf_counter()
+    sol, info = port.hem_sweep(elec, img, nodes, s[idx], kappa[idx], centre, inj[idx], req_abs=1e-6, req_rel=1e-6,
+                               threads=min(cores, nsamp))
+    dt = time.perf_counter() - t0
+    return {"value": nsamp / dt, "unit": "solves/s", "cores": min(cores, nsamp), "kind": "port",
+            "sample": f"{nsamp} strided Laplace samples of the 2048-sample set, path A "
+                      f"(INTG_DOUBLE cubature at req_abs=req_rel=1e-6, zsysv with lwork<=100), "
+                      f"one sample per OpenMP thread, {dt:.1f} s"}, sol, info, idx
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as entry
+    pkg = entry.load_package()
+    elec, img, nodes, s, kappa, inj, centre = workload(pkg)
+    cores = os.cpu_count() or 1
+    nsamp = cores          # one Laplace sample per core per step
+    from oracle import oracle as O
+    port = O.get("port")
+    times = []
+    steps = max(1, min(args.steps, args.ref_steps))
+    for step in range(steps):
+        idx = (np.arange(nsamp) * 127 + step * 61) % len(s)
+        t0 = time.perf_counter()
+        port.hem_sweep(elec, img, nodes, s[idx], kappa[idx], centre, inj[idx], req_abs=1e-6, req_rel=1e-6,
+                       threads=cores)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = nsamp * steps / tot
+    line = {"impl": "reference", "metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)",
+            "value": value, "unit": "solves/s", "n_gpus": 0, "steps": steps, "warmup": 0,
+            "ms_per_step": 1e3 * tot / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c128", "data": "synthetic",
+            "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, N=4537, Alipio soil, "
+                                   "2048 Laplace samples", "samples_per_step": nsamp, "path": "A (traditional HEM)"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{nsamp} Laplace samples per step (one per core), {steps} step(s); the "
+                                       "reference's path A restated in C (oracle/), cubature tolerance 1e-6, "
+                                       "zsysv with lwork<=100; warm-up skipped (no device state)"},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
+    ap.add_argument("--batch", type=int, default=0, help="samples per step (0 = 64 mixed / 8 plain)")
+    ap.add_argument("--cpu-samples", type=int, default=0, help="CPU-baseline samples (0 = host cores)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-steps", type=int, default=2, help="cap on timed steps of the reference arm")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import torch.distributed as dist
+    rank, world, local = dist_env()
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+    pkg = entry.load_package()
+    pkg.build()
+    elec, img, nodes, s, kappa, inj, centre = workload(pkg)
+    m, n = elec.shape[0], nodes.shape[0]
+    N = n + 2 * m
+    mixed = args.precision == "mixed"
+    B = args.batch or (64 if mixed else 8)
+    plan = pkg.Plan(elec, img, nodes, pkg.MIXED if mixed else pkg.PLAIN_FP64, max_batch=B)
+    ns_total = len(s)
+    dev = torch.device("cuda", local)
+    # inputs resident in HBM; each rank takes its own strided share of samples
+    s_d = torch.from_numpy(s).to(dev)
+    k_d = torch.from_numpy(kappa).to(dev)
+    ie_full = np.zeros((ns_total, n), np.complex128)
+    ie_full[:, centre] = inj
+    ie_d = torch.from_numpy(ie_full).to(dev)
+    sol_d = torch.empty((B, N), dtype=torch.complex128, device=dev)
+    info_d = torch.empty((B,), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > L2
+
+    def batch_index(step):
+        start = ((step * world + rank) * B) % ns_total
+        return start, min(B, ns_total - start)
+
+    def run_step(step):
+        k0, nb = batch_index(step)
+        return plan.run_device(s_d[k0:].data_ptr(), k_d[k0:].data_ptr(), nb, 1.0, ie_d[k0:].data_ptr(), centre,
+                               sol_d.data_ptr(), info_d.data_ptr())
+
+    for w in range(args.warmup):
+        run_step(w)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    launches0 = pkg.launch_count()
+    stats_iter, stats_fb = 0, 0
+    dev_time = 0.0
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for st_i in range(args.steps):
+            flush.zero_()
+            st = run_step(args.warmup + st_i)
+            dev_time += st.seconds
+            stats_iter = max(stats_iter, st.max_iterations)
+            stats_fb += st.fallbacks
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    launches = pkg.launch_count() - launches0
+    if world > 1:
+        t = torch.tensor([dev_time], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_time = float(t.item())
+        dist.barrier()
+    samples = B * args.steps * world
+    value = samples / dev_time
+
+    # end to end through the public API with host (pinned) buffers
+    s_h = torch.from_numpy(s).pin_memory()
+    k_h = torch.from_numpy(kappa).pin_memory()
+    ie_h = torch.from_numpy(ie_full).pin_memory()
+    sol_h = torch.empty((B, N), dtype=torch.complex128).pin_memory()
+    info_h = torch.empty((B,), dtype=torch.int32).pin_memory()
+    e2e_steps = max(1, min(args.steps, 4))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for st_i in range(e2e_steps):
+        k0, nb = batch_index(st_i)
+        code = pkg.lib().tags_plan_run(plan.handle, s_h[k0:].data_ptr(), k_h[k0:].data_ptr(), 1.0, nb,
+                                       ie_h[k0:].data_ptr(), centre, sol_h.data_ptr(), info_h.data_ptr(), 0, None)
+        if code != 0:
+            raise RuntimeError(pkg.last_error())
+    e2e_t = time.perf_counter() - t0
+    e2e = {"value": B * e2e_steps / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": B * 16 * (2 + n),
+           "d2h_bytes_per_step": B * (16 * N + 4)}
+
+    if rank != 0:
+        return 0
+    peaks = measured_peaks()
+    # roofline of the dominant kernel family: the LU's trailing update
+    lu_flops = (8.0 / 3.0) * N ** 3
+    achieved_tf = lu_flops * samples / world / dev_time / 1e12
+    roof = {"bound": "tensor", "achieved": achieved_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+            "frac": achieved_tf / peaks["bf16_tflops"], "traffic": None,
+            "note": f"whole-step average of (8/3) N^3 LU flops; peak = {peaks['src']} bf16"}
+    line = {"metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)", "value": value,
+            "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_time / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128" if not mixed else "c64+c128",
+            "data": "synthetic (reference grid generator, Alipio soil, 1.2/50 us current)",
+            "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, 1417 nodes, N=4537, 2048 Laplace "
+                                   "samples (nt=4094, 10 MHz), Alipio soil sigma0=1 mS/m, centre injection",
+                       "precision": args.precision, "samples_per_step": B, "l2": "flushed between steps (256 MB write)"},
+            "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e,
+            "refinement": {"max_iterations": stats_iter, "fallbacks": stats_fb}, "wall_s": wall}
+    if not args.no_cpu_baseline:
+        nsamp = args.cpu_samples or (os.cpu_count() or 1)
+        line["cpu_baseline"] = cpu_baseline(args, elec, img, nodes, s, kappa, inj, centre, nsamp)[0]
+    print(json.dumps(line))
+    plan.close()
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

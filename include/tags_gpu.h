@@ -1,0 +1,157 @@
+/* GB300-native drop-in for the frequency-domain HEM hot path of
+ * pedrohnv/transient-analysis-grounding-systems (TAGS).
+ *
+ * Part 1 -- drop-in entry points. Same names, argument meaning, return codes
+ * and memory contract as the reference C library, so C callers relink against
+ * libtags_gpu.so instead of libhphem.so (host buffers in, host buffers out;
+ * each call copies to and from the GPU):
+ *   calculate_impedances   replaces src/electrode.c:304-377 (decl src/electrode.h:276-281)
+ *   impedances_images      replaces src/electrode.c:379-431 (decl src/electrode.h:310-317)
+ *   fill_incidence_imm     replaces src/linalg.c:12-86      (decl src/linalg.h:38-41)
+ *   fill_impedance_imm     replaces src/linalg.c:88-110     (decl src/linalg.h:56-59)
+ *   solve_immittance       replaces src/linalg.c:112-139    (decl src/linalg.h:79-81)
+ *   laplace_trans          replaces src/auxiliary.c:239-263 (decl src/auxiliary.h:320-321)
+ *   inv_laplace_trans      replaces src/auxiliary.c:265-329 (decl src/auxiliary.h:366-368)
+ *
+ * Part 2 -- batched extension (no counterpart in the reference; it replaces the
+ * per-sample OpenMP loop the reference's examples write around the calls
+ * above, e.g. examples/three_grids.c:286-443): a plan keeps geometry,
+ * incidence and workspaces on the device and solves many Laplace samples per
+ * launch sequence, in plain FP64 or in the mixed-precision form.
+ *
+ * Complex numbers are C99 `double _Complex` (16 bytes, real part first).
+ * Matrices are column-major, as in the reference.
+ */
+#ifndef TAGS_GPU_H_
+#define TAGS_GPU_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+/* Same size, alignment and calling convention as C99 double _Complex on the
+ * x86-64 SysV and AArch64 ABIs (two doubles in floating-point registers). */
+typedef struct { double re, im; } tags_cdouble;
+extern "C" {
+#else
+#include <complex.h>
+typedef double _Complex tags_cdouble;
+#endif
+
+/* The reference's segment record (src/electrode.h:33-45) and integration
+ * types (src/electrode.h:17-31). Defined here only when the reference's
+ * electrode.h was not included first. */
+#ifndef ELECTRODE_H_
+typedef struct {
+    double start_point[3];
+    double end_point[3];
+    double middle_point[3];
+    double length;
+    double radius;
+} Electrode;
+enum Integration_type { INTG_NONE = 1, INTG_DOUBLE = 2, INTG_SINGLE = 3, INTG_MHEM = 4 };
+#endif
+
+/* ---- Part 1: drop-in entry points ----------------------------------------- */
+
+/* Lower triangle (zl[i*m + k], k >= i) of ZL and ZT of the segments. The
+ * cubature tolerances are accepted for source compatibility; the GPU uses a
+ * fixed-order rule that meets ~1e-12 relative accuracy on every pair. zl == zt
+ * is allowed and reproduces the reference's write order. Returns 0, or -10 for
+ * an unknown integration_type, or a negative TAGS_E_* code. */
+int calculate_impedances (tags_cdouble *zl, tags_cdouble *zt, const Electrode *electrodes,
+                          size_t num_electrodes, tags_cdouble gamma, tags_cdouble s, double mur,
+                          tags_cdouble kappa, size_t max_eval, double req_abs_error,
+                          double req_rel_error, int integration_type);
+
+/* Adds (+=) the couplings to the image segments (k >= i, diagonal included). */
+int impedances_images (tags_cdouble *zl, tags_cdouble *zt, const Electrode *electrodes,
+                       const Electrode *images, size_t num_electrodes, tags_cdouble gamma,
+                       tags_cdouble s, double mur, tags_cdouble kappa, tags_cdouble ref_l,
+                       tags_cdouble ref_t, size_t max_eval, double req_abs_error,
+                       double req_rel_error, int integration_type);
+
+/* Incidence blocks A, B (and transposes) of W_G, leading dimension n + 2m.
+ * Returns 1 at the first node without incidence (nodes up to it are written),
+ * -sum(A) or sum(B) - m on a bad checksum, 0 on success. */
+int fill_incidence_imm (tags_cdouble *wg, const Electrode *electrodes, size_t num_electrodes,
+                        const double *nodes, size_t num_nodes);
+
+/* -ZL, -ZT (whole m x m blocks as stored), zero coupling blocks, zero Y_E. */
+int fill_impedance_imm (tags_cdouble *wg, const tags_cdouble *zl, const tags_cdouble *zt,
+                        size_t num_electrodes, size_t num_nodes);
+
+/* Solves W_G x = ie (W_G symmetric, lower half read); ie <- [U; I_L; I_T].
+ * Returns 0, or k > 0 when the k-th pivot of the factorisation is exactly
+ * zero (singular system). wg is left unchanged (the reference leaves its
+ * factorisation there; its content is not part of the contract). */
+int solve_immittance (tags_cdouble *wg, tags_cdouble *ie, size_t num_electrodes, size_t num_nodes);
+
+/* Numerical Laplace transform and its inverse, with the reference's
+ * conventions (s_k = c + j k 2pi/tmax, c = ln(nt^2)/tmax; window `filter` as
+ * the reference's INLT_Filter: 0 none, 1 Blackman, 2 Hanning, 3 Lanczos,
+ * 4 Riesz). */
+int laplace_trans (double *f, tags_cdouble *g, tags_cdouble *s, double tmax, size_t nt);
+int inv_laplace_trans (double *f, tags_cdouble *g, tags_cdouble *s, double tmax, size_t nt,
+                       int filter);
+
+/* ---- Part 2: batched extension -------------------------------------------- */
+
+enum {
+    TAGS_PLAIN_FP64 = 0,  /* FP64 fill, FP64 LU with partial pivoting */
+    TAGS_MIXED = 1        /* FP32/FP64 fill, low-precision LU + FP64 refinement */
+};
+
+/* Error codes (negative) of the extension and of argument checks. */
+enum {
+    TAGS_E_ARG = -101,          /* invalid argument or size */
+    TAGS_E_CUDA = -102,         /* CUDA runtime failure (see tags_gpu_last_error) */
+    TAGS_E_NOMEM = -103,        /* device allocation failed */
+    TAGS_E_GEOMETRY = -104,     /* coincident/overlapping segments (divergent integral) */
+    TAGS_E_NONFINITE = -105     /* NaN or Inf in a result */
+};
+
+/* Run flags. */
+enum {
+    TAGS_RUN_DEVICE_PTRS = 1    /* s, kappa, ie and the outputs are device pointers */
+};
+
+typedef struct tags_plan_s *tags_plan;
+
+/* Per-run statistics (optional). */
+typedef struct {
+    int max_iterations;        /* largest refinement iteration count (mixed) */
+    int fallbacks;             /* samples re-solved in plain FP64 (mixed) */
+    double max_backward_error; /* largest normwise backward error |b - W x| / (|W| |x| + |b|) */
+    double seconds;            /* device time of the run */
+} tags_run_stats;
+
+/* Geometry and incidence are uploaded once. images may be NULL (no images).
+ * max_batch = samples resident at once (0 = sized from free device memory). */
+int tags_plan_create (tags_plan *plan, const Electrode *electrodes, const Electrode *images,
+                      size_t num_electrodes, const double *nodes, size_t num_nodes,
+                      int precision, size_t max_batch);
+
+/* Solve ns samples: s[k], kappa[k] (soil complex conductivity sigma + s eps),
+ * ie: ns x n injected node currents (sample-major; NULL = unit current at
+ * inj_node). Outputs (any may be NULL): sol ns x (n + 2m) = [U; I_L; I_T],
+ * info ns ints (0 ok, >0 singular pivot, <0 error). */
+int tags_plan_run (tags_plan plan, const tags_cdouble *s, const tags_cdouble *kappa, double mur,
+                   size_t ns, const tags_cdouble *ie, size_t inj_node, tags_cdouble *sol,
+                   int *info, int flags, tags_run_stats *stats);
+
+int tags_plan_destroy (tags_plan plan);
+
+/* Number of CUDA kernel launches issued by this library since load. */
+long long tags_gpu_launch_count (void);
+
+/* Last error message of the calling thread ("" if none). */
+const char *tags_gpu_last_error (void);
+
+/* 0/1: suppress the reference-style messages printed on errors. */
+void tags_gpu_set_quiet (int quiet);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAGS_GPU_H_ */

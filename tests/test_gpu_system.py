@@ -1,0 +1,162 @@
+"""GPU parity of the immittance assembly, the solve, the Laplace pair and the
+batched plans (plain FP64 and mixed) against golden fixtures and the oracle."""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_incidence_bit_exact(gpu_pkg, port):
+    pkg = gpu_pkg
+    gd = golden("incidence.npz")
+    e = gd["elec"]
+    pkg.lib().tags_gpu_set_quiet(1)
+    for name in ("ok", "disconnected", "duplicate"):
+        nd = gd[f"{name}_nodes"]
+        N = nd.shape[0] + 2 * e.shape[0]
+        wg = np.full(N * N, 7.0 + 7.0j, dtype=np.complex128)
+        assert pkg.fill_incidence_imm(wg, e, nd) == int(gd[f"{name}_code"])
+        assert np.array_equal(wg, gd[f"{name}_wg"])
+    pkg.lib().tags_gpu_set_quiet(0)
+
+
+def test_fill_impedance_bit_exact(gpu_pkg, port):
+    pkg = gpu_pkg
+    rng = np.random.default_rng(2)
+    m, n = 17, 13
+    N = n + 2 * m
+    zl = rng.standard_normal(m * m) + 1j * rng.standard_normal(m * m)
+    zt = rng.standard_normal(m * m) + 1j * rng.standard_normal(m * m)
+    w1 = rng.standard_normal(N * N) + 1j * rng.standard_normal(N * N)
+    w2 = w1.copy()
+    assert pkg.fill_impedance_imm(w1, zl, zt, m, n) == 0
+    port.fill_impedance_imm(w2, zl, zt, m, n)
+    assert np.array_equal(w1, w2)
+
+
+def _assemble_host(pkg, e, img, nodes, s, kappa):
+    m, n = e.shape[0], nodes.shape[0]
+    N = n + 2 * m
+    gamma, ref_t = pkg.medium(s, kappa)
+    zl = np.zeros(m * m, np.complex128)
+    zt = np.zeros(m * m, np.complex128)
+    pkg.calculate_impedances(zl, zt, e, gamma, s, 1.0, kappa)
+    pkg.impedances_images(zl, zt, e, img, gamma, s, 1.0, kappa, 1.0, ref_t)
+    wg = np.zeros(N * N, np.complex128)
+    assert pkg.fill_incidence_imm(wg, e, nodes) == 0
+    pkg.fill_impedance_imm(wg, zl, zt, m, n)
+    return wg, zl, zt
+
+
+def test_solve_matches_zsysv(gpu_pkg, port):
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    img = pkg.images(e)
+    m, n = e.shape[0], nodes.shape[0]
+    N = n + 2 * m
+    for k in (0, 300, 1023):
+        wg, _, _ = _assemble_host(pkg, e, img, nodes, gd["s"][k], gd["kappa"][k])
+        w2 = wg.copy()
+        x1 = np.zeros(N, np.complex128)
+        x1[0] = gd["inj_s"][k]
+        x2 = x1.copy()
+        assert pkg.solve_immittance(wg, x1, m, n) == 0
+        assert port.solve_immittance(w2, x2, m, n) == 0
+        assert rel_err(x1, x2) < 1e-10
+    # singular system: a disconnected node makes a zero column
+    z = np.zeros(9, np.complex128)
+    w = np.zeros(9, np.complex128)
+    w[0] = 1.0
+    pkg.lib().tags_gpu_set_quiet(1)
+    assert pkg.solve_immittance(w, z[:3].copy(), 1, 1) > 0
+    pkg.lib().tags_gpu_set_quiet(0)
+
+
+def test_laplace_pair_matches_golden(gpu_pkg):
+    pkg = gpu_pkg
+    gd = golden("nlt.npz")
+    for nt in (256, 255):
+        g, s = pkg.laplace_trans(gd[f"f_{nt}"], 1e-4)
+        assert rel_err(g, gd[f"g_{nt}"]) < 1e-12 and rel_err(s, gd[f"s_{nt}"]) < 1e-15
+        for filt in (0, 1, 2, 4):
+            assert rel_err(pkg.inv_laplace_trans(g, s, 1e-4, nt, filt), gd[f"inv_{nt}_{filt}"]) < 1e-11
+        assert np.all(np.isnan(pkg.inv_laplace_trans(g, s, 1e-4, nt, 3)))   # reference's 0/0 at w = 0
+
+
+def test_plain_plan_rod_harmonic_impedance(gpu_pkg):
+    """Config 1: Z(f) of the 3 m rod, 100 frequencies, plain FP64 <= 1e-8."""
+    pkg = gpu_pkg
+    gd = golden("rod_zf.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    sol, info, _ = pkg.hem_sweep(e, pkg.images(e), nodes, gd["s"], gd["kappa"], inj_node=0)
+    assert np.all(info == 0)
+    z = sol[:, 0]
+    assert np.max(np.abs(z - gd["sol"][:, 0]) / np.abs(gd["sol"][:, 0])) < 1e-8
+
+
+def _grid2_gpr(pkg, precision):
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    n = nodes.shape[0]
+    ie = np.zeros((len(gd["s"]), n), np.complex128)
+    ie[:, 0] = gd["inj_s"]
+    sol, info, st = pkg.hem_sweep(e, pkg.images(e), nodes, gd["s"], gd["kappa"], ie=ie, precision=precision)
+    gpr = pkg.inv_laplace_trans(sol[:, 0], gd["s"], float(gd["tmax"]), int(gd["nt"]))
+    return gd, sol, info, st, gpr
+
+
+def test_plain_plan_grid_gpr(gpu_pkg):
+    """Config 2: GPR at the corner node, 1024 samples, plain FP64 <= 1e-8."""
+    gd, sol, info, _, gpr = _grid2_gpr(gpu_pkg, gpu_pkg.PLAIN_FP64)
+    assert np.all(info == 0)
+    assert np.max(np.abs(sol[:, 0] - gd["u0"]) / np.abs(gd["u0"])) < 1e-8
+    assert rel_err(gpr, gd["gpr"]) < 1e-8
+
+
+def test_mixed_plan_grid_gpr(gpu_pkg):
+    """Config 2, mixed form: impedance and GPR <= 1e-6 against the reference."""
+    gd, sol, info, st, gpr = _grid2_gpr(gpu_pkg, gpu_pkg.MIXED)
+    assert np.all(info == 0)
+    assert np.max(np.abs(sol[:, 0] - gd["u0"]) / np.abs(gd["u0"])) < 1e-6
+    assert rel_err(gpr, gd["gpr"]) < 1e-6
+    assert st.max_iterations >= 1
+
+
+def test_full_size_properties(gpu_pkg):
+    """60 x 60 m grid (N = 4537): the plain and mixed plans agree with the
+    drop-in solve, the drop-in solution has an FP64 backward error, and the
+    transfer impedances are reciprocal (W_G symmetric)."""
+    pkg = gpu_pkg
+    e, nodes = pkg.electrode_grid(13, 13, 60.0, 60.0, 5, 5, 7e-3, -0.5)
+    img = pkg.images(e)
+    m, n = e.shape[0], nodes.shape[0]
+    N = n + 2 * m
+    c = np.log(4094.0 ** 2) / 204.7e-6
+    s = np.array([c + 2j * np.pi * 2e4, c + 2j * np.pi * 7e6])
+    kap = []
+    for sk in s:
+        sig, epsr = pkg.alipio_soil(1e-3, sk, 1.26 * (1e-3 * 1e3) ** -0.73, 0.54, 12)
+        kap.append(sig + sk * epsr * pkg.EPS0)
+    kappa = np.array(kap)
+    centre = int(np.argmin(np.linalg.norm(nodes - [30.0, 30.0, -0.5], axis=1)))
+    wg, _, _ = _assemble_host(pkg, e, img, nodes, s[0], kappa[0])
+    W = wg.reshape(N, N).T.copy()
+    Wsym = np.tril(W) + np.tril(W, -1).T
+    x = np.zeros(N, np.complex128)
+    x[centre] = 1.0
+    assert pkg.solve_immittance(wg, x, m, n) == 0
+    b = np.zeros(N, np.complex128)
+    b[centre] = 1.0
+    berr = np.linalg.norm(Wsym @ x - b, np.inf) / (np.linalg.norm(Wsym, np.inf) * np.linalg.norm(x, np.inf))
+    assert berr < 1e-13
+    plain, _, _ = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=centre, precision=pkg.PLAIN_FP64)
+    mixed, info, st = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=centre, precision=pkg.MIXED)
+    assert np.all(info == 0)
+    assert rel_err(plain[0], x) < 1e-9
+    assert np.max(np.abs(mixed[:, :n] - plain[:, :n])) / np.max(np.abs(plain[:, :n])) < 1e-6
+    # reciprocity: potential at node 0 for a current at the centre equals the reverse
+    other, _, _ = pkg.hem_sweep(e, img, nodes, s[:1], kappa[:1], inj_node=0, precision=pkg.PLAIN_FP64)
+    assert abs(other[0, centre] - plain[0, 0]) < 1e-11 * abs(plain[0, 0])

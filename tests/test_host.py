@@ -1,0 +1,85 @@
+"""CPU tests of the host side: geometry/soil helpers against the reference
+(bit for bit), and the C-ABI library's exported symbols (no GPU calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def test_electrode_grid_matches_reference(pkg, ref):
+    class Grid(ctypes.Structure):
+        _fields_ = [("vx", ctypes.c_uint), ("vy", ctypes.c_uint), ("lx", ctypes.c_double), ("ly", ctypes.c_double),
+                    ("nx", ctypes.c_uint), ("ny", ctypes.c_uint), ("r", ctypes.c_double), ("z", ctypes.c_double)]
+    ref.lib.electrode_grid.argtypes = [Grid, ctypes.c_void_p, ctypes.c_void_p]
+    for g in ((5, 5, 10.0, 10.0, 3, 3, 7e-3, -0.5), (13, 13, 60.0, 60.0, 5, 5, 7e-3, -0.5),
+              (4, 7, 17.3, 29.1, 3, 5, 9e-3, -0.73), (2, 2, 1.0, 1.0, 1, 1, 1e-3, 0.0)):
+        m = ref.lib.number_segments(Grid(*g))
+        n = ref.lib.number_nodes(Grid(*g))
+        e = np.zeros((m, 11))
+        nd = np.zeros((n, 3))
+        ref.lib.electrode_grid(Grid(*g), e.ctypes.data, nd.ctypes.data)
+        pe, pn = pkg.electrode_grid(*g)
+        assert (m, n) == (pkg.number_segments(g[0], g[1], g[4], g[5]), pkg.number_nodes(g[0], g[1], g[4], g[5]))
+        assert np.array_equal(pe, e) and np.array_equal(pn, nd)
+
+
+def test_segment_electrode_and_images_match_reference(pkg, ref, orc_mod):
+    for a, b, k in (([0, 0, 0], [0, 0, -3], 10), ([1.5, -2, -0.5], [7.25, 3.1, -4.0], 7)):
+        e1, n1 = ref.segment_electrode(a, b, k, 7e-3)
+        e2, n2 = pkg.segment_electrode(a, b, k, 7e-3)
+        assert np.array_equal(e1, e2) and np.array_equal(n1, n2)
+        assert np.array_equal(pkg.images(e2), orc_mod.images(e1))
+
+
+def test_soil_and_samples_match_reference(pkg, ref):
+    for s in (2j * np.pi * 10.0, 3e4 + 2j * np.pi * 1e6, 8.1e4 + 0j):
+        a = pkg.alipio_soil(1e-3, s, 1.26, 0.54, 12)
+        b = ref.alipio_soil(1e-3, s, 1.26, 0.54, 12)
+        assert abs(a[0] - b[0]) <= 1e-14 * abs(b[0]) and abs(a[1] - b[1]) <= 1e-14 * abs(b[1])
+    g, s = ref.laplace_trans(np.ones(4094), 204.7e-6)
+    assert np.array_equal(pkg.laplace_samples(4094, 204.7e-6), s)
+
+
+def test_logspace_linspace_match_reference(pkg):
+    f = pkg.logspace(2, 7, 100)
+    assert f[-1] == 1e7 and f[0] == 100.0 and len(f) == 100
+    u = pkg.linspace(0.0, -3.0, 11)
+    assert u[-1] == -3.0 and u[1] == 0.0 + 1 * (-3.0 / 10)
+
+
+def _header_functions():
+    text = open(os.path.join(ROOT, "include", "tags_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_ ]*?\s*\*?\s*([A-Za-z_][A-Za-z0-9_]*)\s*\(", text, re.M)
+    return sorted(set(n for n in names if n not in ("if", "sizeof")))
+
+
+def test_library_exports_every_declared_symbol(pkg):
+    pkg.build()
+    lib = ctypes.CDLL(pkg.LIB_PATH)
+    declared = _header_functions()
+    assert len(declared) >= 13
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert set(pkg.EXPORTS) <= set(declared)
+
+
+def test_electrode_record_layout(pkg):
+    # the C-ABI passes the reference's 88-byte Electrode unchanged
+    class Electrode(ctypes.Structure):
+        _fields_ = [("start", ctypes.c_double * 3), ("end", ctypes.c_double * 3), ("mid", ctypes.c_double * 3),
+                    ("length", ctypes.c_double), ("radius", ctypes.c_double)]
+    assert ctypes.sizeof(Electrode) == 88
+    e = pkg.populate_electrode([0, 0, -0.5], [1, 0, -0.5], 7e-3)
+    assert e.dtype == np.float64 and e.shape == (11,)
+
+
+def test_compute_calls_fail_loudly_without_library(pkg, monkeypatch, tmp_path):
+    monkeypatch.setattr(pkg, "_lib", None)
+    monkeypatch.setattr(pkg, "LIB_PATH", str(tmp_path / "missing.so"))
+    with pytest.raises(RuntimeError, match="missing"):
+        pkg.solve_immittance(np.zeros(9, np.complex128), np.zeros(3, np.complex128), 1, 1)

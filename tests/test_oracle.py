@@ -1,0 +1,246 @@
+"""CPU tests of the oracle: its published-method pieces (cubature, DFT), its
+restatement of the reference (bit-for-bit against the reference compiled from
+its own sources, where present) and the committed golden fixtures."""
+import ctypes
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+
+
+# ---- cubature (published Gauss-Kronrod / Genz-Malik rules) ------------------------
+
+CB = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_uint, ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                      ctypes.c_uint, ctypes.POINTER(ctypes.c_double))
+
+
+def hcub(port, f, dim, fdim, max_eval, abs_tol, rel_tol, norm=0):
+    fn = port.lib.hcubature
+    fn.argtypes = [ctypes.c_uint, CB, ctypes.c_void_p, ctypes.c_uint, ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(ctypes.c_double), ctypes.c_size_t, ctypes.c_double, ctypes.c_double,
+                   ctypes.c_int, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+    calls = [0]
+
+    def cb(ndim, x, data, fd, fval):
+        calls[0] += 1
+        vals = f([x[i] for i in range(ndim)])
+        for j in range(fd):
+            fval[j] = vals[j]
+        return 0
+
+    lo = (ctypes.c_double * dim)(*([0.0] * dim))
+    hi = (ctypes.c_double * dim)(*([1.0] * dim))
+    val = (ctypes.c_double * fdim)()
+    err = (ctypes.c_double * fdim)()
+    code = fn(fdim, CB(cb), None, dim, lo, hi, max_eval, abs_tol, rel_tol, norm, val, err)
+    return code, list(val), list(err), calls[0]
+
+
+def test_gk15_exact_to_degree_22(port):
+    for k in (0, 1, 5, 13, 22):
+        code, val, err, n = hcub(port, lambda x, k=k: [x[0] ** k], 1, 1, 15, 0.0, 0.0)
+        assert code == 0 and n == 15
+        assert abs(val[0] - 1.0 / (k + 1)) < 1e-14
+
+
+def test_genz_malik_exact_to_degree_7(port):
+    for a, b in ((0, 0), (3, 4), (7, 0), (2, 5), (1, 1)):
+        code, val, err, n = hcub(port, lambda x, a=a, b=b: [x[0] ** a * x[1] ** b], 2, 1, 17, 0.0, 0.0)
+        assert code == 0 and n == 17
+        assert abs(val[0] - 1.0 / ((a + 1) * (b + 1))) < 1e-14
+        if a + b <= 5:
+            assert err[0] < 1e-14   # embedded degree-5 rule is exact too
+
+
+def test_adaptive_singular_corner(port):
+    # int_0^1 int_0^1 (x + y)^(-1/2) = (4/3)(2 sqrt 2 - 2)
+    exact = 4.0 / 3.0 * (2.0 * math.sqrt(2.0) - 2.0)
+    code, val, err, n = hcub(port, lambda x: [1.0 / math.sqrt(x[0] + x[1]), 0.0], 2, 2, 0, 0.0, 1e-10, 1)
+    assert code == 0
+    assert abs(val[0] - exact) < 1e-9 * exact
+    code, val2, err2, n2 = hcub(port, lambda x: [1.0 / math.sqrt(x[0] + x[1]), 0.0], 2, 2, 200, 0.0, 1e-12, 1)
+    assert n2 <= 200 + 34   # max_eval stops the refinement (checked after each split)
+
+
+def test_dft_matches_numpy(port):
+    rng = np.random.default_rng(3)
+    for nt in (16, 17, 4094, 255):
+        x = rng.standard_normal(nt)
+        g, s = port.laplace_trans(x, 1.0)
+        c = math.log(float(nt) ** 2) / 1.0
+        dt = 1.0 / (nt - 1)
+        w = x * dt * np.exp(-c * np.arange(nt) * dt)
+        assert rel_err(g, np.fft.rfft(w)) < 1e-12
+        y = port.inv_laplace_trans(g, s, 1.0, nt, 0)
+        # the inverse re-applies e^{c t}, up to nt^2 at t_max: eps * nt^2
+        assert rel_err(y, x) < 1e-15 * nt * nt + 1e-12
+
+
+# ---- restatement pinned against the reference build ------------------------------
+
+def _grid_geom(pkg):
+    e, nd = pkg.electrode_grid(4, 3, 9.0, 6.0, 3, 2, 6e-3, -0.4)
+    return e, nd
+
+
+def test_port_equals_reference_fill(pkg, port, ref, orc_mod):
+    O = orc_mod
+    e, nd = _grid_geom(pkg)
+    img = O.images(e)
+    for s in (2j * np.pi * 60.0, 1.3e5 + 2j * np.pi * 3e6):
+        kappa = 1 / 300.0 + s * 15 * O.EPS0
+        for it in (O.INTG_DOUBLE, O.INTG_MHEM, O.INTG_SINGLE, O.INTG_NONE):
+            a = port.hem_impedances(e, img, s, kappa, 1.0, 0, 1e-6, 1e-6, it)
+            b = ref.hem_impedances(e, img, s, kappa, 1.0, 0, 1e-6, 1e-6, it)
+            assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]), it
+
+
+def test_port_equals_reference_integral_and_self(port, ref, pkg):
+    e, _ = _grid_geom(pkg)
+    for i, k in ((0, 1), (0, 5), (2, 9), (7, 3)):
+        for it in (1, 2, 3, 4):
+            a = port.integral(e[i], e[k], 0.3 + 0.4j, 0, 1e-7, 1e-7, it)
+            b = ref.integral(e[i], e[k], 0.3 + 0.4j, 0, 1e-7, 1e-7, it)
+            assert a == b
+    assert port.self_integral(e[0]) == ref.self_integral(e[0])
+    assert port.integral(e[0], e[1], 0.1, 0, 1e-6, 1e-6, 7)[2] == -10
+
+
+def test_port_equals_reference_linalg(pkg, port, ref, orc_mod):
+    O = orc_mod
+    e, nd = _grid_geom(pkg)
+    m, n = e.shape[0], nd.shape[0]
+    N = n + 2 * m
+    img = O.images(e)
+    s = 2e5 + 2j * np.pi * 1e6
+    kappa = 0.01 + s * 10 * O.EPS0
+    zl, zt = ref.hem_impedances(e, img, s, kappa)
+    zlf = np.ascontiguousarray(zl.T).reshape(-1)
+    ztf = np.ascontiguousarray(zt.T).reshape(-1)
+    out = []
+    for lib in (port, ref):
+        wg = np.zeros(N * N, dtype=np.complex128)
+        assert lib.fill_incidence_imm(wg, e, nd) == 0
+        lib.fill_impedance_imm(wg, zlf, ztf, m, n)
+        w0 = wg.copy()
+        ie = np.zeros(N, dtype=np.complex128)
+        ie[0] = 1.0
+        assert lib.solve_immittance(wg, ie, m, n) == 0
+        out.append((w0, ie))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert np.array_equal(out[0][1], out[1][1])
+    # incidence checksums of the reference (src/linalg.c:77-84)
+    W = out[0][0].reshape(N, N).T
+    A = W[n:n + m, :n]
+    B = W[n + m:, :n]
+    assert A.sum() == 0 and B.sum() == m
+
+
+def test_port_equals_reference_nlt_soil_heidler(port, ref):
+    f = np.sin(np.linspace(0, 7, 300)) ** 2
+    g1, s1 = port.laplace_trans(f, 2e-4)
+    g2, s2 = ref.laplace_trans(f, 2e-4)
+    assert np.array_equal(g1, g2) and np.array_equal(s1, s2)
+    for filt in range(5):
+        a = port.inv_laplace_trans(g1, s1, 2e-4, 300, filt)
+        b = ref.inv_laplace_trans(g1, s1, 2e-4, 300, filt)
+        assert np.array_equal(a, b, equal_nan=True)
+    for s in (2j * np.pi * 10.0, 3e4 + 2j * np.pi * 1e6):
+        assert port.alipio_soil(1e-3, s, 1.26, 0.54, 12) == ref.alipio_soil(1e-3, s, 1.26, 0.54, 12)
+    assert port.heidler(1e-6, 1e3, 1.8e-6, 95e-6, 2.0) == ref.heidler(1e-6, 1e3, 1.8e-6, 95e-6, 2.0)
+
+
+def test_port_sweep_matches_reference_calls(pkg, port, ref, orc_mod):
+    O = orc_mod
+    e, nd = pkg.segment_electrode([0, 0, 0], [0, 0, -3], 10, 7e-3)
+    img = O.images(e)
+    s = 2j * np.pi * np.array([1e3, 1e6])
+    kappa = 0.01 + s * 10 * O.EPS0
+    sol, info = port.hem_sweep(e, img, nd, s, kappa, 0, np.ones(2), req_abs=1e-6, req_rel=1e-6, threads=2)
+    assert np.all(info == 0)
+    m, n = e.shape[0], nd.shape[0]
+    N = n + 2 * m
+    for k in range(2):
+        zl, zt = ref.hem_impedances(e, img, s[k], kappa[k])
+        wg = np.zeros(N * N, dtype=np.complex128)
+        ref.fill_incidence_imm(wg, e, nd)
+        ref.fill_impedance_imm(wg, np.ascontiguousarray(zl.T).reshape(-1), np.ascontiguousarray(zt.T).reshape(-1), m, n)
+        ie = np.zeros(N, dtype=np.complex128)
+        ie[0] = 1.0
+        ref.solve_immittance(wg, ie, m, n)
+        assert np.array_equal(ie, sol[k])
+
+
+# ---- golden fixtures (made by the reference) against the restatement ----------------
+
+def test_golden_rod_zf(port, orc_mod):
+    gd = golden("rod_zf.npz")
+    e, nd = gd["elec"], gd["nodes"]
+    img = orc_mod.images(e)
+    idx = [0, 37, 99]
+    sol, info = port.hem_sweep(e, img, nd, gd["s"][idx], gd["kappa"][idx], 0, np.ones(3), req_abs=0.0,
+                               req_rel=1e-11, threads=2)
+    assert np.all(info == 0)
+    assert rel_err(sol[:, 0], gd["sol"][idx, 0]) < 1e-12
+
+
+def test_golden_nlt(port):
+    gd = golden("nlt.npz")
+    for nt in (256, 255):
+        g, s = port.laplace_trans(gd[f"f_{nt}"], 1e-4)
+        assert rel_err(g, gd[f"g_{nt}"]) < 1e-13
+        for filt in (0, 1, 2, 4):
+            assert rel_err(port.inv_laplace_trans(g, s, 1e-4, nt, filt), gd[f"inv_{nt}_{filt}"]) < 1e-12
+        # the reference's Lanczos window divides 0/0 at w = 0 (NaN everywhere)
+        assert np.all(np.isnan(gd[f"inv_{nt}_3"])) == np.all(np.isnan(port.inv_laplace_trans(g, s, 1e-4, nt, 3)))
+
+
+def test_golden_incidence_codes(port):
+    gd = golden("incidence.npz")
+    e = gd["elec"]
+    for name in ("ok", "disconnected", "duplicate"):
+        nd = gd[f"{name}_nodes"]
+        N = nd.shape[0] + 2 * e.shape[0]
+        wg = np.full(N * N, 7.0 + 7.0j, dtype=np.complex128)
+        assert port.fill_incidence_imm(wg, e, nd) == int(gd[f"{name}_code"])
+        assert np.array_equal(wg, gd[f"{name}_wg"])
+
+
+# ---- known answers from the reference's closed forms ------------------------------
+
+def test_self_integral_is_static_reduced_kernel(port, pkg):
+    from scipy import integrate
+    e = pkg.populate_electrode([0, 0, 0], [1.3, 0, 0], 4e-3)
+    L, a = 1.3, 4e-3
+    # \int_0^L \int_0^L dx dy / sqrt((x-y)^2 + a^2) = 2 \int_0^L (L-u)/sqrt(u^2+a^2) du
+    val, _ = integrate.quad(lambda u: 2 * (L - u) / math.sqrt(u * u + a * a), 0, L, epsabs=0, epsrel=1e-13,
+                            limit=200, points=[a, 10 * a])
+    assert abs(port.self_integral(e) - val) < 1e-12 * val
+
+
+def test_mhem_kernel_is_exact_static_integral(port, pkg):
+    # logNf is the exact inner integral of 1/r: INTG_MHEM equals the 2-D static integral
+    from scipy import integrate
+    s_ = pkg.populate_electrode([0, 0, 0], [1.0, 0, 0], 5e-3)
+    r_ = pkg.populate_electrode([0.3, 0.7, 0.2], [0.9, 1.5, -0.4], 5e-3)
+    val, _, code = port.integral(s_, r_, 0.0, 0, 0.0, 1e-13, 4)
+    L0, L1 = r_[9], s_[9]
+
+    def f(t1, t0):
+        pr = r_[0:3] + t0 * (r_[3:6] - r_[0:3])
+        ps = s_[0:3] + t1 * (s_[3:6] - s_[0:3])
+        return 1.0 / np.linalg.norm(pr - ps)
+    num, _ = integrate.dblquad(f, 0, 1, 0, 1, epsabs=0, epsrel=1e-12)
+    assert code == 0
+    assert abs(val.real - num * L0 * L1) < 1e-10 * abs(val.real)
+
+
+@pytest.mark.parametrize("grid,mn", [((5, 5, 10.0, 10.0, 3, 3), (120, 105)),
+                                     ((13, 13, 60.0, 60.0, 5, 5), (1560, 1417)),
+                                     ((25, 25, 120.0, 120.0, 5, 5), (6000, 5425))])
+def test_grid_counts(pkg, grid, mn):
+    vx, vy, lx, ly, nx, ny = grid
+    assert (pkg.number_segments(vx, vy, nx, ny), pkg.number_nodes(vx, vy, nx, ny)) == mn

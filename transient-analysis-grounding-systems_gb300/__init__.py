@@ -1,0 +1,416 @@
+"""GB300-native HEM hot path of TAGS (transient analysis of grounding systems).
+
+Python host-side mirror of the reference C interface for the per-Laplace-sample
+path, backed by the CUDA library ``libtags_gpu.so`` (built from ``csrc/`` by
+``build.py``). The compute functions call the C-ABI declared in
+``include/tags_gpu.h``; they raise if the library is missing instead of
+falling back to any CPU code.
+
+Reference interface mirrored here (pedrohnv/transient-analysis-grounding-systems):
+
+* geometry, host side: ``populate_electrode`` (src/electrode.c:12-32),
+  ``segment_electrode`` (:103-127), ``number_segments`` / ``number_nodes`` /
+  ``electrode_grid`` (src/grid.c:9-92), ``images`` (examples/three_grids.c:206-214);
+* soil: ``alipio_soil`` (src/auxiliary.c:60-70) and the medium terms of
+  examples/three_grids.c:326-333;
+* GPU drop-ins with the reference's names and semantics:
+  ``calculate_impedances``, ``impedances_images``, ``fill_incidence_imm``,
+  ``fill_impedance_imm``, ``solve_immittance``, ``laplace_trans``,
+  ``inv_laplace_trans``;
+* batched extension: :class:`Plan` (``tags_plan_*``) and :func:`hem_sweep`.
+
+Electrode arrays are float64 ``(m, 11)`` arrays with the reference's field order
+(start[3], end[3], middle[3], length, radius); nodes are ``(n, 3)``.
+Impedance buffers are flat complex128 arrays of ``m*m`` in the reference's
+column-major layout (``z[i*m + k]`` = row k, column i).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtags_gpu.so")
+
+INTG_NONE, INTG_DOUBLE, INTG_SINGLE, INTG_MHEM = 1, 2, 3, 4
+FILTER_NONE, FILTER_BLACKMAN, FILTER_HANNING, FILTER_LANCZOS, FILTER_RIESZ = range(5)
+PLAIN_FP64, MIXED = 0, 1
+RUN_DEVICE_PTRS = 1
+E_ARG, E_CUDA, E_NOMEM, E_GEOMETRY, E_NONFINITE = -101, -102, -103, -104, -105
+
+# physical constants of the reference (src/auxiliary.c:17-21)
+PI = 3.1415926535897932384626433832795029
+TWO_PI = 6.283185307179586476925286766559
+FOUR_PI = 12.5663706143591729538505735331
+MU0 = 1.256637061435917e-6
+EPS0 = 8.854187817620e-12
+
+# C-ABI symbols declared in include/tags_gpu.h
+EXPORTS = (
+    "calculate_impedances", "impedances_images", "fill_incidence_imm", "fill_impedance_imm",
+    "solve_immittance", "laplace_trans", "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
+    "tags_plan_destroy", "tags_gpu_launch_count", "tags_gpu_last_error", "tags_gpu_set_quiet",
+)
+
+
+class c_complex(ctypes.Structure):
+    """C99 ``double _Complex`` by value (two doubles in FP registers)."""
+
+    _fields_ = [("re", ctypes.c_double), ("im", ctypes.c_double)]
+
+    @classmethod
+    def of(cls, z) -> "c_complex":
+        z = complex(z)
+        return cls(z.real, z.imag)
+
+
+class RunStats(ctypes.Structure):
+    _fields_ = [("max_iterations", ctypes.c_int), ("fallbacks", ctypes.c_int),
+                ("max_backward_error", ctypes.c_double), ("seconds", ctypes.c_double)]
+
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_vp = ctypes.c_void_p
+_sz = ctypes.c_size_t
+_lock = threading.Lock()
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    from importlib import util
+    spec = util.spec_from_file_location("_tags_gpu_build", os.path.join(HERE, "build.py"))
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build(force=force)
+
+
+def lib() -> ctypes.CDLL:
+    """The loaded C-ABI library; raises if it was not built."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise RuntimeError(f"{LIB_PATH} is missing: build the CUDA library first (build.py)")
+            L = ctypes.CDLL(LIB_PATH)
+            C = c_complex
+            L.calculate_impedances.argtypes = [_vp, _vp, _vp, _sz, C, C, ctypes.c_double, C, _sz,
+                                               ctypes.c_double, ctypes.c_double, ctypes.c_int]
+            L.impedances_images.argtypes = [_vp, _vp, _vp, _vp, _sz, C, C, ctypes.c_double, C, C, C, _sz,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_int]
+            L.fill_incidence_imm.argtypes = [_vp, _vp, _sz, _vp, _sz]
+            L.fill_impedance_imm.argtypes = [_vp, _vp, _vp, _sz, _sz]
+            L.solve_immittance.argtypes = [_vp, _vp, _sz, _sz]
+            L.laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz]
+            L.inv_laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, ctypes.c_int]
+            L.tags_plan_create.argtypes = [ctypes.POINTER(_vp), _vp, _vp, _sz, _vp, _sz, ctypes.c_int, _sz]
+            L.tags_plan_run.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _sz, _vp, _vp,
+                                        ctypes.c_int, ctypes.POINTER(RunStats)]
+            L.tags_plan_destroy.argtypes = [_vp]
+            L.tags_gpu_launch_count.restype = ctypes.c_longlong
+            L.tags_gpu_last_error.restype = ctypes.c_char_p
+            L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
+            for name in ("calculate_impedances", "impedances_images", "fill_incidence_imm",
+                         "fill_impedance_imm", "solve_immittance", "laplace_trans", "inv_laplace_trans",
+                         "tags_plan_create", "tags_plan_run", "tags_plan_destroy"):
+                getattr(L, name).restype = ctypes.c_int
+            _lib = L
+        return _lib
+
+
+def last_error() -> str:
+    return lib().tags_gpu_last_error().decode()
+
+
+def launch_count() -> int:
+    return int(lib().tags_gpu_launch_count())
+
+
+def _addr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+def _check_c128(a, name, size=None):
+    if not isinstance(a, np.ndarray) or a.dtype != np.complex128 or not a.flags.c_contiguous:
+        raise TypeError(f"{name} must be a C-contiguous complex128 numpy array")
+    if size is not None and a.size < size:
+        raise ValueError(f"{name} must hold at least {size} values")
+
+
+def _elec(e) -> np.ndarray:
+    e = np.ascontiguousarray(e, dtype=np.float64)
+    if e.ndim != 2 or e.shape[1] != 11:
+        raise ValueError("electrodes must be an (m, 11) float64 array")
+    return e
+
+
+# ---- geometry (host side, restating the reference) -----------------------------
+
+def vector_length(a, b) -> float:
+    """src/auxiliary.c:110-125 (sum of squared differences, then sqrt)."""
+    return math.sqrt(sum((a[i] - b[i]) ** 2 for i in range(3)))
+
+
+def populate_electrode(start, end, radius) -> np.ndarray:
+    """One electrode row (src/electrode.c:12-32)."""
+    start = [float(v) for v in start]
+    end = [float(v) for v in end]
+    if all(abs(start[i] - end[i]) <= 2.220446049250313e-16 for i in range(3)):
+        raise ValueError("start_point and end_point are equal")
+    if radius <= 0:
+        raise ValueError("radius must be > 0")
+    mid = [(start[i] + end[i]) / 2.0 for i in range(3)]
+    return np.array(start + end + mid + [vector_length(start, end), float(radius)])
+
+
+def linspace(a: float, b: float, n: int) -> np.ndarray:
+    """src/auxiliary.c:24-36: a + i*step with the last point pinned to b."""
+    if n < 2:
+        raise ValueError("n must be >= 2")
+    c = (b - a) / (n - 1)
+    u = np.array([a + i * c for i in range(n - 1)] + [b], dtype=np.float64)
+    return u
+
+
+def logspace(a: float, b: float, n: int) -> np.ndarray:
+    """src/auxiliary.c:38-50."""
+    c = (b - a) / (n - 1)
+    return np.array([10.0 ** (a + i * c) for i in range(n - 1)] + [10.0 ** b])
+
+
+def segment_electrode(start, end, num_segments: int, radius: float):
+    """Split a conductor into equal segments (src/electrode.c:103-127)."""
+    if num_segments < 1:
+        raise ValueError("number of segments should be greater than 0")
+    nn = num_segments + 1
+    xyz = [linspace(start[d], end[d], nn) for d in range(3)]
+    nodes = np.stack(xyz, axis=1)
+    elec = np.stack([populate_electrode(nodes[i], nodes[i + 1], radius) for i in range(num_segments)])
+    return elec, nodes
+
+
+def number_segments(vx, vy, nx, ny) -> int:
+    """src/grid.c:9-17."""
+    return nx * vy * (vx - 1) + ny * vx * (vy - 1)
+
+
+def number_nodes(vx, vy, nx, ny) -> int:
+    """src/grid.c:19-27."""
+    return vx * vy + vx * (vy - 1) * (ny - 1) + vy * (vx - 1) * (nx - 1)
+
+
+def electrode_grid(vertices_x, vertices_y, length_x, length_y, edge_segments_x, edge_segments_y,
+                   radius, depth):
+    """Rectangular grid (src/grid.c:29-92): x-directed conductors row by row,
+    then y-directed column by column, with the reference's node order."""
+    vx, vy, nx, ny = int(vertices_x), int(vertices_y), int(edge_segments_x), int(edge_segments_y)
+    lx = length_x / (nx * (vx - 1))
+    ly = length_y / (ny * (vy - 1))
+    elec, nodes = [], []
+    for h in range(vy):
+        for span in range(vx - 1):
+            for k in range(nx):
+                a = [lx * (span * nx + k), ly * ny * h, depth]
+                b = [a[0] + lx, a[1], depth]
+                elec.append(populate_electrode(a, b, radius))
+                if span == 0 and k == 0:
+                    nodes.append(a)
+                nodes.append(b)
+    for g in range(vx):
+        for span in range(vy - 1):
+            for k in range(ny):
+                a = [lx * nx * g, ly * (span * ny + k), depth]
+                b = [a[0], a[1] + ly, depth]
+                elec.append(populate_electrode(a, b, radius))
+                if k < ny - 1:
+                    nodes.append(b)
+    return np.array(elec), np.array(nodes, dtype=np.float64)
+
+
+def images(elec) -> np.ndarray:
+    """Mirror segments across the soil surface z = 0 (examples/three_grids.c:206-214)."""
+    img = np.array(elec, dtype=np.float64, copy=True)
+    img[:, [2, 5, 8]] *= -1.0
+    return img
+
+
+# ---- soil and medium --------------------------------------------------------------
+
+def alipio_soil(sigma0: float, s: complex, h: float, g: float, eps_ratio: float):
+    """Frequency-dependent soil (src/auxiliary.c:60-70): (sigma, epsr)."""
+    f = complex(s) / (TWO_PI * 1j)
+    sigma = sigma0 + sigma0 * h * (f / 1e6) ** g
+    t = math.tan(PI * g / 2) / (TWO_PI * EPS0 * 1e6 ** g)
+    epsr = eps_ratio + t * sigma0 * h * f ** (g - 1.0)
+    return complex(sigma), complex(epsr)
+
+
+def kappa_of(s, sigma, epsr):
+    """Complex conductivity kappa = sigma + s epsr eps0 (examples/three_grids.c:331)."""
+    return np.asarray(sigma) + np.asarray(s) * np.asarray(epsr) * EPS0
+
+
+def medium(s, kappa, mur=1.0):
+    """gamma = sqrt(s mur mu0 kappa), ref_t = (kappa - s eps0)/(kappa + s eps0)
+    (examples/three_grids.c:326-333)."""
+    s = complex(s)
+    kappa = complex(kappa)
+    gamma = complex(np.sqrt(s * mur * MU0 * kappa))
+    ref_t = (kappa - s * EPS0) / (kappa + s * EPS0)
+    return gamma, ref_t
+
+
+def laplace_samples(nt: int, tmax: float) -> np.ndarray:
+    """s_k = c + j k 2 pi / tmax, c = ln(nt^2)/tmax (src/auxiliary.c:247-252)."""
+    ns = nt // 2 + 1
+    c = math.log(float(nt) ** 2) / tmax
+    dw = TWO_PI / tmax
+    return np.array([c + 1j * dw * k for k in range(ns)])
+
+
+# ---- GPU drop-ins (reference names and semantics) ------------------------------------
+
+def _ret(code: int) -> int:
+    if code in (E_ARG, E_CUDA, E_NOMEM, E_GEOMETRY, E_NONFINITE):
+        raise RuntimeError(f"tags_gpu error {code}: {last_error()}")
+    return code
+
+
+def calculate_impedances(zl, zt, electrodes, gamma, s, mur, kappa, max_eval=0, req_abs_error=1e-6,
+                         req_rel_error=1e-6, integration_type=INTG_DOUBLE) -> int:
+    e = _elec(electrodes)
+    m = e.shape[0]
+    _check_c128(zl, "zl", m * m)
+    _check_c128(zt, "zt", m * m)
+    C = c_complex
+    return _ret(lib().calculate_impedances(_addr(zl), _addr(zt), _addr(e), m, C.of(gamma), C.of(s), float(mur),
+                                           C.of(kappa), int(max_eval), float(req_abs_error),
+                                           float(req_rel_error), int(integration_type)))
+
+
+def impedances_images(zl, zt, electrodes, imgs, gamma, s, mur, kappa, ref_l, ref_t, max_eval=0,
+                      req_abs_error=1e-6, req_rel_error=1e-6, integration_type=INTG_DOUBLE) -> int:
+    e = _elec(electrodes)
+    im = _elec(imgs)
+    m = e.shape[0]
+    _check_c128(zl, "zl", m * m)
+    _check_c128(zt, "zt", m * m)
+    C = c_complex
+    return _ret(lib().impedances_images(_addr(zl), _addr(zt), _addr(e), _addr(im), m, C.of(gamma), C.of(s),
+                                        float(mur), C.of(kappa), C.of(ref_l), C.of(ref_t), int(max_eval),
+                                        float(req_abs_error), float(req_rel_error), int(integration_type)))
+
+
+def fill_incidence_imm(wg, electrodes, nodes) -> int:
+    e = _elec(electrodes)
+    nd = np.ascontiguousarray(nodes, dtype=np.float64)
+    N = nd.shape[0] + 2 * e.shape[0]
+    _check_c128(wg, "wg", N * N)
+    return _ret(lib().fill_incidence_imm(_addr(wg), _addr(e), e.shape[0], _addr(nd), nd.shape[0]))
+
+
+def fill_impedance_imm(wg, zl, zt, num_electrodes: int, num_nodes: int) -> int:
+    m, n = int(num_electrodes), int(num_nodes)
+    _check_c128(wg, "wg", (n + 2 * m) ** 2)
+    _check_c128(zl, "zl", m * m)
+    _check_c128(zt, "zt", m * m)
+    return _ret(lib().fill_impedance_imm(_addr(wg), _addr(zl), _addr(zt), m, n))
+
+
+def solve_immittance(wg, ie, num_electrodes: int, num_nodes: int) -> int:
+    m, n = int(num_electrodes), int(num_nodes)
+    N = n + 2 * m
+    _check_c128(wg, "wg", N * N)
+    _check_c128(ie, "ie", N)
+    return _ret(lib().solve_immittance(_addr(wg), _addr(ie), m, n))
+
+
+def laplace_trans(f, tmax: float):
+    """Returns (g, s) like the reference's laplace_trans."""
+    f = np.ascontiguousarray(f, dtype=np.float64)
+    nt = f.shape[0]
+    g = np.zeros(nt // 2 + 1, dtype=np.complex128)
+    s = np.zeros(nt // 2 + 1, dtype=np.complex128)
+    _ret(lib().laplace_trans(_addr(f), _addr(g), _addr(s), float(tmax), nt))
+    return g, s
+
+
+def inv_laplace_trans(g, s, tmax: float, nt: int, filt: int = FILTER_NONE) -> np.ndarray:
+    g = np.ascontiguousarray(g, dtype=np.complex128)
+    s = np.ascontiguousarray(s, dtype=np.complex128)
+    f = np.zeros(nt, dtype=np.float64)
+    _ret(lib().inv_laplace_trans(_addr(f), _addr(g), _addr(s), float(tmax), int(nt), int(filt)))
+    return f
+
+
+# ---- batched extension ------------------------------------------------------------------
+
+class Plan:
+    """Device-resident geometry + workspaces for many Laplace samples
+    (tags_plan_create / tags_plan_run / tags_plan_destroy)."""
+
+    def __init__(self, electrodes, imgs, nodes, precision=PLAIN_FP64, max_batch=0):
+        self.elec = _elec(electrodes)
+        self.img = None if imgs is None else _elec(imgs)
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        self.m, self.n = self.elec.shape[0], self.nodes.shape[0]
+        self.N = self.n + 2 * self.m
+        self.precision = precision
+        h = ctypes.c_void_p()
+        code = lib().tags_plan_create(ctypes.byref(h), _addr(self.elec),
+                                      None if self.img is None else _addr(self.img), self.m,
+                                      _addr(self.nodes), self.n, int(precision), int(max_batch))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_create failed ({code}): {last_error()}")
+        self.handle = h
+
+    def run(self, s, kappa, mur=1.0, ie=None, inj_node=0, want_solution=True):
+        """Solve for every sample; returns (solution ns x N, info, RunStats)."""
+        s = np.ascontiguousarray(s, dtype=np.complex128)
+        ns = s.shape[0]
+        kappa = np.ascontiguousarray(np.broadcast_to(kappa, (ns,)), dtype=np.complex128)
+        iep = None
+        if ie is not None:
+            ie = np.ascontiguousarray(ie, dtype=np.complex128).reshape(ns, self.n)
+            iep = _addr(ie)
+        sol = np.zeros((ns, self.N), dtype=np.complex128) if want_solution else None
+        info = np.zeros(ns, dtype=np.int32)
+        st = RunStats()
+        code = lib().tags_plan_run(self.handle, _addr(s), _addr(kappa), float(mur), ns, iep, int(inj_node),
+                                   None if sol is None else _addr(sol), _addr(info), 0, ctypes.byref(st))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_run failed ({code}): {last_error()}")
+        return sol, info, st
+
+    def run_device(self, s_ptr, kappa_ptr, ns, mur, ie_ptr, inj_node, sol_ptr, info_ptr):
+        """Same as run() on device pointers (integers); inputs stay in HBM."""
+        st = RunStats()
+        code = lib().tags_plan_run(self.handle, s_ptr, kappa_ptr, float(mur), int(ns), ie_ptr, int(inj_node),
+                                   sol_ptr, info_ptr, RUN_DEVICE_PTRS, ctypes.byref(st))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_run failed ({code}): {last_error()}")
+        return st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().tags_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, precision=PLAIN_FP64,
+              max_batch=0):
+    """Solutions [U; I_L; I_T] for every Laplace sample (one plan, one run)."""
+    plan = Plan(electrodes, imgs, nodes, precision, max_batch)
+    try:
+        return plan.run(s, kappa, mur, ie, inj_node)
+    finally:
+        plan.close()

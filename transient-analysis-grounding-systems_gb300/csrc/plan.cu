@@ -1,0 +1,343 @@
+// Batched plan API (include/tags_gpu.h, part 2): geometry, incidence and
+// workspaces stay on the device; every pass handles `batch` Laplace samples:
+//   plain FP64: W_G assembled in place (incidence + fused direct/image fill,
+//               both triangles), LU with partial pivoting, triangular solves;
+//   mixed:      see mixed.cu.
+// The per-sample medium terms follow examples/three_grids.c:326-333
+// (gamma = sqrt(s mur mu0 kappa), ref_t = (kappa - s eps0)/(kappa + s eps0),
+// ref_l = 1) and the right-hand side is [I_E; 0; 0] (src/linalg.h:61-68).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "tags_common.cuh"
+#include "tags_internal.h"
+#include "../../include/tags_gpu.h"
+#include "plan.h"
+
+namespace {
+
+// principal square root of a complex number
+TAGS_D double2 csqrt_d(double2 z) {
+    double a = hypot(z.x, z.y);
+    if (a == 0.0) return make_double2(0.0, 0.0);
+    double re = sqrt(0.5 * (a + fabs(z.x)));
+    double im = 0.5 * z.y / re;
+    if (z.x >= 0.0) return make_double2(re, im);
+    return make_double2(fabs(im), z.y >= 0.0 ? re : -re);
+}
+
+__global__ void k_coef(const double2* __restrict__ s, const double2* __restrict__ kappa, double mur, int nb,
+                       SampleCoef* __restrict__ coef) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nb) return;
+    double2 sk = s[k], kp = kappa[k];
+    double2 smu = cscale(sk, mur * TAGS_MU0);
+    double2 gamma = csqrt_d(cmul(smu, kp));
+    double2 se = cscale(sk, TAGS_EPS0);
+    double2 ref_t = cdiv(csub(kp, se), cadd(kp, se));
+    double2 cL = cscale(smu, 1.0 / TAGS_FOUR_PI);
+    double2 cT = cdiv(make_double2(1.0, 0.0), cscale(kp, TAGS_FOUR_PI));
+    SampleCoef c;
+    c.gamma = gamma;
+    c.cL = cL;
+    c.cT = cT;
+    c.cLi = cL;                 // ref_l = 1
+    c.cTi = cmul(ref_t, cT);
+    coef[k] = c;
+}
+
+// X (batch x N, sample-major): [ie; 0; 0] or a unit current at inj_node.
+__global__ void k_rhs(double2* __restrict__ X, int N, int n, const double2* __restrict__ ie, int inj_node) {
+    int r = blockIdx.x * blockDim.x + threadIdx.x;
+    int b = blockIdx.y;
+    if (r >= N) return;
+    double2 v = make_double2(0.0, 0.0);
+    if (r < n) {
+        if (ie) v = ie[(long long)b * n + r];
+        else if (r == inj_node) v = make_double2(1.0, 0.0);
+    }
+    X[(long long)b * N + r] = v;
+}
+
+}  // namespace
+
+int tags_plan_coef(tags_plan_s* p, const double2* d_s, const double2* d_kappa, double mur, int nb, cudaStream_t st) {
+    k_coef<<<(nb + 127) / 128, 128, 0, st>>>(d_s, d_kappa, mur, nb, p->d_coef);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+int tags_plan_rhs(tags_plan_s* p, double2* d_X, const double2* d_ie, int inj_node, int nb, cudaStream_t st) {
+    k_rhs<<<dim3((p->N + 255) / 256, nb), 256, 0, st>>>(d_X, p->N, p->n, d_ie, inj_node);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+static int build_incidence(tags_plan_s* p, cudaStream_t st) {
+    const int m = p->m, n = p->n;
+    std::vector<signed char> cond((size_t)n * m);
+    int err = tags_incidence_codes(p->d_elec, m, reinterpret_cast<const double*>(p->d_W), n, p->d_cond, st);
+    if (err) return err;
+    TAGS_CUDA_OK(cudaMemcpyAsync(cond.data(), p->d_cond, cond.size(), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    std::vector<int> nptr(n + 1, 0), sptr(m + 1, 0), nseg, snode;
+    std::vector<signed char> na, sa;
+    long long suma = 0, nb = 0;
+    for (int nd = 0; nd < n; ++nd) {
+        bool any = false;
+        for (int e = 0; e < m; ++e) {
+            int c = cond[(size_t)nd * m + e];
+            if (!c) continue;
+            any = true;
+            nseg.push_back(e);
+            na.push_back(c == 1 ? 1 : -1);
+            suma += c == 1 ? 1 : -1;
+            ++nb;
+            sptr[e + 1]++;
+        }
+        nptr[nd + 1] = (int)nseg.size();
+        if (!any) {
+            char msg[96];
+            snprintf(msg, sizeof(msg), "No electrode is connected to node[%i]", nd);
+            return tags_fail(TAGS_E_ARG, msg);
+        }
+    }
+    if (suma != 0 || nb != 2LL * m) return tags_fail(TAGS_E_ARG, "incidence checksum failed (sum(A) != 0 or sum(B) != m)");
+    for (int e = 0; e < m; ++e) sptr[e + 1] += sptr[e];
+    snode.resize(nseg.size());
+    sa.resize(nseg.size());
+    std::vector<int> fillp(sptr.begin(), sptr.end() - 1);
+    for (int nd = 0; nd < n; ++nd)
+        for (int q = nptr[nd]; q < nptr[nd + 1]; ++q) {
+            int e = nseg[q];
+            snode[fillp[e]] = nd;
+            sa[fillp[e]] = na[q];
+            fillp[e]++;
+        }
+    Incidence& I = p->inc;
+    I.nnz = (int)nseg.size();
+    size_t nnz = std::max<size_t>(1, nseg.size());
+    TAGS_CUDA_OK(cudaMalloc(&I.node_ptr, sizeof(int) * (n + 1)));
+    TAGS_CUDA_OK(cudaMalloc(&I.node_seg, sizeof(int) * nnz));
+    TAGS_CUDA_OK(cudaMalloc(&I.node_a, nnz));
+    TAGS_CUDA_OK(cudaMalloc(&I.seg_ptr, sizeof(int) * (m + 1)));
+    TAGS_CUDA_OK(cudaMalloc(&I.seg_node, sizeof(int) * nnz));
+    TAGS_CUDA_OK(cudaMalloc(&I.seg_a, nnz));
+    TAGS_CUDA_OK(cudaMemcpy(I.node_ptr, nptr.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    TAGS_CUDA_OK(cudaMemcpy(I.seg_ptr, sptr.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
+    if (!nseg.empty()) {
+        TAGS_CUDA_OK(cudaMemcpy(I.node_seg, nseg.data(), sizeof(int) * nseg.size(), cudaMemcpyHostToDevice));
+        TAGS_CUDA_OK(cudaMemcpy(I.node_a, na.data(), na.size(), cudaMemcpyHostToDevice));
+        TAGS_CUDA_OK(cudaMemcpy(I.seg_node, snode.data(), sizeof(int) * snode.size(), cudaMemcpyHostToDevice));
+        TAGS_CUDA_OK(cudaMemcpy(I.seg_a, sa.data(), sa.size(), cudaMemcpyHostToDevice));
+    }
+    return 0;
+}
+
+static void plan_free(tags_plan_s* p) {
+    if (!p) return;
+    cudaSetDevice(p->device);
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    void* ptrs[] = {p->d_elec, p->d_img, p->d_cond, p->d_coef, p->d_status, p->d_info, p->d_ipiv, p->d_W, p->d_x,
+                    p->inc.node_ptr, p->inc.node_seg, p->inc.node_a, p->inc.seg_ptr, p->inc.seg_node, p->inc.seg_a};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    tags_mixed_free(p);
+    if (p->ev0) cudaEventDestroy(p->ev0);
+    if (p->ev1) cudaEventDestroy(p->ev1);
+    if (p->stream) cudaStreamDestroy(p->stream);
+    delete p;
+}
+
+extern "C" int tags_plan_create(tags_plan* out, const Electrode* electrodes, const Electrode* images,
+                                size_t num_electrodes, const double* nodes, size_t num_nodes, int precision,
+                                size_t max_batch) {
+    if (!out || !electrodes || !nodes || num_electrodes == 0 || num_nodes == 0)
+        return tags_fail(TAGS_E_ARG, "tags_plan_create: invalid argument");
+    if (precision != TAGS_PLAIN_FP64 && precision != TAGS_MIXED)
+        return tags_fail(TAGS_E_ARG, "tags_plan_create: unknown precision");
+    const long long N = (long long)num_nodes + 2LL * (long long)num_electrodes;
+    if (N > 60000) return tags_fail(TAGS_E_ARG, "tags_plan_create: system larger than 60000 unknowns");
+    *out = nullptr;
+    DeviceCtx* ctx = tags_ctx();
+    if (!ctx) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
+    tags_plan_s* p = new tags_plan_s();
+    p->device = ctx->device;
+    p->precision = precision;
+    p->m = (int)num_electrodes;
+    p->n = (int)num_nodes;
+    p->N = (int)N;
+    p->has_images = images != nullptr;
+    int err = 0;
+#define PLAN_CHECK(expr)                      \
+    do {                                      \
+        cudaError_t _e = (expr);              \
+        if (_e != cudaSuccess) {              \
+            err = tags_fail_cuda(_e, #expr, __FILE__, __LINE__); \
+            plan_free(p);                     \
+            return err;                       \
+        }                                     \
+    } while (0)
+    PLAN_CHECK(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    PLAN_CHECK(cudaEventCreate(&p->ev0));
+    PLAN_CHECK(cudaEventCreate(&p->ev1));
+    const size_t eb = sizeof(Electrode) * num_electrodes;
+    PLAN_CHECK(cudaMalloc(&p->d_elec, eb));
+    PLAN_CHECK(cudaMalloc(&p->d_img, eb));
+    PLAN_CHECK(cudaMemcpy(p->d_elec, electrodes, eb, cudaMemcpyHostToDevice));
+    PLAN_CHECK(cudaMemcpy(p->d_img, images ? (const void*)images : (const void*)electrodes, eb, cudaMemcpyHostToDevice));
+    PLAN_CHECK(cudaMalloc(&p->d_cond, (size_t)p->n * p->m));
+    PLAN_CHECK(cudaMalloc(&p->d_status, sizeof(int) * 4));
+    // nodes go through a temporary buffer (d_W is reused as staging here)
+    PLAN_CHECK(cudaMalloc(&p->d_W, sizeof(double) * 3 * num_nodes));
+    PLAN_CHECK(cudaMemcpy(p->d_W, nodes, sizeof(double) * 3 * num_nodes, cudaMemcpyHostToDevice));
+    err = build_incidence(p, p->stream);
+    cudaFree(p->d_W);
+    p->d_W = nullptr;
+    if (err) { plan_free(p); return err; }
+    // batch size from free device memory
+    size_t freeb = 0, totb = 0;
+    PLAN_CHECK(cudaMemGetInfo(&freeb, &totb));
+    const double NN = (double)N * (double)N;
+    double per = precision == TAGS_PLAIN_FP64
+                     ? 16.0 * NN + 40.0 * N
+                     : 8.0 * NN + 32.0 * (double)p->m * p->m + 80.0 * N;
+    long long cap = (long long)(0.45 * (double)freeb / per);
+    long long b = max_batch ? (long long)max_batch : std::min<long long>(cap, 64);
+    if (b > cap) b = cap;
+    if (b < 1) { plan_free(p); return tags_fail(TAGS_E_NOMEM, "not enough device memory for one sample"); }
+    p->batch = (int)b;
+    PLAN_CHECK(cudaMalloc(&p->d_coef, sizeof(SampleCoef) * b));
+    PLAN_CHECK(cudaMalloc(&p->d_info, sizeof(int) * b));
+    PLAN_CHECK(cudaMalloc(&p->d_x, sizeof(double2) * N * b));
+    if (precision == TAGS_PLAIN_FP64) {
+        PLAN_CHECK(cudaMalloc(&p->d_ipiv, sizeof(int) * N * b));
+        PLAN_CHECK(cudaMalloc(&p->d_W, sizeof(double2) * (size_t)NN * b));
+    } else {
+        err = tags_mixed_alloc(p);
+        if (err) { plan_free(p); return err; }
+    }
+#undef PLAN_CHECK
+    *out = p;
+    return 0;
+}
+
+extern "C" int tags_plan_destroy(tags_plan plan) {
+    plan_free(plan);
+    return 0;
+}
+
+// Plain FP64 pass over nb samples whose coefficients and right-hand sides are
+// already in p->d_coef and p->d_x.
+int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st) {
+    const long long N = p->N, NN = N * N;
+    TAGS_CUDA_OK(cudaMemsetAsync(p->d_W, 0, sizeof(double2) * NN * nb, st));
+    int err = tags_wg_incidence(p->d_W, N, NN, nb, p->d_cond, p->n, p->m, st);
+    if (err) return err;
+    FillOut out{};
+    out.zl = p->d_W;
+    out.zt = p->d_W;
+    out.ld = N;
+    out.batch_stride = NN;
+    out.row0_l = out.col0_l = p->n;
+    out.row0_t = out.col0_t = p->n + p->m;
+    out.sign = -1.0;
+    out.mirror = 1;
+    out.accumulate = 0;
+    err = tags_launch_fill_fp64(p->d_elec, p->d_img, p->m, p->d_coef, nb, out,
+                                p->has_images ? TAGS_FILL_BOTH : TAGS_FILL_DIRECT, TAGS_INTG_DOUBLE, 1, p->d_status, st);
+    if (err) return err;
+    err = tags_lu_z(p->d_W, (int)N, N, NN, nb, 1, p->d_ipiv, p->d_info, st);
+    if (err) return err;
+    return tags_lu_solve_z(p->d_W, (int)N, N, NN, nb, p->d_ipiv, p->d_x, 1, N, N, st);
+}
+
+extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
+                             const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags,
+                             tags_run_stats* stats) {
+    tags_plan_s* p = plan;
+    if (!p || !s || !kappa) return tags_fail(TAGS_E_ARG, "tags_plan_run: invalid argument");
+    if (!ie && inj_node >= (size_t)p->n) return tags_fail(TAGS_E_ARG, "tags_plan_run: inj_node out of range");
+    if (ns == 0) return 0;
+    TAGS_CUDA_OK(cudaSetDevice(p->device));
+    cudaStream_t st = p->stream;
+    const bool dev = (flags & TAGS_RUN_DEVICE_PTRS) != 0;
+    const long long N = p->N;
+    DeviceCtx* ctx = tags_ctx();
+    if (!ctx) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
+    // staging for host inputs
+    double2* d_in = nullptr;
+    if (!dev) {
+        size_t need = sizeof(double2) * (2 * (size_t)p->batch + (ie ? (size_t)p->batch * p->n : 0));
+        d_in = (double2*)ctx->scratch(9, need);
+        if (!d_in) return tags_fail(TAGS_E_NOMEM, "device allocation failed");
+    }
+    std::vector<int> h_info;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    TAGS_CUDA_OK(cudaMemsetAsync(p->d_status, 0, sizeof(int) * 4, st));
+    TAGS_CUDA_OK(cudaEventRecord(p->ev0, st));
+    for (size_t k0 = 0; k0 < ns; k0 += p->batch) {
+        const int nb = (int)std::min<size_t>(p->batch, ns - k0);
+        const double2 *ds, *dk, *die = nullptr;
+        if (dev) {
+            ds = reinterpret_cast<const double2*>(s) + k0;
+            dk = reinterpret_cast<const double2*>(kappa) + k0;
+            if (ie) die = reinterpret_cast<const double2*>(ie) + k0 * p->n;
+        } else {
+            TAGS_CUDA_OK(cudaMemcpyAsync(d_in, s + k0, sizeof(double2) * nb, cudaMemcpyHostToDevice, st));
+            TAGS_CUDA_OK(cudaMemcpyAsync(d_in + p->batch, kappa + k0, sizeof(double2) * nb, cudaMemcpyHostToDevice, st));
+            ds = d_in;
+            dk = d_in + p->batch;
+            if (ie) {
+                TAGS_CUDA_OK(cudaMemcpyAsync(d_in + 2 * p->batch, ie + k0 * p->n, sizeof(double2) * nb * p->n,
+                                             cudaMemcpyHostToDevice, st));
+                die = d_in + 2 * p->batch;
+            }
+        }
+        int err = tags_plan_coef(p, ds, dk, mur, nb, st);
+        if (!err) err = tags_plan_rhs(p, p->d_x, die, (int)inj_node, nb, st);
+        if (err) return err;
+        if (p->precision == TAGS_PLAIN_FP64) {
+            err = tags_plan_run_plain(p, ds, nb, st);
+            if (err) return err;
+        } else {
+            std::vector<int> iters(nb), conv(nb);
+            std::vector<double> berr(nb);
+            err = tags_mixed_solve_batch(p, nb, nullptr, iters.data(), berr.data(), conv.data(), st);
+            if (err) return err;
+            if (stats) {
+                for (int q = 0; q < nb; ++q) {
+                    stats->max_iterations = std::max(stats->max_iterations, iters[q]);
+                    stats->max_backward_error = std::max(stats->max_backward_error, berr[q]);
+                    if (!conv[q]) stats->fallbacks++;
+                }
+            }
+        }
+        if (sol) {
+            TAGS_CUDA_OK(cudaMemcpyAsync(sol + k0 * N, p->d_x, sizeof(double2) * N * nb,
+                                         dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        }
+        if (info) {
+            TAGS_CUDA_OK(cudaMemcpyAsync(info + k0, p->d_info, sizeof(int) * nb,
+                                         dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        }
+        if (!dev) TAGS_CUDA_OK(cudaStreamSynchronize(st));   // staging buffer reused by the next pass
+    }
+    TAGS_CUDA_OK(cudaEventRecord(p->ev1, st));
+    int status = 0;
+    TAGS_CUDA_OK(cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    if (stats) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+        stats->seconds = ms * 1e-3;
+    }
+    if (status & TAGS_ST_DEGENERATE_PAIR)
+        return tags_fail(TAGS_E_GEOMETRY, "coincident or overlapping segments: the pair integral diverges");
+    if (status & TAGS_ST_NONFINITE) return tags_fail(TAGS_E_NONFINITE, "non-finite value in the impedance fill");
+    return 0;
+}

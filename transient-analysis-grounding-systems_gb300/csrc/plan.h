@@ -1,0 +1,70 @@
+// Device context and batched-plan state shared by the C-ABI translation units.
+#pragma once
+
+#include <complex>
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "tags_internal.h"
+
+struct DeviceCtx {
+    bool ready = false;
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    int* status = nullptr;             // device status word(s)
+    void* scratch_ptr[16] = {};
+    size_t scratch_bytes[16] = {};
+    void* scratch(int slot, size_t bytes);
+};
+
+DeviceCtx* tags_ctx();
+int tags_fail(int code, const char* msg);
+void tags_msg(const char* msg);
+SampleCoef tags_sample_coef(std::complex<double> gamma, std::complex<double> s, double mur,
+                            std::complex<double> kappa, std::complex<double> ref_l, std::complex<double> ref_t);
+
+// Sparse incidence (from the exact node-matching codes): per node the
+// incident segments (CSR by node) and per segment its nodes (CSR by segment),
+// with the A value (+1/-1); B is 0.5 on the same pattern.
+struct Incidence {
+    int* node_ptr = nullptr;   // n + 1
+    int* node_seg = nullptr;   // nnz
+    signed char* node_a = nullptr;
+    int* seg_ptr = nullptr;    // m + 1
+    int* seg_node = nullptr;   // nnz
+    signed char* seg_a = nullptr;
+    int nnz = 0;
+};
+
+struct tags_plan_s {
+    int device = -1;
+    int precision = 0;
+    int m = 0, n = 0, N = 0;
+    int has_images = 0;
+    int batch = 0;               // samples per device pass
+    cudaStream_t stream = nullptr;
+    double* d_elec = nullptr;    // m x 11
+    double* d_img = nullptr;     // m x 11
+    signed char* d_cond = nullptr;  // n x m incidence codes
+    Incidence inc;
+    SampleCoef* d_coef = nullptr;   // batch
+    int* d_status = nullptr;        // 4 words
+    int* d_info = nullptr;          // batch
+    int* d_ipiv = nullptr;          // batch x N
+    double2* d_W = nullptr;         // plain: batch x N x N
+    double2* d_x = nullptr;         // batch x N (solution, FP64)
+    // mixed form
+    double2* d_Z = nullptr;         // batch x 2 x m x m FP64 (ZL, ZT; full symmetric)
+    float2* d_A = nullptr;          // batch x N x N FP32 working matrix (reordered, scaled)
+    double* d_scale = nullptr;      // batch x N symmetric scaling (reordered index)
+    double2* d_r = nullptr;         // batch x N residual (FP64)
+    float2* d_rf = nullptr;         // batch x N correction right-hand side (FP32)
+    double* d_norms = nullptr;      // batch x 4 reductions
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+int tags_plan_run_plain(tags_plan_s* p, const double2* d_s_unused, int nb, cudaStream_t st);
+int tags_mixed_alloc(tags_plan_s* p);
+int tags_mixed_free(tags_plan_s* p);
+int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2* d_b, int* h_iters, double* h_berr,
+                           int* h_conv, cudaStream_t st);

@@ -1,0 +1,72 @@
+// Internal interfaces between the CUDA translation units of the GB300 HEM
+// library (not part of the public C-ABI in include/tags_gpu.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+// Integration types, numbered as the reference's Integration_type
+// (src/electrode.h:17-31).
+enum { TAGS_INTG_NONE = 1, TAGS_INTG_DOUBLE = 2, TAGS_INTG_SINGLE = 3, TAGS_INTG_MHEM = 4 };
+
+// Which couplings a fill launch computes.
+enum { TAGS_FILL_DIRECT = 1, TAGS_FILL_IMAGE = 2, TAGS_FILL_BOTH = 3 };
+
+// Per-sample coefficients, computed on the host from s, kappa, mur:
+//   gamma = sqrt(s mur mu0 kappa), cL = s mur mu0 / 4pi, cT = 1 / (4 pi kappa),
+//   cLi = ref_l cL, cTi = ref_t cT (examples/three_grids.c:326-333,
+//   src/electrode.c:313-319, :391-399).
+struct SampleCoef {
+    double2 gamma;
+    double2 cL, cT;
+    double2 cLi, cTi;
+};
+
+// Where the lower triangle (row k >= col i) of ZL/ZT lands: element (k, i) of
+// ZL goes to zl[(row0_l + k) + ld * (col0_l + i)] (+ batch_stride per sample),
+// multiplied by `sign`; with `mirror` also to the transposed position.
+struct FillOut {
+    double2* zl;
+    double2* zt;
+    long long ld;
+    long long batch_stride;
+    int row0_l, col0_l, row0_t, col0_t;
+    double sign;
+    int mirror;
+    int accumulate;
+};
+
+int tags_fill_tables_init();
+int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, const SampleCoef* d_coef,
+                          int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
+                          cudaStream_t st);
+
+// Bookkeeping of kernel launches (reported by tags_gpu_launch_count).
+void tags_note_launch(long long n = 1);
+
+// assemble.cu
+int tags_incidence_codes(const double* d_elec, int m, const double* d_nodes, int n, signed char* d_cond,
+                         cudaStream_t st);
+int tags_wg_incidence(double2* d_W, long long ld, long long stride, int batch, const signed char* d_cond, int n,
+                      int m, cudaStream_t st);
+int tags_wg_impedance(double2* d_W, long long ld, const double2* d_zl, const double2* d_zt, int m, int n,
+                      cudaStream_t st);
+int tags_symmetrize_lower(double2* d_W, int N, long long ld, long long stride, int batch, cudaStream_t st);
+
+// lu.cu
+int tags_lu_z(double2* A, int n, long long ld, long long stride, int batch, int pivot, int* ipiv, int* info,
+              cudaStream_t st);
+int tags_lu_c(float2* A, int n, long long ld, long long stride, int batch, int pivot, int* ipiv, int* info,
+              cudaStream_t st);
+int tags_lu_solve_z(const double2* A, int n, long long ld, long long stride, int batch, const int* ipiv, double2* X,
+                    int nrhs, long long ldx, long long xstride, cudaStream_t st);
+int tags_lu_solve_c(const float2* A, int n, long long ld, long long stride, int batch, const int* ipiv, float2* X,
+                    int nrhs, long long ldx, long long xstride, cudaStream_t st);
+
+// inlt.cu
+int tags_twiddles(double2* d_tw, long long nt, cudaStream_t st);
+int tags_launch_inlt(const double2* d_g, long long gstride, long long ns, const double2* d_s, const double2* d_tw,
+                     long long nt, double tmax, int filter, double* d_f, long long fstride, int nseries,
+                     cudaStream_t st);
+int tags_launch_nlt(const double* d_f, long long fstride, long long nt, const double2* d_tw, double tmax,
+                    double2* d_g, long long gstride, int nseries, cudaStream_t st);
