@@ -409,6 +409,8 @@ class Plan:
 def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, precision=PLAIN_FP64,
               max_batch=0):
     """Solutions [U; I_L; I_T] for every Laplace sample (one plan, one run)."""
+    if not max_batch:
+        max_batch = min(len(np.atleast_1d(s)), 64)
     plan = Plan(electrodes, imgs, nodes, precision, max_batch)
     try:
         return plan.run(s, kappa, mur, ie, inj_node)

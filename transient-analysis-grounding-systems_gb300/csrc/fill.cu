@@ -348,6 +348,224 @@ __global__ void __launch_bounds__(128) k_fill_fp64(const double* __restrict__ el
     }
 }
 
+// ---- mixed form: plan-time pair classification + FP32 regular-pair fill --------
+
+// Pair code (geometry only, computed once per plan):
+//   bit 15      endpoints touch: Duffy rule in FP64
+//   bit 14      coincident/overlapping segments (divergent integral)
+//   bits 6..11  base Gauss-Legendre order of a panel pair
+//   bits 0..5   panels per segment P (1..32)
+constexpr uint16_t PC_TOUCH = 0x8000, PC_DEGEN = 0x4000;
+
+TAGS_D uint16_t classify_pair(const Seg& S, const Seg& R) {
+    const double lmax = fmax(S.len, R.len);
+    int ia, ib;
+    if (touching(R, S, 1e-9 * lmax, ia, ib)) {
+        const double* ro = ia == 0 ? R.b : R.a;
+        const double* so = ib == 0 ? S.b : S.a;
+        double od = fmax(fabs(ro[0] - so[0]), fmax(fabs(ro[1] - so[1]), fabs(ro[2] - so[2])));
+        return od <= 1e-9 * lmax ? PC_DEGEN : PC_TOUCH;
+    }
+    double dmin = seg_seg_dist(R.a, R.b, S.a, S.b);
+    if (dmin <= 1e-12 * lmax) return PC_DEGEN;
+    double ratio = dmin / lmax;
+    int P = ratio >= 2.0 ? 1 : (int)fmin(32.0, ceil(2.0 / ratio));
+    double rp = ratio * P;
+    int qg = rp >= 8.0 ? 3 : rp >= 4.0 ? 4 : 5;
+    return (uint16_t)(P | (qg << 6));
+}
+
+__global__ void k_pair_plan(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
+                            uint16_t* __restrict__ codes) {
+    const long long npairs = (long long)m * (m + 1) / 2;
+    long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
+    int i, k;
+    pair_index(p, m, i, k);
+    Seg S, R;
+    ld_seg(elec + 11LL * i, S);
+    uint16_t cd = 0, ci = 0;
+    if (k != i) {
+        ld_seg(elec + 11LL * k, R);
+        cd = classify_pair(S, R);
+    }
+    if (has_img) {
+        ld_seg(img + 11LL * k, R);
+        ci = classify_pair(S, R);
+    }
+    codes[2 * p] = cd;
+    codes[2 * p + 1] = ci;
+}
+
+// e^{-gamma r} for r in FP64, result FP32: the exponent and the phase are
+// reduced in FP64 (2^-t with t split into integer and fraction, phase modulo
+// 2 pi), the remaining small arguments are evaluated in FP32.
+TAGS_D float2 anchor_f32(double2 gamma, double r) {
+    const double LOG2E = 1.4426950408889634;
+    double t = gamma.x * r * LOG2E;                  // e^{-Re(gamma) r} = 2^{-t}
+    double ti = floor(t);
+    float mag = ldexpf(exp2f(-(float)(t - ti)), -(int)fmin(ti, 1000.0));
+    double ph = gamma.y * r;                         // e^{-j Im(gamma) r}
+    ph -= TAGS_TWO_PI * rint(ph * (1.0 / TAGS_TWO_PI));
+    float sn, cs;
+    sincosf((float)ph, &sn, &cs);
+    return make_float2(mag * cs, -mag * sn);
+}
+
+constexpr int MIX_SG = 8;   // samples per thread
+
+// Mixed-form fill: one thread per (pair, group of up to MIX_SG samples).
+// Regular pairs in FP32 (panel anchors in FP64), touching pairs in FP64.
+// Writes ZL (at zl) and ZT (at zt), lower + mirrored upper, FP64 storage.
+__global__ void __launch_bounds__(128, 1) k_fill_mixed(const double* __restrict__ elec, const double* __restrict__ img,
+                                                    int m, const uint16_t* __restrict__ codes,
+                                                    const SampleCoef* __restrict__ coef, int nsamp, FillOut out,
+                                                    int has_img, int* status) {
+    __shared__ double sx[GL_TOTAL], sw[GL_TOTAL];
+    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) { sx[t] = g_glx[t]; sw[t] = g_glw[t]; }
+    __syncthreads();
+    GLTab gl{sx, sw};
+    const long long npairs = (long long)m * (m + 1) / 2;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int s0 = blockIdx.y * MIX_SG;
+    if (p >= npairs || s0 >= nsamp) return;
+    const int ns = min(MIX_SG, nsamp - s0);
+    int i, k;
+    pair_index(p, m, i, k);
+    Seg S;
+    ld_seg(elec + 11LL * i, S);
+    const double ds[3] = {S.b[0] - S.a[0], S.b[1] - S.a[1], S.b[2] - S.a[2]};
+    double2 zl[MIX_SG], zt[MIX_SG];
+    double2 gam[MIX_SG];
+    double gmax = 0.0;
+#pragma unroll
+    for (int q = 0; q < MIX_SG; ++q) {
+        zl[q] = zt[q] = cz(0.0, 0.0);
+        gam[q] = q < ns ? coef[s0 + q].gamma : cz(0.0, 0.0);
+        gmax = fmax(gmax, sqrt(cabs2(gam[q])));
+    }
+    for (int kind = 0; kind < 2; ++kind) {
+        if (kind == 1 && !has_img) break;
+        Seg R;
+        if (kind == 0 && k == i) {
+            double intg = self_integral_d(S);
+#pragma unroll
+            for (int q = 0; q < MIX_SG; ++q) {
+                if (q >= ns) break;
+                SampleCoef c = coef[s0 + q];
+                zl[q] = cscale(c.cL, intg);
+                zt[q] = cscale(c.cT, intg / (S.len * S.len));
+            }
+            continue;
+        }
+        ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
+        const uint16_t code = codes[2 * p + kind];
+        double cost = 0.0;
+        for (int d = 0; d < 3; ++d) cost += ds[d] * (R.b[d] - R.a[d]);
+        cost = fabs(cost);
+        const double lsr = S.len * R.len;
+        double2 J[MIX_SG];
+        if (code & PC_DEGEN) {
+            raise_status(status, TAGS_ST_DEGENERATE_PAIR);
+#pragma unroll
+            for (int q = 0; q < MIX_SG; ++q) J[q] = cz(nan(""), nan(""));
+        } else if (code & PC_TOUCH) {
+            int ia, ib;
+            touching(R, S, 1e-9 * fmax(S.len, R.len), ia, ib);
+#pragma unroll
+            for (int q = 0; q < MIX_SG; ++q) {
+                int qt = min(QMAX, 10 + (int)ceil(sqrt(cabs2(gam[q])) * fmax(S.len, R.len)));
+                J[q] = q < ns ? j_touch(R, S, ia, ib, gam[q], false, qt, gl) : cz(0.0, 0.0);
+            }
+        } else {
+            const int P = code & 63;
+            const int qg = (code >> 6) & 63;
+            const int qq = min(24, qg + (int)ceil(gmax * fmax(S.len, R.len) / P));
+            const double* x = gl.x + gl_off(qq);
+            const double* w = gl.w + gl_off(qq);
+            const double h = 1.0 / (double)P;
+            const double dr[3] = {R.b[0] - R.a[0], R.b[1] - R.a[1], R.b[2] - R.a[2]};
+            const float3 hr = make_float3((float)(dr[0] * h), (float)(dr[1] * h), (float)(dr[2] * h));
+            const float3 hs = make_float3((float)(ds[0] * h), (float)(ds[1] * h), (float)(ds[2] * h));
+            float2 acc[MIX_SG];
+            float gre[MIX_SG], gim[MIX_SG];
+#pragma unroll
+            for (int q = 0; q < MIX_SG; ++q) {
+                acc[q] = make_float2(0.f, 0.f);
+                gre[q] = (float)gam[q].x;
+                gim[q] = (float)gam[q].y;
+            }
+            for (int pi = 0; pi < P; ++pi) {
+                for (int pj = 0; pj < P; ++pj) {
+                    double cr[3], dd[3];
+                    for (int d = 0; d < 3; ++d) {
+                        cr[d] = R.a[d] + (pi + 0.5) * h * dr[d];
+                        dd[d] = cr[d] - (S.a[d] + (pj + 0.5) * h * ds[d]);
+                    }
+                    const double rc = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+                    const float3 D = make_float3((float)dd[0], (float)dd[1], (float)dd[2]);
+                    const float rcf = (float)rc;
+                    float2 psum[MIX_SG];
+#pragma unroll
+                    for (int q = 0; q < MIX_SG; ++q) psum[q] = make_float2(0.f, 0.f);
+                    for (int qi = 0; qi < qq; ++qi) {
+                        const float a = (float)(x[qi] - 0.5);
+                        const float wi = (float)w[qi];
+                        for (int qj = 0; qj < qq; ++qj) {
+                            const float b = (float)(x[qj] - 0.5);
+                            // u = a hr - b hs: offset of the point pair from the panel centres
+                            float ux = a * hr.x - b * hs.x, uy = a * hr.y - b * hs.y, uz = a * hr.z - b * hs.z;
+                            float e = 2.f * (D.x * ux + D.y * uy + D.z * uz) + (ux * ux + uy * uy + uz * uz);
+                            float rp = sqrtf(rcf * rcf + e);
+                            float del = e / (rp + rcf);                 // r_p - r_c without cancellation
+                            float wt = wi * (float)w[qj] / rp;
+#pragma unroll
+                            for (int q = 0; q < MIX_SG; ++q) {
+                                float mg = expf(-gre[q] * del);
+                                float sn, cs;
+                                sincosf(gim[q] * del, &sn, &cs);
+                                psum[q].x = fmaf(wt * mg, cs, psum[q].x);
+                                psum[q].y = fmaf(-wt * mg, sn, psum[q].y);
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < MIX_SG; ++q) {
+                        if (q < ns) acc[q] = ffmac(anchor_f32(gam[q], rc), psum[q], acc[q]);
+                    }
+                }
+            }
+            const double h2 = h * h;
+#pragma unroll
+            for (int q = 0; q < MIX_SG; ++q) J[q] = cz((double)acc[q].x * h2, (double)acc[q].y * h2);
+        }
+#pragma unroll
+        for (int q = 0; q < MIX_SG; ++q) {
+            if (q >= ns) break;
+            SampleCoef c = coef[s0 + q];
+            double2 intg = cscale(J[q], lsr);
+            double2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
+            zt[q] = cadd(zt[q], cmul(cscale(cT, 1.0 / lsr), intg));
+            bool keep = kind == 0 ? !(cost < TAGS_DBL_EPSILON) : (cost > TAGS_DBL_EPSILON);
+            if (keep) zl[q] = cadd(zl[q], cscale(cmul(cL, intg), cost / lsr));
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < MIX_SG; ++q) {
+        if (q >= ns) break;
+        const int smp = s0 + q;
+        const long long bs = out.batch_stride * smp;
+        double2 l = cscale(zl[q], out.sign), t = cscale(zt[q], out.sign);
+        if (!isfinite(l.x + l.y + t.x + t.y)) raise_status(status, TAGS_ST_NONFINITE);
+        out.zl[bs + (long long)(out.row0_l + k) + out.ld * (out.col0_l + i)] = l;
+        out.zt[bs + (long long)(out.row0_t + k) + out.ld * (out.col0_t + i)] = t;
+        if (out.mirror && k != i) {
+            out.zl[bs + (long long)(out.row0_l + i) + out.ld * (out.col0_l + k)] = l;
+            out.zt[bs + (long long)(out.row0_t + i) + out.ld * (out.col0_t + k)] = t;
+        }
+    }
+}
+
 // Gauss-Legendre nodes/weights by Newton iteration on P_q (host side).
 void gauss_legendre(int q, double* x, double* w) {
     for (int i = 0; i < q; ++i) {
@@ -386,6 +604,27 @@ int tags_fill_tables_init() {
     for (int q = 1; q <= QMAX; ++q) gauss_legendre(q, hx + q * (q - 1) / 2, hw + q * (q - 1) / 2);
     TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glx, hx, sizeof(hx)));
     TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glw, hw, sizeof(hw)));
+    return 0;
+}
+
+int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, uint16_t* d_codes,
+                          cudaStream_t st) {
+    const long long npairs = (long long)m * (m + 1) / 2;
+    k_pair_plan<<<(unsigned)((npairs + 127) / 128), 128, 0, st>>>(d_elec, d_img, m, has_img, d_codes);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, const uint16_t* d_codes,
+                           const SampleCoef* d_coef, int nsamp, const FillOut& out, int has_img, int* d_status,
+                           cudaStream_t st) {
+    if (m <= 0 || nsamp <= 0) return 0;
+    const long long npairs = (long long)m * (m + 1) / 2;
+    dim3 grid((unsigned)((npairs + 127) / 128), (unsigned)((nsamp + MIX_SG - 1) / MIX_SG));
+    k_fill_mixed<<<grid, 128, 0, st>>>(d_elec, d_img, m, d_codes, d_coef, nsamp, out, has_img, d_status);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
     return 0;
 }
 

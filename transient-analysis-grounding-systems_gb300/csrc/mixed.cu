@@ -5,6 +5,8 @@
 //           [ A  -ZL   0   ]
 //           [ B   0   -ZT  ]
 // solved here as follows:
+//   0. impedance blocks: regular pairs in FP32 around FP64 anchors, pairs
+//      sharing an endpoint (log-singular) in FP64, diagonal closed form;
 //   1. static symmetric ordering P: ZL rows, ZT rows, then node rows, so that
 //      the elimination meets the impedance blocks (large diagonals) before the
 //      zero Y_E block and needs no pivot search;
@@ -183,6 +185,9 @@ __global__ void k_max_rows(const double* __restrict__ rsum, int N, double* __res
 
 int tags_mixed_alloc(tags_plan_s* p) {
     const size_t b = p->batch, N = p->N, m = p->m;
+    TAGS_CUDA_OK(cudaMalloc(&p->d_codes, sizeof(uint16_t) * m * (m + 1)));
+    int err = tags_launch_pair_plan(p->d_elec, p->d_img, p->m, p->has_images, p->d_codes, p->stream);
+    if (err) return err;
     TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(double2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_A, sizeof(float2) * N * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_scale, sizeof(double) * 2 * N * b));   // scale + row sums
@@ -193,7 +198,7 @@ int tags_mixed_alloc(tags_plan_s* p) {
 }
 
 int tags_mixed_free(tags_plan_s* p) {
-    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms};
+    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms, p->d_codes};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     p->d_Z = nullptr;
@@ -249,9 +254,8 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     out.batch_stride = 2LL * m * m;
     out.sign = 1.0;
     out.mirror = 1;
-    int err = tags_launch_fill_fp64(p->d_elec, p->d_img, m, p->d_coef, nb, out,
-                                    p->has_images ? TAGS_FILL_BOTH : TAGS_FILL_DIRECT, TAGS_INTG_DOUBLE, 0,
-                                    p->d_status, st);
+    int err = tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_codes, p->d_coef, nb, out, p->has_images,
+                                     p->d_status, st);
     if (err) return err;
     // 2. scaling
     k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, N);

@@ -60,6 +60,7 @@ struct tags_plan_s {
     double2* d_r = nullptr;         // batch x N residual (FP64)
     float2* d_rf = nullptr;         // batch x N correction right-hand side (FP32)
     double* d_norms = nullptr;      // batch x 4 reductions
+    uint16_t* d_codes = nullptr;    // 2 x m(m+1)/2 pair classes (direct, image)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 

@@ -37,6 +37,11 @@ struct FillOut {
 };
 
 int tags_fill_tables_init();
+int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, uint16_t* d_codes,
+                          cudaStream_t st);
+int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, const uint16_t* d_codes,
+                           const SampleCoef* d_coef, int nsamp, const FillOut& out, int has_img, int* d_status,
+                           cudaStream_t st);
 int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, const SampleCoef* d_coef,
                           int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
                           cudaStream_t st);
