@@ -141,6 +141,25 @@ int tags_plan_run (tags_plan plan, const tags_cdouble *s, const tags_cdouble *ka
 
 int tags_plan_destroy (tags_plan plan);
 
+/* ---- Part 3: solve without device allocation -------------------------------- */
+
+/* No counterpart in the reference. For callers that may not allocate device
+ * memory, e.g. code inside a larger GPU application that owns a fixed memory
+ * pool, or code that must not allocate after start-up: the same solve as
+ * solve_immittance on device buffers the caller owns. d_wg (N x N,
+ * column-major, lower half read) is factorised in place and d_ie (N values) is
+ * overwritten with [U; I_L; I_T]; N = n + 2m must not exceed
+ * TAGS_NOALLOC_MAX_N. The solver's scratch is a fixed device array inside the
+ * library (no cudaMalloc or cudaFree on any call); every GPU that loads the
+ * library holds it until exit. The first call on a device looks the array up:
+ * make that call before any stream capture. All calls share the array, so
+ * calls that overlap on the GPU race. stream may be NULL (default stream).
+ * Returns 0, k > 0 when the k-th pivot is exactly zero (ie unchanged), or a
+ * negative TAGS_E_* code (TAGS_E_ARG for a system above the limit). */
+#define TAGS_NOALLOC_MAX_N 32768
+int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_t num_electrodes,
+                                   size_t num_nodes, void *stream);
+
 /* Number of CUDA kernel launches issued by this library since load. */
 long long tags_gpu_launch_count (void);
 
