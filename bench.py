@@ -127,6 +127,56 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "src": "fallback"}
 
 
+PROFILE_FAMILIES = 10
+TENSOR_FAMILIES = {"ldl_trailing_gemm", "ldl_panel_gemm"}
+FP64_FAMILIES = {"lu_fp64_gemm"}
+FP64_PIPE_TFLOPS = 1.19   # DFMA throughput measured on this machine's GB300 (probe kernel, 8 FMA chains)
+
+
+def read_profile(pkg):
+    import ctypes
+    fn = pkg.lib().tags_gpu_profile_read
+    fn.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_double),
+                   ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), ctypes.c_char_p, ctypes.c_int]
+    out = {}
+    for fam in range(PROFILE_FAMILIES):
+        n = ctypes.c_longlong()
+        ms, fl, by = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        name = ctypes.create_string_buffer(64)
+        if fn(fam, ctypes.byref(n), ctypes.byref(ms), ctypes.byref(fl), ctypes.byref(by), name, 64) == 0 and n.value:
+            out[name.value.decode()] = {"launches": n.value, "ms": ms.value, "flops": fl.value, "bytes": by.value}
+    return out
+
+
+def roofline(prof, peaks):
+    """Roofline of the family with the largest device time."""
+    if not prof:
+        return None, None
+    name, f = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    sec = f["ms"] * 1e-3
+    if name in TENSOR_FAMILIES:
+        ach = f["flops"] / sec / 1e12
+        roof = {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["bf16_tflops"], "traffic": None,
+                "kernel": name, "launches": f["launches"], "avg_launch_ms": f["ms"] / f["launches"],
+                "note": f"algorithmic complex LDL^T flops of the launch (the bf16x3 split executes 3x "
+                        f"as many tensor flops); peak = {peaks['src']} dense bf16"}
+    elif name in FP64_FAMILIES:
+        ach = f["flops"] / sec / 1e12
+        roof = {"bound": "fp64", "achieved": ach, "peak": FP64_PIPE_TFLOPS, "unit": "TFLOP/s",
+                "frac": ach / FP64_PIPE_TFLOPS, "traffic": None, "kernel": name, "launches": f["launches"],
+                "avg_launch_ms": f["ms"] / f["launches"],
+                "note": "FP64 CUDA-core pipe; peak = DFMA throughput of a probe kernel on this pool's GB300"}
+    else:
+        ach = f["bytes"] / sec / 1e9
+        roof = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": ach / peaks["hbm_gbs"], "traffic": None, "kernel": name, "launches": f["launches"],
+                "avg_launch_ms": f["ms"] / f["launches"], "note": f"peak = {peaks['src']} HBM copy"}
+    fams = {k: {"launches": v["launches"], "ms": round(v["ms"], 3),
+                "share": round(v["ms"] / sum(x["ms"] for x in prof.values()), 4)} for k, v in prof.items()}
+    return roof, fams
+
+
 def cpu_baseline(args, elec, img, nodes, s, kappa, inj, centre, nsamp):
     """The oracle (restatement of the reference's path A) on the host cores:
     OpenMP over samples, OpenBLAS on 1 thread, the reference's tolerances."""
@@ -156,7 +206,7 @@ def run_reference(args):
     from oracle import oracle as O
     port = O.get("port")
     times = []
-    steps = max(1, min(args.steps, args.ref_steps))
+    steps = max(1, min(args.steps, args.ref_steps))     # each step is ~10-15 s of all host cores
     for step in range(steps):
         idx = (np.arange(nsamp) * 127 + step * 61) % len(s)
         t0 = time.perf_counter()
@@ -190,7 +240,7 @@ def main():
     ap.add_argument("--batch", type=int, default=0, help="samples per step (0 = 64 mixed / 8 plain)")
     ap.add_argument("--cpu-samples", type=int, default=0, help="CPU-baseline samples (0 = host cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--ref-steps", type=int, default=2, help="cap on timed steps of the reference arm")
+    ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -239,6 +289,7 @@ def main():
     launches0 = pkg.launch_count()
     stats_iter, stats_fb = 0, 0
     dev_time = 0.0
+    pkg.lib().tags_gpu_profile(1)      # per-family CUDA events on the launching stream
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
         for st_i in range(args.steps):
@@ -250,6 +301,8 @@ def main():
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
     launches = pkg.launch_count() - launches0
+    prof = read_profile(pkg)
+    pkg.lib().tags_gpu_profile(0)
     if world > 1:
         t = torch.tensor([dev_time], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
@@ -280,12 +333,7 @@ def main():
     if rank != 0:
         return 0
     peaks = measured_peaks()
-    # roofline of the dominant kernel family: the LU's trailing update
-    lu_flops = (8.0 / 3.0) * N ** 3
-    achieved_tf = lu_flops * samples / world / dev_time / 1e12
-    roof = {"bound": "tensor", "achieved": achieved_tf, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-            "frac": achieved_tf / peaks["bf16_tflops"], "traffic": None,
-            "note": f"whole-step average of (8/3) N^3 LU flops; peak = {peaks['src']} bf16"}
+    roof, fams = roofline(prof, peaks)
     line = {"metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)", "value": value,
             "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dev_time / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -294,7 +342,7 @@ def main():
             "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, 1417 nodes, N=4537, 2048 Laplace "
                                    "samples (nt=4094, 10 MHz), Alipio soil sigma0=1 mS/m, centre injection",
                        "precision": args.precision, "samples_per_step": B, "l2": "flushed between steps (256 MB write)"},
-            "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e,
+            "roofline": roof, "kernel_families": fams, "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e,
             "refinement": {"max_iterations": stats_iter, "fallbacks": stats_fb}, "wall_s": wall}
     if not args.no_cpu_baseline:
         nsamp = args.cpu_samples or (os.cpu_count() or 1)

@@ -160,6 +160,24 @@ int tags_plan_destroy (tags_plan plan);
 int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_t num_electrodes,
                                    size_t num_nodes, void *stream);
 
+/* ---- Part 4: diagnostics -------------------------------------------------------- */
+
+/* No counterpart in the reference. Factorises nb complex symmetric N x N
+ * matrices (host, column-major, sample-major; lower half read) with the mixed
+ * form's tensor-core LDL^T (FP32 storage, bf16x3 products, no pivoting) and
+ * returns L (strictly lower, unit diagonal implied) and D (diagonal) in place,
+ * rounded from FP32. Returns 0, k > 0 for a zero pivot, or a TAGS_E_* code. */
+int tags_debug_ldl (tags_cdouble *a, int N, int nb);
+
+/* Per-family kernel timing with CUDA events on the launching stream (0 = off,
+ * the default). Enabling resets the counters. Families, in this order:
+ * fill_fp64, fill_mixed, ldl_diag, ldl_panel_gemm, ldl_trailing_gemm,
+ * ldl_solve, residual_fp64, build_fp32, lu_fp64_gemm, lu_fp64_other. */
+int tags_gpu_profile (int enable);
+/* launches, device milliseconds, algorithmic flops and bytes of one family. */
+int tags_gpu_profile_read (int family, long long *launches, double *ms, double *flops, double *bytes,
+                           char *name, int name_len);
+
 /* Number of CUDA kernel launches issued by this library since load. */
 long long tags_gpu_launch_count (void);
 

@@ -416,3 +416,31 @@ def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, p
         return plan.run(s, kappa, mur, ie, inj_node)
     finally:
         plan.close()
+
+
+# ---- multi-GPU helpers (host side) ------------------------------------------------------
+
+def shard_samples(ns: int, rank: int, world: int) -> np.ndarray:
+    """Laplace samples handled by `rank` of `world` processes (one GPU each):
+    strided, so every rank sees low and high frequencies alike. The samples are
+    independent, so ranks exchange nothing while they solve."""
+    if not 0 <= rank < world:
+        raise ValueError("rank must be in [0, world)")
+    return np.arange(rank, ns, world)
+
+
+def gather_samples(values: np.ndarray, ns: int, group=None):
+    """Collect every rank's per-sample results (rows in shard_samples order)
+    on rank 0 before the inverse Laplace transform; other ranks get None.
+    The only exchange of the multi-GPU path, done on the host."""
+    import torch.distributed as dist
+    rank, world = dist.get_rank(group), dist.get_world_size(group)
+    parts = [None] * world if rank == 0 else None
+    dist.gather_object(np.asarray(values), parts, dst=0, group=group)
+    if rank != 0:
+        return None
+    first = np.asarray(parts[0])
+    out = np.zeros((ns,) + first.shape[1:], dtype=first.dtype)
+    for r, part in enumerate(parts):
+        out[shard_samples(ns, r, world)] = part
+    return out

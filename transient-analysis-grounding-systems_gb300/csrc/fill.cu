@@ -622,7 +622,9 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, con
     if (m <= 0 || nsamp <= 0) return 0;
     const long long npairs = (long long)m * (m + 1) / 2;
     dim3 grid((unsigned)((npairs + 127) / 128), (unsigned)((nsamp + MIX_SG - 1) / MIX_SG));
+    int pf = tags_prof_begin(TAGS_PROF_FILL_MIXED, st);
     k_fill_mixed<<<grid, 128, 0, st>>>(d_elec, d_img, m, d_codes, d_coef, nsamp, out, has_img, d_status);
+    tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
@@ -634,7 +636,9 @@ int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, cons
     if (m <= 0 || nsamp <= 0) return 0;
     const long long npairs = (long long)m * (m + 1) / 2;
     dim3 grid((unsigned)((npairs + 127) / 128), (unsigned)nsamp);
+    int pf = tags_prof_begin(TAGS_PROF_FILL_FP64, st);
     k_fill_fp64<<<grid, 128, 0, st>>>(d_elec, d_img, m, d_coef, nsamp, out, mode, itype, tight, d_status);
+    tags_prof_end(TAGS_PROF_FILL_FP64, pf, st, 0.0, 0.0);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

@@ -13,6 +13,7 @@
 // (pointer + z * stride). ipiv is 0-based global row indices.
 #include "tags_common.cuh"
 #include "tags_internal.h"
+#include <type_traits>
 
 namespace {
 
@@ -344,7 +345,11 @@ int lu_impl(T* A, int n, long long ld, long long stride, int batch, int pivot, i
             k_trsm_row<T, NB><<<dim3((rest + 31) / 32, 1, batch), 256, 0, st>>>(A, n, ld, stride, j0, jb);
             tags_note_launch();
             dim3 g((rest + 63) / 64, (rest + 63) / 64, batch);
+            int pf = std::is_same<T, double2>::value ? tags_prof_begin(TAGS_PROF_LU64_GEMM, st) : -1;
             k_gemm_update<T, NB><<<g, 256, gsmem, st>>>(A, n, ld, stride, j0, jb);
+            // rank-jb update of a rest x rest block: 8 rest^2 jb real flops
+            tags_prof_end(TAGS_PROF_LU64_GEMM, pf, st, 8.0 * rest * (double)rest * jb * batch,
+                          (32.0 * rest * (double)rest + 32.0 * rest * jb) * batch);
             tags_note_launch();
         }
     }

@@ -11,7 +11,8 @@
 //      the elimination meets the impedance blocks (large diagonals) before the
 //      zero Y_E block and needs no pivot search;
 //   2. symmetric scaling D = diag(1/sqrt(max_j |W'_ij|)), W'' = D P W P^T D;
-//   3. LU of W'' without pivoting in complex FP32 storage;
+//   3. LDL^T of W'' without pivoting, complex FP32 storage, trailing updates
+//      and triangular-solve panels on the tensor cores (ldl_tc.cu);
 //   4. iterative refinement in FP64: r = b - W x is evaluated in FP64 from the
 //      FP64 impedance blocks and the exact incidence (sparse, +-1 / 0.5), the
 //      correction from the FP32 factors, until the correction is below
@@ -73,7 +74,7 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
     rsum[(size_t)b * N + 2 * m + nd] = 1.5 * (double)(node_ptr[nd + 1] - node_ptr[nd]);
 }
 
-// W'' (complex FP32, column-major N x N, reordered and scaled).
+// W'' (complex FP32, column-major N x N, reordered and scaled), lower triangle.
 __global__ void k_build(const double2* __restrict__ Z, const signed char* __restrict__ cond, const double* __restrict__ scale,
                         int m, int n, float2* __restrict__ A) {
     const int N = n + 2 * m;
@@ -81,6 +82,7 @@ __global__ void k_build(const double2* __restrict__ Z, const signed char* __rest
     int b = blockIdx.y;
     if (t >= (long long)N * N) return;
     int i = (int)(t % N), j = (int)(t / N);
+    if (i < j) return;              // the LDL^T reads the lower triangle only
     const double* d = scale + (size_t)b * N;
     const double2* Zb = Z + (size_t)b * 2 * m * m;
     double2 v = make_double2(0.0, 0.0);
@@ -194,11 +196,16 @@ int tags_mixed_alloc(tags_plan_s* p) {
     TAGS_CUDA_OK(cudaMalloc(&p->d_r, sizeof(double2) * 2 * N * b));      // residual + right-hand side
     TAGS_CUDA_OK(cudaMalloc(&p->d_rf, sizeof(float2) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_norms, sizeof(double) * 4 * b + sizeof(int) * b));
+    const size_t ws = tags_ldl_tc_workspace((int)N, (int)b);
+    TAGS_CUDA_OK(cudaMalloc(&p->d_ldlws, ws));
+    TAGS_CUDA_OK(cudaMemset(p->d_ldlws, 0, ws));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_ldlerr, sizeof(int)));
+    TAGS_CUDA_OK(cudaMemset(p->d_ldlerr, 0, sizeof(int)));
     return 0;
 }
 
 int tags_mixed_free(tags_plan_s* p) {
-    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms, p->d_codes};
+    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms, p->d_codes, p->d_ldlws, p->d_ldlerr};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     p->d_Z = nullptr;
@@ -262,17 +269,27 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     k_rowstats_nodes<<<dim3((n + 127) / 128, nb), 128, 0, st>>>(p->inc.node_ptr, n, m, p->d_scale, d_rsum, N);
     tags_note_launch(2);
     // 3. FP32 working matrix and its LU (no pivoting)
+    int pf = tags_prof_begin(TAGS_PROF_BUILD, st);
     k_build<<<dim3((unsigned)((NN + 255) / 256), nb), 256, 0, st>>>(p->d_Z, p->d_cond, p->d_scale, m, n, p->d_A);
+    tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
-    err = tags_lu_c(p->d_A, N, N, (long long)NN, nb, 0, nullptr, p->d_info, st);
+    err = tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m, st);
     if (err) return err;
     // 4. refinement
     std::vector<int> active(nb, 1), conv(nb, 0), iters(nb, 0);
     std::vector<double> prev_dx(nb, INFINITY), hn(4 * nb);
     std::vector<int> info(nb);
+    int tc_err = 0;
     TAGS_CUDA_OK(cudaMemcpyAsync(info.data(), p->d_info, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(&tc_err, p->d_ldlerr, sizeof(int), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    if (tc_err) {
+        // a tensor-core wait ran out: the whole pass goes to the FP64 path
+        tags_fail(TAGS_E_CUDA, "tensor-core factorisation reported a timeout; samples re-solved in FP64");
+        TAGS_CUDA_OK(cudaMemsetAsync(p->d_ldlerr, 0, sizeof(int), st));
+        for (int q = 0; q < nb; ++q) active[q] = 0;
+    }
     for (int q = 0; q < nb; ++q)
         if (info[q] != 0) active[q] = 0;   // zero pivot in the static order: straight to the fallback
     // r = b initially
@@ -295,10 +312,12 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
         dim3 gv((N + 255) / 256, nb);
         k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf);
         tags_note_launch();
-        err = tags_lu_solve_c(p->d_A, N, N, (long long)NN, nb, nullptr, p->d_rf, 1, N, N, st);
+        err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st);
         if (err) return err;
         k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, d_active);
+        pf = tags_prof_begin(TAGS_PROF_RESID, st);
         k_residual<<<gv, 256, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms, d_active);
+        tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 32.0 * m * (double)m * nb);
         tags_note_launch(2);
         TAGS_CUDA_OK(cudaGetLastError());
         TAGS_CUDA_OK(cudaMemcpyAsync(hn.data(), p->d_norms, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st));

@@ -61,6 +61,8 @@ struct tags_plan_s {
     float2* d_rf = nullptr;         // batch x N correction right-hand side (FP32)
     double* d_norms = nullptr;      // batch x 4 reductions
     uint16_t* d_codes = nullptr;    // 2 x m(m+1)/2 pair classes (direct, image)
+    void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
+    int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 

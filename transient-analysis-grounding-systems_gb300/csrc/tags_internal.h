@@ -75,3 +75,20 @@ int tags_launch_inlt(const double2* d_g, long long gstride, long long ns, const 
                      cudaStream_t st);
 int tags_launch_nlt(const double* d_f, long long fstride, long long nt, const double2* d_tw, double tmax,
                     double2* d_g, long long gstride, int nseries, cudaStream_t st);
+
+// ldl_tc.cu: tensor-core LDL^T of complex FP32 symmetric matrices (no pivoting)
+size_t tags_ldl_tc_workspace(int N, int batch);
+// zl_m > 0: the matrix is ordered [ZL (zl_m), ZT (zl_m), rest] with a zero ZL/ZT
+// coupling block, which the factorisation and the solves skip.
+int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
+                int* err, int zl_m, cudaStream_t st);
+int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
+                     float2* x, long long xstride, int zl_m, cudaStream_t st);
+
+// profile.cu: optional CUDA-event timing of kernel families
+enum {
+    TAGS_PROF_FILL_FP64 = 0, TAGS_PROF_FILL_MIXED, TAGS_PROF_LDL_DIAG, TAGS_PROF_LDL_PANEL, TAGS_PROF_LDL_TRAIL,
+    TAGS_PROF_LDL_SOLVE, TAGS_PROF_RESID, TAGS_PROF_BUILD, TAGS_PROF_LU64_GEMM, TAGS_PROF_LU64_OTHER, TAGS_PROF_N
+};
+int tags_prof_begin(int fam, cudaStream_t st);
+void tags_prof_end(int fam, int slot, cudaStream_t st, double flops, double bytes);
