@@ -258,7 +258,7 @@ def main():
     m, n = elec.shape[0], nodes.shape[0]
     N = n + 2 * m
     mixed = args.precision == "mixed"
-    B = args.batch or (64 if mixed else 8)
+    B = args.batch or (128 if mixed else 8)
     plan = pkg.Plan(elec, img, nodes, pkg.MIXED if mixed else pkg.PLAIN_FP64, max_batch=B)
     ns_total = len(s)
     dev = torch.device("cuda", local)

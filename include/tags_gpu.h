@@ -164,10 +164,11 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
 
 /* No counterpart in the reference. Factorises nb complex symmetric N x N
  * matrices (host, column-major, sample-major; lower half read) with the mixed
- * form's tensor-core LDL^T (FP32 storage, bf16x3 products, no pivoting) and
- * returns L (strictly lower, unit diagonal implied) and D (diagonal) in place,
- * rounded from FP32. Returns 0, k > 0 for a zero pivot, or a TAGS_E_* code. */
-int tags_debug_ldl (tags_cdouble *a, int N, int nb);
+ * form's tensor-core LDL^T (FP32 storage, products of bf16 pieces, no
+ * pivoting; pieces = 2 or 3 per real value) and returns L (strictly lower,
+ * unit diagonal implied) and D (diagonal) in place, rounded from FP32.
+ * Returns 0, k > 0 for a zero pivot, or a TAGS_E_* code. */
+int tags_debug_ldl (tags_cdouble *a, int N, int nb, int pieces);
 
 /* Per-family kernel timing with CUDA events on the launching stream (0 = off,
  * the default). Enabling resets the counters. Families, in this order:

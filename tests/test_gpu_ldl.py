@@ -15,28 +15,30 @@ def _sym_matrix(rng, N, dominance):
     return a
 
 
-def _ldl(pkg, mats):
+def _ldl(pkg, mats, pieces=3):
     fn = pkg.lib().tags_debug_ldl
-    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     fn.restype = ctypes.c_int
     nb, N = mats.shape[0], mats.shape[1]
     buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)   # column-major
-    code = fn(buf.ctypes.data, N, nb)
+    code = fn(buf.ctypes.data, N, nb, pieces)
     return code, np.transpose(buf, (0, 2, 1))
 
 
+@pytest.mark.parametrize("pieces,tol", [(2, 2e-5), (3, 2e-6)])
 @pytest.mark.parametrize("N", [128, 300, 517])
-def test_tensor_core_ldl_reconstructs(gpu_pkg, N):
-    """L D L^T reproduces A to the accuracy of the split products (~1e-5)."""
+def test_tensor_core_ldl_reconstructs(gpu_pkg, N, pieces, tol):
+    """L D L^T reproduces A to the accuracy of the split products: ~1e-5 with
+    two bf16 pieces per value (three products), FP32 level with three (six)."""
     rng = np.random.default_rng(N)
-    mats = np.stack([_sym_matrix(rng, N, 4.0), _sym_matrix(rng, N, 2.0)])
-    code, fac = _ldl(gpu_pkg, mats)
+    mats = np.stack([_sym_matrix(rng, N, 4.0), _sym_matrix(rng, N, 2.0), _sym_matrix(rng, N, 3.0)])
+    code, fac = _ldl(gpu_pkg, mats, pieces)
     assert code == 0, gpu_pkg.last_error()
-    for q in range(2):
+    for q in range(3):
         L = np.tril(fac[q], -1) + np.eye(N)
         D = np.diag(np.diag(fac[q]))
         err = np.linalg.norm(L @ D @ L.T - mats[q]) / np.linalg.norm(mats[q])
-        assert err < 2e-5, (N, q, err)
+        assert err < tol, (N, q, err)
 
 
 def test_tensor_core_ldl_matches_fp64_factors(gpu_pkg):

@@ -375,8 +375,17 @@ TAGS_D uint16_t classify_pair(const Seg& S, const Seg& R) {
     return (uint16_t)(P | (qg << 6));
 }
 
+// Geometry of one (pair, kind) for the FP32 path, computed once per plan:
+// receiver-minus-sender midpoint vector, its length split into two floats
+// (hi + lo, ~2^-48 relative), and the ZL factor |d_i . d_k| (zero where the
+// reference drops ZL: cos < DBL_EPSILON direct, cos <= DBL_EPSILON images).
+struct PairRec {
+    float dx, dy, dz, rch, rcl, fl;
+};
+
 __global__ void k_pair_plan(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
-                            uint16_t* __restrict__ codes) {
+                            uint16_t* __restrict__ codes, PairRec* __restrict__ recs, int* __restrict__ ntouch,
+                            int* __restrict__ touch_list) {
     const long long npairs = (long long)m * (m + 1) / 2;
     long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npairs) return;
@@ -384,185 +393,305 @@ __global__ void k_pair_plan(const double* __restrict__ elec, const double* __res
     pair_index(p, m, i, k);
     Seg S, R;
     ld_seg(elec + 11LL * i, S);
-    uint16_t cd = 0, ci = 0;
-    if (k != i) {
-        ld_seg(elec + 11LL * k, R);
-        cd = classify_pair(S, R);
+    uint16_t cc[2] = {0, 0};
+    int special = 0;
+    for (int kind = 0; kind < 2; ++kind) {
+        PairRec rc{0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if ((kind == 0 && k != i) || (kind == 1 && has_img)) {
+            ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
+            cc[kind] = classify_pair(S, R);
+            if (cc[kind] & (PC_TOUCH | PC_DEGEN)) special |= 1 << kind;
+            double d[3] = {R.mid[0] - S.mid[0], R.mid[1] - S.mid[1], R.mid[2] - S.mid[2]};
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            float rh = (float)r;
+            double cost = 0.0;
+            for (int c = 0; c < 3; ++c) cost += (S.b[c] - S.a[c]) * (R.b[c] - R.a[c]);
+            cost = fabs(cost);
+            bool keep = kind == 0 ? !(cost < TAGS_DBL_EPSILON) : (cost > TAGS_DBL_EPSILON);
+            rc = PairRec{(float)d[0], (float)d[1], (float)d[2], rh, (float)(r - (double)rh), keep ? (float)cost : 0.f};
+        }
+        recs[2 * p + kind] = rc;
     }
-    if (has_img) {
-        ld_seg(img + 11LL * k, R);
-        ci = classify_pair(S, R);
+    codes[2 * p] = cc[0];
+    codes[2 * p + 1] = cc[1];
+    if (special) {
+        int slot = atomicAdd(ntouch, 1);
+        touch_list[2 * slot] = (int)p;
+        touch_list[2 * slot + 1] = special;
     }
-    codes[2 * p] = cd;
-    codes[2 * p + 1] = ci;
 }
 
-// e^{-gamma r} for r in FP64, result FP32: the exponent and the phase are
-// reduced in FP64 (2^-t with t split into integer and fraction, phase modulo
-// 2 pi), the remaining small arguments are evaluated in FP32.
-TAGS_D float2 anchor_f32(double2 gamma, double r) {
-    const double LOG2E = 1.4426950408889634;
-    double t = gamma.x * r * LOG2E;                  // e^{-Re(gamma) r} = 2^{-t}
-    double ti = floor(t);
-    float mag = ldexpf(exp2f(-(float)(t - ti)), -(int)fmin(ti, 1000.0));
-    double ph = gamma.y * r;                         // e^{-j Im(gamma) r}
-    ph -= TAGS_TWO_PI * rint(ph * (1.0 / TAGS_TWO_PI));
+// Per-sample constants of the FP32 path: gamma as float pairs (hi + lo) and
+// the scale factors in FP32.
+struct SampleF32 {
+    float grh, grl, gih, gil;
+    float2 cL, cT, cLi, cTi;
+};
+
+__global__ void k_coef32(const SampleCoef* __restrict__ coef, int nsamp, SampleF32* __restrict__ out) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nsamp) return;
+    SampleCoef c = coef[q];
+    SampleF32 o;
+    o.grh = (float)c.gamma.x;
+    o.grl = (float)(c.gamma.x - (double)o.grh);
+    o.gih = (float)c.gamma.y;
+    o.gil = (float)(c.gamma.y - (double)o.gih);
+    o.cL = make_float2((float)c.cL.x, (float)c.cL.y);
+    o.cT = make_float2((float)c.cT.x, (float)c.cT.y);
+    o.cLi = make_float2((float)c.cLi.x, (float)c.cLi.y);
+    o.cTi = make_float2((float)c.cTi.x, (float)c.cTi.y);
+    out[q] = o;
+}
+
+// e^{-gamma r} in FP32 from float pairs (r = rh + rl, gamma = (grh + grl) +
+// j (gih + gil)): the exponent and the phase are formed as float pairs
+// (error-free products) and reduced exactly (2^-t split into integer and
+// fraction, phase modulo 2 pi with a two-float 2 pi), so only the small
+// reduced arguments meet FP32 rounding.
+TAGS_D float2 anchor_df(float grh, float grl, float gih, float gil, float rh, float rl) {
+    const float L2E_HI = 1.44269502162933349609f, L2E_LO = 1.925963033500011e-8f;
+    const float TPI_HI = 6.28318548202514648438f, TPI_LO = -1.7484555314695172e-7f;
+    // t = Re(gamma) r log2(e)
+    float q = grh * rh;
+    float qe = fmaf(grh, rh, -q) + fmaf(grh, rl, grl * rh);
+    float th = q * L2E_HI;
+    float te = fmaf(q, L2E_HI, -th) + fmaf(q, L2E_LO, qe * L2E_HI);
+    float n = floorf(th);
+    float f = (th - n) + te;
+    float mag = ldexpf(exp2f(-f), -(int)fminf(n, 1000.f));
+    // phase = Im(gamma) r, modulo 2 pi
+    float p = gih * rh;
+    float pe = fmaf(gih, rh, -p) + fmaf(gih, rl, gil * rh);
+    float kq = rintf(p * 0.15915494309189535f);
+    float red = fmaf(-kq, TPI_HI, p);
+    red = fmaf(-kq, TPI_LO, red) + pe;
     float sn, cs;
-    sincosf((float)ph, &sn, &cs);
+    sincosf(red, &sn, &cs);
     return make_float2(mag * cs, -mag * sn);
 }
 
 constexpr int MIX_SG = 8;   // samples per thread
 
-// Mixed-form fill: one thread per (pair, group of up to MIX_SG samples).
-// Regular pairs in FP32 (panel anchors in FP64), touching pairs in FP64.
-// Writes ZL (at zl) and ZT (at zt), lower + mirrored upper, FP64 storage.
-__global__ void __launch_bounds__(128, 1) k_fill_mixed(const double* __restrict__ elec, const double* __restrict__ img,
-                                                    int m, const uint16_t* __restrict__ codes,
-                                                    const SampleCoef* __restrict__ coef, int nsamp, FillOut out,
-                                                    int has_img, int* status) {
-    __shared__ double sx[GL_TOTAL], sw[GL_TOTAL];
-    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) { sx[t] = g_glx[t]; sw[t] = g_glw[t]; }
+// Mixed-form fill of the regular pairs, all in FP32: one thread per (pair,
+// group of MIX_SG samples), the group's constants in shared memory. Pairs that
+// share an endpoint (log-singular) are left to k_fill_touch. Z (ZL at zl, ZT at
+// zt, complex FP32) gets the lower element and its mirror.
+__global__ void __launch_bounds__(128) k_fill_mixed(const double* __restrict__ elec, const double* __restrict__ img,
+                                                    const float4* __restrict__ sdir, const float4* __restrict__ idir,
+                                                    const float* __restrict__ selfv, int m,
+                                                    const uint16_t* __restrict__ codes,
+                                                    const PairRec* __restrict__ recs,
+                                                    const SampleF32* __restrict__ coef, int nsamp, float2* zl0,
+                                                    float2* zt0, long long bstride, int has_img, int* status) {
+    __shared__ float sxm[GL_TOTAL], swf[GL_TOTAL];
+    __shared__ SampleF32 sc[MIX_SG];
+    __shared__ float s_gmax;
+    const int s0 = blockIdx.y * MIX_SG;
+    const int ns = min(MIX_SG, nsamp - s0);
+    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) {
+        sxm[t] = (float)(g_glx[t] - 0.5);
+        swf[t] = (float)g_glw[t];
+    }
+    if (threadIdx.x < MIX_SG) {
+        SampleF32 z{};
+        sc[threadIdx.x] = threadIdx.x < ns ? coef[s0 + threadIdx.x] : z;
+    }
     __syncthreads();
-    GLTab gl{sx, sw};
+    if (threadIdx.x == 0) {
+        float gm = 0.f;
+        for (int q = 0; q < ns; ++q) gm = fmaxf(gm, sqrtf(sc[q].grh * sc[q].grh + sc[q].gih * sc[q].gih));
+        s_gmax = gm;
+    }
+    __syncthreads();
+    const float gmax = s_gmax;
     const long long npairs = (long long)m * (m + 1) / 2;
     const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int s0 = blockIdx.y * MIX_SG;
-    if (p >= npairs || s0 >= nsamp) return;
-    const int ns = min(MIX_SG, nsamp - s0);
+    if (p >= npairs || ns <= 0) return;
     int i, k;
     pair_index(p, m, i, k);
-    Seg S;
-    ld_seg(elec + 11LL * i, S);
-    const double ds[3] = {S.b[0] - S.a[0], S.b[1] - S.a[1], S.b[2] - S.a[2]};
-    double2 zl[MIX_SG], zt[MIX_SG];
-    double2 gam[MIX_SG];
-    double gmax = 0.0;
+    const float4 ds = sdir[i];
+    float2 zl[MIX_SG], zt[MIX_SG];
 #pragma unroll
-    for (int q = 0; q < MIX_SG; ++q) {
-        zl[q] = zt[q] = cz(0.0, 0.0);
-        gam[q] = q < ns ? coef[s0 + q].gamma : cz(0.0, 0.0);
-        gmax = fmax(gmax, sqrt(cabs2(gam[q])));
-    }
-    for (int kind = 0; kind < 2; ++kind) {
-        if (kind == 1 && !has_img) break;
-        Seg R;
-        if (kind == 0 && k == i) {
-            double intg = self_integral_d(S);
-#pragma unroll
-            for (int q = 0; q < MIX_SG; ++q) {
-                if (q >= ns) break;
-                SampleCoef c = coef[s0 + q];
-                zl[q] = cscale(c.cL, intg);
-                zt[q] = cscale(c.cT, intg / (S.len * S.len));
-            }
-            continue;
-        }
-        ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
-        const uint16_t code = codes[2 * p + kind];
-        double cost = 0.0;
-        for (int d = 0; d < 3; ++d) cost += ds[d] * (R.b[d] - R.a[d]);
-        cost = fabs(cost);
-        const double lsr = S.len * R.len;
-        double2 J[MIX_SG];
-        if (code & PC_DEGEN) {
-            raise_status(status, TAGS_ST_DEGENERATE_PAIR);
-#pragma unroll
-            for (int q = 0; q < MIX_SG; ++q) J[q] = cz(nan(""), nan(""));
-        } else if (code & PC_TOUCH) {
-            int ia, ib;
-            touching(R, S, 1e-9 * fmax(S.len, R.len), ia, ib);
-#pragma unroll
-            for (int q = 0; q < MIX_SG; ++q) {
-                int qt = min(QMAX, 10 + (int)ceil(sqrt(cabs2(gam[q])) * fmax(S.len, R.len)));
-                J[q] = q < ns ? j_touch(R, S, ia, ib, gam[q], false, qt, gl) : cz(0.0, 0.0);
-            }
-        } else {
-            const int P = code & 63;
-            const int qg = (code >> 6) & 63;
-            const int qq = min(24, qg + (int)ceil(gmax * fmax(S.len, R.len) / P));
-            const double* x = gl.x + gl_off(qq);
-            const double* w = gl.w + gl_off(qq);
-            const double h = 1.0 / (double)P;
-            const double dr[3] = {R.b[0] - R.a[0], R.b[1] - R.a[1], R.b[2] - R.a[2]};
-            const float3 hr = make_float3((float)(dr[0] * h), (float)(dr[1] * h), (float)(dr[2] * h));
-            const float3 hs = make_float3((float)(ds[0] * h), (float)(ds[1] * h), (float)(ds[2] * h));
-            float2 acc[MIX_SG];
-            float gre[MIX_SG], gim[MIX_SG];
-#pragma unroll
-            for (int q = 0; q < MIX_SG; ++q) {
-                acc[q] = make_float2(0.f, 0.f);
-                gre[q] = (float)gam[q].x;
-                gim[q] = (float)gam[q].y;
-            }
-            for (int pi = 0; pi < P; ++pi) {
-                for (int pj = 0; pj < P; ++pj) {
-                    double cr[3], dd[3];
-                    for (int d = 0; d < 3; ++d) {
-                        cr[d] = R.a[d] + (pi + 0.5) * h * dr[d];
-                        dd[d] = cr[d] - (S.a[d] + (pj + 0.5) * h * ds[d]);
-                    }
-                    const double rc = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
-                    const float3 D = make_float3((float)dd[0], (float)dd[1], (float)dd[2]);
-                    const float rcf = (float)rc;
-                    float2 psum[MIX_SG];
-#pragma unroll
-                    for (int q = 0; q < MIX_SG; ++q) psum[q] = make_float2(0.f, 0.f);
-                    for (int qi = 0; qi < qq; ++qi) {
-                        const float a = (float)(x[qi] - 0.5);
-                        const float wi = (float)w[qi];
-                        for (int qj = 0; qj < qq; ++qj) {
-                            const float b = (float)(x[qj] - 0.5);
-                            // u = a hr - b hs: offset of the point pair from the panel centres
-                            float ux = a * hr.x - b * hs.x, uy = a * hr.y - b * hs.y, uz = a * hr.z - b * hs.z;
-                            float e = 2.f * (D.x * ux + D.y * uy + D.z * uz) + (ux * ux + uy * uy + uz * uz);
-                            float rp = sqrtf(rcf * rcf + e);
-                            float del = e / (rp + rcf);                 // r_p - r_c without cancellation
-                            float wt = wi * (float)w[qj] / rp;
-#pragma unroll
-                            for (int q = 0; q < MIX_SG; ++q) {
-                                float mg = expf(-gre[q] * del);
-                                float sn, cs;
-                                sincosf(gim[q] * del, &sn, &cs);
-                                psum[q].x = fmaf(wt * mg, cs, psum[q].x);
-                                psum[q].y = fmaf(-wt * mg, sn, psum[q].y);
-                            }
-                        }
-                    }
-#pragma unroll
-                    for (int q = 0; q < MIX_SG; ++q) {
-                        if (q < ns) acc[q] = ffmac(anchor_f32(gam[q], rc), psum[q], acc[q]);
-                    }
-                }
-            }
-            const double h2 = h * h;
-#pragma unroll
-            for (int q = 0; q < MIX_SG; ++q) J[q] = cz((double)acc[q].x * h2, (double)acc[q].y * h2);
-        }
+    for (int q = 0; q < MIX_SG; ++q) zl[q] = zt[q] = make_float2(0.f, 0.f);
+    if (k == i) {
+        // self term: the reference's static closed form (src/electrode.c:346-348)
+        const float v = selfv[i];
 #pragma unroll
         for (int q = 0; q < MIX_SG; ++q) {
-            if (q >= ns) break;
-            SampleCoef c = coef[s0 + q];
-            double2 intg = cscale(J[q], lsr);
-            double2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
-            zt[q] = cadd(zt[q], cmul(cscale(cT, 1.0 / lsr), intg));
-            bool keep = kind == 0 ? !(cost < TAGS_DBL_EPSILON) : (cost > TAGS_DBL_EPSILON);
-            if (keep) zl[q] = cadd(zl[q], cscale(cmul(cL, intg), cost / lsr));
+            zl[q] = make_float2(sc[q].cL.x * v, sc[q].cL.y * v);
+            zt[q] = make_float2(sc[q].cT.x * v / (ds.w * ds.w), sc[q].cT.y * v / (ds.w * ds.w));
+        }
+    }
+    for (int kind = 0; kind < 2; ++kind) {
+        if (kind == 0 && k == i) continue;
+        if (kind == 1 && !has_img) break;
+        const uint16_t code = codes[2 * p + kind];
+        if (code & (PC_TOUCH | PC_DEGEN)) continue;      // k_fill_touch
+        const float4 dr = kind == 0 ? sdir[k] : idir[k];
+        const PairRec rec = recs[2 * p + kind];
+        const float lmax = fmaxf(ds.w, dr.w);
+        const int P = min(32, max(code & 63, (int)ceilf(gmax * lmax / 1.5f)));
+        const int qg = (code >> 6) & 63;
+        const int qq = min(24, qg + (int)ceilf(gmax * lmax / P));
+        const float* x = sxm + gl_off(qq);
+        const float* w = swf + gl_off(qq);
+        const float h = 1.f / (float)P;
+        const float3 hr = make_float3(dr.x * h, dr.y * h, dr.z * h);
+        const float3 hs = make_float3(ds.x * h, ds.y * h, ds.z * h);
+        float2 acc[MIX_SG];
+#pragma unroll
+        for (int q = 0; q < MIX_SG; ++q) acc[q] = make_float2(0.f, 0.f);
+        for (int pi = 0; pi < P; ++pi) {
+            for (int pj = 0; pj < P; ++pj) {
+                // panel-pair anchor: midpoint vector and its length as a float pair
+                float3 D;
+                float rh, rl;
+                if (P == 1) {
+                    D = make_float3(rec.dx, rec.dy, rec.dz);
+                    rh = rec.rch;
+                    rl = rec.rcl;
+                } else {
+                    const double* SR = (kind == 0 ? elec : img) + 11LL * k;
+                    const double* SS = elec + 11LL * i;
+                    double fr = (pi + 0.5) / P, fs = (pj + 0.5) / P, dd[3];
+                    for (int c = 0; c < 3; ++c)
+                        dd[c] = (SR[c] + fr * (SR[3 + c] - SR[c])) - (SS[c] + fs * (SS[3 + c] - SS[c]));
+                    double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+                    D = make_float3((float)dd[0], (float)dd[1], (float)dd[2]);
+                    rh = (float)r;
+                    rl = (float)(r - (double)rh);
+                }
+                const float rc2 = rh * rh;
+                float2 psum[MIX_SG];
+#pragma unroll
+                for (int q = 0; q < MIX_SG; ++q) psum[q] = make_float2(0.f, 0.f);
+                for (int qi = 0; qi < qq; ++qi) {
+                    const float a = x[qi], wi = w[qi];
+                    const float ax = a * hr.x, ay = a * hr.y, az = a * hr.z;
+                    for (int qj = 0; qj < qq; ++qj) {
+                        const float b = x[qj];
+                        // u = a hr - b hs: offset of the point pair from the panel centres
+                        const float ux = fmaf(-b, hs.x, ax), uy = fmaf(-b, hs.y, ay), uz = fmaf(-b, hs.z, az);
+                        const float e = fmaf(2.f, fmaf(D.x, ux, fmaf(D.y, uy, D.z * uz)),
+                                             fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+                        const float t = rc2 + e;
+                        const float irp = rsqrtf(t);                          // 1 / r_p
+                        const float del = e * __frcp_rn(fmaf(t, irp, rh));    // r_p - r_c
+                        const float wt = wi * w[qj] * irp;
+#pragma unroll
+                        for (int q = 0; q < MIX_SG; ++q) {
+                            const float mg = wt * exp2f(-1.44269502f * sc[q].grh * del);
+                            float sn, cs;
+                            __sincosf(sc[q].gih * del, &sn, &cs);
+                            psum[q].x = fmaf(mg, cs, psum[q].x);
+                            psum[q].y = fmaf(-mg, sn, psum[q].y);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int q = 0; q < MIX_SG; ++q) {
+                    const float2 an = anchor_df(sc[q].grh, sc[q].grl, sc[q].gih, sc[q].gil, rh, rl);
+                    acc[q] = ffmac(an, psum[q], acc[q]);
+                }
+            }
+        }
+        const float h2 = h * h;
+#pragma unroll
+        for (int q = 0; q < MIX_SG; ++q) {
+            const float2 J = make_float2(acc[q].x * h2, acc[q].y * h2);
+            const float2 cL = kind == 0 ? sc[q].cL : sc[q].cLi, cT = kind == 0 ? sc[q].cT : sc[q].cTi;
+            zt[q] = ffmac(cT, J, zt[q]);
+            zl[q] = ffmac(make_float2(cL.x * rec.fl, cL.y * rec.fl), J, zl[q]);
         }
     }
 #pragma unroll
     for (int q = 0; q < MIX_SG; ++q) {
         if (q >= ns) break;
-        const int smp = s0 + q;
-        const long long bs = out.batch_stride * smp;
-        double2 l = cscale(zl[q], out.sign), t = cscale(zt[q], out.sign);
-        if (!isfinite(l.x + l.y + t.x + t.y)) raise_status(status, TAGS_ST_NONFINITE);
-        out.zl[bs + (long long)(out.row0_l + k) + out.ld * (out.col0_l + i)] = l;
-        out.zt[bs + (long long)(out.row0_t + k) + out.ld * (out.col0_t + i)] = t;
-        if (out.mirror && k != i) {
-            out.zl[bs + (long long)(out.row0_l + i) + out.ld * (out.col0_l + k)] = l;
-            out.zt[bs + (long long)(out.row0_t + i) + out.ld * (out.col0_t + k)] = t;
+        const long long bs = bstride * (s0 + q);
+        if (!isfinite(zl[q].x + zl[q].y + zt[q].x + zt[q].y)) raise_status(status, TAGS_ST_NONFINITE);
+        zl0[bs + k + (long long)m * i] = zl[q];
+        zt0[bs + k + (long long)m * i] = zt[q];
+        if (k != i) {
+            zl0[bs + i + (long long)m * k] = zl[q];
+            zt0[bs + i + (long long)m * k] = zt[q];
         }
+    }
+}
+
+// Pairs sharing an endpoint (log-singular): the Duffy rule in FP64, added to
+// what k_fill_mixed wrote. One thread per (listed pair, sample).
+__global__ void __launch_bounds__(128) k_fill_touch(const double* __restrict__ elec, const double* __restrict__ img,
+                                                    int m, const int* __restrict__ list, const int* __restrict__ nlist,
+                                                    const PairRec* __restrict__ recs,
+                                                    const SampleCoef* __restrict__ coef, int nsamp, float2* zl0,
+                                                    float2* zt0, long long bstride, int* status) {
+    __shared__ double sx[GL_TOTAL], sw[GL_TOTAL];
+    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) { sx[t] = g_glx[t]; sw[t] = g_glw[t]; }
+    __syncthreads();
+    GLTab gl{sx, sw};
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    const int smp = blockIdx.y;
+    if (e >= *nlist || smp >= nsamp) return;
+    const long long p = list[2 * e];
+    const int mask = list[2 * e + 1];
+    int i, k;
+    pair_index(p, m, i, k);
+    Seg S, R;
+    ld_seg(elec + 11LL * i, S);
+    const SampleCoef c = coef[smp];
+    double2 dl = cz(0.0, 0.0), dt = cz(0.0, 0.0);
+    for (int kind = 0; kind < 2; ++kind) {
+        if (!(mask & (1 << kind))) continue;
+        ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
+        const double lmax = fmax(S.len, R.len);
+        int ia, ib;
+        if (!touching(R, S, 1e-9 * lmax, ia, ib)) {
+            raise_status(status, TAGS_ST_DEGENERATE_PAIR);      // coincident or overlapping
+            dl = dt = cz(nan(""), nan(""));
+            break;
+        }
+        const double* ro = ia == 0 ? R.b : R.a;
+        const double* so = ib == 0 ? S.b : S.a;
+        if (fmax(fabs(ro[0] - so[0]), fmax(fabs(ro[1] - so[1]), fabs(ro[2] - so[2]))) <= 1e-9 * lmax) {
+            raise_status(status, TAGS_ST_DEGENERATE_PAIR);
+            dl = dt = cz(nan(""), nan(""));
+            break;
+        }
+        const int qt = min(QMAX, 10 + (int)ceil(sqrt(cabs2(c.gamma)) * lmax));
+        const double2 J = j_touch(R, S, ia, ib, c.gamma, false, qt, gl);
+        const double2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
+        dt = cadd(dt, cmul(cT, J));
+        dl = cadd(dl, cscale(cmul(cL, J), (double)recs[2 * p + kind].fl));
+    }
+    if (!isfinite(dl.x + dl.y + dt.x + dt.y)) raise_status(status, TAGS_ST_NONFINITE);
+    const long long bs = bstride * smp;
+    const long long lo = bs + k + (long long)m * i, up = bs + i + (long long)m * k;
+    float2 a = zl0[lo], b = zt0[lo];
+    a = make_float2(a.x + (float)dl.x, a.y + (float)dl.y);
+    b = make_float2(b.x + (float)dt.x, b.y + (float)dt.y);
+    zl0[lo] = a;
+    zt0[lo] = b;
+    if (k != i) {
+        zl0[up] = a;
+        zt0[up] = b;
+    }
+}
+
+__global__ void k_seg_dirs(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
+                           float4* __restrict__ sdir, float4* __restrict__ idir, float* __restrict__ selfv) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    Seg S;
+    ld_seg(elec + 11LL * i, S);
+    sdir[i] = make_float4((float)(S.b[0] - S.a[0]), (float)(S.b[1] - S.a[1]), (float)(S.b[2] - S.a[2]), (float)S.len);
+    selfv[i] = (float)self_integral_d(S);
+    if (has_img) {
+        ld_seg(img + 11LL * i, S);
+        idir[i] = make_float4((float)(S.b[0] - S.a[0]), (float)(S.b[1] - S.a[1]), (float)(S.b[2] - S.a[2]),
+                              (float)S.len);
+    } else {
+        idir[i] = sdir[i];
     }
 }
 
@@ -607,26 +736,84 @@ int tags_fill_tables_init() {
     return 0;
 }
 
-int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, uint16_t* d_codes,
-                          cudaStream_t st) {
+size_t tags_mixed_fill_workspace(int m) {
+    const size_t np = (size_t)m * (m + 1) / 2;
+    return np * 2 * (sizeof(uint16_t) + sizeof(PairRec)) + np * 2 * sizeof(int) + 2 * m * sizeof(float4) +
+           m * sizeof(float) + 4096 * sizeof(SampleF32) + 1024;
+}
+
+struct MixedFillWs {
+    uint16_t* codes;
+    PairRec* recs;
+    int* list;
+    int* nlist;
+    float4* sdir;
+    float4* idir;
+    float* selfv;
+    SampleF32* c32;
+};
+
+static MixedFillWs carve(void* ws, int m) {
+    const size_t np = (size_t)m * (m + 1) / 2;
+    char* b = reinterpret_cast<char*>(ws);
+    MixedFillWs w;
+    w.recs = reinterpret_cast<PairRec*>(b);
+    b += np * 2 * sizeof(PairRec);
+    w.sdir = reinterpret_cast<float4*>(b);
+    b += m * sizeof(float4);
+    w.idir = reinterpret_cast<float4*>(b);
+    b += m * sizeof(float4);
+    w.c32 = reinterpret_cast<SampleF32*>(b);
+    b += 4096 * sizeof(SampleF32);
+    w.list = reinterpret_cast<int*>(b);
+    b += np * 2 * sizeof(int);
+    w.selfv = reinterpret_cast<float*>(b);
+    b += ((m * sizeof(float) + 15) / 16) * 16;
+    w.nlist = reinterpret_cast<int*>(b);
+    b += 16;
+    w.codes = reinterpret_cast<uint16_t*>(b);
+    return w;
+}
+
+int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, void* ws, cudaStream_t st) {
+    MixedFillWs w = carve(ws, m);
     const long long npairs = (long long)m * (m + 1) / 2;
-    k_pair_plan<<<(unsigned)((npairs + 127) / 128), 128, 0, st>>>(d_elec, d_img, m, has_img, d_codes);
-    tags_note_launch();
+    TAGS_CUDA_OK(cudaMemsetAsync(w.nlist, 0, sizeof(int), st));
+    k_seg_dirs<<<(m + 127) / 128, 128, 0, st>>>(d_elec, d_img, m, has_img, w.sdir, w.idir, w.selfv);
+    k_pair_plan<<<(unsigned)((npairs + 127) / 128), 128, 0, st>>>(d_elec, d_img, m, has_img, w.codes, w.recs, w.nlist,
+                                                                 w.list);
+    tags_note_launch(2);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
 }
 
-int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, const uint16_t* d_codes,
-                           const SampleCoef* d_coef, int nsamp, const FillOut& out, int has_img, int* d_status,
-                           cudaStream_t st) {
+int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
+                           int nsamp, float2* d_zl, float2* d_zt, long long bstride, int has_img, int max_touch,
+                           int* d_status, cudaStream_t st) {
     if (m <= 0 || nsamp <= 0) return 0;
+    if (nsamp > 4096) return tags_fail_cuda(cudaErrorInvalidValue, "fill_mixed: batch above 4096", __FILE__, __LINE__);
+    MixedFillWs w = carve(ws, m);
     const long long npairs = (long long)m * (m + 1) / 2;
-    dim3 grid((unsigned)((npairs + 127) / 128), (unsigned)((nsamp + MIX_SG - 1) / MIX_SG));
     int pf = tags_prof_begin(TAGS_PROF_FILL_MIXED, st);
-    k_fill_mixed<<<grid, 128, 0, st>>>(d_elec, d_img, m, d_codes, d_coef, nsamp, out, has_img, d_status);
+    k_coef32<<<(nsamp + 127) / 128, 128, 0, st>>>(d_coef, nsamp, w.c32);
+    dim3 grid((unsigned)((npairs + 127) / 128), (unsigned)((nsamp + MIX_SG - 1) / MIX_SG));
+    k_fill_mixed<<<grid, 128, 0, st>>>(d_elec, d_img, w.sdir, w.idir, w.selfv, m, w.codes, w.recs, w.c32, nsamp, d_zl,
+                                       d_zt, bstride, has_img, d_status);
+    if (max_touch > 0) {
+        dim3 gt((unsigned)((max_touch + 127) / 128), (unsigned)nsamp);
+        k_fill_touch<<<gt, 128, 0, st>>>(d_elec, d_img, m, w.list, w.nlist, w.recs, d_coef, nsamp, d_zl, d_zt, bstride,
+                                         d_status);
+    }
     tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
-    tags_note_launch();
+    tags_note_launch(max_touch > 0 ? 3 : 2);
     TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+int tags_mixed_touch_count(void* ws, int m, cudaStream_t st, int* out) {
+    MixedFillWs w = carve(ws, m);
+    TAGS_CUDA_OK(cudaMemcpyAsync(out, w.nlist, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
     return 0;
 }
 

@@ -35,9 +35,7 @@
 namespace {
 
 constexpr int TB = 128;                 // panel width and tile edge
-constexpr int PLANE_BYTES = TB * TB * 2;        // one bf16 plane of a 128 x 128 tile: 32 KiB
-constexpr int KBLK_BYTES = TB * 64 * 2;         // 64-wide K block of a plane: 16 KiB
-constexpr int GEMM_SMEM = 6 * PLANE_BYTES + 1024 + 256;   // 4 A planes + 2 B slots + align + barriers
+constexpr int SMAX = 3;                 // most bf16 pieces per real value (split products)
 constexpr uint64_t WAIT_NS = 50ull * 1000 * 1000;   // 50 ms per wait
 
 // ---- PTX wrappers ----------------------------------------------------------------
@@ -138,210 +136,309 @@ TAGS_D uint32_t idesc_bf16(bool negate_a) {
     return d;
 }
 
-TAGS_D void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-    hi = __float2bfloat16_rn(x);
-    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+// x = p[0] + p[1] + ... + p[S-1] in bf16 pieces (each the rounded remainder)
+TAGS_D void split_n(float x, __nv_bfloat16* p, int S) {
+    float r = x;
+    for (int q = 0; q < S; ++q) {
+        p[q] = __float2bfloat16_rn(r);
+        r -= __bfloat162float(p[q]);
+    }
 }
 
 }  // namespace
 
 // ---- GEMM on the tensor cores ------------------------------------------------------
+//
+// C (128 x 128 tiles) op= A B^T for complex A, B given as split planes
+// [sample][2S][rows][128] bf16 (real pieces, then imaginary pieces). Persistent:
+// one CTA per SM walks the tile list. Warp 0 streams K blocks of 32 (64-byte
+// rows, 64-byte swizzle) of all planes of A and B through a ring of shared
+// stages with TMA; one thread of warp 1 issues the tcgen05.mma products into
+// one of two tensor-memory accumulator pairs (real, imaginary; 2 x 256
+// columns); warps 2..5 read the other pair back and do the epilogue, so the
+// memory-bound read-modify-write of C overlaps the products of the next tile.
+
+constexpr int BK = 32;                               // K elements per stage
+constexpr int KBLKS = TB / BK;                       // 4 stages per tile
+constexpr int PST = TB * BK * 2;                     // one plane in one stage: 8 KiB
+
+template <int S> struct GemmCfg {
+    static constexpr int NPL = 2 * S;                // planes per operand
+    static constexpr int STAGE = 2 * NPL * PST;      // A and B planes of one K block
+    static constexpr int STAGES = S == 2 ? 3 : 2;
+    static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
+};
+
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512
+// bytes apart (stride byte offset), descriptor version 1.
+TAGS_D uint64_t sdesc64(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(512 >> 4) << 32;           // stride byte offset
+    d |= (uint64_t)1 << 46;                    // version
+    d |= (uint64_t)4 << 61;                    // SWIZZLE_64B
+    return d;
+}
 
 struct GemmArgs {
     int M, Nn;                 // valid rows / columns of the output
     int mode;                  // 0: C -= A B^T into the FP32 matrix; 1: panel output (L21, planes)
     int tri;                   // tiles enumerate the lower triangle (I >= J)
+    int tiles;                 // tiles per sample
+    int nb;                    // samples
     float2* Amat;              // FP32 working matrices
     long long ld, mstride;
     int row0, col0;            // matrix coordinates of output element (0, 0)
     const float2* dinv;        // per sample 128 values (mode 1)
-    __nv_bfloat16* Lp;         // planes written in mode 1: [sample][4][R][128]
+    __nv_bfloat16* Lp;         // planes written in mode 1: [sample][2S][R][128]
     __nv_bfloat16* Wp;
     long long pstride;         // elements per sample of a plane buffer
     int R;                     // rows of a plane buffer
     int* err;
-    int zlo, zhi;              // output rows/cols in [zlo, zhi) are structurally zero (skip tiles inside)
+    int zlo, zhi;              // output rows/cols in [zlo, zhi) are structurally zero (tiles inside skipped)
 };
 
-__global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
+    smp = t / g.tiles;
+    int l = t - smp * g.tiles;
+    if (g.tri) {
+        I = (int)((sqrtf(8.0f * l + 1.0f) - 1.0f) * 0.5f);
+        while ((I + 1) * (I + 2) / 2 <= l) ++I;
+        while (I * (I + 1) / 2 > l) --I;
+        J = l - I * (I + 1) / 2;
+    } else {
+        I = l;
+        J = 0;
+    }
+    skip = false;
+    if (g.zhi > g.zlo) {
+        bool row_zero = TB * I >= g.zlo && TB * I + TB <= g.zhi;
+        bool col_zero = g.mode == 0 && TB * J >= g.zlo && TB * J + TB <= g.zhi;
+        skip = row_zero || col_zero;
+    }
+}
+
+template <int S>
+TAGS_D void split_pieces(float x, __nv_bfloat16* p) {
+    float r = x;
+#pragma unroll
+    for (int q = 0; q < S; ++q) {
+        p[q] = __float2bfloat16_rn(r);
+        r -= __bfloat162float(p[q]);
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
                                                     const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+    using C = GemmCfg<S>;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t base_u32 = (smem_u32(smem_raw) + 1023u) & ~1023u;
     uint8_t* base = smem_raw + (base_u32 - smem_u32(smem_raw));
-    const uint32_t sA = base_u32;                         // 4 planes: r_hi, r_lo, i_hi, i_lo
-    const uint32_t sB = base_u32 + 4 * PLANE_BYTES;       // 2 slots: real, imaginary
-    uint64_t* bars = reinterpret_cast<uint64_t*>(base + 6 * PLANE_BYTES);
-    uint32_t* tslot = reinterpret_cast<uint32_t*>(base + 6 * PLANE_BYTES + 64);
-    const uint32_t barA = smem_u32(&bars[0]), barB = smem_u32(&bars[1]), barM1 = smem_u32(&bars[2]);
-    const uint32_t barB2 = smem_u32(&bars[3]), barAcc = smem_u32(&bars[4]);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + C::STAGES * C::STAGE);
+    // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], drain
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * C::STAGES + 5);
+    auto full = [&](int s) { return smem_u32(&bars[s]); };
+    auto empty = [&](int s) { return smem_u32(&bars[C::STAGES + s]); };
+    auto tfull = [&](int a) { return smem_u32(&bars[2 * C::STAGES + a]); };
+    auto tempty = [&](int a) { return smem_u32(&bars[2 * C::STAGES + 2 + a]); };
+    const uint32_t drain = smem_u32(&bars[2 * C::STAGES + 4]);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int smp = blockIdx.y;
-    int I, J;
-    if (g.tri) {
-        int t = blockIdx.x;
-        I = (int)((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
-        while ((I + 1) * (I + 2) / 2 <= t) ++I;
-        while (I * (I + 1) / 2 > t) --I;
-        J = t - I * (I + 1) / 2;
-    } else {
-        I = blockIdx.x;
-        J = 0;
-    }
-    // tiles that lie entirely in the structurally zero band have nothing to do
-    if (g.zhi > g.zlo) {
-        const bool row_zero = TB * I >= g.zlo && TB * I + TB <= g.zhi;
-        const bool col_zero = g.mode == 0 && TB * J >= g.zlo && TB * J + TB <= g.zhi;
-        if (row_zero || col_zero) return;
-    }
+    const int total = g.tiles * g.nb;
     if (tid == 0) {
-        for (int q = 0; q < 5; ++q) mbar_init(smem_u32(&bars[q]), 1);
+        for (int q = 0; q < C::STAGES; ++q) {
+            mbar_init(full(q), 1);
+            mbar_init(empty(q), 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull(a), 1);
+            mbar_init(tempty(a), 4);
+        }
+        mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    if (warp == 1) tmem_alloc(smem_u32(tslot), 256);
+    if (warp == 1) tmem_alloc(smem_u32(tslot), 512);
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tslot;
-    bool ok = true;
 
-    const int rowA = TB * I, rowB = TB * J;
-    if (tid == 0) {
-        mbar_expect_tx(barA, 4 * PLANE_BYTES);
-        for (int p = 0; p < 4; ++p)
-            for (int kb = 0; kb < 2; ++kb)
-                tma_load_4d(sA + p * PLANE_BYTES + kb * KBLK_BYTES, &tmA, kb * 64, rowA, p, smp, barA);
-        mbar_expect_tx(barB, 2 * PLANE_BYTES);
-        for (int s = 0; s < 2; ++s)            // hi planes of B: real (0) and imaginary (2)
-            for (int kb = 0; kb < 2; ++kb)
-                tma_load_4d(sB + s * PLANE_BYTES + kb * KBLK_BYTES, &tmB, kb * 64, rowB, 2 * s, smp, barB);
-    }
-    const uint32_t accR = tmem, accI = tmem + 128;
-    const uint32_t idp = idesc_bf16(false), idn = idesc_bf16(true);
-    // one product over K = 128 (8 steps of 16): acc += sign * A_plane(pa) * B_slot(sb)^T
-    auto product = [&](uint32_t acc, int pa, int sb, bool neg, bool first) {
-        for (int kk = 0; kk < 8; ++kk) {
-            uint32_t off = (kk >> 2) * KBLK_BYTES + (kk & 3) * 32;
-            mma_bf16(acc, sdesc(sA + pa * PLANE_BYTES + off), sdesc(sB + sb * PLANE_BYTES + off), neg ? idn : idp,
-                     (first && kk == 0) ? 0u : 1u);
-        }
-    };
-    if (tid == 32) {
-        ok = mbar_wait(barA, 0, g.err) && mbar_wait(barB, 0, g.err);
-        if (ok) {
-            tc_fence_after();
-            // B slots hold the hi planes: slot 0 = Br_hi, slot 1 = Bi_hi
-            product(accR, 0, 0, false, true);   // Ar_hi Br_hi
-            product(accR, 1, 0, false, false);  // Ar_lo Br_hi
-            product(accR, 2, 1, true, false);   // -Ai_hi Bi_hi
-            product(accR, 3, 1, true, false);   // -Ai_lo Bi_hi
-            product(accI, 0, 1, false, true);   // Ar_hi Bi_hi
-            product(accI, 1, 1, false, false);  // Ar_lo Bi_hi
-            product(accI, 2, 0, false, false);  // Ai_hi Br_hi
-            product(accI, 3, 0, false, false);  // Ai_lo Br_hi
-        }
-        mma_commit(barM1);
-    }
-    if (tid == 0) {
-        // the lo planes of B replace the hi planes once the first products are done
-        if (mbar_wait(barM1, 0, g.err)) {
-            mbar_expect_tx(barB2, 2 * PLANE_BYTES);
-            for (int s = 0; s < 2; ++s)
-                for (int kb = 0; kb < 2; ++kb)
-                    tma_load_4d(sB + s * PLANE_BYTES + kb * KBLK_BYTES, &tmB, kb * 64, rowB, 2 * s + 1, smp, barB2);
-        } else {
-            ok = false;
-            atomicOr(g.err, 1);
-            mbar_expect_tx(barB2, 0);   // release the waiter below
-        }
-    }
-    if (tid == 32) {
-        bool ok2 = ok && mbar_wait(barB2, 0, g.err);
-        if (ok2) {
-            tc_fence_after();
-            product(accR, 0, 0, false, false);  // Ar_hi Br_lo
-            product(accR, 2, 1, true, false);   // -Ai_hi Bi_lo
-            product(accI, 0, 1, false, false);  // Ar_hi Bi_lo
-            product(accI, 2, 0, false, false);  // Ai_hi Br_lo
-        } else {
-            ok = false;
-            atomicOr(g.err, 2);
-        }
-        mma_commit(barAcc);
-    }
-    // ---- epilogue: all four warps, warp w owns tensor-memory lanes 32w..32w+31
-    bool acc_ok = mbar_wait(barAcc, 0, g.err);
-    if (!acc_ok) {
-        atomicOr(g.err, 4);
-        // let the copies and products already issued land before tensor
-        // memory and shared memory are released
-        if (tid == 0) {
-            const uint64_t t0 = globaltimer_ns();
-            for (int q = 0; q < 5; ++q) {
-                uint32_t okq = 0;
-                while (!okq && globaltimer_ns() - t0 < WAIT_NS) {
-                    asm volatile(
-                        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                        : "=r"(okq)
-                        : "r"(smem_u32(&bars[q])), "r"(0u)
-                        : "memory");
+    if (warp == 0) {
+        // ---- producer: TMA loads of A and B planes, one K block per stage
+        if (lane == 0) {
+            int stage = 0;
+            uint32_t phase = 0;
+            bool alive = true;
+            int issued[4] = {0, 0, 0, 0};     // stages with a load whose completion nobody waited for yet
+            for (int t = blockIdx.x; t < total && alive; t += gridDim.x) {
+                int smp, I, J;
+                bool skip;
+                tile_of(g, t, smp, I, J, skip);
+                if (skip) continue;
+                for (int kb = 0; kb < KBLKS; ++kb) {
+                    if (!mbar_wait(empty(stage), phase ^ 1, g.err)) { alive = false; break; }
+                    issued[stage] = 0;
+                    const uint32_t sb = base_u32 + stage * C::STAGE;
+                    mbar_expect_tx(full(stage), C::STAGE);
+                    for (int p = 0; p < C::NPL; ++p) {
+                        tma_load_4d(sb + p * PST, &tmA, kb * BK, TB * I, p, smp, full(stage));
+                        tma_load_4d(sb + (C::NPL + p) * PST, &tmB, kb * BK, TB * J, p, smp, full(stage));
+                    }
+                    issued[stage] = 1;
+                    if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
                 }
             }
-        }
-    }
-    tc_fence_after();
-    if (acc_ok) {
-        const int r = 32 * warp + lane;          // row within the tile
-        const int gr = TB * I + r;               // row within the output
-        const uint32_t lane_off = (uint32_t)(32 * warp) << 16;
-        for (int cc = 0; cc < TB / 16; ++cc) {
-            float vr[16], vi[16];
-            tmem_ld16(accR + lane_off + cc * 16, vr);
-            tmem_ld16(accI + lane_off + cc * 16, vi);
-            if (gr >= g.M) continue;
-            if (g.mode == 0) {
-                float2* Cb = g.Amat + g.mstride * smp;
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int gc = TB * J + cc * 16 + j;
-                    if (gc < g.Nn) {
-                        float2* p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + gc);
-                        float2 v = *p;
-                        v.x -= vr[j];
-                        v.y -= vi[j];
-                        *p = v;
+            if (!alive) {
+                // let the copies in flight land before the CTA exits
+                const uint64_t t0 = globaltimer_ns();
+                for (int q = 0; q < C::STAGES; ++q) {
+                    if (!issued[q]) continue;
+                    uint32_t okq = 0;
+                    while (!okq && globaltimer_ns() - t0 < WAIT_NS) {
+                        asm volatile(
+                            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                            : "=r"(okq)
+                            : "r"(full(q)), "r"(0u)
+                            : "memory");
+                        if (!okq)
+                            asm volatile(
+                                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                                : "=r"(okq)
+                                : "r"(full(q)), "r"(1u)
+                                : "memory");
                     }
                 }
-            } else {
-                float2* Cb = g.Amat + g.mstride * smp;
-                const float2* dv = g.dinv + (long long)TB * smp;
-                __align__(16) __nv_bfloat16 lp[4][16], wp[4][16];
-#pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int c = cc * 16 + j;
-                    float2 w = make_float2(vr[j], vi[j]);
-                    float2 d = dv[c];
-                    float2 l = fmulc(w, d);
-                    if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = l;
-                    split_bf16(l.x, lp[0][j], lp[1][j]);
-                    split_bf16(l.y, lp[2][j], lp[3][j]);
-                    split_bf16(w.x, wp[0][j], wp[1][j]);
-                    split_bf16(w.y, wp[2][j], wp[3][j]);
+            }
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer
+        if (lane == 0) {
+            const uint32_t idp = idesc_bf16(false), idn = idesc_bf16(true);
+            int stage = 0, acc = 0;
+            uint32_t phase = 0, aphase = 0;
+            bool alive = true;
+            for (int t = blockIdx.x; t < total && alive; t += gridDim.x) {
+                int smp, I, J;
+                bool skip;
+                tile_of(g, t, smp, I, J, skip);
+                if (skip) continue;
+                if (!mbar_wait(tempty(acc), aphase ^ 1, g.err)) { alive = false; break; }
+                tc_fence_after();
+                const uint32_t accR = tmem + acc * 256, accI = accR + 128;
+                for (int kb = 0; kb < KBLKS && alive; ++kb) {
+                    if (!mbar_wait(full(stage), phase, g.err)) { alive = false; break; }
+                    tc_fence_after();
+                    const uint32_t sa = base_u32 + stage * C::STAGE, sbb = sa + C::NPL * PST;
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        const uint32_t off = kk * 32;
+                        bool firstR = kb == 0 && kk == 0, firstI = firstR;
+                        // terms (i, j) with i + j < S of the split product
+                        for (int i = 0; i < S; ++i) {
+                            for (int j = 0; i + j < S; ++j) {
+                                const uint64_t ar = sdesc64(sa + i * PST + off), ai = sdesc64(sa + (S + i) * PST + off);
+                                const uint64_t br = sdesc64(sbb + j * PST + off), bi = sdesc64(sbb + (S + j) * PST + off);
+                                mma_bf16(accR, ar, br, idp, firstR ? 0u : 1u);   // + Ar Br
+                                firstR = false;
+                                mma_bf16(accR, ai, bi, idn, 1u);                 // - Ai Bi
+                                mma_bf16(accI, ar, bi, idp, firstI ? 0u : 1u);   // + Ar Bi
+                                firstI = false;
+                                mma_bf16(accI, ai, br, idp, 1u);                 // + Ai Br
+                            }
+                        }
+                    }
+                    mma_commit(empty(stage));          // stage reusable once these products are done
+                    if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
                 }
-                const long long rowoff = (long long)gr * TB + cc * 16;
+                if (!alive) break;
+                mma_commit(tfull(acc));                // accumulator pair ready for the epilogue
+                if (++acc == 2) { acc = 0; aphase ^= 1; }
+            }
+            // every product issued is complete before tensor memory is released
+            mma_commit(drain);
+            const uint64_t t0 = globaltimer_ns();
+            uint32_t okd = 0;
+            while (!okd && globaltimer_ns() - t0 < WAIT_NS) {
+                asm volatile(
+                    "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                    : "=r"(okd)
+                    : "r"(drain), "r"(0u)
+                    : "memory");
+            }
+        }
+    } else {
+        // ---- epilogue warps 2..5: tensor-memory lanes 32 (warp % 4) ...
+        const int quarter = warp & 3;
+        const int r = 32 * quarter + lane;
+        const uint32_t lane_off = (uint32_t)(32 * quarter) << 16;
+        int acc = 0;
+        uint32_t aphase = 0;
+        for (int t = blockIdx.x; t < total; t += gridDim.x) {
+            int smp, I, J;
+            bool skip;
+            tile_of(g, t, smp, I, J, skip);
+            if (skip) continue;
+            if (!mbar_wait(tfull(acc), aphase, g.err)) break;
+            tc_fence_after();
+            const uint32_t accR = tmem + acc * 256, accI = accR + 128;
+            const int gr = TB * I + r;
+            float2* Cb = g.Amat + g.mstride * smp;
+            for (int cc = 0; cc < TB / 16; ++cc) {
+                float vr[16], vi[16];
+                tmem_ld16(accR + lane_off + cc * 16, vr);
+                tmem_ld16(accI + lane_off + cc * 16, vi);
+                if (gr >= g.M) continue;
+                if (g.mode == 0) {
 #pragma unroll
-                for (int p = 0; p < 4; ++p) {
-                    uint4* dl = reinterpret_cast<uint4*>(g.Lp + g.pstride * smp + (long long)p * g.R * TB + rowoff);
-                    uint4* dw = reinterpret_cast<uint4*>(g.Wp + g.pstride * smp + (long long)p * g.R * TB + rowoff);
-                    dl[0] = reinterpret_cast<const uint4*>(lp[p])[0];
-                    dl[1] = reinterpret_cast<const uint4*>(lp[p])[1];
-                    dw[0] = reinterpret_cast<const uint4*>(wp[p])[0];
-                    dw[1] = reinterpret_cast<const uint4*>(wp[p])[1];
+                    for (int j = 0; j < 16; ++j) {
+                        const int gc = TB * J + cc * 16 + j;
+                        if (gc < g.Nn) {
+                            float2* p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + gc);
+                            float2 v = *p;
+                            v.x -= vr[j];
+                            v.y -= vi[j];
+                            *p = v;
+                        }
+                    }
+                } else {
+                    const float2* dv = g.dinv + (long long)TB * smp;
+                    __align__(16) __nv_bfloat16 lp[2 * S][16], wp[2 * S][16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int c = cc * 16 + j;
+                        float2 w = make_float2(vr[j], vi[j]);
+                        float2 l = fmulc(w, dv[c]);
+                        if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = l;
+                        __nv_bfloat16 pc[S];
+                        split_pieces<S>(l.x, pc);
+                        for (int q = 0; q < S; ++q) lp[q][j] = pc[q];
+                        split_pieces<S>(l.y, pc);
+                        for (int q = 0; q < S; ++q) lp[S + q][j] = pc[q];
+                        split_pieces<S>(w.x, pc);
+                        for (int q = 0; q < S; ++q) wp[q][j] = pc[q];
+                        split_pieces<S>(w.y, pc);
+                        for (int q = 0; q < S; ++q) wp[S + q][j] = pc[q];
+                    }
+                    const long long rowoff = (long long)gr * TB + cc * 16;
+#pragma unroll
+                    for (int p = 0; p < 2 * S; ++p) {
+                        uint4* dl = reinterpret_cast<uint4*>(g.Lp + g.pstride * smp + (long long)p * g.R * TB + rowoff);
+                        uint4* dw = reinterpret_cast<uint4*>(g.Wp + g.pstride * smp + (long long)p * g.R * TB + rowoff);
+                        dl[0] = reinterpret_cast<const uint4*>(lp[p])[0];
+                        dl[1] = reinterpret_cast<const uint4*>(lp[p])[1];
+                        dw[0] = reinterpret_cast<const uint4*>(wp[p])[0];
+                        dw[1] = reinterpret_cast<const uint4*>(wp[p])[1];
+                    }
                 }
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty(acc)) : "memory");
+            if (++acc == 2) { acc = 0; aphase ^= 1; }
         }
     }
     tc_fence_before();
     __syncthreads();
-    if (warp == 1) tmem_dealloc(tmem, 256);
+    if (warp == 1) tmem_dealloc(tmem, 512);
 }
 
 // ---- diagonal block: LDL^T, L11^{-1} -------------------------------------------------
@@ -350,7 +447,7 @@ __global__ void __launch_bounds__(128, 1) k_gemm_tc(const __grid_constant__ CUte
 __global__ void __launch_bounds__(512) k_ldl_diag(float2* __restrict__ A0, long long ld, long long mstride, int j0,
                                                   int jb, __nv_bfloat16* __restrict__ linv_planes,
                                                   float2* __restrict__ dinv, int* __restrict__ info,
-                                                  float2* __restrict__ linv32, long long lstride) {
+                                                  float2* __restrict__ linv32, long long lstride, int NS) {
     extern __shared__ __align__(16) float2 S[];        // S[c * TB + r]
     __shared__ float2 colv[TB];
     const int smp = blockIdx.x, tid = threadIdx.x;
@@ -415,19 +512,23 @@ __global__ void __launch_bounds__(512) k_ldl_diag(float2* __restrict__ A0, long 
         }
         __syncthreads();
     }
-    // L11^{-1} kept in FP32 (row-major, zero outside jb) for the triangular solves
-    float2* X32 = linv32 + lstride * smp + (long long)(j0 / TB) * TB * TB;
+    // L11^{-1} kept in FP32 for the triangular solves, row-major, zero outside
+    // jb: the inverse itself and its transpose (both read row-wise there)
+    float2* X32 = linv32 + lstride * smp + (long long)(j0 / TB) * 2 * TB * TB;
     for (int t = tid; t < TB * TB; t += blockDim.x) {
         int nrow = t / TB, k = t % TB;
-        float2 v = make_float2(0.f, 0.f);
+        float2 v = make_float2(0.f, 0.f), vt = make_float2(0.f, 0.f);
         if (nrow < jb && k < jb) {
-            if (k == nrow) v = make_float2(1.f, 0.f);
+            if (k == nrow) v = vt = make_float2(1.f, 0.f);
             else if (k < nrow) v = S[k * TB + nrow];
+            else vt = S[nrow * TB + k];
         }
         X32[t] = v;
+        X32[TB * TB + t] = vt;
     }
-    // L11^{-1} as split planes, row-major: B[n][k] = X[n][k] (k <= n), rows/cols >= jb zero
-    __nv_bfloat16* P = linv_planes + (long long)smp * 4 * TB * TB;
+    // L11^{-1} as split planes (NS pieces of the real part, then of the
+    // imaginary part), row-major: B[n][k] = X[n][k] (k <= n), zero outside jb
+    __nv_bfloat16* P = linv_planes + (long long)smp * 2 * SMAX * TB * TB;   // sample stride of the tensor map
     for (int t = tid; t < TB * TB; t += blockDim.x) {
         int nrow = t / TB, k = t % TB;
         float2 v = make_float2(0.f, 0.f);
@@ -435,21 +536,19 @@ __global__ void __launch_bounds__(512) k_ldl_diag(float2* __restrict__ A0, long 
             if (k == nrow) v = make_float2(1.f, 0.f);
             else if (k < nrow) v = S[k * TB + nrow];
         }
-        __nv_bfloat16 h, l;
-        split_bf16(v.x, h, l);
-        P[0 * TB * TB + t] = h;
-        P[1 * TB * TB + t] = l;
-        split_bf16(v.y, h, l);
-        P[2 * TB * TB + t] = h;
-        P[3 * TB * TB + t] = l;
+        __nv_bfloat16 pc[SMAX];
+        split_n(v.x, pc, NS);
+        for (int q = 0; q < NS; ++q) P[(long long)q * TB * TB + t] = pc[q];
+        split_n(v.y, pc, NS);
+        for (int q = 0; q < NS; ++q) P[(long long)(NS + q) * TB * TB + t] = pc[q];
     }
 }
 
 // A21 (rows j0+jb .. j0+jb+M, columns j0 .. j0+jb) -> split planes, row-major
-// [sample][4][R][128], columns >= jb zero. Tile: 32 rows x 128 columns.
+// [sample][2 NS][R][128], columns >= jb zero. Tile: 32 rows x 128 columns.
 __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__ A0, long long ld, long long mstride,
                                                       int j0, int jb, int M, __nv_bfloat16* __restrict__ planes,
-                                                      long long pstride, int R) {
+                                                      long long pstride, int R, int NS) {
     __shared__ float2 t[TB][33];
     const int smp = blockIdx.y, r0 = blockIdx.x * 32;
     const float2* A = A0 + mstride * smp;
@@ -465,37 +564,40 @@ __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__
         int c = q % TB, rr = q / TB;
         if (r0 + rr >= M) continue;
         float2 v = t[c][rr];
-        __nv_bfloat16 h, l;
         long long o = (long long)(r0 + rr) * TB + c;
-        split_bf16(v.x, h, l);
-        P[o] = h;
-        P[(long long)R * TB + o] = l;
-        split_bf16(v.y, h, l);
-        P[2LL * R * TB + o] = h;
-        P[3LL * R * TB + o] = l;
+        __nv_bfloat16 pc[SMAX];
+        split_n(v.x, pc, NS);
+        for (int q = 0; q < NS; ++q) P[(long long)q * R * TB + o] = pc[q];
+        split_n(v.y, pc, NS);
+        for (int q = 0; q < NS; ++q) P[(long long)(NS + q) * R * TB + o] = pc[q];
     }
 }
 
 // ---- solves with the factors: L D L^T x = b (one right-hand side per sample) ----------
 
-// z_b = Linv_b * r_b for block b (128 rows); one CTA of 128 threads per sample.
-// transpose = 1 applies Linv_b^T instead.
-__global__ void __launch_bounds__(128) k_blk_inv_apply(const float2* __restrict__ linv32, long long lstride, int blk,
+// z_b = Linv_b * r_b for block b (128 rows), or Linv_b^T * r_b with
+// transpose = 1; one CTA of 256 threads per sample, a warp per output row,
+// lanes over the row (coalesced).
+__global__ void __launch_bounds__(256) k_blk_inv_apply(const float2* __restrict__ linv32, long long lstride, int blk,
                                                        int jb, float2* __restrict__ x0, long long xstride,
                                                        int transpose) {
     __shared__ float2 v[TB];
-    const int smp = blockIdx.x, r = threadIdx.x;
+    const int smp = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     float2* x = x0 + xstride * smp + (long long)blk * TB;
-    const float2* Li = linv32 + lstride * smp + (long long)blk * TB * TB;
-    v[r] = r < jb ? x[r] : make_float2(0.f, 0.f);
+    const float2* Li = linv32 + lstride * smp + (long long)blk * 2 * TB * TB + (transpose ? TB * TB : 0);
+    if (tid < TB) v[tid] = tid < jb ? x[tid] : make_float2(0.f, 0.f);
     __syncthreads();
-    float2 acc = make_float2(0.f, 0.f);
-    if (!transpose) {
-        for (int k = 0; k <= r; ++k) acc = ffmac(Li[r * TB + k], v[k], acc);
-    } else {
-        for (int k = r; k < TB; ++k) acc = ffmac(Li[k * TB + r], v[k], acc);
+    for (int r = warp; r < jb; r += 8) {
+        const float2* row = Li + (long long)r * TB;
+        float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = lane; k < TB; k += 32) acc = ffmac(row[k], v[k], acc);
+        for (int o = 16; o > 0; o >>= 1) {
+            acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+            acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+        }
+        if (lane == 0) x[r] = acc;
     }
-    if (r < jb) x[r] = acc;
 }
 
 // forward: x[i] -= sum_{k in block} L[i][k] x[k] for rows i below the block
@@ -512,19 +614,24 @@ __global__ void k_blk_fwd_update(const float2* __restrict__ A0, long long ld, lo
     x[i] = fsub(x[i], acc);
 }
 
-// backward (L^T): x[r] -= sum_{c in block} L[c][r] x[c] for rows r above the block
-__global__ void k_blk_bwd_update(const float2* __restrict__ A0, long long ld, long long mstride, int j0, int jb,
-                                 float2* __restrict__ x0, long long xstride, int zl_m) {
+// backward (L^T): x[r] -= sum_{c in block} L[c][r] x[c] for rows r above the
+// block; a warp per r, lanes over the block's rows of column r (coalesced).
+__global__ void __launch_bounds__(256) k_blk_bwd_update(const float2* __restrict__ A0, long long ld, long long mstride,
+                                                        int j0, int jb, float2* __restrict__ x0, long long xstride,
+                                                        int zl_m) {
     const int smp = blockIdx.y;
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int r = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (r >= j0) return;
     if (j0 >= zl_m && j0 + jb <= 2 * zl_m && r < zl_m) return;       // L[ZT rows, ZL cols] = 0
-    const float2* A = A0 + mstride * smp;
+    const float2* col = A0 + mstride * smp + ld * (long long)r + j0;
     float2* x = x0 + xstride * smp;
     float2 acc = make_float2(0.f, 0.f);
-    const float2* col = A + ld * (long long)r;
-    for (int c = 0; c < jb; ++c) acc = ffmac(col[j0 + c], x[j0 + c], acc);
-    x[r] = fsub(x[r], acc);
+    for (int c = lane; c < jb; c += 32) acc = ffmac(col[c], x[j0 + c], acc);
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) x[r] = fsub(x[r], acc);
 }
 
 // x[i] /= D[i] (D on the diagonal of the factored matrix)
@@ -560,16 +667,17 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 4-D map over planes [sample][4][rows][128] bf16, box {64, 128, 1, 1}.
-int make_plane_map(CUtensorMap* map, void* base, int rows, int samples) {
+// 4-D map over planes [sample][nplanes][rows][128] bf16, box {32, 128, 1, 1}
+// (64-byte rows, 64-byte swizzle: the K block of one pipeline stage).
+int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samples) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
-    cuuint64_t dims[4] = {(cuuint64_t)TB, (cuuint64_t)rows, 4, (cuuint64_t)samples};
-    cuuint64_t strides[3] = {(cuuint64_t)TB * 2, (cuuint64_t)TB * 2 * rows, (cuuint64_t)TB * 2 * rows * 4};
-    cuuint32_t box[4] = {64, (cuuint32_t)TB, 1, 1};
+    cuuint64_t dims[4] = {(cuuint64_t)TB, (cuuint64_t)rows, (cuuint64_t)nplanes, (cuuint64_t)samples};
+    cuuint64_t strides[3] = {(cuuint64_t)TB * 2, (cuuint64_t)TB * 2 * rows, (cuuint64_t)TB * 2 * rows * nplanes};
+    cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)TB, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, base, dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         char msg[96];
@@ -581,21 +689,49 @@ int make_plane_map(CUtensorMap* map, void* base, int rows, int samples) {
 
 }  // namespace
 
-static long long linv32_stride(int N) { return (long long)((N + TB - 1) / TB) * TB * TB; }
+static long long linv32_stride(int N) { return (long long)((N + TB - 1) / TB) * 2 * TB * TB; }
+
+// Workspace layout (sized for SMAX pieces): A21 planes, L planes, W planes
+// (2 SMAX planes of N x 128 each per sample), L11^{-1} planes, D^{-1}, FP32
+// inverses of all diagonal blocks (and their transposes).
+static long long plane_stride(int N) { return (long long)2 * SMAX * N * TB; }
 
 size_t tags_ldl_tc_workspace(int N, int batch) {
-    // A21 planes, L planes, W planes (R = N rows each), L11^{-1} planes, D^{-1},
-    // FP32 inverses of all diagonal blocks
-    size_t plane = (size_t)4 * N * TB * 2;
-    return (size_t)batch * (3 * plane + (size_t)4 * TB * TB * 2 + TB * sizeof(float2) +
+    size_t plane = (size_t)plane_stride(N) * 2;
+    return (size_t)batch * (3 * plane + (size_t)2 * SMAX * TB * TB * 2 + TB * sizeof(float2) +
                             (size_t)linv32_stride(N) * sizeof(float2)) + 1024;
 }
 
 static float2* linv32_of(void* ws, int N, int batch_cap) {
-    const long long pstride = (long long)4 * N * TB;
+    const long long pstride = plane_stride(N);
     __nv_bfloat16* Lin = reinterpret_cast<__nv_bfloat16*>(ws) + 3 * pstride * batch_cap;
-    float2* dinv = reinterpret_cast<float2*>(Lin + (long long)4 * TB * TB * batch_cap);
+    float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     return dinv + (long long)TB * batch_cap;
+}
+
+static int num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 132;
+    }
+    return n;
+}
+
+template <int S>
+static int launch_gemm(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
+    static bool attr = false;
+    if (!attr) {
+        TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<S>::SMEM));
+        attr = true;
+    }
+    const int total = g.tiles * g.nb;
+    const int grid = total < num_sms() ? total : num_sms();
+    if (grid <= 0) return 0;
+    k_gemm_tc<S><<<grid, 192, GemmCfg<S>::SMEM, st>>>(mA, mB, g);
+    tags_note_launch();
+    return 0;
 }
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
@@ -606,7 +742,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     int pf = tags_prof_begin(TAGS_PROF_LDL_SOLVE, st);
     for (int b = 0; b < nblk; ++b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, TB, 0, st>>>(L32, ls, b, jb, x, xstride, 0);
+        k_blk_inv_apply<<<nb, 256, 0, st>>>(L32, ls, b, jb, x, xstride, 0);
         const int rest = N - j0 - jb;
         if (rest > 0) k_blk_fwd_update<<<dim3((rest + 127) / 128, nb), 128, 0, st>>>(A, ld, mstride, N, j0, jb, x, xstride, zl_m);
         tags_note_launch(rest > 0 ? 2 : 1);
@@ -615,8 +751,8 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     tags_note_launch();
     for (int b = nblk - 1; b >= 0; --b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, TB, 0, st>>>(L32, ls, b, jb, x, xstride, 1);
-        if (j0 > 0) k_blk_bwd_update<<<dim3((j0 + 127) / 128, nb), 128, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m);
+        k_blk_inv_apply<<<nb, 256, 0, st>>>(L32, ls, b, jb, x, xstride, 1);
+        if (j0 > 0) k_blk_bwd_update<<<dim3((j0 + 7) / 8, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m);
         tags_note_launch(j0 > 0 ? 2 : 1);
     }
     // two triangular sweeps over the factor: 8 N^2 real flops, 8 N^2 bytes read
@@ -628,38 +764,42 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
 // LDL^T of `nb` matrices A (N x N complex FP32, column-major, lower triangle
 // used) in place: L strictly below the diagonal, D on it.
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
-                int* err, int zl_m, cudaStream_t st) {
+                int* err, int zl_m, int pieces, cudaStream_t st) {
     static bool attr_done = false;
     if (!attr_done) {
-        TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
         TAGS_CUDA_OK(cudaFuncSetAttribute(k_ldl_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                           (int)(TB * TB * sizeof(float2))));
         attr_done = true;
     }
-    const long long pstride = (long long)4 * N * TB;
+    const int NS = pieces == 3 ? 3 : 2;
+    // planes of this run use 2 NS of the 2 SMAX slots of each sample
+    const long long pstride = plane_stride(N);
     __nv_bfloat16* A21p = reinterpret_cast<__nv_bfloat16*>(ws);
     __nv_bfloat16* Lp = A21p + pstride * batch_cap;
     __nv_bfloat16* Wp = Lp + pstride * batch_cap;
     __nv_bfloat16* Lin = Wp + pstride * batch_cap;
-    float2* dinv = reinterpret_cast<float2*>(Lin + (long long)4 * TB * TB * batch_cap);
+    float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
+    // the maps see a sample stride of 2 SMAX planes: declare that many planes
     CUtensorMap mA21, mL, mW, mLin;
-    int e = make_plane_map(&mA21, A21p, N, batch_cap);
-    if (!e) e = make_plane_map(&mL, Lp, N, batch_cap);
-    if (!e) e = make_plane_map(&mW, Wp, N, batch_cap);
-    if (!e) e = make_plane_map(&mLin, Lin, TB, batch_cap);
+    int e = make_plane_map(&mA21, A21p, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mL, Lp, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mW, Wp, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mLin, Lin, TB, 2 * SMAX, batch_cap);
     if (e) return e;
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * nb, st));
     for (int j0 = 0; j0 < N; j0 += TB) {
         const int jb = N - j0 < TB ? N - j0 : TB;
         const int rest = N - j0 - jb;
         int pf = tags_prof_begin(TAGS_PROF_LDL_DIAG, st);
-        k_ldl_diag<<<nb, 512, TB * TB * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, info, L32, ls);
+        k_ldl_diag<<<nb, 512, TB * TB * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, info, L32, ls,
+                                                              NS);
         tags_prof_end(TAGS_PROF_LDL_DIAG, pf, st, 4.0 / 3.0 * jb * (double)jb * jb * nb, 16.0 * jb * jb * nb);
         tags_note_launch();
         if (rest <= 0) break;
-        k_panel_planes<<<dim3((rest + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, rest, A21p, pstride, N);
+        k_panel_planes<<<dim3((rest + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, rest, A21p, pstride, N,
+                                                                   NS);
         tags_note_launch();
         const int T = (rest + TB - 1) / TB;
         GemmArgs g{};
@@ -674,6 +814,8 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.Nn = jb;
         g.mode = 1;
         g.tri = 0;
+        g.tiles = T;
+        g.nb = nb;
         g.Amat = A;
         g.ld = ld;
         g.mstride = mstride;
@@ -686,23 +828,24 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.R = N;
         g.err = err;
         pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
-        k_gemm_tc<<<dim3(T, nb), 128, GEMM_SMEM, st>>>(mA21, mLin, g);
+        e = NS == 3 ? launch_gemm<3>(mA21, mLin, g, st) : launch_gemm<2>(mA21, mLin, g, st);
+        if (e) return e;
         // triangular solve: rest x jb unknowns against jb x jb, 4 rest jb^2 real flops
         tags_prof_end(TAGS_PROF_LDL_PANEL, pf, st, 4.0 * rest * (double)jb * jb * nb,
                       (8.0 * rest * jb + 16.0 * rest * 128 * 2) * nb);
-        tags_note_launch();
         g.mode = 0;
         g.tri = 1;
+        g.tiles = T * (T + 1) / 2;
         g.Nn = rest;
         g.row0 = j0 + jb;
         g.col0 = j0 + jb;
         pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
-        k_gemm_tc<<<dim3(T * (T + 1) / 2, nb), 128, GEMM_SMEM, st>>>(mL, mW, g);
+        e = NS == 3 ? launch_gemm<3>(mL, mW, g, st) : launch_gemm<2>(mL, mW, g, st);
+        if (e) return e;
         // symmetric rank-jb update of the lower triangle: 8 jb rest(rest+1)/2 real flops;
         // bytes: read + write of that triangle in complex FP32, two panels of split planes
         tags_prof_end(TAGS_PROF_LDL_TRAIL, pf, st, 8.0 * jb * (0.5 * rest * (rest + 1.0)) * nb,
-                      (16.0 * 0.5 * rest * (rest + 1.0) + 2.0 * rest * 128 * 8) * nb);
-        tags_note_launch();
+                      (16.0 * 0.5 * rest * (rest + 1.0) + 2.0 * rest * 128 * 4.0 * NS) * nb);
     }
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
@@ -710,7 +853,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
 
 // ---- diagnostic entry point (declared in include/tags_gpu.h) ------------------------
 
-extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb) {
+extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
     if (!a || N <= 0 || nb <= 0) return tags_fail(TAGS_E_ARG, "tags_debug_ldl: invalid argument");
     DeviceCtx* c = tags_ctx();
     if (!c) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
@@ -733,7 +876,7 @@ extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb) {
         cudaMemcpyAsync(A, hf.data(), sizeof(float2) * NN * nb, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(ws, 0, wsb, st);
         cudaMemsetAsync(err, 0, sizeof(int), st);
-        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, 0, st);
+        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, 0, pieces, st);
     }
     int herr = 0;
     std::vector<int> hinfo(nb, 0);

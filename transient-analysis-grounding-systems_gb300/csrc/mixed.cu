@@ -5,8 +5,10 @@
 //           [ A  -ZL   0   ]
 //           [ B   0   -ZT  ]
 // solved here as follows:
-//   0. impedance blocks: regular pairs in FP32 around FP64 anchors, pairs
-//      sharing an endpoint (log-singular) in FP64, diagonal closed form;
+//   0. impedance blocks: regular pairs in FP32 (anchors from two-float
+//      products), pairs sharing an endpoint (log-singular) in FP64, the
+//      diagonal in its closed form; stored as complex FP32, which is the
+//      matrix the refinement solves (its entries carry the fill's ~1e-7 error);
 //   1. static symmetric ordering P: ZL rows, ZT rows, then node rows, so that
 //      the elimination meets the impedance blocks (large diagonals) before the
 //      zero Y_E block and needs no pivot search;
@@ -38,16 +40,17 @@ TAGS_D void atomic_max_nonneg(double* addr, double v) {
 
 // Row maxima (and row sums) of the impedance blocks: Z is symmetric, so row k
 // equals column k (contiguous). One warp per (row, block, sample).
-__global__ void k_rowstats(const double2* __restrict__ Z, int m, double* __restrict__ scale, double* __restrict__ rsum,
+__global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restrict__ scale, double* __restrict__ rsum,
                            int N) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     int blk = blockIdx.y;       // 0 = ZL, 1 = ZT
     int b = blockIdx.z;
     if (warp >= m) return;
-    const double2* col = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m + (size_t)m * warp;
+    const float2* col = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m + (size_t)m * warp;
     double mx = 0.0, sm = 0.0;
     for (int j = lane; j < m; j += 32) {
-        double a = sqrt(cabs2(col[j]));
+        float2 z = col[j];
+        double a = sqrtf(z.x * z.x + z.y * z.y);
         mx = fmax(mx, a);
         sm += a;
     }
@@ -75,7 +78,7 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 }
 
 // W'' (complex FP32, column-major N x N, reordered and scaled), lower triangle.
-__global__ void k_build(const double2* __restrict__ Z, const signed char* __restrict__ cond, const double* __restrict__ scale,
+__global__ void k_build(const float2* __restrict__ Z, const signed char* __restrict__ cond, const double* __restrict__ scale,
                         int m, int n, float2* __restrict__ A) {
     const int N = n + 2 * m;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -84,14 +87,14 @@ __global__ void k_build(const double2* __restrict__ Z, const signed char* __rest
     int i = (int)(t % N), j = (int)(t / N);
     if (i < j) return;              // the LDL^T reads the lower triangle only
     const double* d = scale + (size_t)b * N;
-    const double2* Zb = Z + (size_t)b * 2 * m * m;
+    const float2* Zb = Z + (size_t)b * 2 * m * m;
     double2 v = make_double2(0.0, 0.0);
     int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
     int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
     if (bi < 2 && bj == bi) {
         int ii = i - bi * m, jj = j - bj * m;
-        double2 z = Zb[(size_t)bi * m * m + ii + (size_t)m * jj];
-        v = make_double2(-z.x, -z.y);
+        float2 z = Zb[(size_t)bi * m * m + ii + (size_t)m * jj];
+        v = make_double2(-(double)z.x, -(double)z.y);
     } else if (bi < 2 && bj == 2) {
         int c = cond[(size_t)(j - 2 * m) * m + (i - bi * m)];
         if (c) v = make_double2(bi == 0 ? (c == 1 ? 1.0 : -1.0) : 0.5, 0.0);
@@ -136,7 +139,7 @@ __global__ void k_ir_update(const float2* __restrict__ y, const double* __restri
 }
 
 // r = b - W x in FP64 with the structure of W_G; norms[2] = max|r|.
-__global__ void k_residual(const double2* __restrict__ Z, const Incidence inc, int m, int n,
+__global__ void k_residual(const float2* __restrict__ Z, const Incidence inc, int m, int n,
                            const double2* __restrict__ bvec, const double2* __restrict__ x, double2* __restrict__ r,
                            double* __restrict__ norms, const int* __restrict__ active) {
     const int N = n + 2 * m;
@@ -161,10 +164,13 @@ __global__ void k_residual(const double2* __restrict__ Z, const Incidence inc, i
             acc.x += a * u.x;
             acc.y += a * u.y;
         }
-        const double2* Zb = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m;
+        const float2* Zb = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m;
         const double2* xs = xb + n + blk * m;
         double2 zx = make_double2(0.0, 0.0);
-        for (int j = 0; j < m; ++j) zx = cfma(Zb[k + (size_t)m * j], xs[j], zx);
+        for (int j = 0; j < m; ++j) {
+            float2 z = Zb[k + (size_t)m * j];
+            zx = cfma(make_double2(z.x, z.y), xs[j], zx);
+        }
         acc = csub(acc, zx);
     }
     double2 rv = csub(bvec[(size_t)b * N + row], acc);
@@ -187,10 +193,12 @@ __global__ void k_max_rows(const double* __restrict__ rsum, int N, double* __res
 
 int tags_mixed_alloc(tags_plan_s* p) {
     const size_t b = p->batch, N = p->N, m = p->m;
-    TAGS_CUDA_OK(cudaMalloc(&p->d_codes, sizeof(uint16_t) * m * (m + 1)));
-    int err = tags_launch_pair_plan(p->d_elec, p->d_img, p->m, p->has_images, p->d_codes, p->stream);
+    TAGS_CUDA_OK(cudaMalloc(&p->d_fillws, tags_mixed_fill_workspace(p->m)));
+    int err = tags_launch_pair_plan(p->d_elec, p->d_img, p->m, p->has_images, p->d_fillws, p->stream);
     if (err) return err;
-    TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(double2) * 2 * m * m * b));
+    err = tags_mixed_touch_count(p->d_fillws, p->m, p->stream, &p->n_touch);
+    if (err) return err;
+    TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_A, sizeof(float2) * N * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_scale, sizeof(double) * 2 * N * b));   // scale + row sums
     TAGS_CUDA_OK(cudaMalloc(&p->d_r, sizeof(double2) * 2 * N * b));      // residual + right-hand side
@@ -205,7 +213,7 @@ int tags_mixed_alloc(tags_plan_s* p) {
 }
 
 int tags_mixed_free(tags_plan_s* p) {
-    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms, p->d_codes, p->d_ldlws, p->d_ldlerr};
+    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms, p->d_fillws, p->d_ldlws, p->d_ldlerr};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     p->d_Z = nullptr;
@@ -253,16 +261,9 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     k_copy_c<<<(unsigned)(((long long)nb * N + 255) / 256), 256, 0, st>>>(p->d_x, d_b, (long long)nb * N);
     tags_note_launch();
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_x, 0, sizeof(double2) * N * nb, st));
-    // 1. impedance blocks in FP64 (full symmetric), direct + images
-    FillOut out{};
-    out.zl = p->d_Z;
-    out.zt = p->d_Z + (size_t)m * m;
-    out.ld = m;
-    out.batch_stride = 2LL * m * m;
-    out.sign = 1.0;
-    out.mirror = 1;
-    int err = tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_codes, p->d_coef, nb, out, p->has_images,
-                                     p->d_status, st);
+    // 1. impedance blocks (full symmetric, complex FP32), direct + images
+    int err = tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z, p->d_Z + (size_t)m * m,
+                                     2LL * m * m, p->has_images, p->n_touch, p->d_status, st);
     if (err) return err;
     // 2. scaling
     k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, N);
@@ -274,7 +275,8 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
-    err = tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m, st);
+    err = tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m,
+                      p->split_pieces, st);
     if (err) return err;
     // 4. refinement
     std::vector<int> active(nb, 1), conv(nb, 0), iters(nb, 0);

@@ -54,15 +54,17 @@ struct tags_plan_s {
     double2* d_W = nullptr;         // plain: batch x N x N
     double2* d_x = nullptr;         // batch x N (solution, FP64)
     // mixed form
-    double2* d_Z = nullptr;         // batch x 2 x m x m FP64 (ZL, ZT; full symmetric)
+    float2* d_Z = nullptr;          // batch x 2 x m x m complex FP32 (ZL, ZT; full symmetric)
     float2* d_A = nullptr;          // batch x N x N FP32 working matrix (reordered, scaled)
     double* d_scale = nullptr;      // batch x N symmetric scaling (reordered index)
     double2* d_r = nullptr;         // batch x N residual (FP64)
     float2* d_rf = nullptr;         // batch x N correction right-hand side (FP32)
     double* d_norms = nullptr;      // batch x 4 reductions
-    uint16_t* d_codes = nullptr;    // 2 x m(m+1)/2 pair classes (direct, image)
+    void* d_fillws = nullptr;       // pair classes and geometry records of the mixed fill
+    int n_touch = 0;                // pairs sharing an endpoint (FP64 Duffy rule)
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
+    int split_pieces = 3;           // bf16 pieces per real value in the tensor-core products
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 

@@ -37,11 +37,14 @@ struct FillOut {
 };
 
 int tags_fill_tables_init();
-int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, uint16_t* d_codes,
-                          cudaStream_t st);
-int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, const uint16_t* d_codes,
-                           const SampleCoef* d_coef, int nsamp, const FillOut& out, int has_img, int* d_status,
-                           cudaStream_t st);
+// mixed-form fill (FP32 regular pairs, FP64 log-singular pairs); the
+// workspace holds the plan-time pair classes and geometry records
+size_t tags_mixed_fill_workspace(int m);
+int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, void* ws, cudaStream_t st);
+int tags_mixed_touch_count(void* ws, int m, cudaStream_t st, int* out);
+int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
+                           int nsamp, float2* d_zl, float2* d_zt, long long bstride, int has_img, int max_touch,
+                           int* d_status, cudaStream_t st);
 int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, const SampleCoef* d_coef,
                           int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
                           cudaStream_t st);
@@ -80,8 +83,10 @@ int tags_launch_nlt(const double* d_f, long long fstride, long long nt, const do
 size_t tags_ldl_tc_workspace(int N, int batch);
 // zl_m > 0: the matrix is ordered [ZL (zl_m), ZT (zl_m), rest] with a zero ZL/ZT
 // coupling block, which the factorisation and the solves skip.
+// pieces: bf16 pieces per real value in the split products (2: three
+// products per real product, ~2^-16; 3: six products, ~2^-23).
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
-                int* err, int zl_m, cudaStream_t st);
+                int* err, int zl_m, int pieces, cudaStream_t st);
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
                      float2* x, long long xstride, int zl_m, cudaStream_t st);
 
