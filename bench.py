@@ -148,19 +148,27 @@ def read_profile(pkg):
     return out
 
 
-def roofline(prof, peaks):
-    """Roofline of the family with the largest device time."""
+def roofline(prof, peaks, pieces=3):
+    """Roofline of the family with the largest device time.
+
+    Tensor families: `achieved` counts the algorithmic complex flops of the
+    update outside the structural zero band (8 per complex multiply-add);
+    the split-bf16 execution runs `products` real bf16 products per real
+    product (6 for three pieces, 3 for two), which `executed_tflops` gives."""
     if not prof:
         return None, None
     name, f = max(prof.items(), key=lambda kv: kv[1]["ms"])
     sec = f["ms"] * 1e-3
     if name in TENSOR_FAMILIES:
         ach = f["flops"] / sec / 1e12
+        products = 6 if pieces == 3 else 3
         roof = {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
                 "frac": ach / peaks["bf16_tflops"], "traffic": None,
                 "kernel": name, "launches": f["launches"], "avg_launch_ms": f["ms"] / f["launches"],
-                "note": f"algorithmic complex LDL^T flops of the launch (the bf16x3 split executes 3x "
-                        f"as many tensor flops); peak = {peaks['src']} dense bf16"}
+                "executed_tflops": ach * products, "executed_frac": ach * products / peaks["bf16_tflops"],
+                "note": f"achieved = algorithmic complex LDL^T flops outside the zero ZL/ZT band; the "
+                        f"{pieces}-piece bf16 split runs {products} bf16 products per real product "
+                        f"(executed_*); peak = {peaks['src']} dense bf16"}
     elif name in FP64_FAMILIES:
         ach = f["flops"] / sec / 1e12
         roof = {"bound": "fp64", "achieved": ach, "peak": FP64_PIPE_TFLOPS, "unit": "TFLOP/s",

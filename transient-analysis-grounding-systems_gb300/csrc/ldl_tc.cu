@@ -136,6 +136,14 @@ TAGS_D uint32_t idesc_bf16(bool negate_a) {
     return d;
 }
 
+// 1 / d for complex FP32 d, scaled against overflow
+TAGS_D float2 crecip_f(float2 d) {
+    const float sc = fmaxf(fabsf(d.x), fabsf(d.y));
+    const float a = d.x / sc, b = d.y / sc;
+    const float den = sc * fmaf(a, a, b * b);
+    return make_float2(a / den, -b / den);
+}
+
 // x = p[0] + p[1] + ... + p[S-1] in bf16 pieces (each the rounded remainder)
 TAGS_D void split_n(float x, __nv_bfloat16* p, int S) {
     float r = x;
@@ -229,9 +237,12 @@ TAGS_D void split_pieces(float x, __nv_bfloat16* p) {
     }
 }
 
-template <int S>
-__global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
-                                                    const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+constexpr int EPI_WARPS = 8;               // two warps per tensor-memory lane quarter
+constexpr int GEMM_THREADS = 32 * (2 + EPI_WARPS);
+
+template <int S, int MODE>
+__global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
+                                                             const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
     using C = GemmCfg<S>;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t base_u32 = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -253,7 +264,7 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUte
         }
         for (int a = 0; a < 2; ++a) {
             mbar_init(tfull(a), 1);
-            mbar_init(tempty(a), 4);
+            mbar_init(tempty(a), EPI_WARPS);
         }
         mbar_init(drain, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -264,17 +275,30 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUte
     const uint32_t tmem = *tslot;
 
     if (warp == 0) {
-        // ---- producer: TMA loads of A and B planes, one K block per stage
-        if (lane == 0) {
-            int stage = 0;
-            uint32_t phase = 0;
-            bool alive = true;
-            int issued[4] = {0, 0, 0, 0};     // stages with a load whose completion nobody waited for yet
-            for (int t = blockIdx.x; t < total && alive; t += gridDim.x) {
-                int smp, I, J;
-                bool skip;
-                tile_of(g, t, smp, I, J, skip);
-                if (skip) continue;
+        // ---- producer: TMA loads of A and B planes, one K block per stage; the
+        // other lanes prefetch the tile's C columns into L2 for the epilogue
+        int stage = 0;
+        uint32_t phase = 0;
+        bool alive = true;
+        int issued[4] = {0, 0, 0, 0};     // stages with a load whose completion nobody waited for yet
+        for (int t = blockIdx.x; t < total && alive; t += gridDim.x) {
+            int smp, I, J;
+            bool skip;
+            tile_of(g, t, smp, I, J, skip);
+            if (skip) continue;
+            if (MODE == 0) {
+                const float2* Cb = g.Amat + g.mstride * smp;
+                const int r0 = g.row0 + TB * I, rows = min(TB, g.M - TB * I);
+                const int c0 = TB * J, cols = min(TB, g.Nn - TB * J);
+                if (rows > 0) {
+                    for (int c = lane; c < cols; c += 32) {
+                        const char* col = reinterpret_cast<const char*>(Cb + (long long)r0 + g.ld * (long long)(g.col0 + c0 + c));
+                        for (int off = 0; off < rows * 8; off += 128)
+                            asm volatile("prefetch.global.L2 [%0];" ::"l"(col + off));
+                    }
+                }
+            }
+            if (lane == 0) {
                 for (int kb = 0; kb < KBLKS; ++kb) {
                     if (!mbar_wait(empty(stage), phase ^ 1, g.err)) { alive = false; break; }
                     issued[stage] = 0;
@@ -288,25 +312,26 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUte
                     if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
                 }
             }
-            if (!alive) {
-                // let the copies in flight land before the CTA exits
-                const uint64_t t0 = globaltimer_ns();
-                for (int q = 0; q < C::STAGES; ++q) {
-                    if (!issued[q]) continue;
-                    uint32_t okq = 0;
-                    while (!okq && globaltimer_ns() - t0 < WAIT_NS) {
+            alive = __shfl_sync(0xffffffffu, alive ? 1 : 0, 0) != 0;
+        }
+        if (lane == 0 && !alive) {
+            // let the copies in flight land before the CTA exits
+            const uint64_t t0 = globaltimer_ns();
+            for (int q = 0; q < C::STAGES; ++q) {
+                if (!issued[q]) continue;
+                uint32_t okq = 0;
+                while (!okq && globaltimer_ns() - t0 < WAIT_NS) {
+                    asm volatile(
+                        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                        : "=r"(okq)
+                        : "r"(full(q)), "r"(0u)
+                        : "memory");
+                    if (!okq)
                         asm volatile(
                             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
                             : "=r"(okq)
-                            : "r"(full(q)), "r"(0u)
+                            : "r"(full(q)), "r"(1u)
                             : "memory");
-                        if (!okq)
-                            asm volatile(
-                                "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                                : "=r"(okq)
-                                : "r"(full(q)), "r"(1u)
-                                : "memory");
-                    }
                 }
             }
         }
@@ -366,8 +391,9 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUte
             }
         }
     } else {
-        // ---- epilogue warps 2..5: tensor-memory lanes 32 (warp % 4) ...
-        const int quarter = warp & 3;
+        // ---- epilogue warps 2..9: warp w reads tensor-memory lanes 32 (w % 4) ...
+        // and one half of the columns
+        const int quarter = warp & 3, half = (warp - 2) >> 2;
         const int r = 32 * quarter + lane;
         const uint32_t lane_off = (uint32_t)(32 * quarter) << 16;
         int acc = 0;
@@ -382,23 +408,21 @@ __global__ void __launch_bounds__(192, 1) k_gemm_tc(const __grid_constant__ CUte
             const uint32_t accR = tmem + acc * 256, accI = accR + 128;
             const int gr = TB * I + r;
             float2* Cb = g.Amat + g.mstride * smp;
-            for (int cc = 0; cc < TB / 16; ++cc) {
+            for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
                 float vr[16], vi[16];
                 tmem_ld16(accR + lane_off + cc * 16, vr);
                 tmem_ld16(accI + lane_off + cc * 16, vi);
                 if (gr >= g.M) continue;
-                if (g.mode == 0) {
+                if (MODE == 0) {
+                    // all loads of the chunk first, then the stores
+                    float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + TB * J + cc * 16);
+                    float2 cv[16];
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const int gc = TB * J + cc * 16 + j;
-                        if (gc < g.Nn) {
-                            float2* p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + gc);
-                            float2 v = *p;
-                            v.x -= vr[j];
-                            v.y -= vi[j];
-                            *p = v;
-                        }
-                    }
+                    for (int j = 0; j < 16; ++j)
+                        if (TB * J + cc * 16 + j < g.Nn) cv[j] = base_p[g.ld * j];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (TB * J + cc * 16 + j < g.Nn) base_p[g.ld * j] = make_float2(cv[j].x - vr[j], cv[j].y - vi[j]);
                 } else {
                     const float2* dv = g.dinv + (long long)TB * smp;
                     __align__(16) __nv_bfloat16 lp[2 * S][16], wp[2 * S][16];
@@ -468,8 +492,7 @@ __global__ void __launch_bounds__(512) k_ldl_diag(float2* __restrict__ A0, long 
     for (int k = 0; k < TB; ++k) {
         const float2 d = S[k * TB + k];
         if (tid == 0 && k < jb && !(d.x != 0.f || d.y != 0.f) && *(info + smp) == 0) info[smp] = j0 + k + 1;
-        double2 dd = cdiv(make_double2(1.0, 0.0), make_double2(d.x, d.y));
-        const float2 di = make_float2((float)dd.x, (float)dd.y);
+        const float2 di = crecip_f(d);
         // column below the pivot: keep W = old values, L = W / d
         for (int i = k + 1 + tid; i < TB; i += blockDim.x) colv[i] = S[k * TB + i];
         __syncthreads();
@@ -492,11 +515,7 @@ __global__ void __launch_bounds__(512) k_ldl_diag(float2* __restrict__ A0, long 
     }
     for (int c = tid; c < TB; c += blockDim.x) {
         float2 v = make_float2(0.f, 0.f);
-        if (c < jb) {
-            float2 d = S[c * TB + c];
-            double2 dd = cdiv(make_double2(1.0, 0.0), make_double2(d.x, d.y));
-            v = make_float2((float)dd.x, (float)dd.y);
-        }
+        if (c < jb) v = crecip_f(S[c * TB + c]);
         dinv[(long long)TB * smp + c] = v;
     }
     __syncthreads();
@@ -640,9 +659,8 @@ __global__ void k_diag_scale(const float2* __restrict__ A0, long long ld, long l
     const int smp = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    float2 d = A0[mstride * smp + i + ld * (long long)i];
-    double2 q = cdiv(make_double2(x0[xstride * smp + i].x, x0[xstride * smp + i].y), make_double2(d.x, d.y));
-    x0[xstride * smp + i] = make_float2((float)q.x, (float)q.y);
+    const float2 d = A0[mstride * smp + i + ld * (long long)i];
+    x0[xstride * smp + i] = fmulc(x0[xstride * smp + i], crecip_f(d));
 }
 
 // ---- host side ---------------------------------------------------------------------
@@ -719,19 +737,25 @@ static int num_sms() {
     return n;
 }
 
-template <int S>
-static int launch_gemm(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
+template <int S, int MODE>
+static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
-        TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, GemmCfg<S>::SMEM));
+        TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc<S, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          GemmCfg<S>::SMEM));
         attr = true;
     }
     const int total = g.tiles * g.nb;
     const int grid = total < num_sms() ? total : num_sms();
     if (grid <= 0) return 0;
-    k_gemm_tc<S><<<grid, 192, GemmCfg<S>::SMEM, st>>>(mA, mB, g);
+    k_gemm_tc<S, MODE><<<grid, GEMM_THREADS, GemmCfg<S>::SMEM, st>>>(mA, mB, g);
     tags_note_launch();
     return 0;
+}
+
+template <int S>
+static int launch_gemm(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
+    return g.mode == 0 ? launch_gemm_m<S, 0>(mA, mB, g, st) : launch_gemm_m<S, 1>(mA, mB, g, st);
 }
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
@@ -830,9 +854,11 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
         e = NS == 3 ? launch_gemm<3>(mA21, mLin, g, st) : launch_gemm<2>(mA21, mLin, g, st);
         if (e) return e;
-        // triangular solve: rest x jb unknowns against jb x jb, 4 rest jb^2 real flops
-        tags_prof_end(TAGS_PROF_LDL_PANEL, pf, st, 4.0 * rest * (double)jb * jb * nb,
-                      (8.0 * rest * jb + 16.0 * rest * 128 * 2) * nb);
+        // triangular solve: r x jb unknowns against jb x jb (r = rest minus
+        // the zero band), 4 r jb^2 real flops
+        const double rp = rest - (double)(g.zhi - g.zlo);
+        tags_prof_end(TAGS_PROF_LDL_PANEL, pf, st, 4.0 * rp * (double)jb * jb * nb,
+                      (8.0 * rp * jb + 16.0 * rp * 128 * 2) * nb);
         g.mode = 0;
         g.tri = 1;
         g.tiles = T * (T + 1) / 2;
@@ -842,10 +868,12 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
         e = NS == 3 ? launch_gemm<3>(mL, mW, g, st) : launch_gemm<2>(mL, mW, g, st);
         if (e) return e;
-        // symmetric rank-jb update of the lower triangle: 8 jb rest(rest+1)/2 real flops;
+        // symmetric rank-jb update of the lower triangle outside the zero
+        // band: 8 jb r(r+1)/2 real flops with r = rest minus the band;
         // bytes: read + write of that triangle in complex FP32, two panels of split planes
-        tags_prof_end(TAGS_PROF_LDL_TRAIL, pf, st, 8.0 * jb * (0.5 * rest * (rest + 1.0)) * nb,
-                      (16.0 * 0.5 * rest * (rest + 1.0) + 2.0 * rest * 128 * 4.0 * NS) * nb);
+        const double r = rest - (double)(g.zhi - g.zlo);
+        tags_prof_end(TAGS_PROF_LDL_TRAIL, pf, st, 8.0 * jb * (0.5 * r * (r + 1.0)) * nb,
+                      (16.0 * 0.5 * r * (r + 1.0) + 2.0 * r * 128 * 4.0 * NS) * nb);
     }
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

@@ -78,32 +78,29 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 }
 
 // W'' (complex FP32, column-major N x N, reordered and scaled), lower triangle.
-__global__ void k_build(const float2* __restrict__ Z, const signed char* __restrict__ cond, const double* __restrict__ scale,
-                        int m, int n, float2* __restrict__ A) {
+// Grid: x over 256-row chunks, y over columns, z over samples.
+__global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const signed char* __restrict__ cond,
+                                               const double* __restrict__ scale, int m, int n,
+                                               float2* __restrict__ A) {
     const int N = n + 2 * m;
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    int b = blockIdx.y;
-    if (t >= (long long)N * N) return;
-    int i = (int)(t % N), j = (int)(t / N);
-    if (i < j) return;              // the LDL^T reads the lower triangle only
+    const int j = blockIdx.y, b = blockIdx.z;
+    const int i = j + blockIdx.x * blockDim.x + threadIdx.x;     // rows i >= j only
+    if (i >= N) return;
     const double* d = scale + (size_t)b * N;
     const float2* Zb = Z + (size_t)b * 2 * m * m;
-    double2 v = make_double2(0.0, 0.0);
-    int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
-    int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
+    float vx = 0.f, vy = 0.f;
+    const int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
+    const int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
     if (bi < 2 && bj == bi) {
-        int ii = i - bi * m, jj = j - bj * m;
-        float2 z = Zb[(size_t)bi * m * m + ii + (size_t)m * jj];
-        v = make_double2(-(double)z.x, -(double)z.y);
-    } else if (bi < 2 && bj == 2) {
-        int c = cond[(size_t)(j - 2 * m) * m + (i - bi * m)];
-        if (c) v = make_double2(bi == 0 ? (c == 1 ? 1.0 : -1.0) : 0.5, 0.0);
+        const float2 z = Zb[(size_t)bi * m * m + (i - bi * m) + (size_t)m * (j - bj * m)];
+        vx = -z.x;
+        vy = -z.y;
     } else if (bi == 2 && bj < 2) {
-        int c = cond[(size_t)(i - 2 * m) * m + (j - bj * m)];
-        if (c) v = make_double2(bj == 0 ? (c == 1 ? 1.0 : -1.0) : 0.5, 0.0);
+        const int c = cond[(size_t)(i - 2 * m) * m + (j - bj * m)];
+        if (c) vx = bj == 0 ? (c == 1 ? 1.f : -1.f) : 0.5f;
     }
-    double s = d[i] * d[j];
-    A[(size_t)b * N * N + t] = make_float2((float)(v.x * s), (float)(v.y * s));
+    const float s = (float)(d[i] * d[j]);
+    A[(size_t)b * N * N + (size_t)j * N + i] = make_float2(vx * s, vy * s);
 }
 
 TAGS_D int orig_of(int ip, int m, int n) {
@@ -138,41 +135,100 @@ __global__ void k_ir_update(const float2* __restrict__ y, const double* __restri
     atomic_max_nonneg(norms + 4 * b + 1, fabs(xv.x) + fabs(xv.y));
 }
 
-// r = b - W x in FP64 with the structure of W_G; norms[2] = max|r|.
-__global__ void k_residual(const float2* __restrict__ Z, const Incidence inc, int m, int n,
-                           const double2* __restrict__ bvec, const double2* __restrict__ x, double2* __restrict__ r,
-                           double* __restrict__ norms, const int* __restrict__ active) {
+// r = b - W x with the structure of W_G; norms[2] = max|r|.
+// Node rows (sparse incidence, exact +-1 / 0.5) in FP64.
+__global__ void k_residual_nodes(const Incidence inc, int m, int n, const double2* __restrict__ bvec,
+                                 const double2* __restrict__ x, double2* __restrict__ r, double* __restrict__ norms,
+                                 const int* __restrict__ active) {
     const int N = n + 2 * m;
     int row = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (row >= N || !active[b]) return;
+    if (row >= n || !active[b]) return;
     const double2* xb = x + (size_t)b * N;
     double2 acc = make_double2(0.0, 0.0);
-    if (row < n) {
-        for (int q = inc.node_ptr[row]; q < inc.node_ptr[row + 1]; ++q) {
-            int e = inc.node_seg[q];
-            double a = inc.node_a[q];
-            double2 il = xb[n + e], it = xb[n + m + e];
-            acc.x += a * il.x + 0.5 * it.x;
-            acc.y += a * il.y + 0.5 * it.y;
-        }
-    } else {
-        int blk = row < n + m ? 0 : 1;
-        int k = row - n - blk * m;
-        for (int q = inc.seg_ptr[k]; q < inc.seg_ptr[k + 1]; ++q) {
-            double2 u = xb[inc.seg_node[q]];
-            double a = blk == 0 ? (double)inc.seg_a[q] : 0.5;
-            acc.x += a * u.x;
-            acc.y += a * u.y;
-        }
-        const float2* Zb = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m;
-        const double2* xs = xb + n + blk * m;
-        double2 zx = make_double2(0.0, 0.0);
-        for (int j = 0; j < m; ++j) {
-            float2 z = Zb[k + (size_t)m * j];
-            zx = cfma(make_double2(z.x, z.y), xs[j], zx);
-        }
-        acc = csub(acc, zx);
+    for (int q = inc.node_ptr[row]; q < inc.node_ptr[row + 1]; ++q) {
+        int e = inc.node_seg[q];
+        double a = inc.node_a[q];
+        double2 il = xb[n + e], it = xb[n + m + e];
+        acc.x += a * il.x + 0.5 * it.x;
+        acc.y += a * il.y + 0.5 * it.y;
     }
+    double2 rv = csub(bvec[(size_t)b * N + row], acc);
+    r[(size_t)b * N + row] = rv;
+    atomic_max_nonneg(norms + 4 * b + 2, fabs(rv.x) + fabs(rv.y));
+}
+
+// Two-float helpers: a value is hi + lo with |lo| <= ulp(hi)/2 (~2^-48 relative).
+struct F2 {
+    float hi, lo;
+};
+TAGS_D F2 f2_add(F2 a, float p, float e) {
+    // a + (p + e), p the leading part of a product, e its rounding error
+    float s = a.hi + p;
+    float v = s - a.hi;
+    float t = (a.hi - (s - v)) + (p - v);
+    t += a.lo + e;
+    F2 o;
+    o.hi = s + t;
+    o.lo = t - (o.hi - s);
+    return o;
+}
+// a += z * (xh + xl) for real z (exact in FP32) and a two-float x
+TAGS_D F2 f2_mac(F2 a, float z, float xh, float xl) {
+    float p = z * xh;
+    float e = fmaf(z, xh, -p);
+    e = fmaf(z, xl, e);
+    return f2_add(a, p, e);
+}
+
+// Impedance rows: r_k = b_k - (incidence terms - sum_j Z_kj x_j). The dense
+// product runs in two-float arithmetic on the FP32 pipe (Z is exact in FP32,
+// x is split into float pairs), so its result is accurate to ~2^-44 of
+// |Z| |x| without FP64 arithmetic in the m^2 loop.
+constexpr int RES_CHUNK = 1024;
+__global__ void __launch_bounds__(256) k_residual_z(const float2* __restrict__ Z, const Incidence inc, int m, int n,
+                                                    const double2* __restrict__ bvec, const double2* __restrict__ x,
+                                                    double2* __restrict__ r, double* __restrict__ norms,
+                                                    const int* __restrict__ active) {
+    __shared__ float4 xs[RES_CHUNK];        // re_hi, re_lo, im_hi, im_lo
+    const int N = n + 2 * m;
+    const int blk = blockIdx.y & 1, b = blockIdx.y >> 1;
+    if (!active[b]) return;
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const double2* xb = x + (size_t)b * N;
+    const float2* Zb = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m;
+    F2 ar{0.f, 0.f}, ai{0.f, 0.f};
+    for (int j0 = 0; j0 < m; j0 += RES_CHUNK) {
+        const int nj = min(RES_CHUNK, m - j0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < nj; t += blockDim.x) {
+            double2 v = xb[n + blk * m + j0 + t];
+            float rh = (float)v.x, ih = (float)v.y;
+            xs[t] = make_float4(rh, (float)(v.x - rh), ih, (float)(v.y - ih));
+        }
+        __syncthreads();
+        if (k < m) {
+            for (int j = 0; j < nj; ++j) {
+                const float2 z = Zb[k + (size_t)m * (j0 + j)];
+                const float4 xv = xs[j];
+                // (zr + i zi)(xr + i xi) = (zr xr - zi xi) + i (zr xi + zi xr)
+                ar = f2_mac(ar, z.x, xv.x, xv.y);
+                ar = f2_mac(ar, -z.y, xv.z, xv.w);
+                ai = f2_mac(ai, z.x, xv.z, xv.w);
+                ai = f2_mac(ai, z.y, xv.x, xv.y);
+            }
+        }
+    }
+    if (k >= m) return;
+    const int row = n + blk * m + k;
+    double2 acc = make_double2(0.0, 0.0);
+    for (int q = inc.seg_ptr[k]; q < inc.seg_ptr[k + 1]; ++q) {
+        double2 u = xb[inc.seg_node[q]];
+        double a = blk == 0 ? (double)inc.seg_a[q] : 0.5;
+        acc.x += a * u.x;
+        acc.y += a * u.y;
+    }
+    acc.x -= (double)ar.hi + (double)ar.lo;
+    acc.y -= (double)ai.hi + (double)ai.lo;
     double2 rv = csub(bvec[(size_t)b * N + row], acc);
     r[(size_t)b * N + row] = rv;
     atomic_max_nonneg(norms + 4 * b + 2, fabs(rv.x) + fabs(rv.y));
@@ -271,7 +327,7 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     tags_note_launch(2);
     // 3. FP32 working matrix and its LU (no pivoting)
     int pf = tags_prof_begin(TAGS_PROF_BUILD, st);
-    k_build<<<dim3((unsigned)((NN + 255) / 256), nb), 256, 0, st>>>(p->d_Z, p->d_cond, p->d_scale, m, n, p->d_A);
+    k_build<<<dim3((unsigned)((N + 255) / 256), N, nb), 256, 0, st>>>(p->d_Z, p->d_cond, p->d_scale, m, n, p->d_A);
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
@@ -318,8 +374,12 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
         if (err) return err;
         k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, d_active);
         pf = tags_prof_begin(TAGS_PROF_RESID, st);
-        k_residual<<<gv, 256, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms, d_active);
-        tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 32.0 * m * (double)m * nb);
+        k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
+                                                                    d_active);
+        k_residual_z<<<dim3((m + 255) / 256, 2 * nb), 256, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r,
+                                                                    p->d_norms, d_active);
+        // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
+        tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
         tags_note_launch(2);
         TAGS_CUDA_OK(cudaGetLastError());
         TAGS_CUDA_OK(cudaMemcpyAsync(hn.data(), p->d_norms, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st));
@@ -330,10 +390,11 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
             double dx = hn[4 * q + 0], xn = hn[4 * q + 1], rn = hn[4 * q + 2];
             h_berr[q] = rn / (wnorm[q] * xn + 1e-300);
             if (!(dx == dx) || !(xn == xn)) { active[q] = 0; continue; }       // NaN: fallback
-            if (dx <= 4.0 * TAGS_DBL_EPSILON * xn) { active[q] = 0; conv[q] = 1; continue; }
+            // the residual is accurate to ~2^-44 |W| |x| (two-float products): stop
+            // once the correction is below that level or stops shrinking
+            if (dx <= 1e-13 * xn) { active[q] = 0; conv[q] = 1; continue; }
             if (it >= 2 && dx > 0.5 * prev_dx[q]) {
-                // stagnation: accept if the backward error is already at FP64 level
-                if (h_berr[q] <= 1e-14) conv[q] = 1;
+                if (h_berr[q] <= 1e-12) conv[q] = 1;
                 active[q] = 0;
                 continue;
             }
