@@ -123,6 +123,7 @@ typedef struct {
     int fallbacks;             /* samples re-solved in plain FP64 (mixed) */
     double max_backward_error; /* largest normwise backward error |b - W x| / (|W| |x| + |b|) */
     double seconds;            /* device time of the run */
+    int split;                 /* split form used by the last pass (mixed; see tags_plan_set_split) */
 } tags_run_stats;
 
 /* Geometry and incidence are uploaded once. images may be NULL (no images).
@@ -140,6 +141,21 @@ int tags_plan_run (tags_plan plan, const tags_cdouble *s, const tags_cdouble *ka
                    int *info, int flags, tags_run_stats *stats);
 
 int tags_plan_destroy (tags_plan plan);
+
+/* Passes as CUDA graphs (default on): each pass shape (samples in the pass,
+ * mur, injection form) is captured once into an executable graph holding
+ * the fill, the factorisation and, for TAGS_MIXED, a conditional while-node
+ * that repeats the refinement step until the device-side stopping test
+ * clears it; later passes of that shape are one graph launch. 0 = launch
+ * the same kernels one by one (the host reads the stopping flag per step). */
+int tags_plan_set_graphs (tags_plan plan, int enable);
+
+/* Split form of the TAGS_MIXED tensor-core products: 3 = three bf16 pieces
+ * per FP32 value (6 products per real product, FP32-level), 2 = two bf16
+ * pieces (3 products, ~16 bits), 16 = two fp16 pieces of 2^8 x (3 products,
+ * 22 bits; a value outside fp16's range makes the plan fall back to 3 and
+ * solve that pass again). Default 3. */
+int tags_plan_set_split (tags_plan plan, int pieces);
 
 /* ---- Part 3: solve without device allocation -------------------------------- */
 
@@ -164,10 +180,11 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
 
 /* No counterpart in the reference. Factorises nb complex symmetric N x N
  * matrices (host, column-major, sample-major; lower half read) with the mixed
- * form's tensor-core LDL^T (FP32 storage, products of bf16 pieces, no
- * pivoting; pieces = 2 or 3 per real value) and returns L (strictly lower,
- * unit diagonal implied) and D (diagonal) in place, rounded from FP32.
- * Returns 0, k > 0 for a zero pivot, or a TAGS_E_* code. */
+ * form's tensor-core LDL^T (FP32 storage, no pivoting; the products use
+ * pieces = 2 or 3 bf16 pieces per real value, or pieces = 16: two fp16
+ * pieces of 2^8 x) and returns L (strictly lower, unit diagonal implied) and
+ * D (diagonal) in place, rounded from FP32. Returns 0, k > 0 for a zero
+ * pivot, or a TAGS_E_* code (TAGS_E_NONFINITE: a value left the fp16 range). */
 int tags_debug_ldl (tags_cdouble *a, int N, int nb, int pieces);
 
 /* Per-family kernel timing with CUDA events on the launching stream (0 = off,

@@ -1,5 +1,6 @@
-"""GPU checks of the mixed form's tensor-core LDL^T (tcgen05 GEMMs, bf16x3
-split products, FP32 storage) through its diagnostic entry point."""
+"""GPU checks of the mixed form's tensor-core LDL^T (tcgen05 GEMMs on split
+products: bf16 pieces or scaled fp16 pairs, FP32 storage) through its
+diagnostic entry point."""
 import ctypes
 
 import numpy as np
@@ -25,11 +26,12 @@ def _ldl(pkg, mats, pieces=3):
     return code, np.transpose(buf, (0, 2, 1))
 
 
-@pytest.mark.parametrize("pieces,tol", [(2, 2e-5), (3, 2e-6)])
+@pytest.mark.parametrize("pieces,tol", [(2, 2e-5), (3, 2e-6), (16, 4e-6)])
 @pytest.mark.parametrize("N", [128, 300, 517])
 def test_tensor_core_ldl_reconstructs(gpu_pkg, N, pieces, tol):
     """L D L^T reproduces A to the accuracy of the split products: ~1e-5 with
-    two bf16 pieces per value (three products), FP32 level with three (six)."""
+    two bf16 pieces per value (three products), FP32 level with three (six),
+    near FP32 level with two fp16 pieces of 2^8 x (three products)."""
     rng = np.random.default_rng(N)
     mats = np.stack([_sym_matrix(rng, N, 4.0), _sym_matrix(rng, N, 2.0), _sym_matrix(rng, N, 3.0)])
     code, fac = _ldl(gpu_pkg, mats, pieces)
@@ -57,3 +59,18 @@ def test_tensor_core_ldl_matches_fp64_factors(gpu_pkg):
         W[k + 1:, k + 1:] -= np.outer(Lr[k + 1:, k], W[k, k + 1:])
     assert np.max(np.abs(np.diag(fac[0]) - d)) < 1e-4 * np.max(np.abs(d))
     assert np.max(np.abs(np.tril(fac[0], -1) - np.tril(Lr, -1))) < 1e-4
+
+
+def test_fp16_split_reports_out_of_range(gpu_pkg):
+    """A block column with entries beyond the fp16 pair's range (|x| > 255
+    after the 2^8 scale) is reported, not used: TAGS_E_NONFINITE."""
+    rng = np.random.default_rng(3)
+    N = 300
+    A = _sym_matrix(rng, N, 3.0)
+    A[200, 5] = A[5, 200] = 4.0e3
+    gpu_pkg.lib().tags_gpu_set_quiet(1)
+    code, _ = _ldl(gpu_pkg, A[None], 16)
+    gpu_pkg.lib().tags_gpu_set_quiet(0)
+    assert code == gpu_pkg.E_NONFINITE
+    code, fac = _ldl(gpu_pkg, A[None], 3)
+    assert code == 0

@@ -163,3 +163,34 @@ def test_full_size_properties(gpu_pkg):
     # reciprocity: potential at node 0 for a current at the centre equals the reverse
     other, _, _ = pkg.hem_sweep(e, img, nodes, s[:1], kappa[:1], inj_node=0, precision=pkg.PLAIN_FP64)
     assert abs(other[0, centre] - plain[0, 0]) < 1e-11 * abs(plain[0, 0])
+
+
+@pytest.mark.parametrize("precision", ["plain", "mixed"])
+def test_graph_passes_match_direct_launches(gpu_pkg, precision):
+    """Config 2 grid, 40 samples in passes of 16 (two full passes and a
+    ragged one of 8): each pass as one CUDA-graph launch (the mixed form's
+    refinement as a conditional while-node) gives the same solutions and
+    iteration counts as launching the kernels one by one."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    img = pkg.images(e)
+    idx = np.linspace(0, len(gd["s"]) - 1, 40).astype(int)
+    s, kappa = gd["s"][idx], gd["kappa"][idx]
+    ie = np.zeros((len(idx), nodes.shape[0]), np.complex128)
+    ie[:, 0] = gd["inj_s"][idx]
+    prec = pkg.PLAIN_FP64 if precision == "plain" else pkg.MIXED
+    out = {}
+    for graphs in (False, True):
+        launches0 = pkg.lib().tags_gpu_launch_count()
+        sol, info, st = pkg.hem_sweep(e, img, nodes, s, kappa, ie=ie, precision=prec, max_batch=16,
+                                      graphs=graphs)
+        out[graphs] = (sol, info, st.max_iterations, st.fallbacks,
+                       pkg.lib().tags_gpu_launch_count() - launches0)
+        assert np.all(info == 0)
+    (sd, _, itd, fbd, nd), (sg, _, itg, fbg, ng) = out[False], out[True]
+    assert itd == itg and fbd == fbg == 0
+    assert np.max(np.abs(sg - sd)) <= 1e-12 * np.max(np.abs(sd))
+    assert np.max(np.abs(sg[:, 0] - gd["u0"][idx]) / np.abs(gd["u0"][idx])) < (1e-8 if precision == "plain" else 1e-6)
+    # the graph path counts the kernels its launches ran: same order as direct
+    assert ng > 0 and abs(ng - nd) <= 0.1 * nd

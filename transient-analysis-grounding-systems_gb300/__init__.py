@@ -41,6 +41,7 @@ FILTER_NONE, FILTER_BLACKMAN, FILTER_HANNING, FILTER_LANCZOS, FILTER_RIESZ = ran
 PLAIN_FP64, MIXED = 0, 1
 RUN_DEVICE_PTRS = 1
 E_ARG, E_CUDA, E_NOMEM, E_GEOMETRY, E_NONFINITE = -101, -102, -103, -104, -105
+SPLIT_BF16_2, SPLIT_BF16_3, SPLIT_F16 = 2, 3, 16
 
 # physical constants of the reference (src/auxiliary.c:17-21)
 PI = 3.1415926535897932384626433832795029
@@ -53,7 +54,8 @@ EPS0 = 8.854187817620e-12
 EXPORTS = (
     "calculate_impedances", "impedances_images", "fill_incidence_imm", "fill_impedance_imm",
     "solve_immittance", "laplace_trans", "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
-    "tags_plan_destroy", "tags_gpu_launch_count", "tags_gpu_last_error", "tags_gpu_set_quiet",
+    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "tags_gpu_set_quiet",
 )
 
 
@@ -70,7 +72,8 @@ class c_complex(ctypes.Structure):
 
 class RunStats(ctypes.Structure):
     _fields_ = [("max_iterations", ctypes.c_int), ("fallbacks", ctypes.c_int),
-                ("max_backward_error", ctypes.c_double), ("seconds", ctypes.c_double)]
+                ("max_backward_error", ctypes.c_double), ("seconds", ctypes.c_double),
+                ("split", ctypes.c_int)]
 
 
 _dp = ctypes.POINTER(ctypes.c_double)
@@ -110,12 +113,15 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_run.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _sz, _vp, _vp,
                                         ctypes.c_int, ctypes.POINTER(RunStats)]
             L.tags_plan_destroy.argtypes = [_vp]
+            L.tags_plan_set_graphs.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
             for name in ("calculate_impedances", "impedances_images", "fill_incidence_imm",
                          "fill_impedance_imm", "solve_immittance", "laplace_trans", "inv_laplace_trans",
-                         "tags_plan_create", "tags_plan_run", "tags_plan_destroy"):
+                         "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
+                         "tags_plan_set_split"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -352,7 +358,7 @@ class Plan:
     """Device-resident geometry + workspaces for many Laplace samples
     (tags_plan_create / tags_plan_run / tags_plan_destroy)."""
 
-    def __init__(self, electrodes, imgs, nodes, precision=PLAIN_FP64, max_batch=0):
+    def __init__(self, electrodes, imgs, nodes, precision=PLAIN_FP64, max_batch=0, graphs=True):
         self.elec = _elec(electrodes)
         self.img = None if imgs is None else _elec(imgs)
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
@@ -366,6 +372,20 @@ class Plan:
         if code != 0:
             raise RuntimeError(f"tags_plan_create failed ({code}): {last_error()}")
         self.handle = h
+        self.set_graphs(graphs)
+
+    def set_split(self, pieces):
+        """Split form of the mixed form's tensor-core products: SPLIT_BF16_3,
+        SPLIT_BF16_2 or SPLIT_F16 (see include/tags_gpu.h)."""
+        code = lib().tags_plan_set_split(self.handle, int(pieces))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_set_split failed ({code}): {last_error()}")
+
+    def set_graphs(self, enable):
+        """Run each pass as one CUDA-graph launch (True) or kernel by kernel."""
+        code = lib().tags_plan_set_graphs(self.handle, 1 if enable else 0)
+        if code != 0:
+            raise RuntimeError(f"tags_plan_set_graphs failed ({code}): {last_error()}")
 
     def run(self, s, kappa, mur=1.0, ie=None, inj_node=0, want_solution=True):
         """Solve for every sample; returns (solution ns x N, info, RunStats)."""
@@ -407,11 +427,13 @@ class Plan:
 
 
 def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, precision=PLAIN_FP64,
-              max_batch=0):
+              max_batch=0, graphs=True, split=None):
     """Solutions [U; I_L; I_T] for every Laplace sample (one plan, one run)."""
     if not max_batch:
         max_batch = min(len(np.atleast_1d(s)), 64)
-    plan = Plan(electrodes, imgs, nodes, precision, max_batch)
+    plan = Plan(electrodes, imgs, nodes, precision, max_batch, graphs)
+    if split is not None:
+        plan.set_split(split)
     try:
         return plan.run(s, kappa, mur, ie, inj_node)
     finally:

@@ -22,6 +22,7 @@
 // returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -113,26 +114,16 @@ TAGS_D void tmem_ld16(uint32_t taddr, float* v) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
-// 1024 bytes apart (stride byte offset), descriptor version 1.
-TAGS_D uint64_t sdesc(uint32_t addr) {
-    uint64_t d = 0;
-    d |= (uint64_t)((addr >> 4) & 0x3FFF);
-    d |= (uint64_t)1 << 16;                    // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset
-    d |= (uint64_t)1 << 46;                    // version
-    d |= (uint64_t)2 << 61;                    // SWIZZLE_128B
-    return d;
-}
-// Instruction descriptor: kind::f16, bf16 x bf16 -> f32, M = N = 128, K-major.
-TAGS_D uint32_t idesc_bf16(bool negate_a) {
+// Instruction descriptor: kind::f16, bf16 x bf16 or fp16 x fp16 -> f32,
+// M = N = 128, both operands K-major.
+TAGS_D uint32_t idesc_mma(bool negate_a, bool f16) {
     uint32_t d = 0;
-    d |= 1u << 4;                   // D format f32
-    d |= 1u << 7;                   // A bf16
-    d |= 1u << 10;                  // B bf16
+    d |= 1u << 4;                            // D format f32
+    d |= (f16 ? 0u : 1u) << 7;               // A format: 0 f16, 1 bf16
+    d |= (f16 ? 0u : 1u) << 10;              // B format: same type as A
     d |= (negate_a ? 1u : 0u) << 13;
-    d |= (uint32_t)(TB >> 3) << 17; // N
-    d |= (uint32_t)(TB >> 4) << 24; // M
+    d |= (uint32_t)(TB >> 3) << 17;          // N
+    d |= (uint32_t)(TB >> 4) << 24;          // M
     return d;
 }
 
@@ -144,12 +135,30 @@ TAGS_D float2 crecip_f(float2 d) {
     return make_float2(a / den, -b / den);
 }
 
-// x = p[0] + p[1] + ... + p[S-1] in bf16 pieces (each the rounded remainder)
-TAGS_D void split_n(float x, __nv_bfloat16* p, int S) {
+// Split forms of an FP32 value, as 16-bit patterns (each piece the rounded
+// remainder of the previous ones):
+//   bf16: x = p[0] + ... + p[S-1], S = 2 or 3 (3 pieces keep FP32 precision);
+//   fp16: 2^8 x = p[0] + p[1] (22 significant bits; the 2^8 keeps values of
+//         the scaled working matrix, |x| <= 255, inside fp16's range and its
+//         small ones off the subnormals; a value outside raises `ovf`).
+constexpr float kF16Scale = 256.f;
+constexpr float kF16Unscale = 1.f / 65536.f;     // a product of two scaled operands
+constexpr int kErrRange = 1;                      // err[1]: an fp16 piece out of range
+
+TAGS_D void split_n(float x, uint16_t* p, int S, bool f16, int& ovf) {
+    if (f16) {
+        const float y = x * kF16Scale;
+        if (!(fabsf(y) <= 65504.f)) ovf = 1;
+        const __half h = __float2half_rn(y);
+        p[0] = __half_as_ushort(h);
+        p[1] = __half_as_ushort(__float2half_rn(y - __half2float(h)));
+        return;
+    }
     float r = x;
     for (int q = 0; q < S; ++q) {
-        p[q] = __float2bfloat16_rn(r);
-        r -= __bfloat162float(p[q]);
+        const __nv_bfloat16 b = __float2bfloat16_rn(r);
+        p[q] = __bfloat16_as_ushort(b);
+        r -= __bfloat162float(b);
     }
 }
 
@@ -174,7 +183,9 @@ template <int S> struct GemmCfg {
     static constexpr int NPL = 2 * S;                // planes per operand
     static constexpr int STAGE = 2 * NPL * PST;      // A and B planes of one K block
     static constexpr int STAGES = S == 2 ? 3 : 2;
-    static constexpr int SMEM = STAGES * STAGE + 1024 + 512;
+    static constexpr int BARS = 512;                  // mbarriers and the TMEM slot
+    static constexpr int DINV = 8 * 64 * 8;           // mode 1: 64 values of D^{-1} per epilogue warp
+    static constexpr int SMEM = STAGES * STAGE + 1024 + BARS + DINV;
 };
 
 // Shared-memory matrix descriptor: K-major, 64-byte swizzle, 8-row groups 512
@@ -199,12 +210,15 @@ struct GemmArgs {
     long long ld, mstride;
     int row0, col0;            // matrix coordinates of output element (0, 0)
     const float2* dinv;        // per sample 128 values (mode 1)
-    __nv_bfloat16* Lp;         // planes written in mode 1: [sample][2S][R][128]
-    __nv_bfloat16* Wp;
+    uint16_t* Lp;              // planes written in mode 1: [sample][2S][R][128]
+    uint16_t* Wp;
     long long pstride;         // elements per sample of a plane buffer
     int R;                     // rows of a plane buffer
-    int* err;
+    int* err;                  // err[0]: a wait ran out (all CTAs stop); err[1]: fp16 range
+    int f16;                   // planes are scaled fp16 pairs (S == 2) instead of bf16 pieces
     int zlo, zhi;              // output rows/cols in [zlo, zhi) are structurally zero (tiles inside skipped)
+    uint16_t* Np;              // mode 0: split planes of the next panel's block column (tiles J = 0, I >= 1), or null
+    int Mn;                    // rows of the next panel's block column
 };
 
 TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
@@ -228,12 +242,45 @@ TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& sk
 }
 
 template <int S>
-TAGS_D void split_pieces(float x, __nv_bfloat16* p) {
+TAGS_D void split_pieces(float x, uint16_t* p, bool f16, int& ovf) {
+    if (S == 2 && f16) {
+        const float y = x * kF16Scale;
+        if (!(fabsf(y) <= 65504.f)) ovf = 1;
+        const __half h = __float2half_rn(y);
+        p[0] = __half_as_ushort(h);
+        p[1] = __half_as_ushort(__float2half_rn(y - __half2float(h)));
+        return;
+    }
     float r = x;
 #pragma unroll
     for (int q = 0; q < S; ++q) {
-        p[q] = __float2bfloat16_rn(r);
-        r -= __bfloat162float(p[q]);
+        const __nv_bfloat16 b = __float2bfloat16_rn(r);
+        p[q] = __bfloat16_as_ushort(b);
+        r -= __bfloat162float(b);
+    }
+}
+
+// Row `row`, columns c0 .. c0+15 of a plane buffer [2S][R][128] (real
+// pieces, then imaginary pieces): the S-piece split of v[0..15].
+template <int S>
+TAGS_D void store_planes16(uint16_t* P, int R, int row, int c0, const float2* v, bool f16, int& ovf) {
+    __align__(16) uint16_t pl[2 * S][16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        uint16_t pc[S];
+        split_pieces<S>(v[j].x, pc, f16, ovf);
+#pragma unroll
+        for (int q = 0; q < S; ++q) pl[q][j] = pc[q];
+        split_pieces<S>(v[j].y, pc, f16, ovf);
+#pragma unroll
+        for (int q = 0; q < S; ++q) pl[S + q][j] = pc[q];
+    }
+    const long long off = (long long)row * TB + c0;
+#pragma unroll
+    for (int p = 0; p < 2 * S; ++p) {
+        uint4* d = reinterpret_cast<uint4*>(P + (long long)p * R * TB + off);
+        d[0] = reinterpret_cast<const uint4*>(pl[p])[0];
+        d[1] = reinterpret_cast<const uint4*>(pl[p])[1];
     }
 }
 
@@ -338,7 +385,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
     } else if (warp == 1) {
         // ---- MMA issuer
         if (lane == 0) {
-            const uint32_t idp = idesc_bf16(false), idn = idesc_bf16(true);
+            const uint32_t idp = idesc_mma(false, g.f16 != 0), idn = idesc_mma(true, g.f16 != 0);
             int stage = 0, acc = 0;
             uint32_t phase = 0, aphase = 0;
             bool alive = true;
@@ -395,14 +442,41 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
         // and one half of the columns
         const int quarter = warp & 3, half = (warp - 2) >> 2;
         const int r = 32 * quarter + lane;
+        float2* dinv_w = reinterpret_cast<float2*>(base + C::STAGES * C::STAGE + C::BARS) + (warp - 2) * 64;
         const uint32_t lane_off = (uint32_t)(32 * quarter) << 16;
+        const bool f16 = S == 2 && g.f16 != 0;
+        const float unscale = f16 ? kF16Unscale : 1.f;
+        int ovf = 0;
         int acc = 0;
         uint32_t aphase = 0;
         for (int t = blockIdx.x; t < total; t += gridDim.x) {
             int smp, I, J;
             bool skip;
             tile_of(g, t, smp, I, J, skip);
-            if (skip) continue;
+            if (skip) {
+                // no update of this tile; if it holds rows of the next panel's
+                // block column, their planes are the current values
+                const int gr = TB * I + r;
+                if (MODE == 0 && g.Np && J == 0 && I >= 1 && gr < g.M && gr - TB < g.Mn) {
+                    const float2* Cb = g.Amat + g.mstride * smp;
+                    for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
+                        const float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + cc * 16);
+                        float2 cv[16];
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            cv[j] = cc * 16 + j < g.Nn ? base_p[g.ld * j] : make_float2(0.f, 0.f);
+                        store_planes16<S>(g.Np + g.pstride * smp, g.R, gr - TB, cc * 16, cv, f16, ovf);
+                    }
+                }
+                continue;
+            }
+            if (MODE == 1) {
+                // this warp's 64 columns of D^{-1}, staged before the wait
+                __syncwarp();
+                dinv_w[lane] = g.dinv[(long long)TB * smp + half * 64 + lane];
+                dinv_w[32 + lane] = g.dinv[(long long)TB * smp + half * 64 + 32 + lane];
+                __syncwarp();
+            }
             if (!mbar_wait(tfull(acc), aphase, g.err)) break;
             tc_fence_after();
             const uint32_t accR = tmem + acc * 256, accI = accR + 128;
@@ -413,6 +487,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                 tmem_ld16(accR + lane_off + cc * 16, vr);
                 tmem_ld16(accI + lane_off + cc * 16, vi);
                 if (gr >= g.M) continue;
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    vr[j] *= unscale;
+                    vi[j] *= unscale;
+                }
                 if (MODE == 0) {
                     // all loads of the chunk first, then the stores
                     float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + TB * J + cc * 16);
@@ -421,37 +500,29 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                     for (int j = 0; j < 16; ++j)
                         if (TB * J + cc * 16 + j < g.Nn) cv[j] = base_p[g.ld * j];
 #pragma unroll
-                    for (int j = 0; j < 16; ++j)
-                        if (TB * J + cc * 16 + j < g.Nn) base_p[g.ld * j] = make_float2(cv[j].x - vr[j], cv[j].y - vi[j]);
+                    for (int j = 0; j < 16; ++j) {
+                        cv[j] = make_float2(cv[j].x - vr[j], cv[j].y - vi[j]);
+                        if (TB * J + cc * 16 + j < g.Nn) base_p[g.ld * j] = cv[j];
+                    }
+                    if (g.Np && J == 0 && I >= 1 && gr - TB < g.Mn) {
+                        // the next panel's block column, as split planes
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (cc * 16 + j >= g.Nn) cv[j] = make_float2(0.f, 0.f);
+                        store_planes16<S>(g.Np + g.pstride * smp, g.R, gr - TB, cc * 16, cv, f16, ovf);
+                    }
                 } else {
-                    const float2* dv = g.dinv + (long long)TB * smp;
-                    __align__(16) __nv_bfloat16 lp[2 * S][16], wp[2 * S][16];
+                    const float2* dv = dinv_w - half * 64;      // indexed by the tile column
+                    float2 lv[16], wv[16];
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int c = cc * 16 + j;
-                        float2 w = make_float2(vr[j], vi[j]);
-                        float2 l = fmulc(w, dv[c]);
-                        if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = l;
-                        __nv_bfloat16 pc[S];
-                        split_pieces<S>(l.x, pc);
-                        for (int q = 0; q < S; ++q) lp[q][j] = pc[q];
-                        split_pieces<S>(l.y, pc);
-                        for (int q = 0; q < S; ++q) lp[S + q][j] = pc[q];
-                        split_pieces<S>(w.x, pc);
-                        for (int q = 0; q < S; ++q) wp[q][j] = pc[q];
-                        split_pieces<S>(w.y, pc);
-                        for (int q = 0; q < S; ++q) wp[S + q][j] = pc[q];
+                        wv[j] = make_float2(vr[j], vi[j]);
+                        lv[j] = fmulc(wv[j], dv[c]);
+                        if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = lv[j];
                     }
-                    const long long rowoff = (long long)gr * TB + cc * 16;
-#pragma unroll
-                    for (int p = 0; p < 2 * S; ++p) {
-                        uint4* dl = reinterpret_cast<uint4*>(g.Lp + g.pstride * smp + (long long)p * g.R * TB + rowoff);
-                        uint4* dw = reinterpret_cast<uint4*>(g.Wp + g.pstride * smp + (long long)p * g.R * TB + rowoff);
-                        dl[0] = reinterpret_cast<const uint4*>(lp[p])[0];
-                        dl[1] = reinterpret_cast<const uint4*>(lp[p])[1];
-                        dw[0] = reinterpret_cast<const uint4*>(wp[p])[0];
-                        dw[1] = reinterpret_cast<const uint4*>(wp[p])[1];
-                    }
+                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, gr, cc * 16, lv, f16, ovf);
+                    store_planes16<S>(g.Wp + g.pstride * smp, g.R, gr, cc * 16, wv, f16, ovf);
                 }
             }
             tc_fence_before();
@@ -459,6 +530,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
             if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tempty(acc)) : "memory");
             if (++acc == 2) { acc = 0; aphase ^= 1; }
         }
+        if (ovf) atomicOr(g.err + kErrRange, 1);
     }
     tc_fence_before();
     __syncthreads();
@@ -467,107 +539,159 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
 
 // ---- diagonal block: LDL^T, L11^{-1} -------------------------------------------------
 
-// One CTA per sample. S (column-major 128 x 128 complex FP32) in shared memory.
-__global__ void __launch_bounds__(512) k_ldl_diag(float2* __restrict__ A0, long long ld, long long mstride, int j0,
-                                                  int jb, __nv_bfloat16* __restrict__ linv_planes,
-                                                  float2* __restrict__ dinv, int* __restrict__ info,
-                                                  float2* __restrict__ linv32, long long lstride, int NS) {
-    extern __shared__ __align__(16) float2 S[];        // S[c * TB + r]
-    __shared__ float2 colv[TB];
-    const int smp = blockIdx.x, tid = threadIdx.x;
+// One CTA of 512 threads per sample. The block lives in registers: thread
+// (lane tx, warp ty) holds the 32 elements (tx + 32 p, ty + 16 q), p < 4,
+// q < 8, so column k belongs to warp k % 16 and row k to lane k % 32 of
+// every warp. Step k of the right-looking LDL^T: the owner warp of column k
+// forms W = A[k+1:, k] and L = W / d into a double-buffered shared pair, one
+// barrier, then every thread updates its elements i >= j > k. The inverse
+// of the unit lower L11 is the same sweep applied to the identity, with
+// the L columns kept in shared memory and the finished row k of L11^{-1}
+// broadcast per step. Outside jb the block is padded with the identity.
+constexpr int DIAG_LD = TB + 1;        // padded row stride of the output staging
+
+__global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, long long ld, long long mstride, int j0,
+                                                     int jb, uint16_t* __restrict__ linv_planes,
+                                                     float2* __restrict__ dinv, int* __restrict__ info,
+                                                     float2* __restrict__ linv32, long long lstride, int NS, int f16,
+                                                     int* __restrict__ err) {
+    extern __shared__ __align__(16) float2 S[];        // L columns S[k * TB + i]; later X staged S[i * DIAG_LD + j]
+    __shared__ float2 wv[2][TB], lv[2][TB], dsh[TB];
+    __shared__ int zero_at;
+    const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5, smp = blockIdx.x;
     float2* A = A0 + mstride * smp;
-    for (int t = tid; t < TB * TB; t += blockDim.x) {
-        int r = t % TB, c = t / TB;
-        float2 v;
-        if (r < jb && c < jb) {
-            int rr = r >= c ? r : c, cc2 = r >= c ? c : r;     // lower triangle, mirrored
-            v = A[(long long)(j0 + rr) + ld * (j0 + cc2)];
-        } else {
-            v = make_float2(r == c ? 1.f : 0.f, 0.f);
+    if (tid == 0) zero_at = 0x7fffffff;
+    float2 a[4][8];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = tx + 32 * p, j = ty + 16 * q;
+            float2 v = make_float2(i == j ? 1.f : 0.f, 0.f);
+            if (i < jb && j < jb && i >= j) v = A[(long long)(j0 + i) + ld * (j0 + j)];
+            a[p][q] = v;
         }
-        S[c * TB + r] = v;
-    }
     __syncthreads();
-    // right-looking LDL^T without pivoting on the lower triangle
-    for (int k = 0; k < TB; ++k) {
-        const float2 d = S[k * TB + k];
-        if (tid == 0 && k < jb && !(d.x != 0.f || d.y != 0.f) && *(info + smp) == 0) info[smp] = j0 + k + 1;
-        const float2 di = crecip_f(d);
-        // column below the pivot: keep W = old values, L = W / d
-        for (int i = k + 1 + tid; i < TB; i += blockDim.x) colv[i] = S[k * TB + i];
-        __syncthreads();
-        const int n = TB - k - 1;
-        for (int t = tid; t < n * n; t += blockDim.x) {
-            int i = k + 1 + t % n, j = k + 1 + t / n;
-            if (i >= j) {
-                // S_ij -= W_i W_j / d
-                float2 li = fmulc(colv[i], di);
-                S[j * TB + i] = fsub(S[j * TB + i], fmulc(li, colv[j]));
+    // ---- LDL^T: k = 16 kq + kw; q index kq and p index kq / 2 are compile-time
+#pragma unroll
+    for (int kq = 0; kq < 8; ++kq) {
+        for (int kw = 0; kw < 16; ++kw) {
+            const int k = 16 * kq + kw, buf = k & 1;
+            if (ty == kw) {
+                const int src = k & 31;
+                float2 d;
+                d.x = __shfl_sync(0xffffffffu, a[kq >> 1][kq].x, src);
+                d.y = __shfl_sync(0xffffffffu, a[kq >> 1][kq].y, src);
+                if (tx == 0) {
+                    dsh[k] = d;
+                    if (!(d.x != 0.f || d.y != 0.f) && k < jb) atomicMin(&zero_at, k);
+                }
+                const float2 di = crecip_f(d);
+#pragma unroll
+                for (int p = 0; p < 4; ++p) {
+                    const int i = tx + 32 * p;
+                    if (i > k) {
+                        const float2 w = a[p][kq], l = fmulc(w, di);
+                        wv[buf][i] = w;
+                        lv[buf][i] = l;
+                        S[k * TB + i] = l;
+                        a[p][kq] = l;
+                    }
+                }
             }
+            __syncthreads();
+            float2 L[4], W[8];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) L[p] = lv[buf][tx + 32 * p];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) W[q] = wv[buf][ty + 16 * q];
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = kq; q < 8; ++q) {       // columns j < 16 kq are finished
+                    const int i = tx + 32 * p, j = ty + 16 * q;
+                    if (j > k && i >= j) a[p][q] = fsub(a[p][q], fmulc(L[p], W[q]));
+                }
         }
-        for (int i = k + 1 + tid; i < TB; i += blockDim.x) S[k * TB + i] = fmulc(colv[i], di);
-        __syncthreads();
     }
-    // write L11 (unit lower) and D back; D^{-1} for the panel epilogue
-    for (int t = tid; t < jb * jb; t += blockDim.x) {
-        int r = t % jb, c = t / jb;
-        if (r >= c) A[(long long)(j0 + r) + ld * (j0 + c)] = S[c * TB + r];
-    }
-    for (int c = tid; c < TB; c += blockDim.x) {
-        float2 v = make_float2(0.f, 0.f);
-        if (c < jb) v = crecip_f(S[c * TB + c]);
-        dinv[(long long)TB * smp + c] = v;
-    }
+    // L11 (unit lower, strictly below the diagonal) and D back to A
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int i = tx + 32 * p, j = ty + 16 * q;
+            if (i < jb && j < jb && i >= j) A[(long long)(j0 + i) + ld * (j0 + j)] = a[p][q];
+        }
     __syncthreads();
-    // in-place inverse of the unit lower L11: for j = 127..0,
-    // X[j+1:, j] = -X[j+1:, j+1:] L[j+1:, j]
-    for (int j = TB - 1; j >= 0; --j) {
-        for (int i = j + 1 + tid; i < TB; i += blockDim.x) colv[i] = S[j * TB + i];
-        __syncthreads();
-        for (int i = j + 1 + tid; i < TB; i += blockDim.x) {
-            float2 acc = colv[i];                       // X[i][i] = 1
-            for (int k = j + 1; k < i; ++k) acc = ffmac(S[k * TB + i], colv[k], acc);
-            S[j * TB + i] = make_float2(-acc.x, -acc.y);
+    if (tid == 0 && zero_at < jb && info[smp] == 0) info[smp] = j0 + zero_at + 1;
+    if (tid < TB) dinv[(long long)TB * smp + tid] = tid < jb ? crecip_f(dsh[tid]) : make_float2(0.f, 0.f);
+    // ---- X = L11^{-1}: for k = 0..126, X[i, j] -= L[i, k] X[k, j] (i > k, j <= k);
+    // row k of X is final once step k - 1 is done. Reuse a[][] for X.
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) a[p][q] = make_float2(tx + 32 * p == ty + 16 * q ? 1.f : 0.f, 0.f);
+#pragma unroll
+    for (int kp = 0; kp < 4; ++kp) {
+        for (int kl = 0; kl < 32; ++kl) {
+            const int k = 32 * kp + kl, buf = k & 1;
+            if (k == TB - 1) break;
+            if (tx == kl) {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) wv[buf][ty + 16 * q] = a[kp][q];
+            }
+            __syncthreads();
+            float2 X[8], L[4];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) X[q] = wv[buf][ty + 16 * q];
+#pragma unroll
+            for (int p = kp; p < 4; ++p) L[p] = S[k * TB + tx + 32 * p];
+#pragma unroll
+            for (int p = kp; p < 4; ++p)             // rows i < 32 kp are finished
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int i = tx + 32 * p, j = ty + 16 * q;
+                    if (i > k && j <= k) a[p][q] = fsub(a[p][q], fmulc(L[p], X[q]));
+                }
         }
-        __syncthreads();
     }
+    __syncthreads();                                    // S (L columns) is dead: stage X row-major, padded
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) S[(tx + 32 * p) * DIAG_LD + ty + 16 * q] = a[p][q];
+    __syncthreads();
     // L11^{-1} kept in FP32 for the triangular solves, row-major, zero outside
     // jb: the inverse itself and its transpose (both read row-wise there)
     float2* X32 = linv32 + lstride * smp + (long long)(j0 / TB) * 2 * TB * TB;
+    // L11^{-1} as split planes (NS pieces of the real part, then of the
+    // imaginary part), row-major: B[n][k] = X[n][k] (k <= n), zero outside jb
+    uint16_t* P = linv_planes + (long long)smp * 2 * SMAX * TB * TB;   // sample stride of the tensor map
+    int ovf = 0;
     for (int t = tid; t < TB * TB; t += blockDim.x) {
-        int nrow = t / TB, k = t % TB;
+        const int n = t / TB, k = t % TB;
         float2 v = make_float2(0.f, 0.f), vt = make_float2(0.f, 0.f);
-        if (nrow < jb && k < jb) {
-            if (k == nrow) v = vt = make_float2(1.f, 0.f);
-            else if (k < nrow) v = S[k * TB + nrow];
-            else vt = S[nrow * TB + k];
+        if (n < jb && k < jb) {
+            v = S[n * DIAG_LD + k];
+            vt = S[k * DIAG_LD + n];
         }
         X32[t] = v;
         X32[TB * TB + t] = vt;
-    }
-    // L11^{-1} as split planes (NS pieces of the real part, then of the
-    // imaginary part), row-major: B[n][k] = X[n][k] (k <= n), zero outside jb
-    __nv_bfloat16* P = linv_planes + (long long)smp * 2 * SMAX * TB * TB;   // sample stride of the tensor map
-    for (int t = tid; t < TB * TB; t += blockDim.x) {
-        int nrow = t / TB, k = t % TB;
-        float2 v = make_float2(0.f, 0.f);
-        if (nrow < jb && k < jb) {
-            if (k == nrow) v = make_float2(1.f, 0.f);
-            else if (k < nrow) v = S[k * TB + nrow];
-        }
-        __nv_bfloat16 pc[SMAX];
-        split_n(v.x, pc, NS);
+        uint16_t pc[SMAX];
+        split_n(v.x, pc, NS, f16 != 0, ovf);
         for (int q = 0; q < NS; ++q) P[(long long)q * TB * TB + t] = pc[q];
-        split_n(v.y, pc, NS);
+        split_n(v.y, pc, NS, f16 != 0, ovf);
         for (int q = 0; q < NS; ++q) P[(long long)(NS + q) * TB * TB + t] = pc[q];
     }
+    if (ovf) atomicOr(err + kErrRange, 1);
 }
 
 // A21 (rows j0+jb .. j0+jb+M, columns j0 .. j0+jb) -> split planes, row-major
 // [sample][2 NS][R][128], columns >= jb zero. Tile: 32 rows x 128 columns.
 __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__ A0, long long ld, long long mstride,
-                                                      int j0, int jb, int M, __nv_bfloat16* __restrict__ planes,
-                                                      long long pstride, int R, int NS) {
+                                                      int j0, int jb, int M, uint16_t* __restrict__ planes,
+                                                      long long pstride, int R, int NS, int f16,
+                                                      int* __restrict__ err) {
     __shared__ float2 t[TB][33];
     const int smp = blockIdx.y, r0 = blockIdx.x * 32;
     const float2* A = A0 + mstride * smp;
@@ -578,18 +702,20 @@ __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__
         t[c][rr] = v;
     }
     __syncthreads();
-    __nv_bfloat16* P = planes + pstride * smp;
+    uint16_t* P = planes + pstride * smp;
+    int ovf = 0;
     for (int q = threadIdx.x; q < 32 * TB; q += blockDim.x) {
         int c = q % TB, rr = q / TB;
         if (r0 + rr >= M) continue;
         float2 v = t[c][rr];
         long long o = (long long)(r0 + rr) * TB + c;
-        __nv_bfloat16 pc[SMAX];
-        split_n(v.x, pc, NS);
+        uint16_t pc[SMAX];
+        split_n(v.x, pc, NS, f16 != 0, ovf);
         for (int q = 0; q < NS; ++q) P[(long long)q * R * TB + o] = pc[q];
-        split_n(v.y, pc, NS);
+        split_n(v.y, pc, NS, f16 != 0, ovf);
         for (int q = 0; q < NS; ++q) P[(long long)(NS + q) * R * TB + o] = pc[q];
     }
+    if (ovf) atomicOr(err + kErrRange, 1);
 }
 
 // ---- solves with the factors: L D L^T x = b (one right-hand side per sample) ----------
@@ -694,7 +820,7 @@ int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samp
     cuuint64_t strides[3] = {(cuuint64_t)TB * 2, (cuuint64_t)TB * 2 * rows, (cuuint64_t)TB * 2 * rows * nplanes};
     cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)TB, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, base, dims, strides, box, estr,
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
@@ -722,7 +848,7 @@ size_t tags_ldl_tc_workspace(int N, int batch) {
 
 static float2* linv32_of(void* ws, int N, int batch_cap) {
     const long long pstride = plane_stride(N);
-    __nv_bfloat16* Lin = reinterpret_cast<__nv_bfloat16*>(ws) + 3 * pstride * batch_cap;
+    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + 3 * pstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     return dinv + (long long)TB * batch_cap;
 }
@@ -738,13 +864,32 @@ static int num_sms() {
 }
 
 template <int S, int MODE>
+static int set_gemm_attr() {
+    TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc<S, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      GemmCfg<S>::SMEM));
+    return 0;
+}
+
+// Kernel attributes and the tensor-map encoder, set once per process before
+// any launch (and so before any graph capture).
+int tags_ldl_tc_prepare() {
+    static std::once_flag once;
+    static int rc = 0;
+    std::call_once(once, [] {
+        rc = set_gemm_attr<2, 0>();
+        if (!rc) rc = set_gemm_attr<2, 1>();
+        if (!rc) rc = set_gemm_attr<3, 0>();
+        if (!rc) rc = set_gemm_attr<3, 1>();
+        if (!rc && cudaFuncSetAttribute(k_ldl_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(TB * DIAG_LD * sizeof(float2))) != cudaSuccess)
+            rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_ldl_diag) failed");
+        if (!rc && !encode_fn()) rc = tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
+    });
+    return rc;
+}
+
+template <int S, int MODE>
 static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc<S, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          GemmCfg<S>::SMEM));
-        attr = true;
-    }
     const int total = g.tiles * g.nb;
     const int grid = total < num_sms() ? total : num_sms();
     if (grid <= 0) return 0;
@@ -789,19 +934,17 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
 // used) in place: L strictly below the diagonal, D on it.
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
                 int* err, int zl_m, int pieces, cudaStream_t st) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        TAGS_CUDA_OK(cudaFuncSetAttribute(k_ldl_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)(TB * TB * sizeof(float2))));
-        attr_done = true;
-    }
+    if (int e0 = tags_ldl_tc_prepare()) return e0;
+    // split forms: 3 = bf16 x 3 pieces (6 products), 2 = bf16 x 2 (3 products),
+    // TAGS_SPLIT_F16 = scaled fp16 x 2 (3 products, range-checked)
+    const int f16 = pieces == TAGS_SPLIT_F16 ? 1 : 0;
     const int NS = pieces == 3 ? 3 : 2;
     // planes of this run use 2 NS of the 2 SMAX slots of each sample
     const long long pstride = plane_stride(N);
-    __nv_bfloat16* A21p = reinterpret_cast<__nv_bfloat16*>(ws);
-    __nv_bfloat16* Lp = A21p + pstride * batch_cap;
-    __nv_bfloat16* Wp = Lp + pstride * batch_cap;
-    __nv_bfloat16* Lin = Wp + pstride * batch_cap;
+    uint16_t* A21p = reinterpret_cast<uint16_t*>(ws);
+    uint16_t* Lp = A21p + pstride * batch_cap;
+    uint16_t* Wp = Lp + pstride * batch_cap;
+    uint16_t* Lin = Wp + pstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
@@ -817,14 +960,17 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         const int jb = N - j0 < TB ? N - j0 : TB;
         const int rest = N - j0 - jb;
         int pf = tags_prof_begin(TAGS_PROF_LDL_DIAG, st);
-        k_ldl_diag<<<nb, 512, TB * TB * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, info, L32, ls,
-                                                              NS);
+        k_ldl_diag<<<nb, 512, TB * DIAG_LD * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, info, L32, ls,
+                                                              NS, f16, err);
         tags_prof_end(TAGS_PROF_LDL_DIAG, pf, st, 4.0 / 3.0 * jb * (double)jb * jb * nb, 16.0 * jb * jb * nb);
         tags_note_launch();
         if (rest <= 0) break;
-        k_panel_planes<<<dim3((rest + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, rest, A21p, pstride, N,
-                                                                   NS);
-        tags_note_launch();
+        if (j0 == 0) {
+            // later panels get their block column's planes from the previous trailing update
+            k_panel_planes<<<dim3((rest + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, rest, A21p, pstride,
+                                                                       N, NS, f16, err);
+            tags_note_launch();
+        }
         const int T = (rest + TB - 1) / TB;
         GemmArgs g{};
         // While the first zl_m columns (the ZL block of the ordering ZL, ZT,
@@ -851,6 +997,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.pstride = pstride;
         g.R = N;
         g.err = err;
+        g.f16 = f16;
         pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
         e = NS == 3 ? launch_gemm<3>(mA21, mLin, g, st) : launch_gemm<2>(mA21, mLin, g, st);
         if (e) return e;
@@ -865,6 +1012,14 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.Nn = rest;
         g.row0 = j0 + jb;
         g.col0 = j0 + jb;
+        // the next panel (columns j0 + jb ...) has rest - jb' rows below its
+        // diagonal block: its split planes come out of this update's first
+        // tile column (A21 planes are free again: the panel GEMM above read them)
+        {
+            const int jbn = rest < TB ? rest : TB;
+            g.Mn = rest - jbn;
+            g.Np = g.Mn > 0 ? A21p : nullptr;
+        }
         pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
         e = NS == 3 ? launch_gemm<3>(mL, mW, g, st) : launch_gemm<2>(mL, mW, g, st);
         if (e) return e;
@@ -895,28 +1050,31 @@ extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
     const size_t wsb = tags_ldl_tc_workspace(N, nb);
     if (cudaMalloc(&A, sizeof(float2) * NN * nb) != cudaSuccess || cudaMalloc(&Ad, sizeof(double2) * NN * nb) != cudaSuccess ||
         cudaMalloc(&ws, wsb) != cudaSuccess || cudaMalloc(&info, sizeof(int) * nb) != cudaSuccess ||
-        cudaMalloc(&err, sizeof(int)) != cudaSuccess) {
+        cudaMalloc(&err, 2 * sizeof(int)) != cudaSuccess) {
         rc = tags_fail(TAGS_E_NOMEM, "device allocation failed");
     }
+    if (!rc && pieces != 2 && pieces != 3 && pieces != TAGS_SPLIT_F16)
+        rc = tags_fail(TAGS_E_ARG, "tags_debug_ldl: pieces must be 2, 3 or 16");
     std::vector<float2> hf(NN * nb);
     if (!rc) {
         for (long long q = 0; q < NN * nb; ++q) hf[q] = make_float2((float)a[q].re, (float)a[q].im);
         cudaMemcpyAsync(A, hf.data(), sizeof(float2) * NN * nb, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(ws, 0, wsb, st);
-        cudaMemsetAsync(err, 0, sizeof(int), st);
+        cudaMemsetAsync(err, 0, 2 * sizeof(int), st);
         rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, 0, pieces, st);
     }
-    int herr = 0;
+    int herr[2] = {0, 0};
     std::vector<int> hinfo(nb, 0);
     if (!rc) {
         cudaMemcpyAsync(hf.data(), A, sizeof(float2) * NN * nb, cudaMemcpyDeviceToHost, st);
-        cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st);
+        cudaMemcpyAsync(herr, err, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
         cudaMemcpyAsync(hinfo.data(), info, sizeof(int) * nb, cudaMemcpyDeviceToHost, st);
         if (cudaStreamSynchronize(st) != cudaSuccess) rc = tags_fail(TAGS_E_CUDA, "tags_debug_ldl: stream failed");
     }
     if (!rc) {
         for (long long q = 0; q < NN * nb; ++q) a[q] = {hf[q].x, hf[q].y};
-        if (herr) rc = tags_fail(TAGS_E_CUDA, "tags_debug_ldl: tensor-core wait ran out");
+        if (herr[0]) rc = tags_fail(TAGS_E_CUDA, "tags_debug_ldl: tensor-core wait ran out");
+        else if (herr[1]) rc = tags_fail(TAGS_E_NONFINITE, "tags_debug_ldl: a value left the fp16 split's range");
         for (int q = 0; q < nb && !rc; ++q)
             if (hinfo[q]) rc = hinfo[q];
     }

@@ -11,9 +11,13 @@
 //
 // Layout: column-major, leading dimension ld, one matrix per blockIdx.z
 // (pointer + z * stride). ipiv is 0-based global row indices.
+#include <mutex>
+#include <type_traits>
+
 #include "tags_common.cuh"
 #include "tags_internal.h"
-#include <type_traits>
+#include "../../include/tags_gpu.h"
+#include "plan.h"
 
 namespace {
 
@@ -320,16 +324,32 @@ __global__ void k_trsv_update(const T* __restrict__ A0, int n, long long ld, lon
 
 constexpr int NB = 32;
 
+}  // namespace
+
+// Kernel attributes of the LU, set once per process before any launch (and
+// so before any graph capture).
+int tags_lu_prepare() {
+    static std::once_flag once;
+    static int rc = 0;
+    std::call_once(once, [] {
+        const int g64 = (int)(2 * NB * 64 * sizeof(double2)), g32 = (int)(2 * NB * 64 * sizeof(float2));
+        if (cudaFuncSetAttribute(k_gemm_update<double2, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, g64) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(k_gemm_update<float2, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, g32) !=
+                cudaSuccess)
+            rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_gemm_update) failed");
+    });
+    return rc;
+}
+
+namespace {
+
 template <typename T>
 int lu_impl(T* A, int n, long long ld, long long stride, int batch, int pivot, int* ipiv, int* info,
             cudaStream_t st) {
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * batch, st));
     const size_t gsmem = 2 * NB * 64 * sizeof(T);
-    static bool attr = false;
-    if (!attr && gsmem > 48 * 1024) {
-        TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_update<T, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)gsmem));
-    }
-    attr = true;
+    if (int e = tags_lu_prepare()) return e;
     for (int j0 = 0; j0 < n; j0 += NB) {
         int jb = min(NB, n - j0);
         k_panel<T><<<dim3(1, 1, batch), PANEL_THREADS, 0, st>>>(A, n, ld, stride, j0, jb, pivot, ipiv, info);

@@ -15,10 +15,13 @@
 //   2. symmetric scaling D = diag(1/sqrt(max_j |W'_ij|)), W'' = D P W P^T D;
 //   3. LDL^T of W'' without pivoting, complex FP32 storage, trailing updates
 //      and triangular-solve panels on the tensor cores (ldl_tc.cu);
-//   4. iterative refinement in FP64: r = b - W x is evaluated in FP64 from the
-//      FP64 impedance blocks and the exact incidence (sparse, +-1 / 0.5), the
-//      correction from the FP32 factors, until the correction is below
-//      4 eps |x| or stops shrinking;
+//   4. iterative refinement: x in FP64, r = b - W x with the exact incidence
+//      (sparse, +-1 / 0.5) in FP64 and the impedance blocks times x in
+//      two-float arithmetic (about 2^-44 relative), the correction from the
+//      FP32 factors; a sample stops once the correction is below 1e-10 |x|
+//      or stops shrinking. The stopping decision runs on the device
+//      (k_ir_decide), so one refinement step is a fixed launch sequence that a
+//      CUDA graph repeats under a conditional while-node;
 //   5. samples that do not converge are re-solved by the plain FP64 path
 //      (LU with partial pivoting).
 #include <algorithm>
@@ -47,11 +50,11 @@ __global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restri
     int b = blockIdx.z;
     if (warp >= m) return;
     const float2* col = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m + (size_t)m * warp;
-    double mx = 0.0, sm = 0.0;
+    float mx = 0.f, sm = 0.f;       // a scaling and a norm estimate: FP32 is plenty
     for (int j = lane; j < m; j += 32) {
-        float2 z = col[j];
-        double a = sqrtf(z.x * z.x + z.y * z.y);
-        mx = fmax(mx, a);
+        const float2 z = col[j];
+        const float a = sqrtf(z.x * z.x + z.y * z.y);
+        mx = fmaxf(mx, a);
         sm += a;
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -61,8 +64,8 @@ __global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restri
     if (lane == 0) {
         double inc = blk == 0 ? 1.0 : 0.5;            // incidence entries of the row
         int row = blk * m + warp;                      // reordered index
-        scale[(size_t)b * N + row] = 1.0 / sqrt(fmax(mx, inc));
-        rsum[(size_t)b * N + row] = sm + 2.0 * inc;
+        scale[(size_t)b * N + row] = 1.0 / sqrt(fmax((double)mx, inc));
+        rsum[(size_t)b * N + row] = (double)sm + 2.0 * inc;
     }
 }
 
@@ -78,8 +81,10 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 }
 
 // W'' (complex FP32, column-major N x N, reordered and scaled), lower triangle.
-// Grid: x over 256-row chunks, y over columns, z over samples.
-__global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const signed char* __restrict__ cond,
+// Grid: x over 256-row chunks, y over columns, z over samples. Node rows of a
+// segment column hold its two incidence entries (start +1 / end -1 in the ZL
+// columns, 0.5 in the ZT columns), read from the per-segment incidence list.
+__global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const Incidence inc,
                                                const double* __restrict__ scale, int m, int n,
                                                float2* __restrict__ A) {
     const int N = n + 2 * m;
@@ -96,10 +101,11 @@ __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, con
         vx = -z.x;
         vy = -z.y;
     } else if (bi == 2 && bj < 2) {
-        const int c = cond[(size_t)(i - 2 * m) * m + (j - bj * m)];
-        if (c) vx = bj == 0 ? (c == 1 ? 1.f : -1.f) : 0.5f;
+        const int e = j - bj * m, nd = i - 2 * m;
+        for (int q = inc.seg_ptr[e]; q < inc.seg_ptr[e + 1]; ++q)
+            if (inc.seg_node[q] == nd) vx = bj == 0 ? (float)inc.seg_a[q] : 0.5f;
     }
-    const float s = (float)(d[i] * d[j]);
+    const float s = (float)d[i] * (float)d[j];
     A[(size_t)b * N * N + (size_t)j * N + i] = make_float2(vx * s, vy * s);
 }
 
@@ -109,10 +115,12 @@ TAGS_D int orig_of(int ip, int m, int n) {
 }
 
 // rf = D P r (FP32)
+// (first kernel of a refinement step: also clears the step's reductions)
 __global__ void k_ir_rhs(const double2* __restrict__ r, const double* __restrict__ scale, int m, int n,
-                         float2* __restrict__ rf) {
+                         float2* __restrict__ rf, double* __restrict__ norms) {
     const int N = n + 2 * m;
     int ip = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (blockIdx.x == 0 && threadIdx.x < 3) norms[4 * b + threadIdx.x] = 0.0;
     if (ip >= N) return;
     double2 v = r[(size_t)b * N + orig_of(ip, m, n)];
     double s = scale[(size_t)b * N + ip];
@@ -245,6 +253,88 @@ __global__ void k_max_rows(const double* __restrict__ rsum, int N, double* __res
     atomic_max_nonneg(norms + 4 * b + 3, rsum[(size_t)b * N + i]);
 }
 
+// Refinement state of a pass (device): per sample active / converged /
+// iterations, previous correction size, max row sum of W, backward error;
+// the step counter and the continue flag.
+struct IrState {
+    int* active;
+    int* conv;
+    int* iters;
+    double* prev_dx;
+    double* wnorm;
+    double* berr;
+    int* step;       // steps done
+    int* cont;       // 1 while another step is wanted
+};
+
+IrState ir_state(tags_plan_s* p) {
+    const int b = p->batch;
+    IrState s;
+    s.active = p->d_iri;
+    s.conv = p->d_iri + b;
+    s.iters = p->d_iri + 2 * b;
+    s.step = p->d_iri + 3 * b;
+    s.cont = p->d_iri + 3 * b + 1;
+    s.prev_dx = p->d_ird;
+    s.wnorm = p->d_ird + b;
+    s.berr = p->d_ird + 2 * b;
+    return s;
+}
+
+// A sample refines unless its static-order factorisation hit a zero pivot
+// or a tensor-core wait ran out (FP64 fallback), or an fp16 split value left
+// its range (the pass is factorised again with bf16 pieces).
+__global__ void k_ir_init(const double* __restrict__ norms, const int* __restrict__ info,
+                          const int* __restrict__ tc_err, int nb, IrState s) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q == 0) {
+        *s.step = 0;
+        *s.cont = 1;
+    }
+    if (q >= nb) return;
+    s.active[q] = info[q] == 0 && tc_err[0] == 0 && tc_err[1] == 0;
+    s.conv[q] = 0;
+    s.iters[q] = 0;
+    s.prev_dx[q] = INFINITY;
+    s.wnorm[q] = norms[4 * q + 3];
+    s.berr[q] = 0.0;
+}
+
+// After a refinement step: per sample, stop once the correction is below
+// 1e-10 |x| (each step contracts the error by about kappa * eps_factor, a few
+// 1e-3 here, so the error left is ~1e-13 |x|, far under the ~1e-7 of the
+// FP32 impedance fill) or once it stops shrinking (accepted when the backward
+// error is below 1e-12); NaN goes to the fallback. One CTA. Sets the continue
+// flag and, inside a graph, the while-node condition.
+__global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ norms, int nb, int max_steps, IrState s,
+                                                    cudaGraphConditionalHandle cond, int set_cond) {
+    const int step = *s.step;
+    int any = 0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) {
+        if (!s.active[q]) continue;
+        s.iters[q] = step + 1;
+        const double dx = norms[4 * q + 0], xn = norms[4 * q + 1], rn = norms[4 * q + 2];
+        const double be = rn / (s.wnorm[q] * xn + 1e-300);
+        s.berr[q] = be;
+        if (!(dx == dx) || !(xn == xn)) { s.active[q] = 0; continue; }
+        if (dx <= 1e-10 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
+        if (step >= 2 && dx > 0.5 * s.prev_dx[q]) {
+            s.conv[q] = be <= 1e-12;
+            s.active[q] = 0;
+            continue;
+        }
+        s.prev_dx[q] = dx;
+        any = 1;
+    }
+    any = __syncthreads_or(any);
+    if (threadIdx.x == 0) {
+        const int c = any && step + 1 < max_steps;
+        *s.step = step + 1;
+        *s.cont = c;
+        if (set_cond) cudaGraphSetConditional(cond, c ? 1u : 0u);
+    }
+}
+
 }  // namespace
 
 int tags_mixed_alloc(tags_plan_s* p) {
@@ -259,17 +349,21 @@ int tags_mixed_alloc(tags_plan_s* p) {
     TAGS_CUDA_OK(cudaMalloc(&p->d_scale, sizeof(double) * 2 * N * b));   // scale + row sums
     TAGS_CUDA_OK(cudaMalloc(&p->d_r, sizeof(double2) * 2 * N * b));      // residual + right-hand side
     TAGS_CUDA_OK(cudaMalloc(&p->d_rf, sizeof(float2) * N * b));
-    TAGS_CUDA_OK(cudaMalloc(&p->d_norms, sizeof(double) * 4 * b + sizeof(int) * b));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_norms, sizeof(double) * 4 * b));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_iri, sizeof(int) * (3 * b + 2)));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_ird, sizeof(double) * 3 * b));
     const size_t ws = tags_ldl_tc_workspace((int)N, (int)b);
     TAGS_CUDA_OK(cudaMalloc(&p->d_ldlws, ws));
     TAGS_CUDA_OK(cudaMemset(p->d_ldlws, 0, ws));
-    TAGS_CUDA_OK(cudaMalloc(&p->d_ldlerr, sizeof(int)));
-    TAGS_CUDA_OK(cudaMemset(p->d_ldlerr, 0, sizeof(int)));
-    return 0;
+    TAGS_CUDA_OK(cudaMalloc(&p->d_ldlerr, 2 * sizeof(int)));     // [0] wait ran out, [1] fp16 range
+    TAGS_CUDA_OK(cudaMemset(p->d_ldlerr, 0, 2 * sizeof(int)));
+    // one-time kernel attributes and driver entry points, outside any capture
+    return tags_ldl_tc_prepare();
 }
 
 int tags_mixed_free(tags_plan_s* p) {
-    void* ptrs[] = {p->d_Z, p->d_A, p->d_scale, p->d_r, p->d_rf, p->d_norms, p->d_fillws, p->d_ldlws, p->d_ldlerr};
+    void* ptrs[] = {p->d_Z,      p->d_A,      p->d_scale, p->d_r,      p->d_rf,  p->d_norms,
+                    p->d_fillws, p->d_ldlws, p->d_ldlerr, p->d_iri, p->d_ird};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     p->d_Z = nullptr;
@@ -306,14 +400,17 @@ static int fallback_plain(tags_plan_s* p, int q, cudaStream_t st) {
     return tags_lu_solve_z(W, (int)N, N, NN, 1, ipiv, x, 1, N, N, st);
 }
 
-int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters, double* h_berr, int* h_conv,
-                           cudaStream_t st) {
+// ---- one pass of nb samples, in four stages -------------------------------------
+// The right-hand side b is in d_x when a pass starts (written by the plan).
+
+static constexpr int kMaxSteps = 40;
+
+// b saved, x = 0, impedance fill, scaling, FP32 working matrix, its LDL^T
+int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     const int m = p->m, n = p->n, N = p->N;
     const size_t NN = (size_t)N * N;
     double* d_rsum = p->d_scale + (size_t)p->batch * N;
     double2* d_b = p->d_r + (size_t)p->batch * N;
-    int* d_active = reinterpret_cast<int*>(p->d_norms + 4 * p->batch);
-    // right-hand side b (written by the plan into d_x), then x = 0
     k_copy_c<<<(unsigned)(((long long)nb * N + 255) / 256), 256, 0, st>>>(p->d_x, d_b, (long long)nb * N);
     tags_note_launch();
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_x, 0, sizeof(double2) * N * nb, st));
@@ -325,93 +422,116 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, N);
     k_rowstats_nodes<<<dim3((n + 127) / 128, nb), 128, 0, st>>>(p->inc.node_ptr, n, m, p->d_scale, d_rsum, N);
     tags_note_launch(2);
-    // 3. FP32 working matrix and its LU (no pivoting)
+    // 3. FP32 working matrix and its LDL^T (no pivoting)
     int pf = tags_prof_begin(TAGS_PROF_BUILD, st);
-    k_build<<<dim3((unsigned)((N + 255) / 256), N, nb), 256, 0, st>>>(p->d_Z, p->d_cond, p->d_scale, m, n, p->d_A);
+    k_build<<<dim3((unsigned)((N + 255) / 256), N, nb), 256, 0, st>>>(p->d_Z, p->inc, p->d_scale, m, n, p->d_A);
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
-    err = tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m,
-                      p->split_pieces, st);
-    if (err) return err;
-    // 4. refinement
-    std::vector<int> active(nb, 1), conv(nb, 0), iters(nb, 0);
-    std::vector<double> prev_dx(nb, INFINITY), hn(4 * nb);
-    std::vector<int> info(nb);
-    int tc_err = 0;
-    TAGS_CUDA_OK(cudaMemcpyAsync(info.data(), p->d_info, sizeof(int) * nb, cudaMemcpyDeviceToHost, st));
-    TAGS_CUDA_OK(cudaMemcpyAsync(&tc_err, p->d_ldlerr, sizeof(int), cudaMemcpyDeviceToHost, st));
-    TAGS_CUDA_OK(cudaStreamSynchronize(st));
-    if (tc_err) {
-        // a tensor-core wait ran out: the whole pass goes to the FP64 path
-        tags_fail(TAGS_E_CUDA, "tensor-core factorisation reported a timeout; samples re-solved in FP64");
-        TAGS_CUDA_OK(cudaMemsetAsync(p->d_ldlerr, 0, sizeof(int), st));
-        for (int q = 0; q < nb; ++q) active[q] = 0;
-    }
-    for (int q = 0; q < nb; ++q)
-        if (info[q] != 0) active[q] = 0;   // zero pivot in the static order: straight to the fallback
-    // r = b initially
+    return tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m,
+                       p->split_pieces, st);
+}
+
+// r = b, max row sum of W per sample, refinement state
+int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st) {
+    const int N = p->N;
+    double* d_rsum = p->d_scale + (size_t)p->batch * N;
+    double2* d_b = p->d_r + (size_t)p->batch * N;
     k_copy_c<<<(unsigned)(((long long)nb * N + 255) / 256), 256, 0, st>>>(d_b, p->d_r, (long long)nb * N);
-    tags_note_launch();
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_norms, 0, sizeof(double) * 4 * nb, st));
     k_max_rows<<<dim3((N + 255) / 256, nb), 256, 0, st>>>(d_rsum, N, p->d_norms);
+    k_ir_init<<<(nb + 255) / 256, 256, 0, st>>>(p->d_norms, p->d_info, p->d_ldlerr, nb, ir_state(p));
+    tags_note_launch(3);
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+// One refinement step: correction from the factors, x update, residual,
+// stopping decision. A fixed launch sequence (graph-capturable).
+int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditionalHandle cond, int set_cond) {
+    const int m = p->m, n = p->n, N = p->N;
+    const size_t NN = (size_t)N * N;
+    double2* d_b = p->d_r + (size_t)p->batch * N;
+    const IrState s = ir_state(p);
+    dim3 gv((N + 255) / 256, nb);
+    k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf, p->d_norms);
     tags_note_launch();
-    std::vector<double> wnorm(nb);
-    TAGS_CUDA_OK(cudaMemcpyAsync(hn.data(), p->d_norms, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st));
+    int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st);
+    if (err) return err;
+    k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active);
+    int pf = tags_prof_begin(TAGS_PROF_RESID, st);
+    k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
+                                                                s.active);
+    k_residual_z<<<dim3((m + 255) / 256, 2 * nb), 256, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
+                                                                s.active);
+    // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
+    tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
+    k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, kMaxSteps, s, cond, set_cond);
+    tags_note_launch(4);
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+// Read the refinement state back, re-solve what did not converge in FP64.
+int tags_mixed_finish(tags_plan_s* p, int nb, cudaStream_t st, int* h_iters, double* h_berr, int* h_conv,
+                      int* h_steps) {
+    const int b = p->batch;
+    std::vector<int> iri(3 * b + 2);
+    std::vector<double> ird(3 * b);
+    int tc_errs[2] = {0, 0};
+    TAGS_CUDA_OK(cudaMemcpyAsync(iri.data(), p->d_iri, sizeof(int) * (3 * b + 2), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(ird.data(), p->d_ird, sizeof(double) * 3 * b, cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(tc_errs, p->d_ldlerr, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaStreamSynchronize(st));
-    for (int q = 0; q < nb; ++q) wnorm[q] = hn[4 * q + 3];
-    const int max_it = 40;
-    for (int it = 0; it < max_it; ++it) {
-        bool any = false;
-        for (int q = 0; q < nb; ++q) any |= active[q] != 0;
-        if (!any) break;
-        TAGS_CUDA_OK(cudaMemcpyAsync(d_active, active.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, st));
-        TAGS_CUDA_OK(cudaMemsetAsync(p->d_norms, 0, sizeof(double) * 4 * nb, st));
-        dim3 gv((N + 255) / 256, nb);
-        k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf);
-        tags_note_launch();
-        err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st);
-        if (err) return err;
-        k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, d_active);
-        pf = tags_prof_begin(TAGS_PROF_RESID, st);
-        k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
-                                                                    d_active);
-        k_residual_z<<<dim3((m + 255) / 256, 2 * nb), 256, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r,
-                                                                    p->d_norms, d_active);
-        // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
-        tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
-        tags_note_launch(2);
-        TAGS_CUDA_OK(cudaGetLastError());
-        TAGS_CUDA_OK(cudaMemcpyAsync(hn.data(), p->d_norms, sizeof(double) * 4 * nb, cudaMemcpyDeviceToHost, st));
-        TAGS_CUDA_OK(cudaStreamSynchronize(st));
-        for (int q = 0; q < nb; ++q) {
-            if (!active[q]) continue;
-            iters[q] = it + 1;
-            double dx = hn[4 * q + 0], xn = hn[4 * q + 1], rn = hn[4 * q + 2];
-            h_berr[q] = rn / (wnorm[q] * xn + 1e-300);
-            if (!(dx == dx) || !(xn == xn)) { active[q] = 0; continue; }       // NaN: fallback
-            // the residual is accurate to ~2^-44 |W| |x| (two-float products): stop
-            // once the correction is below that level or stops shrinking
-            if (dx <= 1e-13 * xn) { active[q] = 0; conv[q] = 1; continue; }
-            if (it >= 2 && dx > 0.5 * prev_dx[q]) {
-                if (h_berr[q] <= 1e-12) conv[q] = 1;
-                active[q] = 0;
-                continue;
-            }
-            prev_dx[q] = dx;
-        }
+    if (tc_errs[1] && !tc_errs[0]) {
+        // an fp16 split value left its range: this plan uses three bf16
+        // pieces from now on (its graphs are recaptured), and the pass is
+        // solved again from its right-hand side
+        TAGS_CUDA_OK(cudaMemsetAsync(p->d_ldlerr, 0, 2 * sizeof(int), st));
+        p->split_pieces = 3;
+        tags_plan_drop_graphs(p);
+        const double2* d_b = p->d_r + (size_t)p->batch * p->N;
+        TAGS_CUDA_OK(cudaMemcpyAsync(p->d_x, d_b, sizeof(double2) * p->N * nb, cudaMemcpyDeviceToDevice, st));
+        int err = tags_mixed_solve_batch(p, nb, nullptr, h_iters, h_berr, h_conv, st);
+        if (h_steps) *h_steps = 0;
+        return err;
     }
-    // 5. fallback for samples that did not converge
+    const int tc_err = tc_errs[0];
+    if (tc_err) {
+        // a tensor-core wait ran out: the pass went to the FP64 path
+        tags_fail(TAGS_E_CUDA, "tensor-core factorisation reported a timeout; samples re-solved in FP64");
+        TAGS_CUDA_OK(cudaMemsetAsync(p->d_ldlerr, 0, 2 * sizeof(int), st));
+    }
+    if (h_steps) *h_steps = iri[3 * b];
     for (int q = 0; q < nb; ++q) {
-        h_iters[q] = iters[q];
-        h_conv[q] = conv[q];
-        if (!conv[q]) {
-            err = fallback_plain(p, q, st);
+        h_iters[q] = iri[2 * b + q];
+        h_conv[q] = iri[b + q];
+        h_berr[q] = ird[2 * b + q];
+        if (!h_conv[q]) {
+            int err = fallback_plain(p, q, st);
             if (err) return err;
         }
     }
     // converged samples report success; fallbacks keep their own LU info
     for (int q = 0; q < nb; ++q)
-        if (conv[q]) TAGS_CUDA_OK(cudaMemsetAsync(p->d_info + q, 0, sizeof(int), st));
+        if (h_conv[q]) TAGS_CUDA_OK(cudaMemsetAsync(p->d_info + q, 0, sizeof(int), st));
     return 0;
+}
+
+// The pass without a graph: the host follows the device's continue flag.
+int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters, double* h_berr, int* h_conv,
+                           cudaStream_t st) {
+    int err = tags_mixed_factor(p, nb, st);
+    if (!err) err = tags_mixed_ir_setup(p, nb, st);
+    if (err) return err;
+    cudaGraphConditionalHandle none = 0;
+    for (int step = 0; step < kMaxSteps; ++step) {
+        err = tags_mixed_ir_step(p, nb, st, none, 0);
+        if (err) return err;
+        int cont = 0;
+        TAGS_CUDA_OK(cudaMemcpyAsync(&cont, p->d_iri + 3 * p->batch + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+        TAGS_CUDA_OK(cudaStreamSynchronize(st));
+        if (!cont) break;
+    }
+    return tags_mixed_finish(p, nb, st, h_iters, h_berr, h_conv, nullptr);
 }

@@ -147,6 +147,9 @@ static void plan_free(tags_plan_s* p) {
     for (void* q : ptrs)
         if (q) cudaFree(q);
     tags_mixed_free(p);
+    tags_plan_drop_graphs(p);
+    if (p->d_sin) cudaFree(p->d_sin);
+    if (p->d_iein) cudaFree(p->d_iein);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
@@ -214,9 +217,12 @@ extern "C" int tags_plan_create(tags_plan* out, const Electrode* electrodes, con
     PLAN_CHECK(cudaMalloc(&p->d_coef, sizeof(SampleCoef) * b));
     PLAN_CHECK(cudaMalloc(&p->d_info, sizeof(int) * b));
     PLAN_CHECK(cudaMalloc(&p->d_x, sizeof(double2) * N * b));
+    PLAN_CHECK(cudaMalloc(&p->d_sin, sizeof(double2) * 2 * b));
     if (precision == TAGS_PLAIN_FP64) {
         PLAN_CHECK(cudaMalloc(&p->d_ipiv, sizeof(int) * N * b));
         PLAN_CHECK(cudaMalloc(&p->d_W, sizeof(double2) * (size_t)NN * b));
+        err = tags_lu_prepare();
+        if (err) { plan_free(p); return err; }
     } else {
         err = tags_mixed_alloc(p);
         if (err) { plan_free(p); return err; }
@@ -256,6 +262,127 @@ int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st)
     return tags_lu_solve_z(p->d_W, (int)N, N, NN, nb, p->d_ipiv, p->d_x, 1, N, N, st);
 }
 
+// ---- graph passes ------------------------------------------------------------------
+
+// Add a while-node after the work captured so far on `st`; its body graph is
+// returned for a separate capture, its condition starts at 1 on every launch.
+static int add_while_node(cudaStream_t st, cudaGraphConditionalHandle* cond, cudaGraph_t* body) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps_rt = nullptr;
+    size_t ndeps = 0;
+    TAGS_CUDA_OK(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps_rt, nullptr, &ndeps));
+    if (cs != cudaStreamCaptureStatusActive) return tags_fail(TAGS_E_CUDA, "stream is not capturing");
+    std::vector<cudaGraphNode_t> deps(deps_rt, deps_rt + ndeps);
+    TAGS_CUDA_OK(cudaGraphConditionalHandleCreate(cond, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = *cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    TAGS_CUDA_OK(cudaGraphAddNode(&node, g, deps.data(), nullptr, deps.size(), &cp));
+    *body = cp.conditional.phGraph_out[0];
+    TAGS_CUDA_OK(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    return 0;
+}
+
+// Capture one pass of nb samples into an executable graph: sample
+// coefficients and right-hand sides from the plan's staging buffers, then the
+// plain FP64 fill + LU + solve, or the mixed factorisation, the refinement
+// set-up and a while-node repeating the refinement step until the device
+// clears the condition. Nothing runs during the capture.
+static int capture_pass(tags_plan_s* p, int nb, double mur, int has_ie, int inj, tags_plan_s::GraphPass* gp) {
+    cudaStream_t st = p->stream;
+    const long long l0 = tags_gpu_launch_count();
+    TAGS_CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    int err = tags_plan_coef(p, p->d_sin, p->d_sin + p->batch, mur, nb, st);
+    if (!err) err = tags_plan_rhs(p, p->d_x, has_ie ? p->d_iein : nullptr, inj, nb, st);
+    cudaGraph_t body = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    if (!err) {
+        if (p->precision == TAGS_PLAIN_FP64) {
+            err = tags_plan_run_plain(p, nullptr, nb, st);
+        } else {
+            err = tags_mixed_factor(p, nb, st);
+            if (!err) err = tags_mixed_ir_setup(p, nb, st);
+            if (!err) err = add_while_node(st, &cond, &body);
+        }
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (!err && ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
+    const long long l1 = tags_gpu_launch_count();
+    if (!err && body) {
+        ce = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (ce != cudaSuccess) {
+            err = tags_fail_cuda(ce, "cudaStreamBeginCaptureToGraph", __FILE__, __LINE__);
+        } else {
+            err = tags_mixed_ir_step(p, nb, st, cond, 1);
+            cudaGraph_t b2 = nullptr;
+            ce = cudaStreamEndCapture(st, &b2);
+            if (!err && ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaStreamEndCapture (body)", __FILE__, __LINE__);
+        }
+    }
+    const long long l2 = tags_gpu_launch_count();
+    tags_note_launch(-(l2 - l0));      // captured, not launched
+    if (!err) {
+        ce = cudaGraphInstantiate(&gp->exec, g, 0);
+        if (ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaGraphInstantiate", __FILE__, __LINE__);
+    }
+    if (g) cudaGraphDestroy(g);
+    if (err) {
+        cudaGetLastError();
+        gp->exec = nullptr;
+        return err;
+    }
+    gp->nb = nb;
+    gp->mur = mur;
+    gp->has_ie = has_ie;
+    gp->inj = inj;
+    gp->launches_fixed = l1 - l0;
+    gp->launches_step = l2 - l1;
+    return 0;
+}
+
+static tags_plan_s::GraphPass* graph_for(tags_plan_s* p, int nb, double mur, int has_ie, int inj, int* err) {
+    *err = 0;
+    for (auto& g : p->graphs)
+        if (g.nb == nb && g.mur == mur && g.has_ie == has_ie && (has_ie || g.inj == inj)) return &g;
+    tags_plan_s::GraphPass gp;
+    *err = capture_pass(p, nb, mur, has_ie, has_ie ? 0 : inj, &gp);
+    if (*err) return nullptr;
+    if (p->graphs.size() >= 8) {        // a few pass shapes per plan: drop the oldest
+        cudaGraphExecDestroy(p->graphs.front().exec);
+        p->graphs.erase(p->graphs.begin());
+    }
+    p->graphs.push_back(gp);
+    return &p->graphs.back();
+}
+
+void tags_plan_drop_graphs(tags_plan_s* p) {
+    for (auto& g : p->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+    p->graphs.clear();
+}
+
+extern "C" int tags_plan_set_split(tags_plan plan, int pieces) {
+    if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_split: invalid plan");
+    if (pieces != 2 && pieces != 3 && pieces != TAGS_SPLIT_F16)
+        return tags_fail(TAGS_E_ARG, "tags_plan_set_split: pieces must be 2, 3 or 16");
+    if (plan->split_pieces != pieces) {
+        plan->split_pieces = pieces;
+        tags_plan_drop_graphs(plan);
+    }
+    return 0;
+}
+
+extern "C" int tags_plan_set_graphs(tags_plan plan, int enable) {
+    if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_graphs: invalid plan");
+    plan->use_graphs = enable ? 1 : 0;
+    return 0;
+}
+
 extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
                              const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags,
                              tags_run_stats* stats) {
@@ -271,7 +398,7 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     if (!ctx) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
     // staging for host inputs
     double2* d_in = nullptr;
-    if (!dev) {
+    if (!dev && !p->use_graphs) {
         size_t need = sizeof(double2) * (2 * (size_t)p->batch + (ie ? (size_t)p->batch * p->n : 0));
         d_in = (double2*)ctx->scratch(9, need);
         if (!d_in) return tags_fail(TAGS_E_NOMEM, "device allocation failed");
@@ -283,7 +410,19 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     for (size_t k0 = 0; k0 < ns; k0 += p->batch) {
         const int nb = (int)std::min<size_t>(p->batch, ns - k0);
         const double2 *ds, *dk, *die = nullptr;
-        if (dev) {
+        if (p->use_graphs) {
+            // inputs go to the plan's staging buffers, which the graph reads
+            const cudaMemcpyKind kind = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+            TAGS_CUDA_OK(cudaMemcpyAsync(p->d_sin, s + k0, sizeof(double2) * nb, kind, st));
+            TAGS_CUDA_OK(cudaMemcpyAsync(p->d_sin + p->batch, kappa + k0, sizeof(double2) * nb, kind, st));
+            ds = p->d_sin;
+            dk = p->d_sin + p->batch;
+            if (ie) {
+                if (!p->d_iein) TAGS_CUDA_OK(cudaMalloc(&p->d_iein, sizeof(double2) * p->batch * p->n));
+                TAGS_CUDA_OK(cudaMemcpyAsync(p->d_iein, ie + k0 * p->n, sizeof(double2) * nb * p->n, kind, st));
+                die = p->d_iein;
+            }
+        } else if (dev) {
             ds = reinterpret_cast<const double2*>(s) + k0;
             dk = reinterpret_cast<const double2*>(kappa) + k0;
             if (ie) die = reinterpret_cast<const double2*>(ie) + k0 * p->n;
@@ -298,17 +437,30 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
                 die = d_in + 2 * p->batch;
             }
         }
-        int err = tags_plan_coef(p, ds, dk, mur, nb, st);
-        if (!err) err = tags_plan_rhs(p, p->d_x, die, (int)inj_node, nb, st);
-        if (err) return err;
-        if (p->precision == TAGS_PLAIN_FP64) {
-            err = tags_plan_run_plain(p, ds, nb, st);
+        int err = 0;
+        std::vector<int> iters(nb), conv(nb);
+        std::vector<double> berr(nb);
+        if (p->use_graphs) {
+            tags_plan_s::GraphPass* gp = graph_for(p, nb, mur, die != nullptr, (int)inj_node, &err);
             if (err) return err;
+            TAGS_CUDA_OK(cudaGraphLaunch(gp->exec, st));
+            long long launched = gp->launches_fixed;
+            if (p->precision != TAGS_PLAIN_FP64) {
+                int steps = 0;
+                err = tags_mixed_finish(p, nb, st, iters.data(), berr.data(), conv.data(), &steps);
+                if (err) return err;
+                launched += (long long)steps * gp->launches_step;
+            }
+            tags_note_launch(launched);
         } else {
-            std::vector<int> iters(nb), conv(nb);
-            std::vector<double> berr(nb);
-            err = tags_mixed_solve_batch(p, nb, nullptr, iters.data(), berr.data(), conv.data(), st);
+            err = tags_plan_coef(p, ds, dk, mur, nb, st);
+            if (!err) err = tags_plan_rhs(p, p->d_x, die, (int)inj_node, nb, st);
             if (err) return err;
+            if (p->precision == TAGS_PLAIN_FP64) err = tags_plan_run_plain(p, ds, nb, st);
+            else err = tags_mixed_solve_batch(p, nb, nullptr, iters.data(), berr.data(), conv.data(), st);
+            if (err) return err;
+        }
+        if (p->precision != TAGS_PLAIN_FP64) {
             if (stats) {
                 for (int q = 0; q < nb; ++q) {
                     stats->max_iterations = std::max(stats->max_iterations, iters[q]);
@@ -335,6 +487,7 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
         float ms = 0.f;
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         stats->seconds = ms * 1e-3;
+        stats->split = p->precision == TAGS_PLAIN_FP64 ? 0 : p->split_pieces;
     }
     if (status & TAGS_ST_DEGENERATE_PAIR)
         return tags_fail(TAGS_E_GEOMETRY, "coincident or overlapping segments: the pair integral diverges");

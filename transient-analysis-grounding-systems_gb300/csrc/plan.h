@@ -64,8 +64,23 @@ struct tags_plan_s {
     int n_touch = 0;                // pairs sharing an endpoint (FP64 Duffy rule)
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
-    int split_pieces = 3;           // bf16 pieces per real value in the tensor-core products
+    int split_pieces = 3;           // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
+    int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue
+    double* d_ird = nullptr;        // refinement state: previous correction, max row sum, backward error
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // CUDA-graph passes: inputs staged in plan-owned buffers, one executable
+    // graph per pass shape (samples, mu_r, injection form)
+    int use_graphs = 1;
+    double2* d_sin = nullptr;       // 2 x batch: s, kappa
+    double2* d_iein = nullptr;      // batch x n injections (allocated on first use)
+    struct GraphPass {
+        int nb = 0, has_ie = 0, inj = 0;
+        double mur = 0.0;
+        cudaGraphExec_t exec = nullptr;
+        long long launches_fixed = 0;   // kernels outside the refinement loop
+        long long launches_step = 0;    // kernels of one refinement step
+    };
+    std::vector<GraphPass> graphs;
 };
 
 int tags_plan_run_plain(tags_plan_s* p, const double2* d_s_unused, int nb, cudaStream_t st);
@@ -73,3 +88,9 @@ int tags_mixed_alloc(tags_plan_s* p);
 int tags_mixed_free(tags_plan_s* p);
 int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2* d_b, int* h_iters, double* h_berr,
                            int* h_conv, cudaStream_t st);
+int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st);
+void tags_plan_drop_graphs(tags_plan_s* p);
+int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st);
+int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditionalHandle cond, int set_cond);
+int tags_mixed_finish(tags_plan_s* p, int nb, cudaStream_t st, int* h_iters, double* h_berr, int* h_conv,
+                      int* h_steps);

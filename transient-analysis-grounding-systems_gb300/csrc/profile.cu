@@ -34,6 +34,9 @@ std::mutex g_pm;
 
 int tags_prof_begin(int fam, cudaStream_t st) {
     if (!g_on.load(std::memory_order_relaxed)) return -1;
+    // launches captured into a graph are not timed per family
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return -1;
     std::lock_guard<std::mutex> lk(g_pm);
     Family& f = g_fam[fam];
     if (f.used + 2 > f.ev.size()) {

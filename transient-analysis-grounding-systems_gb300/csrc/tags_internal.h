@@ -80,6 +80,11 @@ int tags_launch_nlt(const double* d_f, long long fstride, long long nt, const do
                     double2* d_g, long long gstride, int nseries, cudaStream_t st);
 
 // ldl_tc.cu: tensor-core LDL^T of complex FP32 symmetric matrices (no pivoting)
+// Split forms of the tensor-core LDL^T (`pieces` argument of tags_ldl_tc):
+// 2 or 3 bf16 pieces, or TAGS_SPLIT_F16 = two fp16 pieces of 2^8 x.
+constexpr int TAGS_SPLIT_F16 = 16;
+int tags_lu_prepare();
+int tags_ldl_tc_prepare();
 size_t tags_ldl_tc_workspace(int N, int batch);
 // zl_m > 0: the matrix is ordered [ZL (zl_m), ZT (zl_m), rest] with a zero ZL/ZT
 // coupling block, which the factorisation and the solves skip.
