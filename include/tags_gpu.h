@@ -154,7 +154,7 @@ int tags_plan_set_graphs (tags_plan plan, int enable);
  * per FP32 value (6 products per real product, FP32-level), 2 = two bf16
  * pieces (3 products, ~16 bits), 16 = two fp16 pieces of 2^8 x (3 products,
  * 22 bits; a value outside fp16's range makes the plan fall back to 3 and
- * solve that pass again). Default 3. */
+ * solve that pass again). Default 16. */
 int tags_plan_set_split (tags_plan plan, int pieces);
 
 /* ---- Part 3: solve without device allocation -------------------------------- */

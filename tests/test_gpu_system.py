@@ -100,13 +100,14 @@ def test_plain_plan_rod_harmonic_impedance(gpu_pkg):
     assert np.max(np.abs(z - gd["sol"][:, 0]) / np.abs(gd["sol"][:, 0])) < 1e-8
 
 
-def _grid2_gpr(pkg, precision):
+def _grid2_gpr(pkg, precision, split=None):
     gd = golden("grid2.npz")
     e, nodes = gd["elec"], gd["nodes"]
     n = nodes.shape[0]
     ie = np.zeros((len(gd["s"]), n), np.complex128)
     ie[:, 0] = gd["inj_s"]
-    sol, info, st = pkg.hem_sweep(e, pkg.images(e), nodes, gd["s"], gd["kappa"], ie=ie, precision=precision)
+    sol, info, st = pkg.hem_sweep(e, pkg.images(e), nodes, gd["s"], gd["kappa"], ie=ie, precision=precision,
+                                  split=split)
     gpr = pkg.inv_laplace_trans(sol[:, 0], gd["s"], float(gd["tmax"]), int(gd["nt"]))
     return gd, sol, info, st, gpr
 
@@ -119,10 +120,13 @@ def test_plain_plan_grid_gpr(gpu_pkg):
     assert rel_err(gpr, gd["gpr"]) < 1e-8
 
 
-def test_mixed_plan_grid_gpr(gpu_pkg):
-    """Config 2, mixed form: impedance and GPR <= 1e-6 against the reference."""
-    gd, sol, info, st, gpr = _grid2_gpr(gpu_pkg, gpu_pkg.MIXED)
+@pytest.mark.parametrize("split", [3, 16])
+def test_mixed_plan_grid_gpr(gpu_pkg, split):
+    """Config 2, mixed form (bf16 x3 and fp16 x2 products): impedance and GPR
+    <= 1e-6 against the reference, no FP64 fallback."""
+    gd, sol, info, st, gpr = _grid2_gpr(gpu_pkg, gpu_pkg.MIXED, split)
     assert np.all(info == 0)
+    assert st.fallbacks == 0 and st.split == split
     assert np.max(np.abs(sol[:, 0] - gd["u0"]) / np.abs(gd["u0"])) < 1e-6
     assert rel_err(gpr, gd["gpr"]) < 1e-6
     assert st.max_iterations >= 1
@@ -156,10 +160,11 @@ def test_full_size_properties(gpu_pkg):
     berr = np.linalg.norm(Wsym @ x - b, np.inf) / (np.linalg.norm(Wsym, np.inf) * np.linalg.norm(x, np.inf))
     assert berr < 1e-13
     plain, _, _ = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=centre, precision=pkg.PLAIN_FP64)
-    mixed, info, st = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=centre, precision=pkg.MIXED)
-    assert np.all(info == 0)
     assert rel_err(plain[0], x) < 1e-9
-    assert np.max(np.abs(mixed[:, :n] - plain[:, :n])) / np.max(np.abs(plain[:, :n])) < 1e-6
+    for split in (3, 16):
+        mixed, info, st = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=centre, precision=pkg.MIXED, split=split)
+        assert np.all(info == 0) and st.fallbacks == 0 and st.split == split
+        assert np.max(np.abs(mixed[:, :n] - plain[:, :n])) / np.max(np.abs(plain[:, :n])) < 1e-6
     # reciprocity: potential at node 0 for a current at the centre equals the reverse
     other, _, _ = pkg.hem_sweep(e, img, nodes, s[:1], kappa[:1], inj_node=0, precision=pkg.PLAIN_FP64)
     assert abs(other[0, centre] - plain[0, 0]) < 1e-11 * abs(plain[0, 0])

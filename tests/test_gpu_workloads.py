@@ -1,0 +1,74 @@
+"""GPU checks of the other grid workloads: many uneven grids solved at once
+(one plan per grid, plans in flight together) and the 120 x 120 m grid with
+50 rods (N = 17875). The mixed form is held to 1e-6 against the plain FP64
+form on the same samples; each test prints the figures it measured."""
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+def test_uneven_grids_batched(gpu_pkg):
+    """Eight of the 64 uneven grids (sizes spread from the smallest to the
+    largest), 16 of each grid's 256 Laplace samples (nt = 510, 10 MHz), unit
+    current at node 0: every grid's mixed-form node potentials within 1e-6 of
+    the plain FP64 form's, no FP64 fallback."""
+    pkg = gpu_pkg
+    grids = pkg.uneven_grids(64, seed=0)
+    order = np.argsort([len(g["electrodes"]) for g in grids])
+    pick = [int(order[k]) for k in np.linspace(0, 63, 8).astype(int)]
+    s = pkg.laplace_samples(510, 255 / 10e6)[::16]
+    jobs = []
+    for gi in pick:
+        g = grids[gi]
+        jobs.append({"electrodes": g["electrodes"], "images": pkg.images(g["electrodes"]), "nodes": g["nodes"],
+                     "s": s, "kappa": 1.0 / g["rho"] + s * g["epsr"] * pkg.EPS0, "inj_node": 0})
+    t0 = time.perf_counter()
+    mixed = pkg.hem_sweep_grids(jobs, pkg.MIXED, workers=4)
+    t_mixed = time.perf_counter() - t0
+    plain = pkg.hem_sweep_grids(jobs, pkg.PLAIN_FP64, workers=4)
+    errs = []
+    for gi, job, (xm, im, sm), (xp, ip, _) in zip(pick, jobs, mixed, plain):
+        n = len(job["nodes"])
+        assert np.all(im == 0) and np.all(ip == 0)
+        assert sm.fallbacks == 0
+        errs.append(_rel(xm[:, :n], xp[:, :n]))
+    print(f"\nuneven grids: m = {[len(grids[gi]['electrodes']) for gi in pick]}, "
+          f"max rel err vs FP64 per grid = {['%.1e' % e for e in errs]}, "
+          f"mixed {len(pick) * len(s) / t_mixed:.0f} solves/s (wall, incl. plan set-up)")
+    assert max(errs) < 1e-6
+
+
+def test_grid_with_rods_n17875(gpu_pkg):
+    """The 120 x 120 m grid (24 x 24 meshes, 1 m segments) with 50 rods of
+    3 m: m = 6150, n = 5575, N = 17875. Two samples (the lowest and a 6 MHz
+    one of a 512-sample set) in the mixed form, the lowest also in plain FP64:
+    node potentials within 1e-6, refinement without fallback."""
+    pkg = gpu_pkg
+    e, nodes = pkg.grid_with_rods()
+    m, n = e.shape[0], nodes.shape[0]
+    assert (m, n) == (6150, 5575)
+    img = pkg.images(e)
+    s_all = pkg.laplace_samples(1022, 511 / 10e6)
+    s = s_all[[0, 306]]
+    kappa = 1.0 / 100.0 + s * 10.0 * pkg.EPS0
+    centre = int(np.argmin(np.linalg.norm(nodes - [60.0, 60.0, -0.5], axis=1)))
+    t0 = time.perf_counter()
+    xm, im, sm = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=centre, precision=pkg.MIXED, max_batch=2)
+    t_mixed = time.perf_counter() - t0
+    assert np.all(im == 0) and sm.fallbacks == 0
+    t0 = time.perf_counter()
+    xp, ip, _ = pkg.hem_sweep(e, img, nodes, s[:1], kappa[:1], inj_node=centre, precision=pkg.PLAIN_FP64,
+                              max_batch=1)
+    t_plain = time.perf_counter() - t0
+    assert np.all(ip == 0)
+    err = _rel(xm[:1, :n], xp[:, :n])
+    print(f"\nN = 17875: mixed 2 samples {t_mixed:.2f} s (refinement steps <= {sm.max_iterations}, "
+          f"backward error {sm.max_backward_error:.1e}), plain 1 sample {t_plain:.2f} s, rel err {err:.1e}")
+    assert err < 1e-6

@@ -236,6 +236,26 @@ def electrode_grid(vertices_x, vertices_y, length_x, length_y, edge_segments_x, 
     return np.array(elec), np.array(nodes, dtype=np.float64)
 
 
+def grid_with_rods(vertices=25, length=120.0, edge_segments=5, radius=7e-3, depth=-0.5, rods=50,
+                   rod_length=3.0, rod_segments=3, seed=0):
+    """Square grid (electrode_grid) plus vertical rods at `rods` vertices drawn
+    by numpy's default_rng(seed) without replacement, each from the grid's
+    depth down by rod_length in rod_segments segments; a rod's top node is the
+    grid vertex's node. Defaults: the 120 x 120 m grid with 24 x 24 meshes and
+    50 rods of 3 m (6150 segments, 5575 nodes)."""
+    elec, nodes = electrode_grid(vertices, vertices, length, length, edge_segments, edge_segments, radius, depth)
+    pick = np.sort(np.random.default_rng(seed).choice(vertices * vertices, size=rods, replace=False))
+    step = length / (vertices - 1)
+    all_e, all_n = [elec], [nodes]
+    for v in pick:
+        gx, gy = int(v) % vertices, int(v) // vertices
+        top = [step * gx, step * gy, depth]
+        e, nd = segment_electrode(top, [top[0], top[1], depth - rod_length], rod_segments, radius)
+        all_e.append(e)
+        all_n.append(nd[1:])
+    return np.concatenate(all_e), np.concatenate(all_n)
+
+
 def images(elec) -> np.ndarray:
     """Mirror segments across the soil surface z = 0 (examples/three_grids.c:206-214)."""
     img = np.array(elec, dtype=np.float64, copy=True)
@@ -438,6 +458,52 @@ def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, p
         return plan.run(s, kappa, mur, ie, inj_node)
     finally:
         plan.close()
+
+
+def uneven_grids(count: int = 64, seed: int = 0):
+    """A batch of square grids of uneven size (the 64-grid workload): side
+    uniform in 5-40 m, 2-10 meshes per side, 1 m segmentation (ceil(mesh
+    edge / 1 m) segments per edge, as the reference's examples divide edges),
+    depth uniform 0.3-1.0 m, radius uniform 5-10 mm, soil resistivity
+    log-uniform 50-5000 ohm m, relative permittivity uniform 5-40.
+    Returns dicts with electrodes, nodes and the soil of each grid."""
+    rng = np.random.default_rng(seed)
+    grids = []
+    for _ in range(count):
+        side = float(rng.uniform(5.0, 40.0))
+        meshes = int(rng.integers(2, 11))
+        depth = float(rng.uniform(0.3, 1.0))
+        radius = float(rng.uniform(5e-3, 10e-3))
+        rho = float(np.exp(rng.uniform(np.log(50.0), np.log(5000.0))))
+        epsr = float(rng.uniform(5.0, 40.0))
+        div = int(math.ceil(side / meshes / 1.0))
+        elec, nodes = electrode_grid(meshes + 1, meshes + 1, side, side, div, div, radius, -depth)
+        grids.append({"electrodes": elec, "nodes": nodes, "rho": rho, "epsr": epsr, "side": side,
+                      "meshes": meshes, "depth": depth, "radius": radius})
+    return grids
+
+
+def hem_sweep_grids(jobs, precision=MIXED, max_batch=0, workers=8, graphs=True, split=None):
+    """Many grids at once: one plan per job, run from `workers` host threads,
+    so the plans' passes (each a graph launch on the plan's own stream) share
+    the GPU. A job is a dict with electrodes, images (or None), nodes, s,
+    kappa and either ie (ns x n) or inj_node. Returns [(solution, info,
+    RunStats)] in job order."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(job):
+        ns = len(np.atleast_1d(job["s"]))
+        plan = Plan(job["electrodes"], job.get("images"), job["nodes"], precision,
+                    max_batch or min(ns, 256), graphs)
+        try:
+            if split is not None and precision == MIXED:
+                plan.set_split(split)
+            return plan.run(job["s"], job["kappa"], job.get("mur", 1.0), job.get("ie"), job.get("inj_node", 0))
+        finally:
+            plan.close()
+
+    with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
+        return list(ex.map(one, jobs))
 
 
 # ---- multi-GPU helpers (host side) ------------------------------------------------------

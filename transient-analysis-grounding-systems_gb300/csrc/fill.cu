@@ -31,6 +31,10 @@ constexpr int GL_TOTAL = QMAX * (QMAX + 1) / 2;
 
 __device__ double g_glx[GL_TOTAL];            // nodes on [0,1], order q at q(q-1)/2
 __device__ double g_glw[GL_TOTAL];            // weights on [0,1]
+constexpr int QMIX = 24;                      // largest order of the FP32 fill
+constexpr int GL_MIX = QMIX * (QMIX + 1) / 2;
+__device__ float g_glxm[GL_MIX];              // FP32 fill: nodes shifted to [-1/2, 1/2], orders 1..QMIX
+__device__ float g_glwm[GL_MIX];
 
 TAGS_D int gl_off(int q) { return q * (q - 1) / 2; }
 
@@ -471,7 +475,7 @@ TAGS_D float2 anchor_df(float grh, float grl, float gih, float gil, float rh, fl
     return make_float2(mag * cs, -mag * sn);
 }
 
-constexpr int MIX_SG = 8;   // samples per thread
+constexpr int MIX_SG = 4;   // samples per thread (124 registers: four 128-thread CTAs per SM)
 
 // Mixed-form fill of the regular pairs, all in FP32: one thread per (pair,
 // group of MIX_SG samples), the group's constants in shared memory. Pairs that
@@ -484,14 +488,14 @@ __global__ void __launch_bounds__(128) k_fill_mixed(const double* __restrict__ e
                                                     const PairRec* __restrict__ recs,
                                                     const SampleF32* __restrict__ coef, int nsamp, float2* zl0,
                                                     float2* zt0, long long bstride, int has_img, int* status) {
-    __shared__ float sxm[GL_TOTAL], swf[GL_TOTAL];
+    __shared__ float sxm[GL_MIX], swf[GL_MIX];
     __shared__ SampleF32 sc[MIX_SG];
     __shared__ float s_gmax;
     const int s0 = blockIdx.y * MIX_SG;
     const int ns = min(MIX_SG, nsamp - s0);
-    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) {
-        sxm[t] = (float)(g_glx[t] - 0.5);
-        swf[t] = (float)g_glw[t];
+    for (int t = threadIdx.x; t < GL_MIX; t += blockDim.x) {
+        sxm[t] = g_glxm[t];
+        swf[t] = g_glwm[t];
     }
     if (threadIdx.x < MIX_SG) {
         SampleF32 z{};
@@ -533,7 +537,7 @@ __global__ void __launch_bounds__(128) k_fill_mixed(const double* __restrict__ e
         const float lmax = fmaxf(ds.w, dr.w);
         const int P = min(32, max(code & 63, (int)ceilf(gmax * lmax / 1.5f)));
         const int qg = (code >> 6) & 63;
-        const int qq = min(24, qg + (int)ceilf(gmax * lmax / P));
+        const int qq = min(QMIX, qg + (int)ceilf(gmax * lmax / P));
         const float* x = sxm + gl_off(qq);
         const float* w = swf + gl_off(qq);
         const float h = 1.f / (float)P;
@@ -733,6 +737,13 @@ int tags_fill_tables_init() {
     for (int q = 1; q <= QMAX; ++q) gauss_legendre(q, hx + q * (q - 1) / 2, hw + q * (q - 1) / 2);
     TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glx, hx, sizeof(hx)));
     TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glw, hw, sizeof(hw)));
+    static float fx[GL_MIX], fw[GL_MIX];
+    for (int t = 0; t < GL_MIX; ++t) {
+        fx[t] = (float)(hx[t] - 0.5);
+        fw[t] = (float)hw[t];
+    }
+    TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glxm, fx, sizeof(fx)));
+    TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glwm, fw, sizeof(fw)));
     return 0;
 }
 

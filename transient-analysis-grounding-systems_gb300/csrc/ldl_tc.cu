@@ -219,6 +219,9 @@ struct GemmArgs {
     int zlo, zhi;              // output rows/cols in [zlo, zhi) are structurally zero (tiles inside skipped)
     uint16_t* Np;              // mode 0: split planes of the next panel's block column (tiles J = 0, I >= 1), or null
     int Mn;                    // rows of the next panel's block column
+    int kblocks;               // K blocks of BK: 4 (K = 128) or 8 (K = 256: two panels)
+    int offA1, offB1;          // row offset of the operands' first 128 K (maps tmA, tmB)
+    int offA2, offB2;          // row offset of the second 128 K (maps tmA2, tmB2)
 };
 
 TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
@@ -289,7 +292,9 @@ constexpr int GEMM_THREADS = 32 * (2 + EPI_WARPS);
 
 template <int S, int MODE>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
-                                                             const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+                                                             const __grid_constant__ CUtensorMap tmB,
+                                                             const __grid_constant__ CUtensorMap tmA2,
+                                                             const __grid_constant__ CUtensorMap tmB2, GemmArgs g) {
     using C = GemmCfg<S>;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t base_u32 = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -346,14 +351,20 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                 }
             }
             if (lane == 0) {
-                for (int kb = 0; kb < KBLKS; ++kb) {
+                for (int kb = 0; kb < g.kblocks; ++kb) {
                     if (!mbar_wait(empty(stage), phase ^ 1, g.err)) { alive = false; break; }
                     issued[stage] = 0;
                     const uint32_t sb = base_u32 + stage * C::STAGE;
                     mbar_expect_tx(full(stage), C::STAGE);
+                    // K blocks 0..3 from the first operand pair, 4..7 from the second
+                    const bool second = kb >= KBLKS;
+                    const CUtensorMap* mA = second ? &tmA2 : &tmA;
+                    const CUtensorMap* mB = second ? &tmB2 : &tmB;
+                    const int ra = TB * I + (second ? g.offA2 : g.offA1), rb = TB * J + (second ? g.offB2 : g.offB1);
+                    const int kx = (kb % KBLKS) * BK;
                     for (int p = 0; p < C::NPL; ++p) {
-                        tma_load_4d(sb + p * PST, &tmA, kb * BK, TB * I, p, smp, full(stage));
-                        tma_load_4d(sb + (C::NPL + p) * PST, &tmB, kb * BK, TB * J, p, smp, full(stage));
+                        tma_load_4d(sb + p * PST, mA, kx, ra, p, smp, full(stage));
+                        tma_load_4d(sb + (C::NPL + p) * PST, mB, kx, rb, p, smp, full(stage));
                     }
                     issued[stage] = 1;
                     if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
@@ -397,7 +408,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                 if (!mbar_wait(tempty(acc), aphase ^ 1, g.err)) { alive = false; break; }
                 tc_fence_after();
                 const uint32_t accR = tmem + acc * 256, accI = accR + 128;
-                for (int kb = 0; kb < KBLKS && alive; ++kb) {
+                for (int kb = 0; kb < g.kblocks && alive; ++kb) {
                     if (!mbar_wait(full(stage), phase, g.err)) { alive = false; break; }
                     tc_fence_after();
                     const uint32_t sa = base_u32 + stage * C::STAGE, sbb = sa + C::NPL * PST;
@@ -721,41 +732,62 @@ __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__
 // ---- solves with the factors: L D L^T x = b (one right-hand side per sample) ----------
 
 // z_b = Linv_b * r_b for block b (128 rows), or Linv_b^T * r_b with
-// transpose = 1; one CTA of 256 threads per sample, a warp per output row,
-// lanes over the row (coalesced).
-__global__ void __launch_bounds__(256) k_blk_inv_apply(const float2* __restrict__ linv32, long long lstride, int blk,
+// transpose = 1, in place; one CTA of 512 threads per sample: four threads
+// per output row, each a quarter of the row, reading the stored copy whose
+// row index is contiguous across threads (the transpose of the one applied).
+__global__ void __launch_bounds__(512) k_blk_inv_apply(const float2* __restrict__ linv32, long long lstride, int blk,
                                                        int jb, float2* __restrict__ x0, long long xstride,
                                                        int transpose) {
     __shared__ float2 v[TB];
-    const int smp = blockIdx.x, tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    __shared__ float2 part[4][TB];
+    const int smp = blockIdx.x, tid = threadIdx.x, r = tid & (TB - 1), qt = tid >> 7;
     float2* x = x0 + xstride * smp + (long long)blk * TB;
-    const float2* Li = linv32 + lstride * smp + (long long)blk * 2 * TB * TB + (transpose ? TB * TB : 0);
+    // M[r][k] is at Mt[k * TB + r]: Mt = Linv^T (row-major) for z = Linv r, Linv for z = Linv^T r
+    const float2* Mt = linv32 + lstride * smp + (long long)blk * 2 * TB * TB + (transpose ? 0 : TB * TB);
     if (tid < TB) v[tid] = tid < jb ? x[tid] : make_float2(0.f, 0.f);
     __syncthreads();
-    for (int r = warp; r < jb; r += 8) {
-        const float2* row = Li + (long long)r * TB;
-        float2 acc = make_float2(0.f, 0.f);
+    float2 acc = make_float2(0.f, 0.f);
+    const int k0 = 32 * qt;
 #pragma unroll
-        for (int k = lane; k < TB; k += 32) acc = ffmac(row[k], v[k], acc);
-        for (int o = 16; o > 0; o >>= 1) {
-            acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
-            acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
-        }
-        if (lane == 0) x[r] = acc;
+    for (int h = 0; h < 2; ++h) {
+        float2 w[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) w[q] = Mt[(long long)(k0 + 16 * h + q) * TB + r];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc = ffmac(w[q], v[k0 + 16 * h + q], acc);
+    }
+    part[qt][r] = acc;
+    __syncthreads();
+    if (tid < jb) {
+        const float2 a = part[0][tid], b = part[1][tid], c = part[2][tid], d = part[3][tid];
+        x[tid] = make_float2((a.x + b.x) + (c.x + d.x), (a.y + b.y) + (c.y + d.y));
     }
 }
 
-// forward: x[i] -= sum_{k in block} L[i][k] x[k] for rows i below the block
-__global__ void k_blk_fwd_update(const float2* __restrict__ A0, long long ld, long long mstride, int N, int j0, int jb,
-                                 float2* __restrict__ x0, long long xstride, int zl_m) {
+// forward: x[i] -= sum_{k in block} L[i][k] x[k] for rows i below the block;
+// a thread per row, 16 loads in flight, the block's x in shared memory
+__global__ void __launch_bounds__(128) k_blk_fwd_update(const float2* __restrict__ A0, long long ld, long long mstride,
+                                                        int N, int j0, int jb, float2* __restrict__ x0,
+                                                        long long xstride, int zl_m) {
+    __shared__ float2 xs[TB];
     const int smp = blockIdx.y;
+    float2* x = x0 + xstride * smp;
+    if ((int)threadIdx.x < jb) xs[threadIdx.x] = x[j0 + threadIdx.x];
+    __syncthreads();
     const int i = j0 + jb + blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     if (j0 + jb <= zl_m && i >= zl_m && i < 2 * zl_m) return;      // L[ZT rows, ZL cols] = 0
-    const float2* A = A0 + mstride * smp;
-    float2* x = x0 + xstride * smp;
+    const float2* Ai = A0 + mstride * smp + i + ld * (long long)j0;
     float2 acc = make_float2(0.f, 0.f);
-    for (int k = 0; k < jb; ++k) acc = ffmac(A[i + ld * (long long)(j0 + k)], x[j0 + k], acc);
+    int k = 0;
+    for (; k + 16 <= jb; k += 16) {
+        float2 w[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) w[q] = Ai[ld * (long long)(k + q)];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) acc = ffmac(w[q], xs[k + q], acc);
+    }
+    for (; k < jb; ++k) acc = ffmac(Ai[ld * (long long)k], xs[k], acc);
     x[i] = fsub(x[i], acc);
 }
 
@@ -842,13 +874,13 @@ static long long plane_stride(int N) { return (long long)2 * SMAX * N * TB; }
 
 size_t tags_ldl_tc_workspace(int N, int batch) {
     size_t plane = (size_t)plane_stride(N) * 2;
-    return (size_t)batch * (3 * plane + (size_t)2 * SMAX * TB * TB * 2 + TB * sizeof(float2) +
+    return (size_t)batch * (5 * plane + (size_t)2 * SMAX * TB * TB * 2 + TB * sizeof(float2) +
                             (size_t)linv32_stride(N) * sizeof(float2)) + 1024;
 }
 
 static float2* linv32_of(void* ws, int N, int batch_cap) {
     const long long pstride = plane_stride(N);
-    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + 3 * pstride * batch_cap;
+    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + 5 * pstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     return dinv + (long long)TB * batch_cap;
 }
@@ -889,18 +921,23 @@ int tags_ldl_tc_prepare() {
 }
 
 template <int S, int MODE>
-static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
+static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const CUtensorMap& mA2,
+                         const CUtensorMap& mB2, const GemmArgs& g, cudaStream_t st) {
     const int total = g.tiles * g.nb;
     const int grid = total < num_sms() ? total : num_sms();
     if (grid <= 0) return 0;
-    k_gemm_tc<S, MODE><<<grid, GEMM_THREADS, GemmCfg<S>::SMEM, st>>>(mA, mB, g);
+    k_gemm_tc<S, MODE><<<grid, GEMM_THREADS, GemmCfg<S>::SMEM, st>>>(mA, mB, mA2, mB2, g);
     tags_note_launch();
     return 0;
 }
 
-template <int S>
-static int launch_gemm(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
-    return g.mode == 0 ? launch_gemm_m<S, 0>(mA, mB, g, st) : launch_gemm_m<S, 1>(mA, mB, g, st);
+// One GEMM launch; K = 128 from (mA, mB), or K = 256 with (mA2, mB2) for the
+// second half (g.kblocks = 8).
+static int launch_gemm(int NS, const CUtensorMap& mA, const CUtensorMap& mB, const CUtensorMap& mA2,
+                       const CUtensorMap& mB2, const GemmArgs& g, cudaStream_t st) {
+    if (NS == 3)
+        return g.mode == 0 ? launch_gemm_m<3, 0>(mA, mB, mA2, mB2, g, st) : launch_gemm_m<3, 1>(mA, mB, mA2, mB2, g, st);
+    return g.mode == 0 ? launch_gemm_m<2, 0>(mA, mB, mA2, mB2, g, st) : launch_gemm_m<2, 1>(mA, mB, mA2, mB2, g, st);
 }
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
@@ -911,7 +948,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     int pf = tags_prof_begin(TAGS_PROF_LDL_SOLVE, st);
     for (int b = 0; b < nblk; ++b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, 256, 0, st>>>(L32, ls, b, jb, x, xstride, 0);
+        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 0);
         const int rest = N - j0 - jb;
         if (rest > 0) k_blk_fwd_update<<<dim3((rest + 127) / 128, nb), 128, 0, st>>>(A, ld, mstride, N, j0, jb, x, xstride, zl_m);
         tags_note_launch(rest > 0 ? 2 : 1);
@@ -920,7 +957,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     tags_note_launch();
     for (int b = nblk - 1; b >= 0; --b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, 256, 0, st>>>(L32, ls, b, jb, x, xstride, 1);
+        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 1);
         if (j0 > 0) k_blk_bwd_update<<<dim3((j0 + 7) / 8, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m);
         tags_note_launch(j0 > 0 ? 2 : 1);
     }
@@ -942,93 +979,143 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
     // planes of this run use 2 NS of the 2 SMAX slots of each sample
     const long long pstride = plane_stride(N);
     uint16_t* A21p = reinterpret_cast<uint16_t*>(ws);
-    uint16_t* Lp = A21p + pstride * batch_cap;
-    uint16_t* Wp = Lp + pstride * batch_cap;
-    uint16_t* Lin = Wp + pstride * batch_cap;
+    uint16_t* La = A21p + pstride * batch_cap;       // L and W planes of the first panel of a pair
+    uint16_t* Wa = La + pstride * batch_cap;
+    uint16_t* Lb = Wa + pstride * batch_cap;         // ... and of the second
+    uint16_t* Wb = Lb + pstride * batch_cap;
+    uint16_t* Lin = Wb + pstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
     // the maps see a sample stride of 2 SMAX planes: declare that many planes
-    CUtensorMap mA21, mL, mW, mLin;
+    CUtensorMap mA21, mLa, mWa, mLb, mWb, mLin;
     int e = make_plane_map(&mA21, A21p, N, 2 * SMAX, batch_cap);
-    if (!e) e = make_plane_map(&mL, Lp, N, 2 * SMAX, batch_cap);
-    if (!e) e = make_plane_map(&mW, Wp, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mLa, La, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mWa, Wa, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mLb, Lb, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mWb, Wb, N, 2 * SMAX, batch_cap);
     if (!e) e = make_plane_map(&mLin, Lin, TB, 2 * SMAX, batch_cap);
     if (e) return e;
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * nb, st));
-    for (int j0 = 0; j0 < N; j0 += TB) {
-        const int jb = N - j0 < TB ? N - j0 : TB;
-        const int rest = N - j0 - jb;
+
+    auto base = [&]() {
+        GemmArgs g{};
+        g.nb = nb;
+        g.Amat = A;
+        g.ld = ld;
+        g.mstride = mstride;
+        g.dinv = dinv;
+        g.pstride = pstride;
+        g.R = N;
+        g.err = err;
+        g.f16 = f16;
+        g.kblocks = KBLKS;
+        return g;
+    };
+    // While the first zl_m columns (the ZL block of the ordering ZL, ZT,
+    // nodes) are eliminated, rows/columns zl_m .. 2 zl_m (ZT) of the block
+    // columns and of the trailing matrix stay exactly zero: with all
+    // eliminated columns below `jend` <= zl_m, that band (relative to jend)
+    // is skipped.
+    auto band = [&](GemmArgs& g, int jend) {
+        if (zl_m > 0 && jend <= zl_m) {
+            g.zlo = zl_m - jend;
+            g.zhi = 2 * zl_m - jend;
+        }
+    };
+    auto diag = [&](int j0, int jb) {
         int pf = tags_prof_begin(TAGS_PROF_LDL_DIAG, st);
         k_ldl_diag<<<nb, 512, TB * DIAG_LD * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, info, L32, ls,
                                                               NS, f16, err);
         tags_prof_end(TAGS_PROF_LDL_DIAG, pf, st, 4.0 / 3.0 * jb * (double)jb * jb * nb, 16.0 * jb * jb * nb);
         tags_note_launch();
-        if (rest <= 0) break;
-        if (j0 == 0) {
-            // later panels get their block column's planes from the previous trailing update
-            k_panel_planes<<<dim3((rest + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, rest, A21p, pstride,
-                                                                       N, NS, f16, err);
-            tags_note_launch();
-        }
-        const int T = (rest + TB - 1) / TB;
-        GemmArgs g{};
-        // While the first zl_m columns (the ZL block of the ordering ZL, ZT,
-        // nodes) are eliminated, the rows/columns zl_m .. 2 zl_m (ZT) of the
-        // block column and of the trailing matrix stay exactly zero.
-        if (zl_m > 0 && j0 + jb <= zl_m) {
-            g.zlo = zl_m - (j0 + jb);
-            g.zhi = 2 * zl_m - (j0 + jb);
-        }
+    };
+    // W21 = A21 L11^{-T}, L21 = W21 D^{-1} for the panel at j0 (rows below it):
+    // FP32 L21 into A, both as split planes into (Lx, Wx)
+    auto panel = [&](int j0, int jb, int rest, uint16_t* Lx, uint16_t* Wx) {
+        GemmArgs g = base();
+        band(g, j0 + jb);
         g.M = rest;
         g.Nn = jb;
         g.mode = 1;
-        g.tri = 0;
-        g.tiles = T;
-        g.nb = nb;
-        g.Amat = A;
-        g.ld = ld;
-        g.mstride = mstride;
+        g.tiles = (rest + TB - 1) / TB;
         g.row0 = j0 + jb;
         g.col0 = j0;
-        g.dinv = dinv;
-        g.Lp = Lp;
-        g.Wp = Wp;
-        g.pstride = pstride;
-        g.R = N;
-        g.err = err;
-        g.f16 = f16;
-        pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
-        e = NS == 3 ? launch_gemm<3>(mA21, mLin, g, st) : launch_gemm<2>(mA21, mLin, g, st);
-        if (e) return e;
-        // triangular solve: r x jb unknowns against jb x jb (r = rest minus
-        // the zero band), 4 r jb^2 real flops
+        g.Lp = Lx;
+        g.Wp = Wx;
+        int pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
+        int e1 = launch_gemm(NS, mA21, mLin, mA21, mLin, g, st);
+        // triangular solve: r x jb unknowns against jb x jb (r = rest minus the band), 4 r jb^2 flops
         const double rp = rest - (double)(g.zhi - g.zlo);
         tags_prof_end(TAGS_PROF_LDL_PANEL, pf, st, 4.0 * rp * (double)jb * jb * nb,
                       (8.0 * rp * jb + 16.0 * rp * 128 * 2) * nb);
+        return e1;
+    };
+    // C -= L W^T on rows (and, tri, columns) row0 .. row0 + M of A, K = 128
+    // (first operand pair) or 256 (both pairs); the first tile column's new
+    // values also become the next panel's block-column planes (Mn rows).
+    auto update = [&](int row0, int M, int Nn, bool tri, int jend, const CUtensorMap& mA1, const CUtensorMap& mB1,
+                      int off1, const CUtensorMap* mA2, const CUtensorMap* mB2, int Mn) {
+        GemmArgs g = base();
+        band(g, jend);
+        const int T = (M + TB - 1) / TB;
+        g.M = M;
+        g.Nn = Nn;
         g.mode = 0;
-        g.tri = 1;
-        g.tiles = T * (T + 1) / 2;
-        g.Nn = rest;
-        g.row0 = j0 + jb;
-        g.col0 = j0 + jb;
-        // the next panel (columns j0 + jb ...) has rest - jb' rows below its
-        // diagonal block: its split planes come out of this update's first
-        // tile column (A21 planes are free again: the panel GEMM above read them)
-        {
-            const int jbn = rest < TB ? rest : TB;
-            g.Mn = rest - jbn;
-            g.Np = g.Mn > 0 ? A21p : nullptr;
+        g.tri = tri ? 1 : 0;
+        g.tiles = tri ? T * (T + 1) / 2 : T;
+        g.row0 = row0;
+        g.col0 = row0;
+        g.offA1 = g.offB1 = off1;
+        g.kblocks = mA2 ? 2 * KBLKS : KBLKS;
+        g.Mn = Mn;
+        g.Np = Mn > 0 ? A21p : nullptr;
+        int pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
+        int e1 = launch_gemm(NS, mA1, mB1, mA2 ? *mA2 : mA1, mB2 ? *mB2 : mB1, g, st);
+        // rank-K update outside the zero band: 8 K r c flops (c = r(r+1)/2 / r for the triangle)
+        const double r = M - (double)(g.zhi - g.zlo);
+        const double K = g.kblocks * BK;
+        const double cells = tri ? 0.5 * r * (r + 1.0) : r * (double)Nn;
+        tags_prof_end(TAGS_PROF_LDL_TRAIL, pf, st, 8.0 * K * cells * nb,
+                      (16.0 * cells + 2.0 * r * K * 2.0 * NS) * nb);
+        return e1;
+    };
+
+    // Panels of 128 columns, two at a time: panel a, the update of panel b's
+    // columns by a (which also yields b's block-column planes), panel b, then
+    // one trailing update with K = 256 over both; a last single panel uses K = 128.
+    int j0 = 0;
+    while (j0 < N) {
+        const int jba = N - j0 < TB ? N - j0 : TB;
+        const int resta = N - j0 - jba;
+        diag(j0, jba);
+        if (resta <= 0) break;
+        if (j0 == 0) {
+            // later panels get their block column's planes from the previous update
+            k_panel_planes<<<dim3((resta + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jba, resta, A21p, pstride,
+                                                                        N, NS, f16, err);
+            tags_note_launch();
         }
-        pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
-        e = NS == 3 ? launch_gemm<3>(mL, mW, g, st) : launch_gemm<2>(mL, mW, g, st);
+        e = panel(j0, jba, resta, La, Wa);
         if (e) return e;
-        // symmetric rank-jb update of the lower triangle outside the zero
-        // band: 8 jb r(r+1)/2 real flops with r = rest minus the band;
-        // bytes: read + write of that triangle in complex FP32, two panels of split planes
-        const double r = rest - (double)(g.zhi - g.zlo);
-        tags_prof_end(TAGS_PROF_LDL_TRAIL, pf, st, 8.0 * jb * (0.5 * r * (r + 1.0)) * nb,
-                      (16.0 * 0.5 * r * (r + 1.0) + 2.0 * r * 128 * 4.0 * NS) * nb);
+        const int jbb = resta < TB ? resta : TB;
+        const int restb = resta - jbb;
+        if (restb <= 0 || jba < TB) {
+            e = update(j0 + jba, resta, resta, true, j0 + jba, mLa, mWa, 0, nullptr, nullptr, resta - jbb);
+            if (e) return e;
+            j0 += jba;
+            continue;
+        }
+        // panel b's block column (rows j0 + jba ..., its jbb columns)
+        e = update(j0 + jba, resta, jbb, false, j0 + jba, mLa, mWa, 0, nullptr, nullptr, restb);
+        if (e) return e;
+        diag(j0 + jba, jbb);
+        e = panel(j0 + jba, jbb, restb, Lb, Wb);
+        if (e) return e;
+        const int jbn = restb < TB ? restb : TB;
+        e = update(j0 + jba + jbb, restb, restb, true, j0 + jba + jbb, mLa, mWa, jbb, &mLb, &mWb, restb - jbn);
+        if (e) return e;
+        j0 += jba + jbb;
     }
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

@@ -81,32 +81,50 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 }
 
 // W'' (complex FP32, column-major N x N, reordered and scaled), lower triangle.
-// Grid: x over 256-row chunks, y over columns, z over samples. Node rows of a
-// segment column hold its two incidence entries (start +1 / end -1 in the ZL
-// columns, 0.5 in the ZT columns), read from the per-segment incidence list.
+// One CTA per (column j, sample) walks rows j .. N-1. Node rows of a segment
+// column hold its two incidence entries (start +1 / end -1 in the ZL columns,
+// 0.5 in the ZT columns), read once per CTA from the per-segment list.
 __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const Incidence inc,
                                                const double* __restrict__ scale, int m, int n,
                                                float2* __restrict__ A) {
     const int N = n + 2 * m;
-    const int j = blockIdx.y, b = blockIdx.z;
-    const int i = j + blockIdx.x * blockDim.x + threadIdx.x;     // rows i >= j only
-    if (i >= N) return;
+    const int j = blockIdx.x, b = blockIdx.y;
     const double* d = scale + (size_t)b * N;
     const float2* Zb = Z + (size_t)b * 2 * m * m;
-    float vx = 0.f, vy = 0.f;
-    const int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
+    float2* Aj = A + (size_t)b * N * N + (size_t)j * N;
     const int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
-    if (bi < 2 && bj == bi) {
-        const float2 z = Zb[(size_t)bi * m * m + (i - bi * m) + (size_t)m * (j - bj * m)];
-        vx = -z.x;
-        vy = -z.y;
-    } else if (bi == 2 && bj < 2) {
-        const int e = j - bj * m, nd = i - 2 * m;
-        for (int q = inc.seg_ptr[e]; q < inc.seg_ptr[e + 1]; ++q)
-            if (inc.seg_node[q] == nd) vx = bj == 0 ? (float)inc.seg_a[q] : 0.5f;
+    const float dj = (float)d[j];
+    // the segment's incidence entries (two for a well-formed grid)
+    __shared__ int s_nd[8];
+    __shared__ float s_a[8];
+    int q0 = 0, cnt = 0;
+    if (bj < 2) {
+        const int e = j - bj * m;
+        q0 = inc.seg_ptr[e];
+        cnt = inc.seg_ptr[e + 1] - q0;
     }
-    const float s = (float)d[i] * (float)d[j];
-    A[(size_t)b * N * N + (size_t)j * N + i] = make_float2(vx * s, vy * s);
+    if ((int)threadIdx.x < min(cnt, 8)) {
+        s_nd[threadIdx.x] = inc.seg_node[q0 + threadIdx.x];
+        s_a[threadIdx.x] = bj == 0 ? (float)inc.seg_a[q0 + threadIdx.x] : 0.5f;
+    }
+    __syncthreads();
+    for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
+        const int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
+        float vx = 0.f, vy = 0.f;
+        if (bi < 2 && bj == bi) {
+            const float2 z = Zb[(size_t)bi * m * m + (i - bi * m) + (size_t)m * (j - bj * m)];
+            vx = -z.x;
+            vy = -z.y;
+        } else if (bi == 2 && bj < 2) {
+            const int nd = i - 2 * m;
+            for (int q = 0; q < cnt; ++q) {
+                const int ndq = q < 8 ? s_nd[q] : inc.seg_node[q0 + q];
+                if (ndq == nd) vx = q < 8 ? s_a[q] : (bj == 0 ? (float)inc.seg_a[q0 + q] : 0.5f);
+            }
+        }
+        const float s = (float)d[i] * dj;
+        Aj[i] = make_float2(vx * s, vy * s);
+    }
 }
 
 TAGS_D int orig_of(int ip, int m, int n) {
@@ -373,11 +391,18 @@ int tags_mixed_free(tags_plan_s* p) {
 
 // Re-solve sample `q` of the current pass in plain FP64 (partial pivoting).
 static int fallback_plain(tags_plan_s* p, int q, cudaStream_t st) {
-    DeviceCtx* c = tags_ctx();
     const long long N = p->N, NN = N * N;
-    double2* W = (double2*)c->scratch(10, sizeof(double2) * NN);
-    int* ipiv = (int*)c->scratch(11, sizeof(int) * (N + 1));
-    if (!W || !ipiv) return tags_fail(TAGS_E_NOMEM, "device allocation failed (fallback)");
+    if (!p->d_fbW) {
+        if (cudaMalloc(&p->d_fbW, sizeof(double2) * NN) != cudaSuccess ||
+            cudaMalloc(&p->d_fbpiv, sizeof(int) * (N + 1)) != cudaSuccess) {
+            cudaGetLastError();
+            if (p->d_fbW) cudaFree(p->d_fbW);
+            p->d_fbW = nullptr;
+            return tags_fail(TAGS_E_NOMEM, "device allocation failed (FP64 fallback)");
+        }
+    }
+    double2* W = p->d_fbW;
+    int* ipiv = p->d_fbpiv;
     TAGS_CUDA_OK(cudaMemsetAsync(W, 0, sizeof(double2) * NN, st));
     int err = tags_wg_incidence(W, N, NN, 1, p->d_cond, p->n, p->m, st);
     if (err) return err;
@@ -424,7 +449,7 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     tags_note_launch(2);
     // 3. FP32 working matrix and its LDL^T (no pivoting)
     int pf = tags_prof_begin(TAGS_PROF_BUILD, st);
-    k_build<<<dim3((unsigned)((N + 255) / 256), N, nb), 256, 0, st>>>(p->d_Z, p->inc, p->d_scale, m, n, p->d_A);
+    k_build<<<dim3((unsigned)N, nb), 256, 0, st>>>(p->d_Z, p->inc, p->d_scale, m, n, p->d_A);
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());

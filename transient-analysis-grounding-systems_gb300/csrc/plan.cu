@@ -149,6 +149,9 @@ static void plan_free(tags_plan_s* p) {
     tags_mixed_free(p);
     tags_plan_drop_graphs(p);
     if (p->d_sin) cudaFree(p->d_sin);
+    if (p->d_stage) cudaFree(p->d_stage);
+    if (p->d_fbW) cudaFree(p->d_fbW);
+    if (p->d_fbpiv) cudaFree(p->d_fbpiv);
     if (p->d_iein) cudaFree(p->d_iein);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
@@ -400,8 +403,14 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     double2* d_in = nullptr;
     if (!dev && !p->use_graphs) {
         size_t need = sizeof(double2) * (2 * (size_t)p->batch + (ie ? (size_t)p->batch * p->n : 0));
-        d_in = (double2*)ctx->scratch(9, need);
-        if (!d_in) return tags_fail(TAGS_E_NOMEM, "device allocation failed");
+        if (need > p->stage_bytes) {
+            if (p->d_stage) cudaFree(p->d_stage);
+            p->d_stage = nullptr;
+            p->stage_bytes = 0;
+            TAGS_CUDA_OK(cudaMalloc(&p->d_stage, need));
+            p->stage_bytes = need;
+        }
+        d_in = p->d_stage;
     }
     std::vector<int> h_info;
     if (stats) memset(stats, 0, sizeof(*stats));

@@ -64,7 +64,7 @@ struct tags_plan_s {
     int n_touch = 0;                // pairs sharing an endpoint (FP64 Duffy rule)
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
-    int split_pieces = 3;           // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
+    int split_pieces = TAGS_SPLIT_F16;   // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue
     double* d_ird = nullptr;        // refinement state: previous correction, max row sum, backward error
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -81,6 +81,12 @@ struct tags_plan_s {
         long long launches_step = 0;    // kernels of one refinement step
     };
     std::vector<GraphPass> graphs;
+    // plan-owned scratch (so distinct plans run concurrently from several host
+    // threads): host-input staging of kernel-by-kernel passes, FP64 fallback
+    double2* d_stage = nullptr;
+    size_t stage_bytes = 0;
+    double2* d_fbW = nullptr;       // N x N (allocated on the first fallback)
+    int* d_fbpiv = nullptr;         // N + 1
 };
 
 int tags_plan_run_plain(tags_plan_s* p, const double2* d_s_unused, int nb, cudaStream_t st);
