@@ -253,6 +253,7 @@ def main():
     ap.add_argument("--cpu-samples", type=int, default=0, help="CPU-baseline samples (0 = host cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernel by kernel in the measured pass")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the 16-sample check against plain FP64")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     args = ap.parse_args()
@@ -359,6 +360,22 @@ def main():
     e2e = {"value": B * e2e_steps / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": B * 16 * (2 + n),
            "d2h_bytes_per_step": B * (16 * N + 4)}
 
+    # accuracy of the measured form against the plain FP64 form: 16 strided
+    # samples, node potentials for the injected current (outside the timed region)
+    accuracy = None
+    if mixed and rank == 0 and not args.no_accuracy:
+        idx = np.arange(0, ns_total, max(1, ns_total // 16))[:16]
+        sol_m, _, _ = plan.run(s[idx], kappa[idx], 1.0, ie_full[idx])
+        ref = pkg.Plan(elec, img, nodes, pkg.PLAIN_FP64, max_batch=8)
+        try:
+            sol_p, _, _ = ref.run(s[idx], kappa[idx], 1.0, ie_full[idx])
+        finally:
+            ref.close()
+        um, up = sol_m[:, :n], sol_p[:, :n]
+        accuracy = {"samples": int(len(idx)), "reference": "plain FP64 form of this library",
+                    "max_rel_err_u_inj": float(np.max(np.abs(um[:, centre] - up[:, centre]) / np.abs(up[:, centre]))),
+                    "max_rel_err_u_all": float(np.max(np.abs(um - up)) / np.max(np.abs(up)))}
+
     if rank != 0:
         return 0
     peaks = measured_peaks()
@@ -377,7 +394,8 @@ def main():
                               "note": "same steps launched kernel by kernel with per-family CUDA events; "
                                       "roofline and kernel_families come from this pass"},
             "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e,
-            "refinement": {"max_iterations": stats_iter, "fallbacks": stats_fb, "split": split}, "wall_s": wall}
+            "refinement": {"max_iterations": stats_iter, "fallbacks": stats_fb, "split": split},
+            "accuracy": accuracy, "wall_s": wall}
     if not args.no_cpu_baseline:
         nsamp = args.cpu_samples or (os.cpu_count() or 1)
         line["cpu_baseline"] = cpu_baseline(args, elec, img, nodes, s, kappa, inj, centre, nsamp)[0]

@@ -157,6 +157,25 @@ int tags_plan_set_graphs (tags_plan plan, int enable);
  * solve that pass again). Default 16. */
 int tags_plan_set_split (tags_plan plan, int pieces);
 
+/* Result of tags_plan_tune: the configuration kept and its measured rate. */
+typedef struct {
+    int samples_per_pass;      /* samples factorised together (<= the plan's capacity) */
+    int pair_panels;           /* 1: two 128-column panels per trailing update (K = 256); 0: one */
+    int split;                 /* split form kept (TAGS_MIXED; 0 for TAGS_PLAIN_FP64) */
+    double solves_per_second;  /* device rate of the kept configuration on the given samples */
+    int candidates;            /* configurations timed */
+} tags_tune_result;
+
+/* Autotuner: times one pass for each candidate configuration (samples per
+ * pass in powers of two up to the plan's capacity; for TAGS_MIXED also one or
+ * two panels per trailing update and the fp16 or three-piece bf16 split) on
+ * the first samples of s / kappa (ns >= 1; unit current at inj_node; flags as
+ * in tags_plan_run) and keeps the fastest in the plan. Quadrature orders are
+ * not tuned: they follow the fill's error model, so accuracy does not depend
+ * on the tuner. out may be NULL. */
+int tags_plan_tune (tags_plan plan, const tags_cdouble *s, const tags_cdouble *kappa, double mur, size_t ns,
+                    size_t inj_node, int flags, tags_tune_result *out);
+
 /* ---- Part 3: solve without device allocation -------------------------------- */
 
 /* No counterpart in the reference. For callers that may not allocate device
@@ -186,6 +205,14 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
  * D (diagonal) in place, rounded from FP32. Returns 0, k > 0 for a zero
  * pivot, or a TAGS_E_* code (TAGS_E_NONFINITE: a value left the fp16 range). */
 int tags_debug_ldl (tags_cdouble *a, int N, int nb, int pieces);
+
+/* No counterpart in the reference. As tags_debug_ldl, then one solve
+ * L D L^T x = b per matrix with the factors (no refinement); b (N x nb,
+ * sample-major) is replaced by x, rounded from FP32. zl_m > 0 declares rows
+ * and columns zl_m .. 2 zl_m - 1 structurally zero against columns 0 ..
+ * zl_m - 1 (the ZL/ZT coupling of the immittance system), which the
+ * factorisation and the solves skip. */
+int tags_debug_ldl_solve (tags_cdouble *a, tags_cdouble *b, int N, int nb, int pieces, int zl_m);
 
 /* Per-family kernel timing with CUDA events on the launching stream (0 = off,
  * the default). Enabling resets the counters. Families, in this order:

@@ -199,3 +199,25 @@ def test_graph_passes_match_direct_launches(gpu_pkg, precision):
     assert np.max(np.abs(sg[:, 0] - gd["u0"][idx]) / np.abs(gd["u0"][idx])) < (1e-8 if precision == "plain" else 1e-6)
     # the graph path counts the kernels its launches ran: same order as direct
     assert ng > 0 and abs(ng - nd) <= 0.1 * nd
+
+
+def test_autotuner_keeps_a_valid_configuration(gpu_pkg):
+    """tags_plan_tune times the candidate configurations on 64 samples of the
+    config-2 grid and keeps the fastest; solutions after tuning stay within
+    1e-6 of the reference."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    plan = pkg.Plan(e, pkg.images(e), nodes, pkg.MIXED, max_batch=64)
+    try:
+        res = plan.tune(gd["s"][:64], gd["kappa"][:64], inj_node=0)
+        assert res.candidates >= 8
+        assert res.samples_per_pass in (16, 32, 64) and res.pair_panels in (0, 1) and res.split in (3, 16)
+        assert res.solves_per_second > 0
+        ie = np.zeros((len(gd["s"]), nodes.shape[0]), np.complex128)
+        ie[:, 0] = gd["inj_s"]
+        sol, info, st = plan.run(gd["s"], gd["kappa"], ie=ie)
+        assert np.all(info == 0) and st.fallbacks == 0
+        assert np.max(np.abs(sol[:, 0] - gd["u0"]) / np.abs(gd["u0"])) < 1e-6
+    finally:
+        plan.close()

@@ -54,7 +54,7 @@ EPS0 = 8.854187817620e-12
 EXPORTS = (
     "calculate_impedances", "impedances_images", "fill_incidence_imm", "fill_impedance_imm",
     "solve_immittance", "laplace_trans", "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
-    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_gpu_set_quiet",
 )
 
@@ -68,6 +68,11 @@ class c_complex(ctypes.Structure):
     def of(cls, z) -> "c_complex":
         z = complex(z)
         return cls(z.real, z.imag)
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("samples_per_pass", ctypes.c_int), ("pair_panels", ctypes.c_int), ("split", ctypes.c_int),
+                ("solves_per_second", ctypes.c_double), ("candidates", ctypes.c_int)]
 
 
 class RunStats(ctypes.Structure):
@@ -115,13 +120,15 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_destroy.argtypes = [_vp]
             L.tags_plan_set_graphs.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_tune.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int,
+                                         ctypes.POINTER(TuneResult)]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
             for name in ("calculate_impedances", "impedances_images", "fill_incidence_imm",
                          "fill_impedance_imm", "solve_immittance", "laplace_trans", "inv_laplace_trans",
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
-                         "tags_plan_set_split"):
+                         "tags_plan_set_split", "tags_plan_tune"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -400,6 +407,18 @@ class Plan:
         code = lib().tags_plan_set_split(self.handle, int(pieces))
         if code != 0:
             raise RuntimeError(f"tags_plan_set_split failed ({code}): {last_error()}")
+
+    def tune(self, s, kappa, mur=1.0, inj_node=0):
+        """Autotune samples per pass, panels per trailing update and the split
+        form on these samples (tags_plan_tune); returns the kept TuneResult."""
+        s = np.ascontiguousarray(s, dtype=np.complex128)
+        kappa = np.ascontiguousarray(np.broadcast_to(kappa, s.shape), dtype=np.complex128)
+        res = TuneResult()
+        code = lib().tags_plan_tune(self.handle, _addr(s), _addr(kappa), float(mur), s.shape[0], int(inj_node), 0,
+                                    ctypes.byref(res))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_tune failed ({code}): {last_error()}")
+        return res
 
     def set_graphs(self, enable):
         """Run each pass as one CUDA-graph launch (True) or kernel by kernel."""

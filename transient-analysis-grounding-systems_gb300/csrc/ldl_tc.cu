@@ -792,23 +792,53 @@ __global__ void __launch_bounds__(128) k_blk_fwd_update(const float2* __restrict
 }
 
 // backward (L^T): x[r] -= sum_{c in block} L[c][r] x[c] for rows r above the
-// block; a warp per r, lanes over the block's rows of column r (coalesced).
+// block; a warp per 4 consecutive r, lanes over the block's rows of column r
+// (coalesced), 16 loads in flight per lane.
 __global__ void __launch_bounds__(256) k_blk_bwd_update(const float2* __restrict__ A0, long long ld, long long mstride,
                                                         int j0, int jb, float2* __restrict__ x0, long long xstride,
                                                         int zl_m) {
-    const int smp = blockIdx.y;
-    const int r = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
-    if (r >= j0) return;
-    if (j0 >= zl_m && j0 + jb <= 2 * zl_m && r < zl_m) return;       // L[ZT rows, ZL cols] = 0
-    const float2* col = A0 + mstride * smp + ld * (long long)r + j0;
+    __shared__ float2 xs[TB];
+    const int smp = blockIdx.y, lane = threadIdx.x & 31;
     float2* x = x0 + xstride * smp;
-    float2 acc = make_float2(0.f, 0.f);
-    for (int c = lane; c < jb; c += 32) acc = ffmac(col[c], x[j0 + c], acc);
-    for (int o = 16; o > 0; o >>= 1) {
-        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
-        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    // zero beyond jb: the products there have zero weights, and 0 * NaN would not vanish
+    if ((int)threadIdx.x < TB) xs[threadIdx.x] = (int)threadIdx.x < jb ? x[j0 + threadIdx.x] : make_float2(0.f, 0.f);
+    __syncthreads();
+    const int r0 = (blockIdx.x * 8 + (threadIdx.x >> 5)) * 4;
+    if (r0 >= j0) return;
+    const bool zero_cols = j0 >= zl_m && j0 + jb <= 2 * zl_m;         // L[ZT rows, ZL cols] = 0
+    const float2* A = A0 + mstride * smp;
+    float2 acc[4];
+    float2 w[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        acc[q] = make_float2(0.f, 0.f);
+        const int r = r0 + q;
+        const float2* col = A + ld * (long long)r + j0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int c = lane + 32 * t;
+            w[q][t] = r < j0 && c < jb && !(zero_cols && r < zl_m) ? col[c] : make_float2(0.f, 0.f);
+        }
     }
-    if (lane == 0) x[r] = fsub(x[r], acc);
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int t = 0; t < 4; ++t) acc[q] = ffmac(w[q][t], xs[lane + 32 * t], acc[q]);
+    // butterfly: every lane ends with all four totals (lane q writes row r0 + q)
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        for (int o = 16; o > 0; o >>= 1) {
+            acc[q].x += __shfl_xor_sync(0xffffffffu, acc[q].x, o);
+            acc[q].y += __shfl_xor_sync(0xffffffffu, acc[q].y, o);
+        }
+    if (lane < 4) {
+        const int r = r0 + lane;
+        float2 a = acc[0];
+#pragma unroll
+        for (int q = 1; q < 4; ++q)
+            if (lane == q) a = acc[q];
+        if (r < j0 && !(zero_cols && r < zl_m)) x[r] = fsub(x[r], a);
+    }
 }
 
 // x[i] /= D[i] (D on the diagonal of the factored matrix)
@@ -958,7 +988,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     for (int b = nblk - 1; b >= 0; --b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
         k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 1);
-        if (j0 > 0) k_blk_bwd_update<<<dim3((j0 + 7) / 8, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m);
+        if (j0 > 0) k_blk_bwd_update<<<dim3((j0 + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m);
         tags_note_launch(j0 > 0 ? 2 : 1);
     }
     // two triangular sweeps over the factor: 8 N^2 real flops, 8 N^2 bytes read
@@ -970,7 +1000,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
 // LDL^T of `nb` matrices A (N x N complex FP32, column-major, lower triangle
 // used) in place: L strictly below the diagonal, D on it.
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
-                int* err, int zl_m, int pieces, cudaStream_t st) {
+                int* err, int zl_m, int pieces, int pair_panels, cudaStream_t st) {
     if (int e0 = tags_ldl_tc_prepare()) return e0;
     // split forms: 3 = bf16 x 3 pieces (6 products), 2 = bf16 x 2 (3 products),
     // TAGS_SPLIT_F16 = scaled fp16 x 2 (3 products, range-checked)
@@ -1081,9 +1111,10 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         return e1;
     };
 
-    // Panels of 128 columns, two at a time: panel a, the update of panel b's
-    // columns by a (which also yields b's block-column planes), panel b, then
-    // one trailing update with K = 256 over both; a last single panel uses K = 128.
+    // Panels of 128 columns, two at a time (pair_panels): panel a, the update
+    // of panel b's columns by a (which also yields b's block-column planes),
+    // panel b, then one trailing update with K = 256 over both; otherwise (and
+    // for a last single panel) one panel and a K = 128 update.
     int j0 = 0;
     while (j0 < N) {
         const int jba = N - j0 < TB ? N - j0 : TB;
@@ -1100,7 +1131,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         if (e) return e;
         const int jbb = resta < TB ? resta : TB;
         const int restb = resta - jbb;
-        if (restb <= 0 || jba < TB) {
+        if (!pair_panels || restb <= 0 || jba < TB) {
             e = update(j0 + jba, resta, resta, true, j0 + jba, mLa, mWa, 0, nullptr, nullptr, resta - jbb);
             if (e) return e;
             j0 += jba;
@@ -1121,10 +1152,22 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
     return 0;
 }
 
-// ---- diagnostic entry point (declared in include/tags_gpu.h) ------------------------
+// ---- diagnostic entry points (declared in include/tags_gpu.h) -----------------------
+
+static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m);
 
 extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
-    if (!a || N <= 0 || nb <= 0) return tags_fail(TAGS_E_ARG, "tags_debug_ldl: invalid argument");
+    return debug_ldl_impl(a, nullptr, N, nb, pieces, 0);
+}
+
+extern "C" int tags_debug_ldl_solve(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m) {
+    if (!b) return tags_fail(TAGS_E_ARG, "tags_debug_ldl_solve: invalid argument");
+    return debug_ldl_impl(a, b, N, nb, pieces, zl_m);
+}
+
+static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m) {
+    if (!a || N <= 0 || nb <= 0 || zl_m < 0 || 2 * zl_m > N)
+        return tags_fail(TAGS_E_ARG, "tags_debug_ldl: invalid argument");
     DeviceCtx* c = tags_ctx();
     if (!c) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
     cudaStream_t st = c->stream;
@@ -1143,12 +1186,24 @@ extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
     if (!rc && pieces != 2 && pieces != 3 && pieces != TAGS_SPLIT_F16)
         rc = tags_fail(TAGS_E_ARG, "tags_debug_ldl: pieces must be 2, 3 or 16");
     std::vector<float2> hf(NN * nb);
+    float2* X = nullptr;
+    std::vector<float2> hx;
+    if (!rc && b) {
+        if (cudaMalloc(&X, sizeof(float2) * N * nb) != cudaSuccess) rc = tags_fail(TAGS_E_NOMEM, "device allocation failed");
+        hx.resize((size_t)N * nb);
+        for (size_t q = 0; q < hx.size(); ++q) hx[q] = make_float2((float)b[q].re, (float)b[q].im);
+    }
     if (!rc) {
         for (long long q = 0; q < NN * nb; ++q) hf[q] = make_float2((float)a[q].re, (float)a[q].im);
         cudaMemcpyAsync(A, hf.data(), sizeof(float2) * NN * nb, cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(ws, 0, wsb, st);
         cudaMemsetAsync(err, 0, 2 * sizeof(int), st);
-        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, 0, pieces, st);
+        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, zl_m, pieces, 1, st);
+        if (!rc && b) {
+            cudaMemcpyAsync(X, hx.data(), sizeof(float2) * N * nb, cudaMemcpyHostToDevice, st);
+            rc = tags_ldl_solve_c(A, N, N, NN, nb, nb, ws, X, N, zl_m, st);
+            if (!rc) cudaMemcpyAsync(hx.data(), X, sizeof(float2) * N * nb, cudaMemcpyDeviceToHost, st);
+        }
     }
     int herr[2] = {0, 0};
     std::vector<int> hinfo(nb, 0);
@@ -1160,6 +1215,8 @@ extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
     }
     if (!rc) {
         for (long long q = 0; q < NN * nb; ++q) a[q] = {hf[q].x, hf[q].y};
+        if (b)
+            for (size_t q = 0; q < hx.size(); ++q) b[q] = {hx[q].x, hx[q].y};
         if (herr[0]) rc = tags_fail(TAGS_E_CUDA, "tags_debug_ldl: tensor-core wait ran out");
         else if (herr[1]) rc = tags_fail(TAGS_E_NONFINITE, "tags_debug_ldl: a value left the fp16 split's range");
         for (int q = 0; q < nb && !rc; ++q)
@@ -1170,5 +1227,6 @@ extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
     cudaFree(ws);
     cudaFree(info);
     cudaFree(err);
+    if (X) cudaFree(X);
     return rc;
 }

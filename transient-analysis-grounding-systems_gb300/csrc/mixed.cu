@@ -18,7 +18,7 @@
 //   4. iterative refinement: x in FP64, r = b - W x with the exact incidence
 //      (sparse, +-1 / 0.5) in FP64 and the impedance blocks times x in
 //      two-float arithmetic (about 2^-44 relative), the correction from the
-//      FP32 factors; a sample stops once the correction is below 1e-10 |x|
+//      FP32 factors; a sample stops once the correction is below 1e-9 |x|
 //      or stops shrinking. The stopping decision runs on the device
 //      (k_ir_decide), so one refinement step is a fixed launch sequence that a
 //      CUDA graph repeats under a conditional while-node;
@@ -233,10 +233,25 @@ __global__ void __launch_bounds__(256) k_residual_z(const float2* __restrict__ Z
         }
         __syncthreads();
         if (k < m) {
-            for (int j = 0; j < nj; ++j) {
-                const float2 z = Zb[k + (size_t)m * (j0 + j)];
+            const float2* zc = Zb + k + (size_t)m * j0;
+            int j = 0;
+            for (; j + 8 <= nj; j += 8) {
+                float2 z[8];                               // eight loads in flight
+#pragma unroll
+                for (int q = 0; q < 8; ++q) z[q] = zc[(size_t)m * (j + q)];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const float4 xv = xs[j + q];
+                    // (zr + i zi)(xr + i xi) = (zr xr - zi xi) + i (zr xi + zi xr)
+                    ar = f2_mac(ar, z[q].x, xv.x, xv.y);
+                    ar = f2_mac(ar, -z[q].y, xv.z, xv.w);
+                    ai = f2_mac(ai, z[q].x, xv.z, xv.w);
+                    ai = f2_mac(ai, z[q].y, xv.x, xv.y);
+                }
+            }
+            for (; j < nj; ++j) {
+                const float2 z = zc[(size_t)m * j];
                 const float4 xv = xs[j];
-                // (zr + i zi)(xr + i xi) = (zr xr - zi xi) + i (zr xi + zi xr)
                 ar = f2_mac(ar, z.x, xv.x, xv.y);
                 ar = f2_mac(ar, -z.y, xv.z, xv.w);
                 ai = f2_mac(ai, z.x, xv.z, xv.w);
@@ -319,8 +334,8 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
 }
 
 // After a refinement step: per sample, stop once the correction is below
-// 1e-10 |x| (each step contracts the error by about kappa * eps_factor, a few
-// 1e-3 here, so the error left is ~1e-13 |x|, far under the ~1e-7 of the
+// 1e-9 |x| (each step contracts the error by about kappa * eps_factor, a few
+// 1e-3 here, so the error left is ~1e-12 |x|, far under the ~1e-7 of the
 // FP32 impedance fill) or once it stops shrinking (accepted when the backward
 // error is below 1e-12); NaN goes to the fallback. One CTA. Sets the continue
 // flag and, inside a graph, the while-node condition.
@@ -335,7 +350,7 @@ __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ n
         const double be = rn / (s.wnorm[q] * xn + 1e-300);
         s.berr[q] = be;
         if (!(dx == dx) || !(xn == xn)) { s.active[q] = 0; continue; }
-        if (dx <= 1e-10 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
+        if (dx <= 1e-9 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
         if (step >= 2 && dx > 0.5 * s.prev_dx[q]) {
             s.conv[q] = be <= 1e-12;
             s.active[q] = 0;
@@ -454,7 +469,7 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m,
-                       p->split_pieces, st);
+                       p->split_pieces, p->pair_panels, st);
 }
 
 // r = b, max row sum of W per sample, refinement state

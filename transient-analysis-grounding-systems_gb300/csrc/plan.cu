@@ -380,6 +380,73 @@ extern "C" int tags_plan_set_split(tags_plan plan, int pieces) {
     return 0;
 }
 
+// forward declaration: the tuner times the public run path
+extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
+                             const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags,
+                             tags_run_stats* stats);
+
+extern "C" int tags_plan_tune(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
+                              size_t inj_node, int flags, tags_tune_result* out) {
+    tags_plan_s* p = plan;
+    if (!p || !s || !kappa || ns == 0) return tags_fail(TAGS_E_ARG, "tags_plan_tune: invalid argument");
+    const int cap = (int)std::min<size_t>(p->batch, ns);
+    std::vector<int> sizes;
+    for (int b = 16; b < cap; b *= 2) sizes.push_back(b);
+    sizes.push_back(cap);
+    const bool mixed = p->precision != TAGS_PLAIN_FP64;
+    const int pairs[2] = {1, 0};
+    const int splits[2] = {TAGS_SPLIT_F16, 3};
+    tags_tune_result best{};
+    best.solves_per_second = -1.0;
+    const int saved_pass = p->pass_batch, saved_pair = p->pair_panels, saved_split = p->split_pieces;
+    int count = 0;
+    for (int b : sizes)
+        for (int ip = 0; ip < (mixed ? 2 : 1); ++ip)
+            for (int is = 0; is < (mixed ? 2 : 1); ++is) {
+                p->pass_batch = b;
+                if (mixed) {
+                    p->pair_panels = pairs[ip];
+                    p->split_pieces = splits[is];
+                }
+                tags_plan_drop_graphs(p);
+                tags_run_stats st{};
+                // the first pass captures the graph of this shape; the second is timed
+                int rc = tags_plan_run(p, s, kappa, mur, (size_t)b, nullptr, inj_node, nullptr, nullptr, flags, &st);
+                if (!rc) rc = tags_plan_run(p, s, kappa, mur, (size_t)b, nullptr, inj_node, nullptr, nullptr, flags, &st);
+                if (rc) {
+                    // a candidate that fails is skipped; the error stays in tags_gpu_last_error
+                    cudaGetLastError();
+                    continue;
+                }
+                ++count;
+                const double rate = st.seconds > 0 ? b / st.seconds : 0.0;
+                // the fp16 split may have fallen back to three pieces inside the run
+                const int used_split = mixed ? st.split : 0;
+                if (rate > best.solves_per_second) {
+                    best.samples_per_pass = b;
+                    best.pair_panels = mixed ? p->pair_panels : 0;
+                    best.split = used_split;
+                    best.solves_per_second = rate;
+                }
+            }
+    if (best.solves_per_second < 0) {
+        p->pass_batch = saved_pass;
+        p->pair_panels = saved_pair;
+        p->split_pieces = saved_split;
+        tags_plan_drop_graphs(p);
+        return tags_fail(TAGS_E_CUDA, "tags_plan_tune: no candidate ran");
+    }
+    p->pass_batch = best.samples_per_pass;
+    if (mixed) {
+        p->pair_panels = best.pair_panels;
+        p->split_pieces = best.split;
+    }
+    tags_plan_drop_graphs(p);
+    best.candidates = count;
+    if (out) *out = best;
+    return 0;
+}
+
 extern "C" int tags_plan_set_graphs(tags_plan plan, int enable) {
     if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_graphs: invalid plan");
     plan->use_graphs = enable ? 1 : 0;
@@ -416,8 +483,9 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     if (stats) memset(stats, 0, sizeof(*stats));
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_status, 0, sizeof(int) * 4, st));
     TAGS_CUDA_OK(cudaEventRecord(p->ev0, st));
-    for (size_t k0 = 0; k0 < ns; k0 += p->batch) {
-        const int nb = (int)std::min<size_t>(p->batch, ns - k0);
+    const size_t per_pass = p->pass_batch > 0 && p->pass_batch < p->batch ? p->pass_batch : p->batch;
+    for (size_t k0 = 0; k0 < ns; k0 += per_pass) {
+        const int nb = (int)std::min<size_t>(per_pass, ns - k0);
         const double2 *ds, *dk, *die = nullptr;
         if (p->use_graphs) {
             // inputs go to the plan's staging buffers, which the graph reads
