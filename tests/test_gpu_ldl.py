@@ -84,22 +84,23 @@ def _banded_sym(rng, N, zl_m, dominance):
     return a
 
 
-@pytest.mark.parametrize("pieces", [3, 16])
+@pytest.mark.parametrize("pieces,group", [(3, 4), (16, 4), (16, 2), (16, 1)])
 @pytest.mark.parametrize("N,zl_m", [(300, 0), (517, 0), (700, 150), (1000, 300)])
-def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces):
+def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group):
     """One solve with the tensor-core factors (block-inverse sweeps, the
-    diagonal, the zero ZL/ZT band skipped when zl_m > 0) against numpy's
-    solve of the same matrices: FP32-level agreement on these well-conditioned
-    matrices, partial last blocks included."""
+    diagonal, the zero ZL/ZT band skipped when zl_m > 0; 4, 2 or 1 panels per
+    trailing update) against numpy's solve of the same matrices: FP32-level
+    agreement on these well-conditioned matrices, partial last blocks included."""
     fn = gpu_pkg.lib().tags_debug_ldl_solve
-    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_int]
     fn.restype = ctypes.c_int
     rng = np.random.default_rng(N + zl_m)
     mats = np.stack([_banded_sym(rng, N, zl_m, d) for d in (4.0, 3.0)])
     rhs = rng.standard_normal((2, N)) + 1j * rng.standard_normal((2, N))
     buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)
     x = rhs.copy()
-    code = fn(buf.ctypes.data, x.ctypes.data, N, 2, pieces, zl_m)
+    code = fn(buf.ctypes.data, x.ctypes.data, N, 2, pieces, zl_m, group)
     assert code == 0, gpu_pkg.last_error()
     for q in range(2):
         ref = np.linalg.solve(mats[q], rhs[q])

@@ -211,8 +211,8 @@ def test_autotuner_keeps_a_valid_configuration(gpu_pkg):
     plan = pkg.Plan(e, pkg.images(e), nodes, pkg.MIXED, max_batch=64)
     try:
         res = plan.tune(gd["s"][:64], gd["kappa"][:64], inj_node=0)
-        assert res.candidates >= 8
-        assert res.samples_per_pass in (16, 32, 64) and res.pair_panels in (0, 1) and res.split in (3, 16)
+        assert res.candidates >= 12
+        assert res.samples_per_pass in (16, 32, 64) and res.panels_per_update in (1, 2, 4) and res.split in (3, 16)
         assert res.solves_per_second > 0
         ie = np.zeros((len(gd["s"]), nodes.shape[0]), np.complex128)
         ie[:, 0] = gd["inj_s"]

@@ -71,7 +71,7 @@ class c_complex(ctypes.Structure):
 
 
 class TuneResult(ctypes.Structure):
-    _fields_ = [("samples_per_pass", ctypes.c_int), ("pair_panels", ctypes.c_int), ("split", ctypes.c_int),
+    _fields_ = [("samples_per_pass", ctypes.c_int), ("panels_per_update", ctypes.c_int), ("split", ctypes.c_int),
                 ("solves_per_second", ctypes.c_double), ("candidates", ctypes.c_int)]
 
 

@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -36,6 +37,8 @@
 namespace {
 
 constexpr int TB = 128;                 // panel width and tile edge
+constexpr int GMAX = 4;                 // most panels per trailing update (K up to 512)
+constexpr int KG = TB * GMAX;           // K extent (row length) of a group's plane buffers
 constexpr int SMAX = 3;                 // most bf16 pieces per real value (split products)
 constexpr uint64_t WAIT_NS = 50ull * 1000 * 1000;   // 50 ms per wait
 
@@ -210,18 +213,21 @@ struct GemmArgs {
     long long ld, mstride;
     int row0, col0;            // matrix coordinates of output element (0, 0)
     const float2* dinv;        // per sample 128 values (mode 1)
-    uint16_t* Lp;              // planes written in mode 1: [sample][2S][R][128]
+    uint16_t* Lp;              // planes written in mode 1: [sample][2S][R][KG] (a group's buffers)
     uint16_t* Wp;
-    long long pstride;         // elements per sample of a plane buffer
+    int prow0;                 // mode 1: buffer row of output row 0
+    int kcol0;                 // mode 1: buffer column of output column 0 (128 x panel index in the group)
+    int band_planes;           // mode 1: skipped band tiles still write (zero) planes
+    long long pstride;         // elements per sample of the group buffers (Lp, Wp)
+    long long npstride;        // elements per sample of the block-column buffer (Np), rows of 128
     int R;                     // rows of a plane buffer
     int* err;                  // err[0]: a wait ran out (all CTAs stop); err[1]: fp16 range
     int f16;                   // planes are scaled fp16 pairs (S == 2) instead of bf16 pieces
     int zlo, zhi;              // output rows/cols in [zlo, zhi) are structurally zero (tiles inside skipped)
     uint16_t* Np;              // mode 0: split planes of the next panel's block column (tiles J = 0, I >= 1), or null
     int Mn;                    // rows of the next panel's block column
-    int kblocks;               // K blocks of BK: 4 (K = 128) or 8 (K = 256: two panels)
-    int offA1, offB1;          // row offset of the operands' first 128 K (maps tmA, tmB)
-    int offA2, offB2;          // row offset of the second 128 K (maps tmA2, tmB2)
+    int kblocks;               // K blocks of BK (4 per panel of the group)
+    int off;                   // row offset of the operand rows (tile row TB * I reads row TB * I + off)
 };
 
 TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
@@ -244,46 +250,50 @@ TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& sk
     }
 }
 
-template <int S>
-TAGS_D void split_pieces(float x, uint16_t* p, bool f16, int& ovf) {
-    if (S == 2 && f16) {
-        const float y = x * kF16Scale;
-        if (!(fabsf(y) <= 65504.f)) ovf = 1;
-        const __half h = __float2half_rn(y);
-        p[0] = __half_as_ushort(h);
-        p[1] = __half_as_ushort(__float2half_rn(y - __half2float(h)));
-        return;
-    }
-    float r = x;
-#pragma unroll
-    for (int q = 0; q < S; ++q) {
-        const __nv_bfloat16 b = __float2bfloat16_rn(r);
-        p[q] = __bfloat16_as_ushort(b);
-        r -= __bfloat162float(b);
-    }
-}
-
 // Row `row`, columns c0 .. c0+15 of a plane buffer [2S][R][128] (real
-// pieces, then imaginary pieces): the S-piece split of v[0..15].
+// pieces, then imaginary pieces): the split of v[0..15], two columns at a
+// time with the packed conversions (one instruction per pair of values).
 template <int S>
-TAGS_D void store_planes16(uint16_t* P, int R, int row, int c0, const float2* v, bool f16, int& ovf) {
-    __align__(16) uint16_t pl[2 * S][16];
+TAGS_D void store_planes16(uint16_t* P, int R, int ks, int row, int c0, const float2* v, bool f16, int& ovf) {
+    const long long off = (long long)row * ks + c0;
+    __align__(16) uint32_t pl[2 * S][8];        // 8 packed pairs = 16 columns per plane
+    if (S == 2 && f16) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-        uint16_t pc[S];
-        split_pieces<S>(v[j].x, pc, f16, ovf);
+        for (int j = 0; j < 8; ++j) {
 #pragma unroll
-        for (int q = 0; q < S; ++q) pl[q][j] = pc[q];
-        split_pieces<S>(v[j].y, pc, f16, ovf);
+            for (int c = 0; c < 2; ++c) {       // 0: real parts, 1: imaginary parts
+                const float a = (c ? v[2 * j].y : v[2 * j].x) * kF16Scale;
+                const float b = (c ? v[2 * j + 1].y : v[2 * j + 1].x) * kF16Scale;
+                if (!(fmaxf(fabsf(a), fabsf(b)) <= 65504.f)) ovf = 1;
+                const __half2 hi = __floats2half2_rn(a, b);
+                const float2 hf = __half22float2(hi);
+                const __half2 lo = __floats2half2_rn(a - hf.x, b - hf.y);
+                pl[2 * c][j] = *reinterpret_cast<const uint32_t*>(&hi);
+                pl[2 * c + 1][j] = *reinterpret_cast<const uint32_t*>(&lo);
+            }
+        }
+    } else {
 #pragma unroll
-        for (int q = 0; q < S; ++q) pl[S + q][j] = pc[q];
+        for (int j = 0; j < 8; ++j) {
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                float2 r = c ? make_float2(v[2 * j].y, v[2 * j + 1].y) : make_float2(v[2 * j].x, v[2 * j + 1].x);
+#pragma unroll
+                for (int q = 0; q < S; ++q) {
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(r.x, r.y);
+                    const float2 f = __bfloat1622float2(h);
+                    r.x -= f.x;
+                    r.y -= f.y;
+                    pl[c * S + q][j] = *reinterpret_cast<const uint32_t*>(&h);
+                }
+            }
+        }
     }
-    const long long off = (long long)row * TB + c0;
 #pragma unroll
     for (int p = 0; p < 2 * S; ++p) {
-        uint4* d = reinterpret_cast<uint4*>(P + (long long)p * R * TB + off);
-        d[0] = reinterpret_cast<const uint4*>(pl[p])[0];
-        d[1] = reinterpret_cast<const uint4*>(pl[p])[1];
+        uint4* d = reinterpret_cast<uint4*>(P + (long long)p * R * ks + off);
+        d[0] = make_uint4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
+        d[1] = make_uint4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
     }
 }
 
@@ -292,9 +302,7 @@ constexpr int GEMM_THREADS = 32 * (2 + EPI_WARPS);
 
 template <int S, int MODE>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_constant__ CUtensorMap tmA,
-                                                             const __grid_constant__ CUtensorMap tmB,
-                                                             const __grid_constant__ CUtensorMap tmA2,
-                                                             const __grid_constant__ CUtensorMap tmB2, GemmArgs g) {
+                                                             const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
     using C = GemmCfg<S>;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t base_u32 = (smem_u32(smem_raw) + 1023u) & ~1023u;
@@ -327,8 +335,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
     const uint32_t tmem = *tslot;
 
     if (warp == 0) {
-        // ---- producer: TMA loads of A and B planes, one K block per stage; the
-        // other lanes prefetch the tile's C columns into L2 for the epilogue
+        // ---- producer: TMA loads of A and B planes, one K block per stage
         int stage = 0;
         uint32_t phase = 0;
         bool alive = true;
@@ -338,33 +345,16 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
             bool skip;
             tile_of(g, t, smp, I, J, skip);
             if (skip) continue;
-            if (MODE == 0) {
-                const float2* Cb = g.Amat + g.mstride * smp;
-                const int r0 = g.row0 + TB * I, rows = min(TB, g.M - TB * I);
-                const int c0 = TB * J, cols = min(TB, g.Nn - TB * J);
-                if (rows > 0) {
-                    for (int c = lane; c < cols; c += 32) {
-                        const char* col = reinterpret_cast<const char*>(Cb + (long long)r0 + g.ld * (long long)(g.col0 + c0 + c));
-                        for (int off = 0; off < rows * 8; off += 128)
-                            asm volatile("prefetch.global.L2 [%0];" ::"l"(col + off));
-                    }
-                }
-            }
             if (lane == 0) {
                 for (int kb = 0; kb < g.kblocks; ++kb) {
                     if (!mbar_wait(empty(stage), phase ^ 1, g.err)) { alive = false; break; }
                     issued[stage] = 0;
                     const uint32_t sb = base_u32 + stage * C::STAGE;
                     mbar_expect_tx(full(stage), C::STAGE);
-                    // K blocks 0..3 from the first operand pair, 4..7 from the second
-                    const bool second = kb >= KBLKS;
-                    const CUtensorMap* mA = second ? &tmA2 : &tmA;
-                    const CUtensorMap* mB = second ? &tmB2 : &tmB;
-                    const int ra = TB * I + (second ? g.offA2 : g.offA1), rb = TB * J + (second ? g.offB2 : g.offB1);
-                    const int kx = (kb % KBLKS) * BK;
+                    const int ra = TB * I + g.off, rb = TB * J + g.off, kx = kb * BK;
                     for (int p = 0; p < C::NPL; ++p) {
-                        tma_load_4d(sb + p * PST, mA, kx, ra, p, smp, full(stage));
-                        tma_load_4d(sb + (C::NPL + p) * PST, mB, kx, rb, p, smp, full(stage));
+                        tma_load_4d(sb + p * PST, &tmA, kx, ra, p, smp, full(stage));
+                        tma_load_4d(sb + (C::NPL + p) * PST, &tmB, kx, rb, p, smp, full(stage));
                     }
                     issued[stage] = 1;
                     if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
@@ -465,9 +455,21 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
             bool skip;
             tile_of(g, t, smp, I, J, skip);
             if (skip) {
+                const int gr = TB * I + r;
+                if (MODE == 1 && g.band_planes && gr < g.M) {
+                    // rows of the zero band: L21 = W21 = 0 there; their planes are
+                    // written (as zeros) so that a later update that no longer
+                    // skips the band reads zeros, not another panel's values
+                    float2 zv[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) zv[j] = make_float2(0.f, 0.f);
+                    for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
+                        store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, zv, f16, ovf);
+                        store_planes16<S>(g.Wp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, zv, f16, ovf);
+                    }
+                }
                 // no update of this tile; if it holds rows of the next panel's
                 // block column, their planes are the current values
-                const int gr = TB * I + r;
                 if (MODE == 0 && g.Np && J == 0 && I >= 1 && gr < g.M && gr - TB < g.Mn) {
                     const float2* Cb = g.Amat + g.mstride * smp;
                     for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
@@ -476,7 +478,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
                             cv[j] = cc * 16 + j < g.Nn ? base_p[g.ld * j] : make_float2(0.f, 0.f);
-                        store_planes16<S>(g.Np + g.pstride * smp, g.R, gr - TB, cc * 16, cv, f16, ovf);
+                        store_planes16<S>(g.Np + g.npstride * smp, g.R, TB, gr - TB, cc * 16, cv, f16, ovf);
                     }
                 }
                 continue;
@@ -520,7 +522,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
                             if (cc * 16 + j >= g.Nn) cv[j] = make_float2(0.f, 0.f);
-                        store_planes16<S>(g.Np + g.pstride * smp, g.R, gr - TB, cc * 16, cv, f16, ovf);
+                        store_planes16<S>(g.Np + g.npstride * smp, g.R, TB, gr - TB, cc * 16, cv, f16, ovf);
                     }
                 } else {
                     const float2* dv = dinv_w - half * 64;      // indexed by the tile column
@@ -532,8 +534,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                         lv[j] = fmulc(wv[j], dv[c]);
                         if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = lv[j];
                     }
-                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, gr, cc * 16, lv, f16, ovf);
-                    store_planes16<S>(g.Wp + g.pstride * smp, g.R, gr, cc * 16, wv, f16, ovf);
+                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, lv, f16, ovf);
+                    store_planes16<S>(g.Wp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, wv, f16, ovf);
                 }
             }
             tc_fence_before();
@@ -875,11 +877,11 @@ EncodeTiledFn encode_fn() {
 
 // 4-D map over planes [sample][nplanes][rows][128] bf16, box {32, 128, 1, 1}
 // (64-byte rows, 64-byte swizzle: the K block of one pipeline stage).
-int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samples) {
+int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samples, int klen = TB) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
-    cuuint64_t dims[4] = {(cuuint64_t)TB, (cuuint64_t)rows, (cuuint64_t)nplanes, (cuuint64_t)samples};
-    cuuint64_t strides[3] = {(cuuint64_t)TB * 2, (cuuint64_t)TB * 2 * rows, (cuuint64_t)TB * 2 * rows * nplanes};
+    cuuint64_t dims[4] = {(cuuint64_t)klen, (cuuint64_t)rows, (cuuint64_t)nplanes, (cuuint64_t)samples};
+    cuuint64_t strides[3] = {(cuuint64_t)klen * 2, (cuuint64_t)klen * 2 * rows, (cuuint64_t)klen * 2 * rows * nplanes};
     cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)TB, 1, 1};
     cuuint32_t estr[4] = {1, 1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, base, dims, strides, box, estr,
@@ -902,15 +904,18 @@ static long long linv32_stride(int N) { return (long long)((N + TB - 1) / TB) * 
 // inverses of all diagonal blocks (and their transposes).
 static long long plane_stride(int N) { return (long long)2 * SMAX * N * TB; }
 
+// Workspace per sample: the block-column planes (rows of 128), the L and W
+// planes of a group of up to GMAX panels (rows of KG), the L11^{-1} planes,
+// D^{-1}, and the FP32 inverses of all diagonal blocks.
 size_t tags_ldl_tc_workspace(int N, int batch) {
     size_t plane = (size_t)plane_stride(N) * 2;
-    return (size_t)batch * (5 * plane + (size_t)2 * SMAX * TB * TB * 2 + TB * sizeof(float2) +
+    return (size_t)batch * ((1 + 2 * GMAX) * plane + (size_t)2 * SMAX * TB * TB * 2 + TB * sizeof(float2) +
                             (size_t)linv32_stride(N) * sizeof(float2)) + 1024;
 }
 
 static float2* linv32_of(void* ws, int N, int batch_cap) {
     const long long pstride = plane_stride(N);
-    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + 5 * pstride * batch_cap;
+    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + (1 + 2 * GMAX) * pstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     return dinv + (long long)TB * batch_cap;
 }
@@ -951,23 +956,19 @@ int tags_ldl_tc_prepare() {
 }
 
 template <int S, int MODE>
-static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const CUtensorMap& mA2,
-                         const CUtensorMap& mB2, const GemmArgs& g, cudaStream_t st) {
+static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
     const int total = g.tiles * g.nb;
     const int grid = total < num_sms() ? total : num_sms();
     if (grid <= 0) return 0;
-    k_gemm_tc<S, MODE><<<grid, GEMM_THREADS, GemmCfg<S>::SMEM, st>>>(mA, mB, mA2, mB2, g);
+    k_gemm_tc<S, MODE><<<grid, GEMM_THREADS, GemmCfg<S>::SMEM, st>>>(mA, mB, g);
     tags_note_launch();
     return 0;
 }
 
-// One GEMM launch; K = 128 from (mA, mB), or K = 256 with (mA2, mB2) for the
-// second half (g.kblocks = 8).
-static int launch_gemm(int NS, const CUtensorMap& mA, const CUtensorMap& mB, const CUtensorMap& mA2,
-                       const CUtensorMap& mB2, const GemmArgs& g, cudaStream_t st) {
-    if (NS == 3)
-        return g.mode == 0 ? launch_gemm_m<3, 0>(mA, mB, mA2, mB2, g, st) : launch_gemm_m<3, 1>(mA, mB, mA2, mB2, g, st);
-    return g.mode == 0 ? launch_gemm_m<2, 0>(mA, mB, mA2, mB2, g, st) : launch_gemm_m<2, 1>(mA, mB, mA2, mB2, g, st);
+// One GEMM launch: K = 32 g.kblocks from the operand maps (mA, mB).
+static int launch_gemm(int NS, const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
+    if (NS == 3) return g.mode == 0 ? launch_gemm_m<3, 0>(mA, mB, g, st) : launch_gemm_m<3, 1>(mA, mB, g, st);
+    return g.mode == 0 ? launch_gemm_m<2, 0>(mA, mB, g, st) : launch_gemm_m<2, 1>(mA, mB, g, st);
 }
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
@@ -1000,33 +1001,31 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
 // LDL^T of `nb` matrices A (N x N complex FP32, column-major, lower triangle
 // used) in place: L strictly below the diagonal, D on it.
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
-                int* err, int zl_m, int pieces, int pair_panels, cudaStream_t st) {
+                int* err, int zl_m, int pieces, int group_panels, cudaStream_t st) {
     if (int e0 = tags_ldl_tc_prepare()) return e0;
     // split forms: 3 = bf16 x 3 pieces (6 products), 2 = bf16 x 2 (3 products),
     // TAGS_SPLIT_F16 = scaled fp16 x 2 (3 products, range-checked)
     const int f16 = pieces == TAGS_SPLIT_F16 ? 1 : 0;
     const int NS = pieces == 3 ? 3 : 2;
     // planes of this run use 2 NS of the 2 SMAX slots of each sample
-    const long long pstride = plane_stride(N);
+    const long long pstride = plane_stride(N);           // block-column buffer, rows of 128
+    const long long gstride = pstride * GMAX;             // group buffers, rows of KG
     uint16_t* A21p = reinterpret_cast<uint16_t*>(ws);
-    uint16_t* La = A21p + pstride * batch_cap;       // L and W planes of the first panel of a pair
-    uint16_t* Wa = La + pstride * batch_cap;
-    uint16_t* Lb = Wa + pstride * batch_cap;         // ... and of the second
-    uint16_t* Wb = Lb + pstride * batch_cap;
-    uint16_t* Lin = Wb + pstride * batch_cap;
+    uint16_t* Lg = A21p + pstride * batch_cap;            // L and W planes of the current group of panels
+    uint16_t* Wg = Lg + gstride * batch_cap;
+    uint16_t* Lin = Wg + gstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
     float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
     // the maps see a sample stride of 2 SMAX planes: declare that many planes
-    CUtensorMap mA21, mLa, mWa, mLb, mWb, mLin;
+    CUtensorMap mA21, mLg, mWg, mLin;
     int e = make_plane_map(&mA21, A21p, N, 2 * SMAX, batch_cap);
-    if (!e) e = make_plane_map(&mLa, La, N, 2 * SMAX, batch_cap);
-    if (!e) e = make_plane_map(&mWa, Wa, N, 2 * SMAX, batch_cap);
-    if (!e) e = make_plane_map(&mLb, Lb, N, 2 * SMAX, batch_cap);
-    if (!e) e = make_plane_map(&mWb, Wb, N, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mLg, Lg, N, 2 * SMAX, batch_cap, KG);
+    if (!e) e = make_plane_map(&mWg, Wg, N, 2 * SMAX, batch_cap, KG);
     if (!e) e = make_plane_map(&mLin, Lin, TB, 2 * SMAX, batch_cap);
     if (e) return e;
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * nb, st));
+    const int G = group_panels < 1 ? 1 : (group_panels > GMAX ? GMAX : group_panels);
 
     auto base = [&]() {
         GemmArgs g{};
@@ -1035,7 +1034,8 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.ld = ld;
         g.mstride = mstride;
         g.dinv = dinv;
-        g.pstride = pstride;
+        g.pstride = gstride;
+        g.npstride = pstride;
         g.R = N;
         g.err = err;
         g.f16 = f16;
@@ -1060,34 +1060,38 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         tags_prof_end(TAGS_PROF_LDL_DIAG, pf, st, 4.0 / 3.0 * jb * (double)jb * jb * nb, 16.0 * jb * jb * nb);
         tags_note_launch();
     };
-    // W21 = A21 L11^{-T}, L21 = W21 D^{-1} for the panel at j0 (rows below it):
-    // FP32 L21 into A, both as split planes into (Lx, Wx)
-    auto panel = [&](int j0, int jb, int rest, uint16_t* Lx, uint16_t* Wx) {
+    // W21 = A21 L11^{-T}, L21 = W21 D^{-1} for panel p of the group starting at
+    // jg (columns jp = jg + 128 p .. jp + jb): FP32 L21 into A, both as split
+    // planes into the group buffers at rows (row - jg) and columns 128 p ...
+    auto panel = [&](int jg, int p, int jb, int rest, bool band_planes) {
+        const int jp = jg + TB * p;
         GemmArgs g = base();
-        band(g, j0 + jb);
+        band(g, jp + jb);
+        g.band_planes = band_planes ? 1 : 0;
         g.M = rest;
         g.Nn = jb;
         g.mode = 1;
         g.tiles = (rest + TB - 1) / TB;
-        g.row0 = j0 + jb;
-        g.col0 = j0;
-        g.Lp = Lx;
-        g.Wp = Wx;
+        g.row0 = jp + jb;
+        g.col0 = jp;
+        g.Lp = Lg;
+        g.Wp = Wg;
+        g.prow0 = jp + jb - jg;
+        g.kcol0 = TB * p;
         int pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
-        int e1 = launch_gemm(NS, mA21, mLin, mA21, mLin, g, st);
+        int e1 = launch_gemm(NS, mA21, mLin, g, st);
         // triangular solve: r x jb unknowns against jb x jb (r = rest minus the band), 4 r jb^2 flops
         const double rp = rest - (double)(g.zhi - g.zlo);
         tags_prof_end(TAGS_PROF_LDL_PANEL, pf, st, 4.0 * rp * (double)jb * jb * nb,
                       (8.0 * rp * jb + 16.0 * rp * 128 * 2) * nb);
         return e1;
     };
-    // C -= L W^T on rows (and, tri, columns) row0 .. row0 + M of A, K = 128
-    // (first operand pair) or 256 (both pairs); the first tile column's new
+    // C -= L W^T over the first `np` panels of the group starting at jg, on
+    // rows (and, tri, columns) row0 .. row0 + M; the first tile column's new
     // values also become the next panel's block-column planes (Mn rows).
-    auto update = [&](int row0, int M, int Nn, bool tri, int jend, const CUtensorMap& mA1, const CUtensorMap& mB1,
-                      int off1, const CUtensorMap* mA2, const CUtensorMap* mB2, int Mn) {
+    auto update = [&](int jg, int np, int row0, int M, int Nn, bool tri, int Mn) {
         GemmArgs g = base();
-        band(g, jend);
+        band(g, jg + TB * np);
         const int T = (M + TB - 1) / TB;
         g.M = M;
         g.Nn = Nn;
@@ -1096,13 +1100,13 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.tiles = tri ? T * (T + 1) / 2 : T;
         g.row0 = row0;
         g.col0 = row0;
-        g.offA1 = g.offB1 = off1;
-        g.kblocks = mA2 ? 2 * KBLKS : KBLKS;
+        g.off = row0 - jg;
+        g.kblocks = KBLKS * np;
         g.Mn = Mn;
         g.Np = Mn > 0 ? A21p : nullptr;
         int pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
-        int e1 = launch_gemm(NS, mA1, mB1, mA2 ? *mA2 : mA1, mB2 ? *mB2 : mB1, g, st);
-        // rank-K update outside the zero band: 8 K r c flops (c = r(r+1)/2 / r for the triangle)
+        int e1 = launch_gemm(NS, mLg, mWg, g, st);
+        // rank-K update outside the zero band: 8 K cells flops (cells: the triangle or the block column)
         const double r = M - (double)(g.zhi - g.zlo);
         const double K = g.kblocks * BK;
         const double cells = tri ? 0.5 * r * (r + 1.0) : r * (double)Nn;
@@ -1111,42 +1115,50 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         return e1;
     };
 
-    // Panels of 128 columns, two at a time (pair_panels): panel a, the update
-    // of panel b's columns by a (which also yields b's block-column planes),
-    // panel b, then one trailing update with K = 256 over both; otherwise (and
-    // for a last single panel) one panel and a K = 128 update.
-    int j0 = 0;
-    while (j0 < N) {
-        const int jba = N - j0 < TB ? N - j0 : TB;
-        const int resta = N - j0 - jba;
-        diag(j0, jba);
-        if (resta <= 0) break;
-        if (j0 == 0) {
-            // later panels get their block column's planes from the previous update
-            k_panel_planes<<<dim3((resta + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jba, resta, A21p, pstride,
-                                                                        N, NS, f16, err);
-            tags_note_launch();
-        }
-        e = panel(j0, jba, resta, La, Wa);
-        if (e) return e;
-        const int jbb = resta < TB ? resta : TB;
-        const int restb = resta - jbb;
-        if (!pair_panels || restb <= 0 || jba < TB) {
-            e = update(j0 + jba, resta, resta, true, j0 + jba, mLa, mWa, 0, nullptr, nullptr, resta - jbb);
+    // Groups of G panels of 128 columns: panel p of a group first takes the
+    // update from panels 0 .. p-1 of its group on its own block column
+    // (K = 128 p; this also yields its block-column planes), then its
+    // diagonal block and panel GEMM; one trailing update with K = 128 G
+    // follows each group.
+    int jg = 0;
+    bool done = false;
+    while (!done && jg < N) {
+        int np = 0;
+        // the group's last update reaches column jg + 128 * panels: if that is past
+        // the ZL block, it reads the band rows its panels skipped, so those panels
+        // write zero planes there
+        const int npg = std::min(G, (N - jg + TB - 1) / TB);
+        const bool band_planes = zl_m > 0 && jg + TB * npg > zl_m;
+        for (int p = 0; p < G; ++p) {
+            const int jp = jg + TB * p;
+            if (jp >= N) break;
+            const int jb = N - jp < TB ? N - jp : TB;
+            const int rest = N - jp - jb;
+            if (p > 0) {
+                e = update(jg, p, jp, N - jp, jb, false, rest);
+                if (e) return e;
+            }
+            diag(jp, jb);
+            np = p + 1;
+            if (rest <= 0) {
+                done = true;
+                break;
+            }
+            if (jp == 0) {
+                // later panels get their block column's planes from the update before them
+                k_panel_planes<<<dim3((rest + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, jp, jb, rest, A21p,
+                                                                           pstride, N, NS, f16, err);
+                tags_note_launch();
+            }
+            e = panel(jg, p, jb, rest, band_planes);
             if (e) return e;
-            j0 += jba;
-            continue;
         }
-        // panel b's block column (rows j0 + jba ..., its jbb columns)
-        e = update(j0 + jba, resta, jbb, false, j0 + jba, mLa, mWa, 0, nullptr, nullptr, restb);
+        if (done) break;
+        const int jt = jg + TB * np, rt = N - jt;
+        if (rt <= 0) break;
+        e = update(jg, np, jt, rt, rt, true, rt - (rt < TB ? rt : TB));
         if (e) return e;
-        diag(j0 + jba, jbb);
-        e = panel(j0 + jba, jbb, restb, Lb, Wb);
-        if (e) return e;
-        const int jbn = restb < TB ? restb : TB;
-        e = update(j0 + jba + jbb, restb, restb, true, j0 + jba + jbb, mLa, mWa, jbb, &mLb, &mWb, restb - jbn);
-        if (e) return e;
-        j0 += jba + jbb;
+        jg = jt;
     }
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
@@ -1154,18 +1166,18 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
 
 // ---- diagnostic entry points (declared in include/tags_gpu.h) -----------------------
 
-static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m);
+static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m, int group);
 
 extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
-    return debug_ldl_impl(a, nullptr, N, nb, pieces, 0);
+    return debug_ldl_impl(a, nullptr, N, nb, pieces, 0, GMAX);
 }
 
-extern "C" int tags_debug_ldl_solve(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m) {
-    if (!b) return tags_fail(TAGS_E_ARG, "tags_debug_ldl_solve: invalid argument");
-    return debug_ldl_impl(a, b, N, nb, pieces, zl_m);
+extern "C" int tags_debug_ldl_solve(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m, int group) {
+    if (!b || group < 1 || group > GMAX) return tags_fail(TAGS_E_ARG, "tags_debug_ldl_solve: invalid argument");
+    return debug_ldl_impl(a, b, N, nb, pieces, zl_m, group);
 }
 
-static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m) {
+static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m, int group) {
     if (!a || N <= 0 || nb <= 0 || zl_m < 0 || 2 * zl_m > N)
         return tags_fail(TAGS_E_ARG, "tags_debug_ldl: invalid argument");
     DeviceCtx* c = tags_ctx();
@@ -1196,9 +1208,10 @@ static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int p
     if (!rc) {
         for (long long q = 0; q < NN * nb; ++q) hf[q] = make_float2((float)a[q].re, (float)a[q].im);
         cudaMemcpyAsync(A, hf.data(), sizeof(float2) * NN * nb, cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(ws, 0, wsb, st);
+        // plane buffers start as NaN patterns: a read of a row no kernel wrote shows
+        cudaMemsetAsync(ws, 0xFF, wsb, st);
         cudaMemsetAsync(err, 0, 2 * sizeof(int), st);
-        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, zl_m, pieces, 1, st);
+        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, zl_m, pieces, group, st);
         if (!rc && b) {
             cudaMemcpyAsync(X, hx.data(), sizeof(float2) * N * nb, cudaMemcpyHostToDevice, st);
             rc = tags_ldl_solve_c(A, N, N, NN, nb, nb, ws, X, N, zl_m, st);

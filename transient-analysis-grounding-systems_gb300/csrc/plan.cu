@@ -394,18 +394,18 @@ extern "C" int tags_plan_tune(tags_plan plan, const tags_cdouble* s, const tags_
     for (int b = 16; b < cap; b *= 2) sizes.push_back(b);
     sizes.push_back(cap);
     const bool mixed = p->precision != TAGS_PLAIN_FP64;
-    const int pairs[2] = {1, 0};
+    const int groups[3] = {4, 2, 1};
     const int splits[2] = {TAGS_SPLIT_F16, 3};
     tags_tune_result best{};
     best.solves_per_second = -1.0;
-    const int saved_pass = p->pass_batch, saved_pair = p->pair_panels, saved_split = p->split_pieces;
+    const int saved_pass = p->pass_batch, saved_group = p->group_panels, saved_split = p->split_pieces;
     int count = 0;
     for (int b : sizes)
-        for (int ip = 0; ip < (mixed ? 2 : 1); ++ip)
+        for (int ip = 0; ip < (mixed ? 3 : 1); ++ip)
             for (int is = 0; is < (mixed ? 2 : 1); ++is) {
                 p->pass_batch = b;
                 if (mixed) {
-                    p->pair_panels = pairs[ip];
+                    p->group_panels = groups[ip];
                     p->split_pieces = splits[is];
                 }
                 tags_plan_drop_graphs(p);
@@ -424,21 +424,21 @@ extern "C" int tags_plan_tune(tags_plan plan, const tags_cdouble* s, const tags_
                 const int used_split = mixed ? st.split : 0;
                 if (rate > best.solves_per_second) {
                     best.samples_per_pass = b;
-                    best.pair_panels = mixed ? p->pair_panels : 0;
+                    best.panels_per_update = mixed ? p->group_panels : 0;
                     best.split = used_split;
                     best.solves_per_second = rate;
                 }
             }
     if (best.solves_per_second < 0) {
         p->pass_batch = saved_pass;
-        p->pair_panels = saved_pair;
+        p->group_panels = saved_group;
         p->split_pieces = saved_split;
         tags_plan_drop_graphs(p);
         return tags_fail(TAGS_E_CUDA, "tags_plan_tune: no candidate ran");
     }
     p->pass_batch = best.samples_per_pass;
     if (mixed) {
-        p->pair_panels = best.pair_panels;
+        p->group_panels = best.panels_per_update;
         p->split_pieces = best.split;
     }
     tags_plan_drop_graphs(p);

@@ -65,7 +65,7 @@ struct tags_plan_s {
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
     int split_pieces = TAGS_SPLIT_F16;   // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
-    int pair_panels = 1;            // tensor-core LDL^T: two panels per trailing update (K = 256)
+    int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue
     double* d_ird = nullptr;        // refinement state: previous correction, max row sum, backward error
