@@ -10,6 +10,11 @@
  *   fill_incidence_imm     replaces src/linalg.c:12-86      (decl src/linalg.h:38-41)
  *   fill_impedance_imm     replaces src/linalg.c:88-110     (decl src/linalg.h:56-59)
  *   solve_immittance       replaces src/linalg.c:112-139    (decl src/linalg.h:79-81)
+ *   fill_incidence_adm     replaces src/linalg.c:142-204    (decl src/linalg.h:103-106)
+ *   fill_impedance_adm     replaces src/linalg.c:206-259    (decl src/linalg.h:123-126)
+ *   calculate_yla_ytb      replaces src/linalg.c:261-300    (decl src/linalg.h:145-149)
+ *   fill_impedance_adm2    replaces src/linalg.c:302-325    (decl src/linalg.h:169-173)
+ *   solve_admittance       replaces src/linalg.c:327-350    (decl src/linalg.h:192-193)
  *   laplace_trans          replaces src/auxiliary.c:239-263 (decl src/auxiliary.h:320-321)
  *   inv_laplace_trans      replaces src/auxiliary.c:265-329 (decl src/auxiliary.h:366-368)
  *
@@ -86,6 +91,34 @@ int fill_impedance_imm (tags_cdouble *wg, const tags_cdouble *zl, const tags_cdo
  * factorisation there; its content is not part of the contract). */
 int solve_immittance (tags_cdouble *wg, tags_cdouble *ie, size_t num_electrodes, size_t num_nodes);
 
+/* ---- nodal admittance formulation (the reference's mHEM examples) ---------- */
+
+/* A (+1 start, -1 end) and B (0.5), num_electrodes x num_nodes column-major.
+ * Written in the reference's order (b before a at a match: a == b leaves A);
+ * returns 1 at the first node without incidence, -sum(A) or sum(B) - m on a
+ * bad checksum (read back from the arrays), 0 on success. */
+int fill_incidence_adm (tags_cdouble *a, tags_cdouble *b, const Electrode *electrodes, size_t num_electrodes,
+                        const double *nodes, size_t num_nodes);
+
+/* yn (n x n) = A^T ZL^{-1} A + B^T ZT^{-1} B from the lower triangles of
+ * zl, zt (m x m), which are overwritten by the inverses' lower triangles as
+ * the reference's zsytrf + zsytri leave them. Returns 0 or the order k > 0 of
+ * an exactly zero pivot. */
+int fill_impedance_adm (tags_cdouble *yn, tags_cdouble *zl, tags_cdouble *zt, tags_cdouble *a, tags_cdouble *b,
+                        size_t num_electrodes, size_t num_nodes);
+
+/* yla = ZL^{-1} A, ytb = ZT^{-1} B (m x n); zl, zt as in fill_impedance_adm. */
+int calculate_yla_ytb (tags_cdouble *yla, tags_cdouble *ytb, tags_cdouble *zl, tags_cdouble *zt,
+                       tags_cdouble *a, tags_cdouble *b, size_t num_electrodes, size_t num_nodes);
+
+/* yn = A^T yla + B^T ytb (n x n). */
+int fill_impedance_adm2 (tags_cdouble *yn, tags_cdouble *yla, tags_cdouble *ytb, tags_cdouble *a,
+                         tags_cdouble *b, size_t num_electrodes, size_t num_nodes);
+
+/* Solves YN u = ic (YN symmetric, lower half read); ic <- u. Returns 0 or
+ * k > 0 for an exactly zero pivot. yn is left unchanged. */
+int solve_admittance (tags_cdouble *yn, tags_cdouble *ic, size_t num_nodes);
+
 /* Numerical Laplace transform and its inverse, with the reference's
  * conventions (s_k = c + j k 2pi/tmax, c = ln(nt^2)/tmax; window `filter` as
  * the reference's INLT_Filter: 0 none, 1 Blackman, 2 Hanning, 3 Lanczos,
@@ -156,6 +189,15 @@ int tags_plan_set_graphs (tags_plan plan, int enable);
  * 22 bits; a value outside fp16's range makes the plan fall back to 3 and
  * solve that pass again). Default 16. */
 int tags_plan_set_split (tags_plan plan, int pieces);
+
+/* Impedance model of the plan's passes: 2 (the reference's INTG_DOUBLE,
+ * default) fills ZL/ZT with the double line integrals of e^{-gamma r}/r;
+ * 4 (INTG_MHEM) uses the reference's mHEM examples' model: static potentials
+ * (INTG_MHEM integrals, computed once here) times e^{-gamma rbar} of the
+ * segments' midpoint distance, images with ref_l = 1 and ref_t
+ * (examples/three_grids.c:335-350). The node potentials then equal those of
+ * the examples' nodal admittance solve (Y_N is W_G's node Schur complement). */
+int tags_plan_set_fill (tags_plan plan, int integration_type);
 
 /* Result of tags_plan_tune: the configuration kept and its measured rate. */
 typedef struct {

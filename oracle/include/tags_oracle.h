@@ -77,6 +77,24 @@ int oracle_fill_incidence_imm (double _Complex *wg, const OracleElectrode *e, si
 int oracle_fill_impedance_imm (double _Complex *wg, const double _Complex *zl,
                                const double _Complex *zt, size_t m, size_t n);
 int oracle_solve_immittance (double _Complex *wg, double _Complex *ie, size_t m, size_t n);
+int oracle_fill_incidence_adm (double _Complex *a, double _Complex *b, const OracleElectrode *e, size_t m,
+                               const double *nodes, size_t n);
+int oracle_calculate_yla_ytb (double _Complex *yla, double _Complex *ytb, double _Complex *zl,
+                              double _Complex *zt, double _Complex *a, double _Complex *b, size_t m, size_t n);
+int oracle_fill_impedance_adm2 (double _Complex *yn, double _Complex *yla, double _Complex *ytb,
+                                double _Complex *a, double _Complex *b, size_t m, size_t n);
+int oracle_fill_impedance_adm (double _Complex *yn, double _Complex *zl, double _Complex *zt,
+                               double _Complex *a, double _Complex *b, size_t m, size_t n);
+int oracle_solve_admittance (double _Complex *yn, double _Complex *ic, size_t n);
+int oracle_mhem_impedances (const OracleElectrode *e, const OracleElectrode *img, size_t m,
+                            const double _Complex *potzl, const double _Complex *potzt,
+                            const double _Complex *potzli, const double _Complex *potzti,
+                            double _Complex s, double _Complex kappa, double mur,
+                            double _Complex *zl, double _Complex *zt);
+int oracle_mhem_sweep (const OracleElectrode *e, const OracleElectrode *img, size_t m, const double *nodes,
+                       size_t n, const double _Complex *s, const double _Complex *kappa, size_t ns, double mur,
+                       size_t inj_node, const double _Complex *inj, size_t max_eval, double req_abs,
+                       double req_rel, int threads, double _Complex *sol, int *info);
 
 /* numerical Laplace transform pair (src/auxiliary.c:239-336) */
 int oracle_laplace_trans (const double *f, double _Complex *g, double _Complex *s,

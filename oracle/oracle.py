@@ -156,6 +156,20 @@ class Oracle:
         f = self._fn("solve_immittance")
         f.argtypes = [_dp, _dp, _sz, _sz]
         f.restype = ctypes.c_int
+        # nodal admittance formulation (src/linalg.c:142-321)
+        f = self._fn("fill_incidence_adm")
+        f.argtypes = [_dp, _dp, _dp, _sz, _dp, _sz]
+        f.restype = ctypes.c_int
+        f = self._fn("calculate_yla_ytb")
+        f.argtypes = [_dp, _dp, _dp, _dp, _dp, _dp, _sz, _sz]
+        f.restype = ctypes.c_int
+        for name in ("fill_impedance_adm2", "fill_impedance_adm"):
+            f = self._fn(name)
+            f.argtypes = [_dp, _dp, _dp, _dp, _dp, _sz, _sz]
+            f.restype = ctypes.c_int
+        f = self._fn("solve_admittance")
+        f.argtypes = [_dp, _dp, _sz]
+        f.restype = ctypes.c_int
         f = self._fn("laplace_trans")
         f.argtypes = [_dp, _dp, _dp, ctypes.c_double, _sz]
         f.restype = ctypes.c_int
@@ -180,6 +194,13 @@ class Oracle:
             f = self.lib.oracle_hem_impedances
             f.argtypes = [_dp, _dp, _sz, C, C, ctypes.c_double, _sz, ctypes.c_double,
                           ctypes.c_double, ctypes.c_int, _dp, _dp]
+            f.restype = ctypes.c_int
+            f = self.lib.oracle_mhem_impedances
+            f.argtypes = [_dp, _dp, _sz, _dp, _dp, _dp, _dp, C, C, ctypes.c_double, _dp, _dp]
+            f.restype = ctypes.c_int
+            f = self.lib.oracle_mhem_sweep
+            f.argtypes = [_dp, _dp, _sz, _dp, _sz, _dp, _dp, _sz, ctypes.c_double, _sz, _dp,
+                          _sz, ctypes.c_double, ctypes.c_double, ctypes.c_int, _dp, _ip]
             f.restype = ctypes.c_int
 
     # -- geometry ------------------------------------------------------------
@@ -256,6 +277,46 @@ class Oracle:
 
     def solve_immittance(self, wg_flat, ie, m: int, n: int) -> int:
         return self._fn("solve_immittance")(_ptr(wg_flat), _ptr(ie), m, n)
+
+    # -- nodal admittance formulation -------------------------------------------
+    def fill_incidence_adm(self, a_flat, b_flat, elec, nodes) -> int:
+        e = np.ascontiguousarray(elec, dtype=float)
+        nd = np.ascontiguousarray(nodes, dtype=float)
+        return self._fn("fill_incidence_adm")(_ptr(a_flat), _ptr(b_flat), _ptr(e), e.shape[0], _ptr(nd),
+                                              nd.shape[0])
+
+    def calculate_yla_ytb(self, yla, ytb, zl, zt, a, b, m: int, n: int) -> int:
+        return self._fn("calculate_yla_ytb")(_ptr(yla), _ptr(ytb), _ptr(zl), _ptr(zt), _ptr(a), _ptr(b), m, n)
+
+    def fill_impedance_adm2(self, yn, yla, ytb, a, b, m: int, n: int) -> int:
+        return self._fn("fill_impedance_adm2")(_ptr(yn), _ptr(yla), _ptr(ytb), _ptr(a), _ptr(b), m, n)
+
+    def fill_impedance_adm(self, yn, zl, zt, a, b, m: int, n: int) -> int:
+        return self._fn("fill_impedance_adm")(_ptr(yn), _ptr(zl), _ptr(zt), _ptr(a), _ptr(b), m, n)
+
+    def solve_admittance(self, yn, ic, n: int) -> int:
+        return self._fn("solve_admittance")(_ptr(yn), _ptr(ic), n)
+
+    def mhem_sweep(self, elec, img, nodes, s, kappa, inj_node, inj, mur=1.0, max_eval=0, req_abs=1e-6,
+                   req_rel=1e-6, threads=0):
+        """Node potentials (ns x n) of the mHEM + nodal-admittance sample loop and the zsysv infos."""
+        if self.kind != "port":
+            raise NotImplementedError("the sweep driver is part of the restatement")
+        e = np.ascontiguousarray(elec, dtype=float)
+        im = np.ascontiguousarray(img, dtype=float)
+        nd = np.ascontiguousarray(nodes, dtype=float)
+        s = np.ascontiguousarray(s, dtype=np.complex128)
+        kappa = np.ascontiguousarray(np.broadcast_to(kappa, s.shape), dtype=np.complex128)
+        inj = np.ascontiguousarray(np.broadcast_to(inj, s.shape), dtype=np.complex128)
+        m, n, ns = e.shape[0], nd.shape[0], s.shape[0]
+        sol = np.zeros((ns, n), dtype=np.complex128)
+        info = np.zeros(ns, dtype=np.int32)
+        err = self.lib.oracle_mhem_sweep(_ptr(e), _ptr(im), m, _ptr(nd), n, _ptr(s), _ptr(kappa), ns, mur,
+                                         inj_node, _ptr(inj), max_eval, req_abs, req_rel, threads, _ptr(sol),
+                                         info.ctypes.data_as(_ip))
+        if err:
+            raise RuntimeError(f"mhem_sweep set-up failed: {err}")
+        return sol, info
 
     # -- Laplace pair --------------------------------------------------------
     def laplace_trans(self, f, tmax: float):

@@ -450,6 +450,133 @@ int oracle_solve_immittance (double _Complex *wg, double _Complex *ie, size_t m,
     return info;
 }
 
+/* ---- nodal admittance formulation (mHEM examples) -------------------------- */
+
+void tags_zsytrf_ (char *uplo, int *n, double _Complex *a, int *lda, int *ipiv, double _Complex *work,
+                   int *lwork, int *info);
+void tags_zsytri_ (char *uplo, int *n, double _Complex *a, int *lda, int *ipiv, double _Complex *work,
+                   int *info);
+void tags_zsymm_ (char *side, char *uplo, int *m, int *n, double _Complex *alpha, double _Complex *a, int *lda,
+                  double _Complex *b, int *ldb, double _Complex *beta, double _Complex *c, int *ldc);
+void tags_zgemm_ (char *ta, char *tb, int *m, int *n, int *k, double _Complex *alpha, double _Complex *a,
+                  int *lda, double _Complex *b, int *ldb, double _Complex *beta, double _Complex *c, int *ldc);
+
+/* src/linalg.c:142-204: A (+1 start, -1 end) and B (0.5) as dense m x n
+ * column-major arrays (element (k, node) at k + m * node), the same node
+ * matching and checksums as the immittance version. */
+int oracle_fill_incidence_adm (double _Complex *a, double _Complex *b, const OracleElectrode *e, size_t m,
+                               const double *nodes, size_t n)
+{
+    const double tol = 1e-5;
+    long int suma = 0;
+    double sumb = 0.0;
+    for (size_t nd = 0; nd < n; nd++) {
+        bool none = true;
+        for (size_t k = 0; k < m; k++) {
+            int cond = 0;
+            if (equal_points_tol(e[k].start_point, nodes + nd * 3, tol)) cond = 1;
+            else if (equal_points_tol(e[k].end_point, nodes + nd * 3, tol)) cond = 2;
+            size_t pos = m * nd + k;
+            /* the reference's write order: b before a at a match, so that
+             * a == b (documented in src/linalg.h:90) leaves A */
+            if (cond == 1) { b[pos] = 0.5; a[pos] = 1.0; }
+            else if (cond == 2) { b[pos] = 0.5; a[pos] = -1.0; }
+            else { a[pos] = 0.0; b[pos] = 0.0; }
+            if (cond) none = false;
+            suma += (long int) creal(a[pos]);
+            sumb += creal(b[pos]);
+        }
+        if (none) return 1;
+    }
+    if (suma != 0) return (int) -suma;
+    if (sumb != (double) m) return (int) (sumb - (double) m);
+    return 0;
+}
+
+/* inv(Z) in place (lower triangle) by zsytrf + zsytri with the queried
+ * workspace, as src/linalg.c:226-237 and :278-289. */
+static int sym_inverse (double _Complex *z, int ne, int *ipiv)
+{
+    char uplo = 'L';
+    int lwork = -1, info = 0;
+    double _Complex q;
+    tags_zsytrf_(&uplo, &ne, z, &ne, ipiv, &q, &lwork, &info);
+    if (info != 0) return info;
+    lwork = (int) creal(q);
+    if (lwork < 1) lwork = 1;
+    double _Complex *work = malloc(lwork * sizeof(double _Complex));
+    if (!work) return -1000;
+    tags_zsytrf_(&uplo, &ne, z, &ne, ipiv, work, &lwork, &info);
+    if (info == 0) tags_zsytri_(&uplo, &ne, z, &ne, ipiv, work, &info);
+    free(work);
+    return info;
+}
+
+/* src/linalg.c:261-300: yla = inv(ZL) A, ytb = inv(ZT) B (zsymm on the lower
+ * triangles); ZL and ZT are overwritten by their inverses. */
+int oracle_calculate_yla_ytb (double _Complex *yla, double _Complex *ytb, double _Complex *zl,
+                              double _Complex *zt, double _Complex *a, double _Complex *b, size_t m, size_t n)
+{
+    int ne = (int) m, nn = (int) n;
+    int *ipiv = malloc((m > 0 ? m : 1) * sizeof(int));
+    if (!ipiv) return -1000;
+    int info = sym_inverse(zl, ne, ipiv);
+    if (info == 0) info = sym_inverse(zt, ne, ipiv);
+    if (info == 0) {
+        char side = 'L', uplo = 'L';
+        double _Complex one = 1.0, zero = 0.0;
+        tags_zsymm_(&side, &uplo, &ne, &nn, &one, zl, &ne, a, &ne, &zero, yla, &ne);
+        tags_zsymm_(&side, &uplo, &ne, &nn, &one, zt, &ne, b, &ne, &zero, ytb, &ne);
+    }
+    free(ipiv);
+    return info;
+}
+
+/* src/linalg.c:302-325: yn = A^T yla + B^T ytb (n x n). */
+int oracle_fill_impedance_adm2 (double _Complex *yn, double _Complex *yla, double _Complex *ytb,
+                                double _Complex *a, double _Complex *b, size_t m, size_t n)
+{
+    int ne = (int) m, nn = (int) n;
+    char notrans = 'N', trans = 'T';
+    double _Complex one = 1.0, zero = 0.0;
+    tags_zgemm_(&trans, &notrans, &nn, &nn, &ne, &one, a, &ne, yla, &ne, &zero, yn, &nn);
+    tags_zgemm_(&trans, &notrans, &nn, &nn, &ne, &one, b, &ne, ytb, &ne, &one, yn, &nn);
+    return 0;
+}
+
+/* src/linalg.c:206-259: yn = A^T inv(ZL) A + B^T inv(ZT) B in one call. */
+int oracle_fill_impedance_adm (double _Complex *yn, double _Complex *zl, double _Complex *zt,
+                               double _Complex *a, double _Complex *b, size_t m, size_t n)
+{
+    double _Complex *c1 = malloc((m * n > 0 ? m * n : 1) * sizeof(double _Complex));
+    double _Complex *c2 = malloc((m * n > 0 ? m * n : 1) * sizeof(double _Complex));
+    if (!c1 || !c2) { free(c1); free(c2); return -1000; }
+    int info = oracle_calculate_yla_ytb(c1, c2, zl, zt, a, b, m, n);
+    if (info == 0) oracle_fill_impedance_adm2(yn, c1, c2, a, b, m, n);
+    free(c1);
+    free(c2);
+    return info;
+}
+
+/* src/linalg.c:327-350: zsysv('L') on YN with the queried workspace. */
+int oracle_solve_admittance (double _Complex *yn, double _Complex *ic, size_t n)
+{
+    int nn = (int) n, nrhs = 1, info = 0, lwork = -1;
+    char uplo = 'L';
+    int *ipiv = malloc((n > 0 ? n : 1) * sizeof(int));
+    double _Complex q;
+    if (!ipiv) return -1000;
+    tags_zsysv_(&uplo, &nn, &nrhs, yn, &nn, ipiv, ic, &nn, &q, &lwork, &info);
+    lwork = (int) creal(q);
+    if (lwork < 1) lwork = 1;
+    double _Complex *work = malloc(lwork * sizeof(double _Complex));
+    if (!work) { free(ipiv); return -1000; }
+    tags_zsysv_(&uplo, &nn, &nrhs, yn, &nn, ipiv, ic, &nn, work, &lwork, &info);
+    free(work);
+    free(ipiv);
+    return info;
+}
+
 /* ---- numerical Laplace transform ----------------------------------------- */
 
 /* src/auxiliary.c:239-263: s_k = c + j k dw with c = ln(nt^2)/tmax,
@@ -543,6 +670,104 @@ int oracle_hem_impedances (const OracleElectrode *e, const OracleElectrode *img,
         err = oracle_impedances_images(zl, zt, e, img, m, gamma, s, mur, kappa, 1.0, ref_t,
                                        max_eval, req_abs, req_rel, type);
     return err;
+}
+
+/* mHEM per-sample impedances, examples/three_grids.c:335-350: the static
+ * potentials (INTG_MHEM integrals, computed once) times e^{-gamma rbar} of
+ * the segments' midpoint distance, images with ref_l = 1 and ref_t, scaled by
+ * s mur MU0 / (4 pi) and 1 / (4 pi kappa); lower triangle (k >= i) written. */
+int oracle_mhem_impedances (const OracleElectrode *e, const OracleElectrode *img, size_t m,
+                            const double _Complex *potzl, const double _Complex *potzt,
+                            const double _Complex *potzli, const double _Complex *potzti,
+                            double _Complex s, double _Complex kappa, double mur,
+                            double _Complex *zl, double _Complex *zt)
+{
+    double _Complex gamma, ref_t;
+    medium(s, kappa, mur, &gamma, &ref_t);
+    const double _Complex ref_l = 1.0;
+    const double _Complex iwu_4pi = s * mur * ORACLE_MU0 / ORACLE_FOUR_PI;
+    const double _Complex one_4pik = 1.0 / (ORACLE_FOUR_PI * kappa);
+    for (size_t i = 0; i < m; i++) {
+        for (size_t k = i; k < m; k++) {
+            double rbar = oracle_vector_length(e[k].middle_point, e[i].middle_point);
+            double _Complex exp_gr = cexp(-gamma * rbar);
+            zl[i * m + k] = exp_gr * potzl[i * m + k];
+            zt[i * m + k] = exp_gr * potzt[i * m + k];
+            rbar = oracle_vector_length(e[k].middle_point, img[i].middle_point);
+            exp_gr = cexp(-gamma * rbar);
+            zl[i * m + k] += ref_l * exp_gr * potzli[i * m + k];
+            zt[i * m + k] += ref_t * exp_gr * potzti[i * m + k];
+            zl[i * m + k] *= iwu_4pi;
+            zt[i * m + k] *= one_4pik;
+        }
+    }
+    return 0;
+}
+
+/* The mHEM + nodal-admittance sample loop of examples/three_grids.c:270-392:
+ * incidence and static potentials once, then per sample the mHEM rescale,
+ * yla/ytb, YN and zsysv; sol (ns x n) receives the node potentials for the
+ * injection inj[k] at inj_node. */
+int oracle_mhem_sweep (const OracleElectrode *e, const OracleElectrode *img, size_t m, const double *nodes,
+                       size_t n, const double _Complex *s, const double _Complex *kappa, size_t ns, double mur,
+                       size_t inj_node, const double _Complex *inj, size_t max_eval, double req_abs,
+                       double req_rel, int threads, double _Complex *sol, int *info)
+{
+    double _Complex *a = calloc(m * n, sizeof(double _Complex));
+    double _Complex *b = calloc(m * n, sizeof(double _Complex));
+    double _Complex *pl = calloc(m * m, sizeof(double _Complex));
+    double _Complex *pt = calloc(m * m, sizeof(double _Complex));
+    double _Complex *pli = calloc(m * m, sizeof(double _Complex));
+    double _Complex *pti = calloc(m * m, sizeof(double _Complex));
+    int err = (!a || !b || !pl || !pt || !pli || !pti) ? -1000 : 0;
+    if (!err) err = oracle_fill_incidence_adm(a, b, e, m, nodes, n);
+    if (!err) err = oracle_calculate_impedances(pl, pt, e, m, 0.0, 0.0, 0.0, 0.0, max_eval, req_abs, req_rel,
+                                                ORACLE_INTG_MHEM);
+    if (!err) err = oracle_impedances_images(pli, pti, e, img, m, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, max_eval,
+                                             req_abs, req_rel, ORACLE_INTG_MHEM);
+    int setup_err = err;
+    if (!err) {
+#ifdef _OPENMP
+        int nthr = threads > 0 ? threads : omp_get_max_threads();
+#pragma omp parallel num_threads(nthr)
+#else
+        (void) threads;
+#endif
+        {
+            double _Complex *zl = calloc(m * m, sizeof(double _Complex));
+            double _Complex *zt = calloc(m * m, sizeof(double _Complex));
+            double _Complex *yla = malloc(m * n * sizeof(double _Complex));
+            double _Complex *ytb = malloc(m * n * sizeof(double _Complex));
+            double _Complex *yn = malloc(n * n * sizeof(double _Complex));
+            bool ok = zl && zt && yla && ytb && yn;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 1)
+#endif
+            for (size_t k = 0; k < ns; k++) {
+                if (!ok) { info[k] = -1000; continue; }
+                oracle_mhem_impedances(e, img, m, pl, pt, pli, pti, s[k], kappa[k], mur, zl, zt);
+                int ierr = oracle_calculate_yla_ytb(yla, ytb, zl, zt, a, b, m, n);
+                if (ierr) { info[k] = ierr; continue; }
+                oracle_fill_impedance_adm2(yn, yla, ytb, a, b, m, n);
+                double _Complex *x = sol + k * n;
+                for (size_t q = 0; q < n; q++) x[q] = 0.0;
+                x[inj_node] = inj[k];
+                info[k] = oracle_solve_admittance(yn, x, n);
+            }
+            free(zl);
+            free(zt);
+            free(yla);
+            free(ytb);
+            free(yn);
+        }
+    }
+    free(a);
+    free(b);
+    free(pl);
+    free(pt);
+    free(pli);
+    free(pti);
+    return setup_err;
 }
 
 int oracle_hem_sweep (const OracleElectrode *e, const OracleElectrode *img, size_t m,

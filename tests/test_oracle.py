@@ -174,6 +174,104 @@ def test_port_sweep_matches_reference_calls(pkg, port, ref, orc_mod):
         assert np.array_equal(ie, sol[k])
 
 
+def _mhem_potentials(lib, e, img):
+    m = e.shape[0]
+    pot = [np.zeros(m * m, dtype=np.complex128) for _ in range(4)]
+    assert lib.calculate_impedances(pot[0], pot[1], e, 0.0, 0.0, 0.0, 0.0, itype=4) == 0
+    assert lib.impedances_images(pot[2], pot[3], e, img, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, itype=4) == 0
+    return pot
+
+
+def test_port_equals_reference_admittance(pkg, port, ref, orc_mod):
+    """Nodal admittance formulation (src/linalg.c:142-350): incidence, yla /
+    ytb (inverses overwrite ZL, ZT), YN in one and in two calls, zsysv on YN;
+    restatement and reference agree bit for bit."""
+    O = orc_mod
+    e, nd = _grid_geom(pkg)
+    m, n = e.shape[0], nd.shape[0]
+    img = O.images(e)
+    s = 2e5 + 2j * np.pi * 1e6
+    kappa = 0.01 + s * 10 * O.EPS0
+    zl, zt = ref.hem_impedances(e, img, s, kappa)
+    zlf = np.ascontiguousarray(zl.T).reshape(-1)
+    ztf = np.ascontiguousarray(zt.T).reshape(-1)
+    out = []
+    for lib in (port, ref):
+        a = np.zeros(m * n, dtype=np.complex128)
+        b = np.zeros(m * n, dtype=np.complex128)
+        assert lib.fill_incidence_adm(a, b, e, nd) == 0
+        zl1, zt1 = zlf.copy(), ztf.copy()
+        yla = np.zeros(m * n, dtype=np.complex128)
+        ytb = np.zeros(m * n, dtype=np.complex128)
+        assert lib.calculate_yla_ytb(yla, ytb, zl1, zt1, a, b, m, n) == 0
+        yn2 = np.zeros(n * n, dtype=np.complex128)
+        lib.fill_impedance_adm2(yn2, yla, ytb, a, b, m, n)
+        yn1 = np.zeros(n * n, dtype=np.complex128)
+        assert lib.fill_impedance_adm(yn1, zlf.copy(), ztf.copy(), a, b, m, n) == 0
+        ic = np.zeros(n, dtype=np.complex128)
+        ic[0] = 1.0
+        assert lib.solve_admittance(yn1.copy(), ic, n) == 0
+        out.append((a, b, zl1, zt1, yla, ytb, yn2, yn1, ic))
+    for x, y in zip(out[0], out[1]):
+        assert np.array_equal(x, y)
+    # the admittance potentials are the immittance ones (YN is W_G's node Schur complement)
+    N = n + 2 * m
+    wg = np.zeros(N * N, dtype=np.complex128)
+    ref.fill_incidence_imm(wg, e, nd)
+    ref.fill_impedance_imm(wg, zlf, ztf, m, n)
+    ie = np.zeros(N, dtype=np.complex128)
+    ie[0] = 1.0
+    ref.solve_immittance(wg, ie, m, n)
+    assert np.max(np.abs(out[0][8] - ie[:n])) < 1e-10 * np.max(np.abs(ie[:n]))
+
+
+def test_mhem_sweep_follows_the_example_loop(pkg, port, ref, orc_mod):
+    """The mHEM sample loop (examples/three_grids.c:270-392): per-sample
+    impedances from the static potentials (numpy restatement of the loop's
+    rescale), then the reference's yla/ytb, YN and zsysv; the restated sweep
+    gives the same node potentials bit for bit."""
+    O = orc_mod
+    e, nd = _grid_geom(pkg)
+    m, n = e.shape[0], nd.shape[0]
+    img = O.images(e)
+    s = np.array([3e4 + 2j * np.pi * 1e3, 3e4 + 2j * np.pi * 2e6])
+    kappa = 0.01 + s * 10 * O.EPS0
+    inj = np.array([1.0 + 0.5j, 2.0])
+    sol, info = port.mhem_sweep(e, img, nd, s, kappa, 3, inj, threads=2)
+    assert np.all(info == 0)
+    pl, pt, pli, pti = (np.ascontiguousarray(x) for x in _mhem_potentials(ref, e, img))
+    a = np.zeros(m * n, dtype=np.complex128)
+    b = np.zeros(m * n, dtype=np.complex128)
+    ref.fill_incidence_adm(a, b, e, nd)
+    for k in range(2):
+        gamma, ref_t = O.medium(s[k], kappa[k])
+        iwu = s[k] * O.MU0 / (4 * np.pi)
+        one_4pik = 1.0 / (4 * np.pi * kappa[k])
+        zl = np.zeros(m * m, dtype=np.complex128)
+        zt = np.zeros(m * m, dtype=np.complex128)
+        for i in range(m):
+            for j in range(i, m):
+                rb = np.linalg.norm(e[j, 6:9] - e[i, 6:9])
+                eg = np.exp(-gamma * rb)
+                zl[i * m + j] = eg * pl[i * m + j]
+                zt[i * m + j] = eg * pt[i * m + j]
+                rb = np.linalg.norm(e[j, 6:9] - img[i, 6:9])
+                eg = np.exp(-gamma * rb)
+                zl[i * m + j] += 1.0 * eg * pli[i * m + j]
+                zt[i * m + j] += ref_t * eg * pti[i * m + j]
+                zl[i * m + j] *= iwu
+                zt[i * m + j] *= one_4pik
+        yla = np.zeros(m * n, dtype=np.complex128)
+        ytb = np.zeros(m * n, dtype=np.complex128)
+        assert ref.calculate_yla_ytb(yla, ytb, zl, zt, a.copy(), b.copy(), m, n) == 0
+        yn = np.zeros(n * n, dtype=np.complex128)
+        ref.fill_impedance_adm2(yn, yla, ytb, a.copy(), b.copy(), m, n)
+        ic = np.zeros(n, dtype=np.complex128)
+        ic[3] = inj[k]
+        assert ref.solve_admittance(yn, ic, n) == 0
+        assert np.max(np.abs(ic - sol[k])) <= 1e-12 * np.max(np.abs(ic))
+
+
 # ---- golden fixtures (made by the reference) against the restatement ----------------
 
 def test_golden_rod_zf(port, orc_mod):

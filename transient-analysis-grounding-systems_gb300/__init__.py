@@ -53,8 +53,9 @@ EPS0 = 8.854187817620e-12
 # C-ABI symbols declared in include/tags_gpu.h
 EXPORTS = (
     "calculate_impedances", "impedances_images", "fill_incidence_imm", "fill_impedance_imm",
-    "solve_immittance", "laplace_trans", "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
-    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "solve_immittance", "fill_incidence_adm", "fill_impedance_adm", "calculate_yla_ytb", "fill_impedance_adm2",
+    "solve_admittance", "laplace_trans", "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
+    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_gpu_set_quiet",
 )
 
@@ -112,6 +113,11 @@ def lib() -> ctypes.CDLL:
             L.fill_incidence_imm.argtypes = [_vp, _vp, _sz, _vp, _sz]
             L.fill_impedance_imm.argtypes = [_vp, _vp, _vp, _sz, _sz]
             L.solve_immittance.argtypes = [_vp, _vp, _sz, _sz]
+            L.fill_incidence_adm.argtypes = [_vp, _vp, _vp, _sz, _vp, _sz]
+            L.fill_impedance_adm.argtypes = [_vp, _vp, _vp, _vp, _vp, _sz, _sz]
+            L.calculate_yla_ytb.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _sz]
+            L.fill_impedance_adm2.argtypes = [_vp, _vp, _vp, _vp, _vp, _sz, _sz]
+            L.solve_admittance.argtypes = [_vp, _vp, _sz]
             L.laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz]
             L.inv_laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, ctypes.c_int]
             L.tags_plan_create.argtypes = [ctypes.POINTER(_vp), _vp, _vp, _sz, _vp, _sz, ctypes.c_int, _sz]
@@ -120,15 +126,18 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_destroy.argtypes = [_vp]
             L.tags_plan_set_graphs.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_set_fill.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_tune.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int,
                                          ctypes.POINTER(TuneResult)]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
             for name in ("calculate_impedances", "impedances_images", "fill_incidence_imm",
-                         "fill_impedance_imm", "solve_immittance", "laplace_trans", "inv_laplace_trans",
+                         "fill_impedance_imm", "solve_immittance", "fill_incidence_adm", "fill_impedance_adm",
+                         "calculate_yla_ytb", "fill_impedance_adm2", "solve_admittance", "laplace_trans",
+                         "inv_laplace_trans",
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
-                         "tags_plan_set_split", "tags_plan_tune"):
+                         "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -361,6 +370,48 @@ def solve_immittance(wg, ie, num_electrodes: int, num_nodes: int) -> int:
     return _ret(lib().solve_immittance(_addr(wg), _addr(ie), m, n))
 
 
+# nodal admittance formulation (src/linalg.c:142-350), used by the reference's mHEM examples
+
+def fill_incidence_adm(a, b, electrodes, nodes) -> int:
+    """A and B (m x n column-major, flat complex128); a may be b (then A)."""
+    e = _elec(electrodes)
+    nd = np.ascontiguousarray(nodes, dtype=np.float64)
+    _check_c128(a, "a", e.shape[0] * nd.shape[0])
+    _check_c128(b, "b", e.shape[0] * nd.shape[0])
+    return _ret(lib().fill_incidence_adm(_addr(a), _addr(b), _addr(e), e.shape[0], _addr(nd), nd.shape[0]))
+
+
+def calculate_yla_ytb(yla, ytb, zl, zt, a, b, num_electrodes: int, num_nodes: int) -> int:
+    m, n = int(num_electrodes), int(num_nodes)
+    for arr, name, size in ((yla, "yla", m * n), (ytb, "ytb", m * n), (zl, "zl", m * m), (zt, "zt", m * m),
+                            (a, "a", m * n), (b, "b", m * n)):
+        _check_c128(arr, name, size)
+    return _ret(lib().calculate_yla_ytb(_addr(yla), _addr(ytb), _addr(zl), _addr(zt), _addr(a), _addr(b), m, n))
+
+
+def fill_impedance_adm2(yn, yla, ytb, a, b, num_electrodes: int, num_nodes: int) -> int:
+    m, n = int(num_electrodes), int(num_nodes)
+    for arr, name, size in ((yn, "yn", n * n), (yla, "yla", m * n), (ytb, "ytb", m * n), (a, "a", m * n),
+                            (b, "b", m * n)):
+        _check_c128(arr, name, size)
+    return _ret(lib().fill_impedance_adm2(_addr(yn), _addr(yla), _addr(ytb), _addr(a), _addr(b), m, n))
+
+
+def fill_impedance_adm(yn, zl, zt, a, b, num_electrodes: int, num_nodes: int) -> int:
+    m, n = int(num_electrodes), int(num_nodes)
+    for arr, name, size in ((yn, "yn", n * n), (zl, "zl", m * m), (zt, "zt", m * m), (a, "a", m * n),
+                            (b, "b", m * n)):
+        _check_c128(arr, name, size)
+    return _ret(lib().fill_impedance_adm(_addr(yn), _addr(zl), _addr(zt), _addr(a), _addr(b), m, n))
+
+
+def solve_admittance(yn, ic, num_nodes: int) -> int:
+    n = int(num_nodes)
+    _check_c128(yn, "yn", n * n)
+    _check_c128(ic, "ic", n)
+    return _ret(lib().solve_admittance(_addr(yn), _addr(ic), n))
+
+
 def laplace_trans(f, tmax: float):
     """Returns (g, s) like the reference's laplace_trans."""
     f = np.ascontiguousarray(f, dtype=np.float64)
@@ -420,6 +471,13 @@ class Plan:
             raise RuntimeError(f"tags_plan_tune failed ({code}): {last_error()}")
         return res
 
+    def set_fill(self, integration_type):
+        """Impedance model: INTG_DOUBLE (double line integrals) or INTG_MHEM
+        (static potentials rescaled per sample, as the reference's mHEM examples)."""
+        code = lib().tags_plan_set_fill(self.handle, int(integration_type))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_set_fill failed ({code}): {last_error()}")
+
     def set_graphs(self, enable):
         """Run each pass as one CUDA-graph launch (True) or kernel by kernel."""
         code = lib().tags_plan_set_graphs(self.handle, 1 if enable else 0)
@@ -466,13 +524,16 @@ class Plan:
 
 
 def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, precision=PLAIN_FP64,
-              max_batch=0, graphs=True, split=None):
-    """Solutions [U; I_L; I_T] for every Laplace sample (one plan, one run)."""
+              max_batch=0, graphs=True, split=None, fill=None):
+    """Solutions [U; I_L; I_T] for every Laplace sample (one plan, one run);
+    fill = INTG_MHEM selects the mHEM impedance model."""
     if not max_batch:
         max_batch = min(len(np.atleast_1d(s)), 64)
     plan = Plan(electrodes, imgs, nodes, precision, max_batch, graphs)
     if split is not None:
         plan.set_split(split)
+    if fill is not None:
+        plan.set_fill(fill)
     try:
         return plan.run(s, kappa, mur, ie, inj_node)
     finally:

@@ -43,6 +43,10 @@ bool quiet() {
 
 void tags_note_launch(long long n) { g_launches += n; }
 
+// drop-ins in other translation units share the scratch slots, so they
+// serialise on the same lock
+std::mutex& tags_dropin_mutex() { return g_mutex; }
+
 int tags_fail_cuda(cudaError_t e, const char* what, const char* file, int line) {
     char buf[512];
     snprintf(buf, sizeof(buf), "CUDA error %s (%s) at %s:%d in %s", cudaGetErrorName(e), cudaGetErrorString(e), file,

@@ -830,6 +830,152 @@ int tags_mixed_touch_count(void* ws, int m, cudaStream_t st, int* out) {
     return 0;
 }
 
+// ---- mHEM: per-sample rescale of static potentials ----------------------------
+//
+// The reference's mHEM examples (examples/three_grids.c:335-350) fill ZL/ZT
+// per sample from static potentials computed once (INTG_MHEM integrals,
+// direct and image) times e^{-gamma rbar} of the segments' midpoint distance:
+//   ZL = iwu (e^{-gamma r} PL + ref_l e^{-gamma r'} PLi),
+//   ZT = 1/(4 pi kappa) (e^{-gamma r} PT + ref_t e^{-gamma r'} PTi),
+// r' the distance to the image; the coefficients come as cL = iwu, cLi =
+// ref_l iwu, cT, cTi. pot holds PL, PT, PLi, PTi (lower triangles, element
+// (k, i) at k + m i).
+
+TAGS_D double mid_dist(const double* a, const double* b) {
+    const double dx = a[6] - b[6], dy = a[7] - b[7], dz = a[8] - b[8];
+    return sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+__global__ void k_mhem_fp64(const double* __restrict__ elec, const double* __restrict__ img, int m,
+                            const double2* __restrict__ pot, const SampleCoef* __restrict__ coef, int nsamp,
+                            FillOut out, int has_img, int* status) {
+    const long long npairs = (long long)m * (m + 1) / 2;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int smp = blockIdx.y;
+    if (p >= npairs || smp >= nsamp) return;
+    int i, k;
+    pair_index(p, m, i, k);
+    const SampleCoef c = coef[smp];
+    const long long mm = (long long)m * m, e = k + (long long)m * i;
+    const double2 ng = make_double2(-c.gamma.x, -c.gamma.y);
+    const double2 e1 = cexp_d(cscale(ng, mid_dist(elec + 11LL * k, elec + 11LL * i)));
+    double2 zl = cmul(cmul(e1, pot[e]), c.cL);
+    double2 zt = cmul(cmul(e1, pot[mm + e]), c.cT);
+    if (has_img) {
+        const double2 e2 = cexp_d(cscale(ng, mid_dist(elec + 11LL * k, img + 11LL * i)));
+        zl = cadd(zl, cmul(cmul(e2, pot[2 * mm + e]), c.cLi));
+        zt = cadd(zt, cmul(cmul(e2, pot[3 * mm + e]), c.cTi));
+    }
+    if (!isfinite(zl.x + zl.y + zt.x + zt.y)) raise_status(status, TAGS_ST_NONFINITE);
+    zl = cscale(zl, out.sign);
+    zt = cscale(zt, out.sign);
+    const long long bs = out.batch_stride * smp;
+    store(out.zl + bs, (long long)(out.row0_l + k) + out.ld * (out.col0_l + i), zl, out.accumulate != 0);
+    store(out.zt + bs, (long long)(out.row0_t + k) + out.ld * (out.col0_t + i), zt, out.accumulate != 0);
+    if (out.mirror && k != i) {
+        store(out.zl + bs, (long long)(out.row0_l + i) + out.ld * (out.col0_l + k), zl, out.accumulate != 0);
+        store(out.zt + bs, (long long)(out.row0_t + i) + out.ld * (out.col0_t + k), zt, out.accumulate != 0);
+    }
+}
+
+// Mixed form: the exponentials from the pair plan's two-float midpoint
+// distances (anchor_df, exact range reduction), products in FP32; ZL at zl,
+// ZT at zt (complex FP32, both triangles). A thread per (pair, sample group).
+__global__ void __launch_bounds__(128) k_mhem_mixed(int m, const double2* __restrict__ pot,
+                                                    const PairRec* __restrict__ recs,
+                                                    const SampleF32* __restrict__ coef, int nsamp, float2* zl0,
+                                                    float2* zt0, long long bstride, int has_img, int* status) {
+    const long long npairs = (long long)m * (m + 1) / 2;
+    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int s0 = blockIdx.y * MIX_SG;
+    if (p >= npairs || s0 >= nsamp) return;
+    int i, k;
+    pair_index(p, m, i, k);
+    const long long mm = (long long)m * m, e = k + (long long)m * i;
+    const double2 pl = pot[e], pt = pot[mm + e];
+    const float2 PL = make_float2((float)pl.x, (float)pl.y), PT = make_float2((float)pt.x, (float)pt.y);
+    float2 PLi = make_float2(0.f, 0.f), PTi = make_float2(0.f, 0.f);
+    if (has_img) {
+        const double2 pli = pot[2 * mm + e], pti = pot[3 * mm + e];
+        PLi = make_float2((float)pli.x, (float)pli.y);
+        PTi = make_float2((float)pti.x, (float)pti.y);
+    }
+    const PairRec r1 = recs[2 * p], r2 = recs[2 * p + 1];     // r1 has r = 0 on the diagonal
+#pragma unroll
+    for (int q = 0; q < MIX_SG; ++q) {
+        if (s0 + q >= nsamp) break;
+        const SampleF32 c = coef[s0 + q];
+        const float2 a1 = anchor_df(c.grh, c.grl, c.gih, c.gil, k == i ? 0.f : r1.rch, k == i ? 0.f : r1.rcl);
+        float2 zl = fmulc(fmulc(a1, PL), c.cL), zt = fmulc(fmulc(a1, PT), c.cT);
+        if (has_img) {
+            const float2 a2 = anchor_df(c.grh, c.grl, c.gih, c.gil, r2.rch, r2.rcl);
+            zl = ffmac(fmulc(a2, PLi), c.cLi, zl);
+            zt = ffmac(fmulc(a2, PTi), c.cTi, zt);
+        }
+        if (!isfinite(zl.x + zl.y + zt.x + zt.y)) raise_status(status, TAGS_ST_NONFINITE);
+        const long long bs = bstride * (s0 + q);
+        zl0[bs + k + (long long)m * i] = zl;
+        zt0[bs + k + (long long)m * i] = zt;
+        if (k != i) {
+            zl0[bs + i + (long long)m * k] = zl;
+            zt0[bs + i + (long long)m * k] = zt;
+        }
+    }
+}
+
+// Static potentials of the mHEM fill (once per geometry): direct into pot[0..1],
+// images into pot[2..3], lower triangles.
+int tags_launch_mhem_potentials(const double* d_elec, const double* d_img, int m, int has_img, double2* d_pot,
+                                SampleCoef* d_coef1, int* d_status, cudaStream_t st) {
+    const long long mm = (long long)m * m;
+    TAGS_CUDA_OK(cudaMemsetAsync(d_pot, 0, sizeof(double2) * 4 * mm, st));
+    SampleCoef one{};          // scale factors are 1 for INTG_MHEM; gamma unused
+    TAGS_CUDA_OK(cudaMemcpyAsync(d_coef1, &one, sizeof(one), cudaMemcpyHostToDevice, st));
+    FillOut out{};
+    out.zl = d_pot;
+    out.zt = d_pot + mm;
+    out.ld = m;
+    out.sign = 1.0;
+    int err = tags_launch_fill_fp64(d_elec, d_img, m, d_coef1, 1, out, TAGS_FILL_DIRECT, TAGS_INTG_MHEM, 1, d_status, st);
+    if (!err && has_img) {
+        out.zl = d_pot + 2 * mm;
+        out.zt = d_pot + 3 * mm;
+        err = tags_launch_fill_fp64(d_elec, d_img, m, d_coef1, 1, out, TAGS_FILL_IMAGE, TAGS_INTG_MHEM, 1, d_status,
+                                    st);
+    }
+    return err;
+}
+
+int tags_launch_mhem_fp64(const double* d_elec, const double* d_img, int m, int has_img, const double2* d_pot,
+                          const SampleCoef* d_coef, int nsamp, const FillOut& out, int* d_status, cudaStream_t st) {
+    if (m <= 0 || nsamp <= 0) return 0;
+    const long long npairs = (long long)m * (m + 1) / 2;
+    int pf = tags_prof_begin(TAGS_PROF_FILL_FP64, st);
+    k_mhem_fp64<<<dim3((unsigned)((npairs + 127) / 128), (unsigned)nsamp), 128, 0, st>>>(d_elec, d_img, m, d_pot,
+                                                                                       d_coef, nsamp, out, has_img,
+                                                                                       d_status);
+    tags_prof_end(TAGS_PROF_FILL_FP64, pf, st, 0.0, 0.0);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+int tags_launch_mhem_mixed(int m, int has_img, const double2* d_pot, void* ws, const SampleCoef* d_coef, int nsamp,
+                           float2* d_zl, float2* d_zt, long long bstride, int* d_status, cudaStream_t st) {
+    if (m <= 0 || nsamp <= 0) return 0;
+    if (nsamp > 4096) return tags_fail_cuda(cudaErrorInvalidValue, "mhem_mixed: batch above 4096", __FILE__, __LINE__);
+    MixedFillWs w = carve(ws, m);
+    const long long npairs = (long long)m * (m + 1) / 2;
+    int pf = tags_prof_begin(TAGS_PROF_FILL_MIXED, st);
+    k_coef32<<<(nsamp + 127) / 128, 128, 0, st>>>(d_coef, nsamp, w.c32);
+    k_mhem_mixed<<<dim3((unsigned)((npairs + 127) / 128), (unsigned)((nsamp + MIX_SG - 1) / MIX_SG)), 128, 0, st>>>(
+        m, d_pot, w.recs, w.c32, nsamp, d_zl, d_zt, bstride, has_img, d_status);
+    tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
+    tags_note_launch(2);
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
 int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, const SampleCoef* d_coef,
                           int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
                           cudaStream_t st) {

@@ -356,9 +356,10 @@ int lu_impl(T* A, int n, long long ld, long long stride, int batch, int pivot, i
         tags_note_launch();
         if (pivot) {
             int ncols = n - jb;
-            if (ncols > 0)
+            if (ncols > 0) {
                 k_laswp<T><<<dim3((ncols + 127) / 128, 1, batch), 128, 0, st>>>(A, n, ld, stride, j0, jb, ipiv);
                 tags_note_launch();
+            }
         }
         int rest = n - j0 - jb;
         if (rest > 0) {
@@ -380,28 +381,31 @@ int lu_impl(T* A, int n, long long ld, long long stride, int batch, int pivot, i
 template <typename T>
 int lu_solve_impl(const T* A, int n, long long ld, long long stride, int batch, const int* ipiv, T* X, int nrhs,
                   long long ldx, long long xstride, cudaStream_t st) {
-    if (ipiv)
+    if (ipiv) {
         k_rhs_swap<T><<<dim3((nrhs + 31) / 32, 1, batch), 32, 0, st>>>(X, n, nrhs, ldx, xstride, ipiv);
         tags_note_launch();
+    }
     for (int j0 = 0; j0 < n; j0 += NB) {
         int jb = min(NB, n - j0);
         k_trsv_diag<T, NB><<<dim3(1, 1, batch), 256, 0, st>>>(A, n, ld, stride, X, nrhs, ldx, xstride, j0, jb, 0);
         tags_note_launch();
         int rest = n - j0 - jb;
-        if (rest > 0)
+        if (rest > 0) {
             k_trsv_update<T><<<dim3((rest + 127) / 128, nrhs, batch), 128, 0, st>>>(A, n, ld, stride, X, nrhs, ldx,
                                                                                  xstride, j0, jb, 0);
             tags_note_launch();
+        }
     }
     int last = ((n - 1) / NB) * NB;
     for (int j0 = last; j0 >= 0; j0 -= NB) {
         int jb = min(NB, n - j0);
         k_trsv_diag<T, NB><<<dim3(1, 1, batch), 256, 0, st>>>(A, n, ld, stride, X, nrhs, ldx, xstride, j0, jb, 1);
         tags_note_launch();
-        if (j0 > 0)
+        if (j0 > 0) {
             k_trsv_update<T><<<dim3((j0 + 127) / 128, nrhs, batch), 128, 0, st>>>(A, n, ld, stride, X, nrhs, ldx,
                                                                                xstride, j0, jb, 1);
             tags_note_launch();
+        }
     }
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

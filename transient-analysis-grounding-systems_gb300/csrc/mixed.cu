@@ -429,8 +429,7 @@ static int fallback_plain(tags_plan_s* p, int q, cudaStream_t st) {
     out.row0_t = out.col0_t = p->n + p->m;
     out.sign = -1.0;
     out.mirror = 1;
-    err = tags_launch_fill_fp64(p->d_elec, p->d_img, p->m, p->d_coef + q, 1, out,
-                                p->has_images ? TAGS_FILL_BOTH : TAGS_FILL_DIRECT, TAGS_INTG_DOUBLE, 1, p->d_status, st);
+    err = tags_plan_fill_fp64(p, p->d_coef + q, 1, out, st);
     if (err) return err;
     err = tags_lu_z(W, (int)N, N, NN, 1, 1, ipiv, p->d_info + q, st);
     if (err) return err;
@@ -454,9 +453,14 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     k_copy_c<<<(unsigned)(((long long)nb * N + 255) / 256), 256, 0, st>>>(p->d_x, d_b, (long long)nb * N);
     tags_note_launch();
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_x, 0, sizeof(double2) * N * nb, st));
-    // 1. impedance blocks (full symmetric, complex FP32), direct + images
-    int err = tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z, p->d_Z + (size_t)m * m,
-                                     2LL * m * m, p->has_images, p->n_touch, p->d_status, st);
+    // 1. impedance blocks (full symmetric, complex FP32), direct + images: double
+    //    line integrals, or the mHEM rescale of the static potentials
+    int err = p->fill_model == TAGS_INTG_MHEM
+                  ? tags_launch_mhem_mixed(m, p->has_images, p->d_pot, p->d_fillws, p->d_coef, nb, p->d_Z,
+                                           p->d_Z + (size_t)m * m, 2LL * m * m, p->d_status, st)
+                  : tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z,
+                                           p->d_Z + (size_t)m * m, 2LL * m * m, p->has_images, p->n_touch,
+                                           p->d_status, st);
     if (err) return err;
     // 2. scaling
     k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, N);

@@ -152,6 +152,8 @@ static void plan_free(tags_plan_s* p) {
     if (p->d_stage) cudaFree(p->d_stage);
     if (p->d_fbW) cudaFree(p->d_fbW);
     if (p->d_fbpiv) cudaFree(p->d_fbpiv);
+    if (p->d_pot) cudaFree(p->d_pot);
+    if (p->d_coef1) cudaFree(p->d_coef1);
     if (p->d_iein) cudaFree(p->d_iein);
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
@@ -240,6 +242,35 @@ extern "C" int tags_plan_destroy(tags_plan plan) {
     return 0;
 }
 
+int tags_plan_fill_fp64(tags_plan_s* p, const SampleCoef* d_coef, int nb, const FillOut& out, cudaStream_t st) {
+    if (p->fill_model == TAGS_INTG_MHEM)
+        return tags_launch_mhem_fp64(p->d_elec, p->d_img, p->m, p->has_images, p->d_pot, d_coef, nb, out, p->d_status,
+                                     st);
+    return tags_launch_fill_fp64(p->d_elec, p->d_img, p->m, d_coef, nb, out,
+                                 p->has_images ? TAGS_FILL_BOTH : TAGS_FILL_DIRECT, TAGS_INTG_DOUBLE, 1, p->d_status, st);
+}
+
+extern "C" int tags_plan_set_fill(tags_plan plan, int integration_type) {
+    tags_plan_s* p = plan;
+    if (!p) return tags_fail(TAGS_E_ARG, "tags_plan_set_fill: invalid plan");
+    if (integration_type != TAGS_INTG_DOUBLE && integration_type != TAGS_INTG_MHEM)
+        return tags_fail(TAGS_E_ARG, "tags_plan_set_fill: INTG_DOUBLE (2) or INTG_MHEM (4)");
+    if (integration_type == p->fill_model) return 0;
+    TAGS_CUDA_OK(cudaSetDevice(p->device));
+    if (integration_type == TAGS_INTG_MHEM && !p->d_pot) {
+        // the static potentials, once per geometry
+        TAGS_CUDA_OK(cudaMalloc(&p->d_pot, sizeof(double2) * 4 * (size_t)p->m * p->m));
+        TAGS_CUDA_OK(cudaMalloc(&p->d_coef1, sizeof(SampleCoef)));
+        int err = tags_launch_mhem_potentials(p->d_elec, p->d_img, p->m, p->has_images, p->d_pot, p->d_coef1,
+                                              p->d_status, p->stream);
+        if (err) return err;
+        TAGS_CUDA_OK(cudaStreamSynchronize(p->stream));
+    }
+    p->fill_model = integration_type;
+    tags_plan_drop_graphs(p);
+    return 0;
+}
+
 // Plain FP64 pass over nb samples whose coefficients and right-hand sides are
 // already in p->d_coef and p->d_x.
 int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st) {
@@ -257,8 +288,7 @@ int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st)
     out.sign = -1.0;
     out.mirror = 1;
     out.accumulate = 0;
-    err = tags_launch_fill_fp64(p->d_elec, p->d_img, p->m, p->d_coef, nb, out,
-                                p->has_images ? TAGS_FILL_BOTH : TAGS_FILL_DIRECT, TAGS_INTG_DOUBLE, 1, p->d_status, st);
+    err = tags_plan_fill_fp64(p, p->d_coef, nb, out, st);
     if (err) return err;
     err = tags_lu_z(p->d_W, (int)N, N, NN, nb, 1, p->d_ipiv, p->d_info, st);
     if (err) return err;

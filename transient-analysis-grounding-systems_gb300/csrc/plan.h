@@ -2,6 +2,7 @@
 #pragma once
 
 #include <complex>
+#include <mutex>
 #include <vector>
 #include <cuda_runtime.h>
 
@@ -18,6 +19,7 @@ struct DeviceCtx {
 };
 
 DeviceCtx* tags_ctx();
+std::mutex& tags_dropin_mutex();
 int tags_fail(int code, const char* msg);
 void tags_msg(const char* msg);
 SampleCoef tags_sample_coef(std::complex<double> gamma, std::complex<double> s, double mur,
@@ -65,6 +67,9 @@ struct tags_plan_s {
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
     int split_pieces = TAGS_SPLIT_F16;   // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
+    int fill_model = TAGS_INTG_DOUBLE;  // TAGS_INTG_DOUBLE (double line integrals) or TAGS_INTG_MHEM
+    double2* d_pot = nullptr;       // mHEM: 4 x m x m static potentials (direct ZL, ZT; images ZL, ZT)
+    SampleCoef* d_coef1 = nullptr;  // unit coefficients for the potentials
     int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue
@@ -97,6 +102,8 @@ int tags_mixed_free(tags_plan_s* p);
 int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2* d_b, int* h_iters, double* h_berr,
                            int* h_conv, cudaStream_t st);
 int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st);
+// the impedance fill of a pass into W_G (plain) per the plan's fill model
+int tags_plan_fill_fp64(tags_plan_s* p, const SampleCoef* d_coef, int nb, const FillOut& out, cudaStream_t st);
 void tags_plan_drop_graphs(tags_plan_s* p);
 int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st);
 int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditionalHandle cond, int set_cond);

@@ -37,6 +37,13 @@ struct FillOut {
 };
 
 int tags_fill_tables_init();
+// mHEM fill: static potentials once per geometry, then a rescale per sample
+int tags_launch_mhem_potentials(const double* d_elec, const double* d_img, int m, int has_img, double2* d_pot,
+                                SampleCoef* d_coef1, int* d_status, cudaStream_t st);
+int tags_launch_mhem_fp64(const double* d_elec, const double* d_img, int m, int has_img, const double2* d_pot,
+                          const SampleCoef* d_coef, int nsamp, const FillOut& out, int* d_status, cudaStream_t st);
+int tags_launch_mhem_mixed(int m, int has_img, const double2* d_pot, void* ws, const SampleCoef* d_coef, int nsamp,
+                           float2* d_zl, float2* d_zt, long long bstride, int* d_status, cudaStream_t st);
 // mixed-form fill (FP32 regular pairs, FP64 log-singular pairs); the
 // workspace holds the plan-time pair classes and geometry records
 size_t tags_mixed_fill_workspace(int m);
