@@ -15,6 +15,11 @@
  *   calculate_yla_ytb      replaces src/linalg.c:261-300    (decl src/linalg.h:145-149)
  *   fill_impedance_adm2    replaces src/linalg.c:302-325    (decl src/linalg.h:169-173)
  *   solve_admittance       replaces src/linalg.c:327-350    (decl src/linalg.h:192-193)
+ * and host-side helpers of the reference (no device work):
+ *   electrodes_file        src/electrode.c:45-80    (decl src/electrode.h:127-128)
+ *   nodes_file             src/electrode.c:82-101   (decl src/electrode.h:140-141)
+ *   alipio_soil            src/auxiliary.c:60-70    (decl src/auxiliary.h:101-103)
+ *   smith_longmire_soil    src/auxiliary.c:72-93    (decl src/auxiliary.h:119-121)
  *   laplace_trans          replaces src/auxiliary.c:239-263 (decl src/auxiliary.h:320-321)
  *   inv_laplace_trans      replaces src/auxiliary.c:265-329 (decl src/auxiliary.h:366-368)
  *
@@ -91,6 +96,24 @@ int fill_impedance_imm (tags_cdouble *wg, const tags_cdouble *zl, const tags_cdo
  * factorisation there; its content is not part of the contract). */
 int solve_immittance (tags_cdouble *wg, tags_cdouble *ie, size_t num_electrodes, size_t num_nodes);
 
+/* ---- geometry files and soil models (host only) ----------------------------- */
+
+/* Reads num_electrodes lines "x0, y0, z0, x1, y1, z1, r". Returns 0, -10 if
+ * the file cannot be opened, (values read - 7) at the first bad line, or
+ * 1 / 2 for coincident end points / a radius <= 0. */
+int electrodes_file (const char file_name[], Electrode *electrodes, size_t num_electrodes);
+
+/* Reads num_nodes lines "x, y, z" into nodes (3 per node). Returns 0, -10 if
+ * the file cannot be opened, or (values read - 3) at the first bad line. */
+int nodes_file (const char file_name[], double *nodes, size_t num_nodes);
+
+/* Alipio-Visacro soil: conductivity and relative permittivity at s. */
+int alipio_soil (tags_cdouble *sigma, tags_cdouble *epsr, double sigma0, tags_cdouble s, double h, double g,
+                 double eps_ratio);
+
+/* Smith-Longmire soil: conductivity and relative permittivity at s. */
+int smith_longmire_soil (tags_cdouble *sigma, tags_cdouble *epsr, double sigma0, tags_cdouble s, double erinf);
+
 /* ---- nodal admittance formulation (the reference's mHEM examples) ---------- */
 
 /* A (+1 start, -1 end) and B (0.5), num_electrodes x num_nodes column-major.
@@ -126,6 +149,16 @@ int solve_admittance (tags_cdouble *yn, tags_cdouble *ic, size_t num_nodes);
 int laplace_trans (double *f, tags_cdouble *g, tags_cdouble *s, double tmax, size_t nt);
 int inv_laplace_trans (double *f, tags_cdouble *g, tags_cdouble *s, double tmax, size_t nt,
                        int filter);
+
+/* No counterpart function in the reference: the inverse transform of many
+ * series at once in the layout of the examples' fftw_plan_many_dft_c2r
+ * (examples/three_grids.c:229-242): g[series + k * nseries] for the ns =
+ * nt/2 + 1 samples (sample-major, e.g. node potentials of every sample), f
+ * [series + j * nseries] for nt times, scaled by e^{c t_j} / (nt dt) as the
+ * examples' output loop does (:447-465); filter as in inv_laplace_trans.
+ * flags: TAGS_RUN_DEVICE_PTRS for device pointers (declared below). */
+int tags_inv_laplace_batch (double *f, const tags_cdouble *g, const tags_cdouble *s, double tmax, size_t nt,
+                            size_t nseries, int filter, int flags);
 
 /* ---- Part 2: batched extension -------------------------------------------- */
 

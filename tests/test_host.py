@@ -83,3 +83,64 @@ def test_compute_calls_fail_loudly_without_library(pkg, monkeypatch, tmp_path):
     monkeypatch.setattr(pkg, "LIB_PATH", str(tmp_path / "missing.so"))
     with pytest.raises(RuntimeError, match="missing"):
         pkg.solve_immittance(np.zeros(9, np.complex128), np.zeros(3, np.complex128), 1, 1)
+
+
+def _ref_lib(orc_mod):
+    if not orc_mod.available("ref"):
+        pytest.skip("reference build (oracle/_ref) not present here")
+    return orc_mod.get("ref").lib
+
+
+def test_geometry_files_match_reference(pkg, orc_mod, tmp_path):
+    """electrodes_file / nodes_file (src/electrode.c:45-101): the library's
+    host readers give the reference's arrays and return codes, bad lines and
+    degenerate segments included."""
+    ref = _ref_lib(orc_mod)
+    for name in ("electrodes_file", "nodes_file"):
+        getattr(ref, name).argtypes = [ctypes.c_char_p, ctypes.c_void_p, ctypes.c_size_t]
+        getattr(ref, name).restype = ctypes.c_int
+    rng = np.random.default_rng(4)
+    good = tmp_path / "elec.csv"
+    rows = np.round(rng.uniform(-5, 5, (6, 7)), 6)
+    rows[:, 6] = np.abs(rows[:, 6]) + 1e-3
+    good.write_text("\n".join(", ".join(f"{v:.6f}" for v in r) for r in rows) + "\n")
+    short = tmp_path / "short.csv"
+    short.write_text("0, 0, 0, 1, 0, 0, 0.01\n1, 0, 0, 2, 0\n")
+    degen = tmp_path / "degen.csv"
+    degen.write_text("0, 0, 0, 1, 0, 0, 0.01\n3, 3, 3, 3, 3, 3, 0.01\n")
+    for path, m in ((good, 6), (short, 2), (degen, 2), (tmp_path / "missing.csv", 1)):
+        pkg.lib().tags_gpu_set_quiet(1)
+        code, e = pkg.electrodes_file(str(path), m)
+        pkg.lib().tags_gpu_set_quiet(0)
+        e_ref = np.zeros((m, 11))
+        code_ref = ref.electrodes_file(str(path).encode(), e_ref.ctypes.data, m)
+        assert code == code_ref and np.array_equal(e, e_ref), path.name
+    nodes = tmp_path / "nodes.csv"
+    nodes.write_text("1.5, -2, 0.25\n3, 4, 5\n7, 8\n")
+    for n in (2, 3):
+        pkg.lib().tags_gpu_set_quiet(1)
+        code, nd = pkg.nodes_file(str(nodes), n)
+        pkg.lib().tags_gpu_set_quiet(0)
+        nd_ref = np.zeros((n, 3))
+        code_ref = ref.nodes_file(str(nodes).encode(), nd_ref.ctypes.data, n)
+        assert code == code_ref and np.array_equal(nd, nd_ref)
+
+
+def test_soil_models_match_reference(pkg, orc_mod):
+    """alipio_soil / smith_longmire_soil (src/auxiliary.c:60-93) exported by
+    the library: within 1e-13 of the reference (C++ complex pow against C's
+    cpow)."""
+    ref = _ref_lib(orc_mod)
+    C = pkg.c_complex
+    ref.smith_longmire_soil.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, C, ctypes.c_double]
+    ref.alipio_soil.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, C, ctypes.c_double,
+                                ctypes.c_double, ctypes.c_double]
+    for s in (2j * np.pi * 50.0, 1e4 + 2j * np.pi * 3e5, 8e4 + 2j * np.pi * 1e7):
+        want = np.zeros(2, np.complex128)
+        ref.smith_longmire_soil(want[:1].ctypes.data, want[1:].ctypes.data, 1e-3, C.of(s), 10.0)
+        got = pkg.smith_longmire_soil(1e-3, s, 10.0)
+        assert abs(got[0] - want[0]) <= 1e-13 * abs(want[0]) and abs(got[1] - want[1]) <= 1e-13 * abs(want[1])
+        ref.alipio_soil(want[:1].ctypes.data, want[1:].ctypes.data, 1e-3, C.of(s), 1.26, 0.54, 12.0)
+        out = np.zeros(2, np.complex128)
+        pkg.lib().alipio_soil(out[:1].ctypes.data, out[1:].ctypes.data, 1e-3, C.of(s), 1.26, 0.54, 12.0)
+        assert np.max(np.abs(out - want) / np.abs(want)) <= 1e-13

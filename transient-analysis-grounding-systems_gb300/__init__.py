@@ -54,8 +54,9 @@ EPS0 = 8.854187817620e-12
 EXPORTS = (
     "calculate_impedances", "impedances_images", "fill_incidence_imm", "fill_impedance_imm",
     "solve_immittance", "fill_incidence_adm", "fill_impedance_adm", "calculate_yla_ytb", "fill_impedance_adm2",
-    "solve_admittance", "laplace_trans", "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
-    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
+    "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
+    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_gpu_set_quiet",
 )
 
@@ -118,6 +119,10 @@ def lib() -> ctypes.CDLL:
             L.calculate_yla_ytb.argtypes = [_vp, _vp, _vp, _vp, _vp, _vp, _sz, _sz]
             L.fill_impedance_adm2.argtypes = [_vp, _vp, _vp, _vp, _vp, _sz, _sz]
             L.solve_admittance.argtypes = [_vp, _vp, _sz]
+            L.electrodes_file.argtypes = [ctypes.c_char_p, _vp, _sz]
+            L.nodes_file.argtypes = [ctypes.c_char_p, _vp, _sz]
+            L.alipio_soil.argtypes = [_vp, _vp, ctypes.c_double, C, ctypes.c_double, ctypes.c_double, ctypes.c_double]
+            L.smith_longmire_soil.argtypes = [_vp, _vp, ctypes.c_double, C, ctypes.c_double]
             L.laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz]
             L.inv_laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, ctypes.c_int]
             L.tags_plan_create.argtypes = [ctypes.POINTER(_vp), _vp, _vp, _sz, _vp, _sz, ctypes.c_int, _sz]
@@ -127,6 +132,7 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_graphs.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_fill.argtypes = [_vp, ctypes.c_int]
+            L.tags_inv_laplace_batch.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int, ctypes.c_int]
             L.tags_plan_tune.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int,
                                          ctypes.POINTER(TuneResult)]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
@@ -134,10 +140,11 @@ def lib() -> ctypes.CDLL:
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
             for name in ("calculate_impedances", "impedances_images", "fill_incidence_imm",
                          "fill_impedance_imm", "solve_immittance", "fill_incidence_adm", "fill_impedance_adm",
-                         "calculate_yla_ytb", "fill_impedance_adm2", "solve_admittance", "laplace_trans",
+                         "calculate_yla_ytb", "fill_impedance_adm2", "solve_admittance", "electrodes_file",
+                         "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
                          "inv_laplace_trans",
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
-                         "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill"):
+                         "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -368,6 +375,43 @@ def solve_immittance(wg, ie, num_electrodes: int, num_nodes: int) -> int:
     _check_c128(wg, "wg", N * N)
     _check_c128(ie, "ie", N)
     return _ret(lib().solve_immittance(_addr(wg), _addr(ie), m, n))
+
+
+def electrodes_file(path: str, num_electrodes: int):
+    """(code, electrodes m x 11) read by the reference's CSV rule (electrodes_file)."""
+    e = np.zeros((int(num_electrodes), 11))
+    code = lib().electrodes_file(os.fsencode(path), _addr(e), int(num_electrodes))
+    return code, e
+
+
+def nodes_file(path: str, num_nodes: int):
+    """(code, nodes n x 3) read by the reference's CSV rule (nodes_file)."""
+    nd = np.zeros((int(num_nodes), 3))
+    code = lib().nodes_file(os.fsencode(path), _addr(nd), int(num_nodes))
+    return code, nd
+
+
+def smith_longmire_soil(sigma0: float, s: complex, erinf: float):
+    """(sigma, eps_r) of the Smith-Longmire soil model at s."""
+    out = np.zeros(2, dtype=np.complex128)
+    lib().smith_longmire_soil(_addr(out[:1]), _addr(out[1:]), float(sigma0), c_complex.of(s), float(erinf))
+    return complex(out[0]), complex(out[1])
+
+
+def inv_laplace_batch(g, s, tmax: float, nt: int, filt: int = FILTER_NONE) -> np.ndarray:
+    """Inverse transform of every column of g (ns x nseries, sample-major, e.g.
+    node potentials of all samples) at once: nt x nseries, scaled as the
+    reference examples' output loop (tags_inv_laplace_batch)."""
+    g = np.ascontiguousarray(g, dtype=np.complex128)
+    if g.ndim == 1:
+        g = g[:, None]
+    ns, nser = g.shape
+    if ns != nt // 2 + 1:
+        raise ValueError("g needs nt // 2 + 1 rows")
+    s = np.ascontiguousarray(s, dtype=np.complex128)
+    f = np.zeros((nt, nser))
+    _ret(lib().tags_inv_laplace_batch(_addr(f), _addr(g), _addr(s), float(tmax), int(nt), int(nser), int(filt), 0))
+    return f
 
 
 # nodal admittance formulation (src/linalg.c:142-350), used by the reference's mHEM examples

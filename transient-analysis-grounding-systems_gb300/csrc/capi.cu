@@ -414,6 +414,43 @@ extern "C" int inv_laplace_trans(double* f, tags_cdouble* g, tags_cdouble* s, do
     return 0;
 }
 
+// Batched inverse over many series in the examples' layout (no counterpart
+// function in the reference; it replaces the examples' fftw_plan_many_dft_c2r
+// and the scaling loop, examples/three_grids.c:229-242 and :447-465).
+extern "C" int tags_inv_laplace_batch(double* f, const tags_cdouble* g, const tags_cdouble* s, double tmax, size_t nt,
+                                      size_t nseries, int filter, int flags) {
+    std::lock_guard<std::mutex> lk(g_mutex);
+    if (nt < 2 || nseries == 0 || !f || !g || !s) return tags_fail(TAGS_E_ARG, "invalid argument");
+    if (nt > (size_t)1 << 26 || nseries > (size_t)1 << 26) return tags_fail(TAGS_E_ARG, "transform too large");
+    DeviceCtx* c = tags_ctx();
+    if (!c) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
+    cudaStream_t st = c->stream;
+    const bool dev = (flags & TAGS_RUN_DEVICE_PTRS) != 0;
+    const size_t ns = nt / 2 + 1;
+    double2* d_tw = (double2*)c->scratch(6, sizeof(double2) * (nt + ns));
+    if (!d_tw) return tags_fail(TAGS_E_NOMEM, "device allocation failed");
+    double2* d_s = d_tw + nt;
+    const double2* d_g = reinterpret_cast<const double2*>(g);
+    double* d_f = f;
+    if (!dev) {
+        double2* dg = (double2*)c->scratch(8, sizeof(double2) * ns * nseries);
+        d_f = (double*)c->scratch(7, sizeof(double) * nt * nseries);
+        if (!dg || !d_f) return tags_fail(TAGS_E_NOMEM, "device allocation failed");
+        TAGS_CUDA_OK(cudaMemcpyAsync(dg, g, sizeof(double2) * ns * nseries, cudaMemcpyHostToDevice, st));
+        d_g = dg;
+    }
+    TAGS_CUDA_OK(cudaMemcpyAsync(d_s, s, sizeof(double2) * ns, dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                 st));
+    int err = tags_twiddles(d_tw, (long long)nt, st);
+    if (!err)
+        err = tags_launch_inlt_rows(d_g, (long long)ns, d_s, d_tw, (long long)nt, tmax,
+                                    (filter >= 1 && filter <= 4) ? filter : 0, d_f, (long long)nseries, st);
+    if (err) return err;
+    if (!dev) TAGS_CUDA_OK(cudaMemcpyAsync(f, d_f, sizeof(double) * nt * nseries, cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    return 0;
+}
+
 // ---- library info ------------------------------------------------------------------
 
 extern "C" long long tags_gpu_launch_count(void) { return g_launches.load(); }

@@ -60,6 +60,31 @@ __global__ void k_inlt(const double2* __restrict__ g, long long gstride, long lo
     f[fstride * srs + j] = acc * exp(c * (double)j * dt) / ((double)nt * dt);
 }
 
+// Batched inverse in the examples' layout (examples/three_grids.c:229-242,
+// :447-465): g[series + k nser] (sample-major), f[series + j nser], scaled by
+// e^{c t_j} / (nt dt). One thread per (series, time index): threads run along
+// the series, so the reads of g and the writes of f are contiguous and the
+// twiddle is the same for the whole block.
+__global__ void k_inlt_rows(const double2* __restrict__ g, long long ns, const double2* __restrict__ s,
+                            const double2* __restrict__ tw, long long nt, double tmax, int filter,
+                            double* __restrict__ f, long long nser) {
+    const long long srs = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long j = blockIdx.y;
+    if (srs >= nser || j >= nt) return;
+    const double omega = s[ns - 1].y;
+    const long long half = nt / 2;
+    double acc = g[srs].x * window(filter, s[0].y, omega);
+    const long long kmax = (nt % 2 == 0) ? half - 1 : half;
+    for (long long k = 1; k <= kmax; ++k) {
+        const double2 t = tw[(j * k) % nt];
+        const double2 v = g[srs + k * nser];
+        acc += 2.0 * window(filter, s[k].y, omega) * (v.x * t.x - v.y * t.y);
+    }
+    if (nt % 2 == 0 && nt > 1) acc += ((j & 1) ? -1.0 : 1.0) * g[srs + half * nser].x * window(filter, s[half].y, omega);
+    const double dt = tmax / (double)(nt - 1);
+    f[srs + j * nser] = acc * exp(s[0].x * (double)j * dt) / ((double)nt * dt);
+}
+
 // Forward transform with the damping of the numerical Laplace transform.
 __global__ void k_nlt(const double* __restrict__ f, long long fstride, long long nt, const double2* __restrict__ tw,
                       double tmax, double2* __restrict__ g, long long gstride, int nseries) {
@@ -94,6 +119,15 @@ int tags_launch_inlt(const double2* d_g, long long gstride, long long ns, const 
                      cudaStream_t st) {
     dim3 grid((unsigned)((nt + 127) / 128), nseries);
     k_inlt<<<grid, 128, 0, st>>>(d_g, gstride, ns, d_s, d_tw, nt, tmax, filter, d_f, fstride, nseries);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+int tags_launch_inlt_rows(const double2* d_g, long long ns, const double2* d_s, const double2* d_tw, long long nt,
+                          double tmax, int filter, double* d_f, long long nser, cudaStream_t st) {
+    dim3 grid((unsigned)((nser + 127) / 128), (unsigned)nt);
+    k_inlt_rows<<<grid, 128, 0, st>>>(d_g, ns, d_s, d_tw, nt, tmax, filter, d_f, nser);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

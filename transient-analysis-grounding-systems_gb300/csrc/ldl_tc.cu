@@ -38,7 +38,14 @@ namespace {
 
 constexpr int TB = 128;                 // panel width and tile edge
 constexpr int GMAX = 4;                 // most panels per trailing update (K up to 512)
-constexpr int KG = TB * GMAX;           // K extent (row length) of a group's plane buffers
+constexpr int KG = TB * GMAX;           // K extent of a group's plane buffers
+
+// Split planes are K-block-major: plane p of a buffer with R rows and K
+// columns holds blocks of 32 columns, each R rows x 32 (64-byte rows), so a
+// TMA box of 32 columns x 128 rows is one contiguous 8 KiB piece.
+TAGS_HD long long plane_elem(int p, int R, int K, int row, int col) {
+    return (long long)p * R * K + (long long)(col >> 5) * R * 32 + (long long)row * 32 + (col & 31);
+}
 constexpr int SMAX = 3;                 // most bf16 pieces per real value (split products)
 constexpr uint64_t WAIT_NS = 50ull * 1000 * 1000;   // 50 ms per wait
 
@@ -79,11 +86,12 @@ TAGS_D bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
         }
     }
 }
-TAGS_D void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, uint32_t bar) {
+TAGS_D void tma_load_5d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                        uint32_t bar) {
     asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
-        "[%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5, "
+        "%6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
         : "memory");
 }
 TAGS_D void tmem_alloc(uint32_t slot, uint32_t ncols) {
@@ -255,7 +263,6 @@ TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& sk
 // time with the packed conversions (one instruction per pair of values).
 template <int S>
 TAGS_D void store_planes16(uint16_t* P, int R, int ks, int row, int c0, const float2* v, bool f16, int& ovf) {
-    const long long off = (long long)row * ks + c0;
     __align__(16) uint32_t pl[2 * S][8];        // 8 packed pairs = 16 columns per plane
     if (S == 2 && f16) {
 #pragma unroll
@@ -291,7 +298,7 @@ TAGS_D void store_planes16(uint16_t* P, int R, int ks, int row, int c0, const fl
     }
 #pragma unroll
     for (int p = 0; p < 2 * S; ++p) {
-        uint4* d = reinterpret_cast<uint4*>(P + (long long)p * R * ks + off);
+        uint4* d = reinterpret_cast<uint4*>(P + plane_elem(p, R, ks, row, c0));
         d[0] = make_uint4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
         d[1] = make_uint4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
     }
@@ -351,10 +358,10 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                     issued[stage] = 0;
                     const uint32_t sb = base_u32 + stage * C::STAGE;
                     mbar_expect_tx(full(stage), C::STAGE);
-                    const int ra = TB * I + g.off, rb = TB * J + g.off, kx = kb * BK;
+                    const int ra = TB * I + g.off, rb = TB * J + g.off;
                     for (int p = 0; p < C::NPL; ++p) {
-                        tma_load_4d(sb + p * PST, &tmA, kx, ra, p, smp, full(stage));
-                        tma_load_4d(sb + (C::NPL + p) * PST, &tmB, kx, rb, p, smp, full(stage));
+                        tma_load_5d(sb + p * PST, &tmA, 0, ra, kb, p, smp, full(stage));
+                        tma_load_5d(sb + (C::NPL + p) * PST, &tmB, 0, rb, kb, p, smp, full(stage));
                     }
                     issued[stage] = 1;
                     if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
@@ -692,9 +699,9 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
         X32[TB * TB + t] = vt;
         uint16_t pc[SMAX];
         split_n(v.x, pc, NS, f16 != 0, ovf);
-        for (int q = 0; q < NS; ++q) P[(long long)q * TB * TB + t] = pc[q];
+        for (int q = 0; q < NS; ++q) P[plane_elem(q, TB, TB, n, k)] = pc[q];
         split_n(v.y, pc, NS, f16 != 0, ovf);
-        for (int q = 0; q < NS; ++q) P[(long long)(NS + q) * TB * TB + t] = pc[q];
+        for (int q = 0; q < NS; ++q) P[plane_elem(NS + q, TB, TB, n, k)] = pc[q];
     }
     if (ovf) atomicOr(err + kErrRange, 1);
 }
@@ -721,12 +728,11 @@ __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__
         int c = q % TB, rr = q / TB;
         if (r0 + rr >= M) continue;
         float2 v = t[c][rr];
-        long long o = (long long)(r0 + rr) * TB + c;
         uint16_t pc[SMAX];
         split_n(v.x, pc, NS, f16 != 0, ovf);
-        for (int q = 0; q < NS; ++q) P[(long long)q * R * TB + o] = pc[q];
+        for (int q = 0; q < NS; ++q) P[plane_elem(q, R, TB, r0 + rr, c)] = pc[q];
         split_n(v.y, pc, NS, f16 != 0, ovf);
-        for (int q = 0; q < NS; ++q) P[(long long)(NS + q) * R * TB + o] = pc[q];
+        for (int q = 0; q < NS; ++q) P[plane_elem(NS + q, R, TB, r0 + rr, c)] = pc[q];
     }
     if (ovf) atomicOr(err + kErrRange, 1);
 }
@@ -877,14 +883,18 @@ EncodeTiledFn encode_fn() {
 
 // 4-D map over planes [sample][nplanes][rows][128] bf16, box {32, 128, 1, 1}
 // (64-byte rows, 64-byte swizzle: the K block of one pipeline stage).
+// 5-D map over K-block-major planes [sample][plane][K / 32][rows][32] (16-bit),
+// box {32, 128, 1, 1, 1}: one K block of 128 rows (64-byte rows, 64-byte swizzle).
 int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samples, int klen = TB) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
-    cuuint64_t dims[4] = {(cuuint64_t)klen, (cuuint64_t)rows, (cuuint64_t)nplanes, (cuuint64_t)samples};
-    cuuint64_t strides[3] = {(cuuint64_t)klen * 2, (cuuint64_t)klen * 2 * rows, (cuuint64_t)klen * 2 * rows * nplanes};
-    cuuint32_t box[4] = {(cuuint32_t)BK, (cuuint32_t)TB, 1, 1};
-    cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 4, base, dims, strides, box, estr,
+    const cuuint64_t kblk = (cuuint64_t)klen / BK;
+    cuuint64_t dims[5] = {(cuuint64_t)BK, (cuuint64_t)rows, kblk, (cuuint64_t)nplanes, (cuuint64_t)samples};
+    cuuint64_t strides[4] = {(cuuint64_t)BK * 2, (cuuint64_t)BK * 2 * rows, (cuuint64_t)BK * 2 * rows * kblk,
+                             (cuuint64_t)BK * 2 * rows * kblk * nplanes};
+    cuuint32_t box[5] = {(cuuint32_t)BK, (cuuint32_t)TB, 1, 1, 1};
+    cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {

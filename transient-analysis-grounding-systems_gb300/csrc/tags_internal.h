@@ -83,6 +83,8 @@ int tags_twiddles(double2* d_tw, long long nt, cudaStream_t st);
 int tags_launch_inlt(const double2* d_g, long long gstride, long long ns, const double2* d_s, const double2* d_tw,
                      long long nt, double tmax, int filter, double* d_f, long long fstride, int nseries,
                      cudaStream_t st);
+int tags_launch_inlt_rows(const double2* d_g, long long ns, const double2* d_s, const double2* d_tw, long long nt,
+                          double tmax, int filter, double* d_f, long long nser, cudaStream_t st);
 int tags_launch_nlt(const double* d_f, long long fstride, long long nt, const double2* d_tw, double tmax,
                     double2* d_g, long long gstride, int nseries, cudaStream_t st);
 
