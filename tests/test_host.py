@@ -88,7 +88,9 @@ def test_compute_calls_fail_loudly_without_library(pkg, monkeypatch, tmp_path):
 def _ref_lib(orc_mod):
     if not orc_mod.available("ref"):
         pytest.skip("reference build (oracle/_ref) not present here")
-    return orc_mod.get("ref").lib
+    # A private handle: argtypes set here must not leak into the shared
+    # oracle object's function table.
+    return ctypes.CDLL(orc_mod.get("ref").lib._name)
 
 
 def test_geometry_files_match_reference(pkg, orc_mod, tmp_path):
