@@ -126,6 +126,29 @@ int oracle_hem_impedances (const OracleElectrode *e, const OracleElectrode *img,
                            size_t max_eval, double req_abs, double req_rel, int type,
                            double _Complex *zl, double _Complex *zt);
 
+/* Post-processing: potentials, fields and path voltage (src/electrode.c:434-668)
+ * and the closed-form mHEM ground potential (examples/visacro57emc01.c:406-430). */
+double _Complex oracle_electric_potential (const double *point, const OracleElectrode *e, size_t m,
+                                           const double _Complex *it, double _Complex gamma,
+                                           double _Complex kappa, size_t max_eval, double req_abs,
+                                           double req_rel, int *failure);
+int oracle_magnetic_potential (const double *point, const OracleElectrode *e, size_t m,
+                               const double _Complex *il, double _Complex gamma, double mur,
+                               size_t max_eval, double req_abs, double req_rel, double _Complex *va);
+int oracle_electric_field (const double *point, const OracleElectrode *e, size_t m,
+                           const double _Complex *il, const double _Complex *it,
+                           double _Complex gamma, double _Complex s, double mur,
+                           double _Complex kappa, size_t max_eval, double req_abs, double req_rel,
+                           double _Complex *ve);
+double _Complex oracle_voltage (const double *point1, const double *point2, const OracleElectrode *e,
+                                size_t m, const double _Complex *il, const double _Complex *it,
+                                double _Complex gamma, double _Complex s, double mur,
+                                double _Complex kappa, size_t max_eval, double req_abs, double req_rel,
+                                int *failure);
+int oracle_gpd_mhem (const double *points, size_t np, const OracleElectrode *e, size_t m,
+                     const double _Complex *it, size_t nrhs, double _Complex gamma,
+                     double _Complex kappa, double _Complex *gpd);
+
 /* LAPACK binding (oracle/lapack_shim.c) */
 int tags_lapack_bind (const char *name, void *fn);
 int tags_lapack_ready (void);

@@ -186,6 +186,23 @@ class Oracle:
         f = self._fn("segment_electrode")
         f.argtypes = [_dp, _dp, _sz, _dp, _dp, ctypes.c_double]
         f.restype = ctypes.c_int
+        # post-processing (src/electrode.c:434-668); the restatement adds a
+        # failure out-argument to the two functions that return the value
+        tail = [_ip] if self.kind == "port" else []
+        f = self._fn("electric_potential")
+        f.argtypes = [_dp, _dp, _sz, _dp, C, C, _sz, ctypes.c_double, ctypes.c_double] + tail
+        f.restype = C
+        f = self._fn("magnetic_potential")
+        f.argtypes = [_dp, _dp, _sz, _dp, C, ctypes.c_double, _sz, ctypes.c_double, ctypes.c_double, _dp]
+        f.restype = ctypes.c_int
+        f = self._fn("electric_field")
+        f.argtypes = [_dp, _dp, _sz, _dp, _dp, C, C, ctypes.c_double, C, _sz, ctypes.c_double,
+                      ctypes.c_double, _dp]
+        f.restype = ctypes.c_int
+        f = self._fn("voltage")
+        f.argtypes = [_dp, _dp, _dp, _sz, _dp, _dp, C, C, ctypes.c_double, C, _sz, ctypes.c_double,
+                      ctypes.c_double] + tail
+        f.restype = C
         if self.kind == "port":
             f = self.lib.oracle_hem_sweep
             f.argtypes = [_dp, _dp, _sz, _dp, _sz, _dp, _dp, _sz, ctypes.c_double, _sz, _dp,
@@ -197,6 +214,9 @@ class Oracle:
             f.restype = ctypes.c_int
             f = self.lib.oracle_mhem_impedances
             f.argtypes = [_dp, _dp, _sz, _dp, _dp, _dp, _dp, C, C, ctypes.c_double, _dp, _dp]
+            f.restype = ctypes.c_int
+            f = self.lib.oracle_gpd_mhem
+            f.argtypes = [_dp, _sz, _dp, _sz, _dp, _sz, C, C, _dp]
             f.restype = ctypes.c_int
             f = self.lib.oracle_mhem_sweep
             f.argtypes = [_dp, _dp, _sz, _dp, _sz, _dp, _dp, _sz, ctypes.c_double, _sz, _dp,
@@ -344,6 +364,77 @@ class Oracle:
         eps = np.zeros(1, dtype=np.complex128)
         self._fn("alipio_soil")(_ptr(sig), _ptr(eps), sigma0, c_complex.of(s), h, g, eps_ratio)
         return complex(sig[0]), complex(eps[0])
+
+    # -- post-processing: potentials, fields, path voltage ------------------------
+    def electric_potential(self, point, elec, it, gamma, kappa, max_eval=0, req_abs=1e-6, req_rel=1e-6):
+        p = np.ascontiguousarray(point, dtype=float)
+        e = np.ascontiguousarray(elec, dtype=float)
+        it = np.ascontiguousarray(it, dtype=np.complex128)
+        args = [_ptr(p), _ptr(e), e.shape[0], _ptr(it), c_complex.of(gamma), c_complex.of(kappa), max_eval,
+                req_abs, req_rel]
+        if self.kind == "port":
+            fail = ctypes.c_int(0)
+            v = self._fn("electric_potential")(*args, ctypes.byref(fail))
+            if fail.value:
+                raise RuntimeError(f"electric_potential failed: {fail.value}")
+        else:
+            v = self._fn("electric_potential")(*args)
+        return v.value()
+
+    def magnetic_potential(self, point, elec, il, gamma, mur=1.0, max_eval=0, req_abs=1e-6, req_rel=1e-6):
+        p = np.ascontiguousarray(point, dtype=float)
+        e = np.ascontiguousarray(elec, dtype=float)
+        il = np.ascontiguousarray(il, dtype=np.complex128)
+        va = np.zeros(3, dtype=np.complex128)
+        code = self._fn("magnetic_potential")(_ptr(p), _ptr(e), e.shape[0], _ptr(il), c_complex.of(gamma), mur,
+                                              max_eval, req_abs, req_rel, _ptr(va))
+        if code:
+            raise RuntimeError(f"magnetic_potential failed: {code}")
+        return va
+
+    def electric_field(self, point, elec, il, it, gamma, s, kappa, mur=1.0, max_eval=0, req_abs=1e-6,
+                       req_rel=1e-6, ve=None):
+        """E at a point; ``ve`` (3 complex) is the array the reference adds to when |s| is 0."""
+        p = np.ascontiguousarray(point, dtype=float)
+        e = np.ascontiguousarray(elec, dtype=float)
+        il = np.ascontiguousarray(il, dtype=np.complex128)
+        it = np.ascontiguousarray(it, dtype=np.complex128)
+        ve = np.zeros(3, dtype=np.complex128) if ve is None else np.array(ve, dtype=np.complex128)
+        code = self._fn("electric_field")(_ptr(p), _ptr(e), e.shape[0], _ptr(il), _ptr(it), c_complex.of(gamma),
+                                          c_complex.of(s), mur, c_complex.of(kappa), max_eval, req_abs, req_rel,
+                                          _ptr(ve))
+        return ve, code
+
+    def voltage(self, p1, p2, elec, il, it, gamma, s, kappa, mur=1.0, max_eval=0, req_abs=1e-6, req_rel=1e-6):
+        a = np.ascontiguousarray(p1, dtype=float)
+        b = np.ascontiguousarray(p2, dtype=float)
+        e = np.ascontiguousarray(elec, dtype=float)
+        il = np.ascontiguousarray(il, dtype=np.complex128)
+        it = np.ascontiguousarray(it, dtype=np.complex128)
+        args = [_ptr(a), _ptr(b), _ptr(e), e.shape[0], _ptr(il), _ptr(it), c_complex.of(gamma), c_complex.of(s),
+                mur, c_complex.of(kappa), max_eval, req_abs, req_rel]
+        if self.kind == "port":
+            fail = ctypes.c_int(0)
+            v = self._fn("voltage")(*args, ctypes.byref(fail))
+        else:
+            v = self._fn("voltage")(*args)
+        return v.value()
+
+    def gpd_mhem(self, points, elec, it, gamma, kappa):
+        """Closed-form mHEM ground potential (np x nrhs); it is (m x nrhs)."""
+        if self.kind != "port":
+            raise NotImplementedError("the ground-potential loop belongs to an example, not the library")
+        pts = np.ascontiguousarray(points, dtype=float)
+        e = np.ascontiguousarray(elec, dtype=float)
+        it = np.asarray(it, dtype=np.complex128)
+        if it.ndim == 1:
+            it = it[:, None]
+        nrhs = it.shape[1]
+        itc = np.ascontiguousarray(it.T)          # column-major (m x nrhs)
+        out = np.zeros((pts.shape[0], nrhs), dtype=np.complex128)
+        self.lib.oracle_gpd_mhem(_ptr(pts), pts.shape[0], _ptr(e), e.shape[0], _ptr(itc), nrhs,
+                                 c_complex.of(gamma), c_complex.of(kappa), _ptr(out))
+        return out
 
     def heidler(self, t, imax, tau1, tau2, n):
         return self._fn("heidler")(t, imax, tau1, tau2, n)

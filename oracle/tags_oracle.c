@@ -821,3 +821,208 @@ int oracle_hem_sweep (const OracleElectrode *e, const OracleElectrode *img, size
     free(wg0);
     return setup_err;
 }
+
+/* ---- post-processing: potentials, fields, voltage ------------------------ */
+
+/* src/electrode.c:434-457: the scalar potential at a point, one INTG_SINGLE
+ * integral per electrode towards the point (as a receiver's middle point),
+ * times it[m] / L_m, over 4 pi kappa. No skipping of small currents. */
+double _Complex oracle_electric_potential (const double *point, const OracleElectrode *e, size_t m,
+                                           const double _Complex *it, double _Complex gamma,
+                                           double _Complex kappa, size_t max_eval, double req_abs,
+                                           double req_rel, int *failure)
+{
+    OracleElectrode pe;
+    memset(&pe, 0, sizeof(pe));
+    for (int i = 0; i < 3; i++) pe.middle_point[i] = point[i];
+    double result[2], error[2];
+    double _Complex pot = 0.0;
+    *failure = 0;
+    for (size_t k = 0; k < m; k++) {
+        int f = oracle_integral(&e[k], &pe, gamma, max_eval, req_abs, req_rel, ORACLE_INTG_SINGLE,
+                                result, error);
+        if (f) { *failure = f; return f; }
+        pot += (result[0] + I * result[1]) * it[k] / e[k].length;
+    }
+    return pot / (ORACLE_FOUR_PI * kappa);
+}
+
+/* src/electrode.c:459-493: vector potential; electrodes with |il| below
+ * DBL_EPSILON are skipped; va is overwritten. */
+int oracle_magnetic_potential (const double *point, const OracleElectrode *e, size_t m,
+                               const double _Complex *il, double _Complex gamma, double mur,
+                               size_t max_eval, double req_abs, double req_rel, double _Complex *va)
+{
+    OracleElectrode pe;
+    memset(&pe, 0, sizeof(pe));
+    double result[2], error[2];
+    for (int i = 0; i < 3; i++) {
+        pe.middle_point[i] = point[i];
+        va[i] = 0.0;
+    }
+    for (size_t k = 0; k < m; k++) {
+        if (cabs(il[k]) < DBL_EPSILON) continue;
+        double dx = e[k].end_point[0] - e[k].start_point[0];
+        double dy = e[k].end_point[1] - e[k].start_point[1];
+        double dz = e[k].end_point[2] - e[k].start_point[2];
+        int f = oracle_integral(&e[k], &pe, gamma, max_eval, req_abs, req_rel, ORACLE_INTG_SINGLE,
+                                result, error);
+        if (f) return f;
+        double _Complex pot = (result[0] + I * result[1]) * il[k] / e[k].length;
+        va[0] += pot * dx;
+        va[1] += pot * dy;
+        va[2] += pot * dz;
+    }
+    double _Complex u_4pi = mur * ORACLE_MU0 / ORACLE_FOUR_PI;
+    for (int i = 0; i < 3; i++) va[i] *= u_4pi;
+    return 0;
+}
+
+typedef struct {
+    const double *point1, *point2;
+    const OracleElectrode *e;
+    size_t m;
+    const double _Complex *il, *it;
+    double _Complex gamma, s, kappa;
+    double mur;
+    size_t max_eval;
+    double req_abs, req_rel;
+} field_data;
+
+/* src/electrode.c:495-520: (1 + gamma r) e^{-gamma r} / r^2 along (p - x)/r;
+ * r is taken before r^2 is clamped to DBL_EPSILON. */
+static int integrand_efield (unsigned ndim, const double *t, void *aux, unsigned fdim, double *fval)
+{
+    (void) ndim; (void) fdim;
+    const field_data *p = aux;
+    const OracleElectrode *el = p->e;
+    double dx[3], r2 = 0.0;
+    for (int i = 0; i < 3; i++) {
+        double x = t[0] * (el->end_point[i] - el->start_point[i]) + el->start_point[i];
+        dx[i] = p->point1[i] - x;
+        r2 += pow(dx[i], 2.0);
+    }
+    double r1 = sqrt(r2);
+    if (r2 < DBL_EPSILON) r2 = DBL_EPSILON;
+    double _Complex ef = (1 + p->gamma * r1) * cexp(-p->gamma * r1) / r2;
+    for (int i = 0; i < 3; i++) {
+        double _Complex ex = ef * dx[i] / r1;
+        fval[2 * i] = creal(ex);
+        fval[2 * i + 1] = cimag(ex);
+    }
+    return 0;
+}
+
+/* src/electrode.c:522-560: E = -s A (only when |s| > DBL_EPSILON, which
+ * overwrites ve) plus the conservative part accumulated into ve, one 1-D
+ * cubature (6 outputs, ERROR_PAIRED) per electrode with |it| >= DBL_EPSILON. */
+int oracle_electric_field (const double *point, const OracleElectrode *e, size_t m,
+                           const double _Complex *il, const double _Complex *it,
+                           double _Complex gamma, double _Complex s, double mur,
+                           double _Complex kappa, size_t max_eval, double req_abs, double req_rel,
+                           double _Complex *ve)
+{
+    if (cabs(s) > DBL_EPSILON) {
+        oracle_magnetic_potential(point, e, m, il, gamma, mur, max_eval, req_abs, req_rel, ve);
+        for (int i = 0; i < 3; i++) ve[i] *= -s;
+    }
+    field_data aux;
+    memset(&aux, 0, sizeof(aux));
+    aux.point1 = point;
+    aux.gamma = gamma;
+    const double tmin[1] = {0.0}, tmax[1] = {1.0};
+    double result[6], error[6];
+    int failure = 0;
+    for (size_t k = 0; k < m; k++) {
+        if (cabs(it[k]) < DBL_EPSILON) continue;
+        aux.e = e + k;
+        failure = hcubature(6, integrand_efield, &aux, 1, tmin, tmax, max_eval, req_abs, req_rel,
+                            ERROR_PAIRED, result, error);
+        double _Complex it_4pik = it[k] / (ORACLE_FOUR_PI * kappa);
+        for (int i = 0; i < 3; i++) ve[i] += (result[2 * i] + I * result[2 * i + 1]) * it_4pik;
+    }
+    return failure;
+}
+
+/* src/electrode.c:599-635: E at p1 + t (p2 - p1) projected on the unit
+ * direction of the path; 1 (failure) for a path shorter than DBL_EPSILON.
+ * The field starts from zero (the reference passes an uninitialised array,
+ * which electric_field overwrites whenever |s| > DBL_EPSILON). */
+static int integrand_voltage (unsigned ndim, const double *t, void *aux, unsigned fdim, double *fval)
+{
+    (void) ndim; (void) fdim;
+    const field_data *p = aux;
+    double point[3], dx[3], length = 0.0;
+    for (int i = 0; i < 3; i++) {
+        dx[i] = p->point2[i] - p->point1[i];
+        point[i] = t[0] * dx[i] + p->point1[i];
+        length += pow(dx[i], 2.0);
+    }
+    if (length < DBL_EPSILON) return 1;
+    length = sqrt(length);
+    double _Complex ve[3] = {0.0, 0.0, 0.0};
+    oracle_electric_field(point, p->e, p->m, p->il, p->it, p->gamma, p->s, p->mur, p->kappa,
+                          p->max_eval, p->req_abs, p->req_rel, ve);
+    double _Complex vc = 0.0;
+    for (int i = 0; i < 3; i++) vc += ve[i] * dx[i];
+    vc /= length;
+    fval[0] = creal(vc);
+    fval[1] = cimag(vc);
+    return 0;
+}
+
+/* src/electrode.c:637-668: the integral over t in [0, 1] of E . (p2 - p1) /
+ * |p2 - p1| (nested cubature; the result is the path voltage divided by the
+ * path length, as the reference returns it). */
+double _Complex oracle_voltage (const double *point1, const double *point2, const OracleElectrode *e,
+                                size_t m, const double _Complex *il, const double _Complex *it,
+                                double _Complex gamma, double _Complex s, double mur,
+                                double _Complex kappa, size_t max_eval, double req_abs, double req_rel,
+                                int *failure)
+{
+    field_data aux;
+    memset(&aux, 0, sizeof(aux));
+    aux.point1 = point1;
+    aux.point2 = point2;
+    aux.e = e;
+    aux.m = m;
+    aux.il = il;
+    aux.it = it;
+    aux.gamma = gamma;
+    aux.s = s;
+    aux.mur = mur;
+    aux.kappa = kappa;
+    aux.max_eval = max_eval;
+    aux.req_abs = req_abs;
+    aux.req_rel = req_rel;
+    const double tmin[1] = {0.0}, tmax[1] = {1.0};
+    double result[2] = {0.0, 0.0}, error[2];
+    *failure = hcubature(2, integrand_voltage, &aux, 1, tmin, tmax, max_eval, req_abs, req_rel,
+                         ERROR_PAIRED, result, error);
+    return result[0] + I * result[1];
+}
+
+/* Ground potential by the closed-form mHEM loop of
+ * examples/visacro57emc01.c:406-430: for each point p and electrode m,
+ * e^{-gamma rbar} log((r1 + r2 + L) / (r1 + r2 - L)) / L with rbar, r1, r2 the
+ * distances from p to the midpoint and the ends, times it[m] / (4 pi kappa).
+ * it holds the transversal currents already multiplied by (1 + ref_t) and is
+ * laid out (ne x nrhs) column-major; gpd[p * nrhs + k]. */
+int oracle_gpd_mhem (const double *points, size_t np, const OracleElectrode *e, size_t m,
+                     const double _Complex *it, size_t nrhs, double _Complex gamma,
+                     double _Complex kappa, double _Complex *gpd)
+{
+    const double _Complex one_4pik = 1.0 / (ORACLE_FOUR_PI * kappa);
+    for (size_t p = 0; p < np; p++) {
+        for (size_t k = 0; k < nrhs; k++) gpd[p * nrhs + k] = 0.0;
+        for (size_t q = 0; q < m; q++) {
+            double rbar = oracle_vector_length(points + p * 3, e[q].middle_point);
+            double r1 = oracle_vector_length(points + p * 3, e[q].start_point);
+            double r2 = oracle_vector_length(points + p * 3, e[q].end_point);
+            double r0 = (r1 + r2 + e[q].length) / (r1 + r2 - e[q].length);
+            double _Complex exp_gr = cexp(-gamma * rbar) * log(r0) / e[q].length;
+            for (size_t k = 0; k < nrhs; k++) gpd[p * nrhs + k] += one_4pik * it[q + m * k] * exp_gr;
+        }
+    }
+    return 0;
+}

@@ -8,6 +8,7 @@ that the quadrature method does not limit the comparison. Needs the reference
 sources at build time; the fixtures it writes are what travels.
 
     python tests/golden/make_golden.py            # all fixtures
+    python tests/golden/make_golden.py fields     # one of them
 """
 from __future__ import annotations
 
@@ -27,6 +28,7 @@ sys.path.insert(0, ROOT)
 # examples/three_grids.c:956-960 with the standard 1.2/50 constants)
 I0, K12, ALPHA, BETA = 1000.0, 1.037, 1.0 / 68.2e-6, 1.0 / 0.405e-6
 TIGHT = 1e-11
+FABS = 1e-13
 
 
 def ref():
@@ -181,11 +183,79 @@ def make_incidence():
     np.savez_compressed(os.path.join(HERE, "incidence.npz"), **out)
 
 
+def field_case():
+    """Geometry, currents and observation points of the post-processing
+    fixture: a 2 x 2-mesh grid at 0.5 m depth with a 3-segment rod at one
+    corner, seeded complex currents for two injections and three samples, and
+    points from far away to 1 cm off an electrode (and on a rod's axis below
+    its tip)."""
+    import __graft_entry__ as g
+    from oracle import oracle as O
+    pkg = g.load_package()
+    grid, _ = pkg.electrode_grid(3, 3, 4.0, 4.0, 2, 2, 6e-3, -0.5)
+    rod, _ = pkg.segment_electrode([0.0, 0.0, -0.5], [0.0, 0.0, -2.0], 3, 8e-3)
+    elec = np.vstack([grid, rod])
+    m = elec.shape[0]
+    rng = np.random.default_rng(11)
+    freq = np.array([60.0, 2.0e5, 8.0e6])
+    s = 2j * np.pi * freq + np.array([0.0, 3.0e3, 4.0e4])
+    kappa = 1.0 / 300.0 + s * 12.0 * O.EPS0
+    gamma = np.array([O.medium(sk, kk)[0] for sk, kk in zip(s, kappa)])
+    nrhs = 2
+    il = rng.normal(size=(3, nrhs, m)) + 1j * rng.normal(size=(3, nrhs, m))
+    it = rng.normal(size=(3, nrhs, m)) + 1j * rng.normal(size=(3, nrhs, m))
+    il[:, 1, 5] = 0.0          # skipped electrodes (|I| < DBL_EPSILON)
+    it[:, 1, 7] = 1e-17
+    points = np.array([[1.0, 1.0, 0.0], [2.0, 0.5, 0.0], [-3.0, 7.0, 0.0], [25.0, -10.0, 0.0],
+                       [0.7, 2.0, -0.49], [1.0, 0.01, -0.5], [0.0, 0.0, -2.6], [4.3, 4.1, -0.3]])
+    paths = np.array([[-1.0, -1.0, 0.0, 1.0, 1.0, 0.0], [2.0, 2.0, 0.0, 6.0, 2.0, 0.0],
+                      [0.5, 3.5, 0.0, 0.5, 3.5, -0.3]])
+    return elec, s, kappa, gamma, il, it, points, paths
+
+
+def make_fields():
+    """electric_potential, magnetic_potential, electric_field (|s| > 0 and
+    s = 0 with a nonzero ve to add to) and voltage from the reference itself.
+    A small absolute tolerance (1e-13 on integrals of order one, 1e-11 on the
+    nested voltage) ends the subdivision of field components that vanish by
+    symmetry, which a purely relative request never satisfies."""
+    R = ref()
+    elec, s, kappa, gamma, il, it, points, paths = field_case()
+    ns, nrhs = il.shape[0], il.shape[1]
+    P, NL = points.shape[0], paths.shape[0]
+    pot = np.zeros((ns, P, nrhs), np.complex128)
+    vec = np.zeros((ns, P, nrhs, 3), np.complex128)
+    ef = np.zeros((ns, P, nrhs, 3), np.complex128)
+    ef0 = np.zeros((ns, P, nrhs, 3), np.complex128)
+    ve0 = np.array([1.0 + 2.0j, -3.0, 0.5j])
+    volt = np.zeros((ns, NL, nrhs), np.complex128)
+    for k in range(ns):
+        for r in range(nrhs):
+            for p in range(P):
+                pot[k, p, r] = R.electric_potential(points[p], elec, it[k, r], gamma[k], kappa[k], 0, FABS, TIGHT)
+                vec[k, p, r] = R.magnetic_potential(points[p], elec, il[k, r], gamma[k], 1.0, 0, FABS, TIGHT)
+                ef[k, p, r], _ = R.electric_field(points[p], elec, il[k, r], it[k, r], gamma[k], s[k], kappa[k],
+                                                  1.0, 0, FABS, TIGHT)
+                ef0[k, p, r], _ = R.electric_field(points[p], elec, il[k, r], it[k, r], gamma[k], 0.0, kappa[k],
+                                                   1.0, 0, FABS, TIGHT, ve=ve0)
+            for l in range(NL):
+                volt[k, l, r] = R.voltage(paths[l, :3], paths[l, 3:], elec, il[k, r], it[k, r], gamma[k], s[k],
+                                          kappa[k], 1.0, 0, 1e-11, 1e-10)
+    np.savez_compressed(os.path.join(HERE, "fields.npz"), elec=elec, s=s, kappa=kappa, gamma=gamma, il=il, it=it,
+                        points=points, paths=paths, pot=pot, vecpot=vec, efield=ef, efield_s0=ef0, ve0=ve0,
+                        voltage=volt)
+
+
 if __name__ == "__main__":
     from oracle import oracle as O
     O.build(ref=True)
+    if len(sys.argv) > 1:
+        for name in sys.argv[1:]:
+            globals()["make_" + name]()
+        sys.exit(0)
     make_nlt()
     make_incidence()
+    make_fields()
     make_rod()
     make_grid2()
     print("fixtures written to", HERE)

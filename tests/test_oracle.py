@@ -342,3 +342,105 @@ def test_mhem_kernel_is_exact_static_integral(port, pkg):
 def test_grid_counts(pkg, grid, mn):
     vx, vy, lx, ly, nx, ny = grid
     assert (pkg.number_segments(vx, vy, nx, ny), pkg.number_nodes(vx, vy, nx, ny)) == mn
+
+
+# ---- post-processing: potentials, fields, path voltage -----------------------
+
+def test_port_equals_reference_fields(port, ref):
+    """The restatement of src/electrode.c:434-668 against the reference's own
+    functions (same cubature, same expression order: equal to rounding)."""
+    d = golden("fields.npz")
+    e = d["elec"]
+    for k in (0, 2):
+        for p in (0, 5, 6):
+            pt = d["points"][p]
+            a = port.electric_potential(pt, e, d["it"][k, 0], d["gamma"][k], d["kappa"][k], 0, 1e-13, 1e-11)
+            b = ref.electric_potential(pt, e, d["it"][k, 0], d["gamma"][k], d["kappa"][k], 0, 1e-13, 1e-11)
+            assert a == b
+            va = port.magnetic_potential(pt, e, d["il"][k, 1], d["gamma"][k], 1.0, 0, 1e-13, 1e-11)
+            vb = ref.magnetic_potential(pt, e, d["il"][k, 1], d["gamma"][k], 1.0, 0, 1e-13, 1e-11)
+            assert np.array_equal(va, vb)
+            for sv, ve in ((d["s"][k], None), (0.0, d["ve0"])):
+                fa, ca = port.electric_field(pt, e, d["il"][k, 1], d["it"][k, 1], d["gamma"][k], sv, d["kappa"][k],
+                                             1.0, 0, 1e-13, 1e-11, ve=ve)
+                fb, cb = ref.electric_field(pt, e, d["il"][k, 1], d["it"][k, 1], d["gamma"][k], sv, d["kappa"][k],
+                                            1.0, 0, 1e-13, 1e-11, ve=ve)
+                assert ca == cb and np.array_equal(fa, fb)
+        pa = d["paths"][0]
+        a = port.voltage(pa[:3], pa[3:], e, d["il"][k, 0], d["it"][k, 0], d["gamma"][k], d["s"][k], d["kappa"][k],
+                         1.0, 0, 1e-11, 1e-9)
+        b = ref.voltage(pa[:3], pa[3:], e, d["il"][k, 0], d["it"][k, 0], d["gamma"][k], d["s"][k], d["kappa"][k],
+                        1.0, 0, 1e-11, 1e-9)
+        assert a == b
+
+
+def test_golden_fields(port):
+    """The restatement reproduces the reference's fixture (tests/golden/fields.npz)."""
+    d = golden("fields.npz")
+    e = d["elec"]
+    for k in range(3):
+        for r in range(2):
+            for p in range(d["points"].shape[0]):
+                u = port.electric_potential(d["points"][p], e, d["it"][k, r], d["gamma"][k], d["kappa"][k], 0, 1e-13,
+                                            1e-11)
+                assert abs(u - d["pot"][k, p, r]) <= 1e-12 * abs(d["pot"][k, p, r])
+            l = 1
+            v = port.voltage(d["paths"][l, :3], d["paths"][l, 3:], e, d["il"][k, r], d["it"][k, r], d["gamma"][k],
+                             d["s"][k], d["kappa"][k], 1.0, 0, 1e-11, 1e-10)
+            assert abs(v - d["voltage"][k, l, r]) <= 1e-12 * abs(d["voltage"][k, l, r])
+
+
+def test_voltage_closed_form_equals_nested_cubature(port, orc_mod):
+    """The identity the GPU path voltage rests on: the reference's nested
+    integral of E . dl / |dl| over t equals (u(p1) - u(p2)) / |p2 - p1| (u the
+    field-convention potential) minus s mu / 4pi sum_m il_m (D_m . t_hat)
+    JJ_m, JJ_m the double integral of e^{-gamma r}/r between the path and
+    electrode m (the INTG_DOUBLE pair integral)."""
+    O = orc_mod
+    d = golden("fields.npz")
+    e = d["elec"]
+    for k in (1, 2):
+        for l in range(d["paths"].shape[0]):
+            p1, p2 = d["paths"][l, :3], d["paths"][l, 3:]
+            lp = float(np.linalg.norm(p2 - p1))
+            th = (p2 - p1) / lp
+            line = np.zeros(11)
+            line[0:3], line[3:6], line[6:9], line[9] = p1, p2, (p1 + p2) / 2, lp
+            it = d["it"][k, 1].copy()
+            it[np.abs(it) < np.finfo(float).eps] = 0.0        # the field skips these
+            u1 = port.electric_potential(p1, e, it, d["gamma"][k], d["kappa"][k], 0, 1e-14, 1e-12)
+            u2 = port.electric_potential(p2, e, it, d["gamma"][k], d["kappa"][k], 0, 1e-14, 1e-12)
+            acc = 0.0
+            for q in range(e.shape[0]):
+                il = d["il"][k, 1, q]
+                if abs(il) < np.finfo(float).eps:
+                    continue
+                jj, _, code = port.integral(e[q], line, d["gamma"][k], 0, 1e-14, 1e-12, O.INTG_DOUBLE)
+                assert code == 0
+                acc += il * np.dot(e[q, 3:6] - e[q, 0:3], th) * jj / (lp * e[q, 9])
+            v = (u1 - u2) / lp - d["s"][k] * O.MU0 / (4 * np.pi) * acc
+            assert abs(v - d["voltage"][k, l, 1]) <= 1e-9 * abs(d["voltage"][k, l, 1])
+
+
+def test_gpd_mhem_restates_the_example_loop(port, orc_mod):
+    """examples/visacro57emc01.c:406-430 written out in numpy against the
+    oracle's C restatement, and the mHEM closed form close to the full
+    potential far from the grid."""
+    O = orc_mod
+    d = golden("fields.npz")
+    e = d["elec"]
+    pts = np.array([[1.0, 1.0, 0.0], [30.0, 20.0, 0.0]])
+    k = 1
+    it = d["it"][k].T                                          # (m, nrhs)
+    want = np.zeros((2, 2), np.complex128)
+    for p in range(2):
+        for q in range(e.shape[0]):
+            rbar = np.sqrt(np.sum((pts[p] - e[q, 6:9]) ** 2))
+            r1 = np.sqrt(np.sum((pts[p] - e[q, 0:3]) ** 2))
+            r2 = np.sqrt(np.sum((pts[p] - e[q, 3:6]) ** 2))
+            r0 = (r1 + r2 + e[q, 9]) / (r1 + r2 - e[q, 9])
+            want[p] += it[q] * np.exp(-d["gamma"][k] * rbar) * np.log(r0) / e[q, 9] / (O.FOUR_PI * d["kappa"][k])
+    got = port.gpd_mhem(pts, e, it, d["gamma"][k], d["kappa"][k])
+    assert np.max(np.abs(got - want) / np.abs(want)) <= 1e-13
+    full = port.electric_potential(pts[1], e, it[:, 0], d["gamma"][k], d["kappa"][k], 0, 1e-13, 1e-11)
+    assert abs(got[1, 0] - full) <= 2e-3 * abs(full)
