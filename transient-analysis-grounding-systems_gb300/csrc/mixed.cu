@@ -334,10 +334,11 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
 }
 
 // After a refinement step: per sample, stop once the correction is below
-// 1e-9 |x| (each step contracts the error by about kappa * eps_factor, a few
-// 1e-3 here, so the error left is ~1e-12 |x|, far under the ~1e-7 of the
-// FP32 impedance fill) or once it stops shrinking (accepted when the backward
-// error is below 1e-12); NaN goes to the fallback. One CTA. Sets the continue
+// 1e-9 |x|, or once the correction times the measured contraction predicts an
+// error under 1e-8 |x| (each step contracts the error by about kappa *
+// eps_factor, a few 1e-3 here; the FP32 impedance fill itself is good to
+// ~1e-7), or once it stops shrinking (accepted when the backward error is
+// below 1e-12); NaN goes to the fallback. One CTA. Sets the continue
 // flag and, inside a graph, the while-node condition.
 __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ norms, int nb, int max_steps, IrState s,
                                                     cudaGraphConditionalHandle cond, int set_cond) {
@@ -351,6 +352,14 @@ __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ n
         s.berr[q] = be;
         if (!(dx == dx) || !(xn == xn)) { s.active[q] = 0; continue; }
         if (dx <= 1e-9 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
+        // contraction estimate rho = dx_k / dx_{k-1} (step 0 starts from x =
+        // 0, so dx_0 = |x_0| and rho_1 is already one): the error left after
+        // this correction is about rho dx_k; stop when four times that is
+        // below 1e-8 |x|, a decade under the FP32 fill's own error
+        if (step >= 1) {
+            const double rho = dx / s.prev_dx[q];
+            if (rho <= 0.25 && 4.0 * rho * dx <= 1e-8 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
+        }
         if (step >= 2 && dx > 0.5 * s.prev_dx[q]) {
             s.conv[q] = be <= 1e-12;
             s.active[q] = 0;
