@@ -15,6 +15,10 @@
  *   calculate_yla_ytb      replaces src/linalg.c:261-300    (decl src/linalg.h:145-149)
  *   fill_impedance_adm2    replaces src/linalg.c:302-325    (decl src/linalg.h:169-173)
  *   solve_admittance       replaces src/linalg.c:327-350    (decl src/linalg.h:192-193)
+ *   electric_potential     replaces src/electrode.c:434-457 (decl src/electrode.h:333-337)
+ *   magnetic_potential     replaces src/electrode.c:459-493 (decl src/electrode.h:355-360)
+ *   electric_field         replaces src/electrode.c:522-560 (decl src/electrode.h:398-403)
+ *   voltage                replaces src/electrode.c:637-668 (decl src/electrode.h:440-446)
  * and host-side helpers of the reference (no device work):
  *   electrodes_file        src/electrode.c:45-80    (decl src/electrode.h:127-128)
  *   nodes_file             src/electrode.c:82-101   (decl src/electrode.h:140-141)
@@ -159,6 +163,73 @@ int inv_laplace_trans (double *f, tags_cdouble *g, tags_cdouble *s, double tmax,
  * flags: TAGS_RUN_DEVICE_PTRS for device pointers (declared below). */
 int tags_inv_laplace_batch (double *f, const tags_cdouble *g, const tags_cdouble *s, double tmax, size_t nt,
                             size_t nseries, int filter, int flags);
+
+/* ---- post-processing: potentials, fields, path voltage --------------------- */
+/* The tolerance arguments (max_eval, req_abs_error, req_rel_error) are
+ * accepted and unused: the GPU rules integrate to ~1e-12 relative. A point on
+ * an electrode (divergent integral) gives NaN. */
+
+/* Scalar potential to remote earth at `point` from the transversal currents
+ * it (num_electrodes): sum it[m] \int e^{-gamma r}/r dt / (4 pi kappa). */
+tags_cdouble electric_potential (const double *point, const Electrode *electrodes, size_t num_electrodes,
+                                 const tags_cdouble *it, tags_cdouble gamma, tags_cdouble kappa, size_t max_eval,
+                                 double req_abs_error, double req_rel_error);
+
+/* Magnetic vector potential (3 components, overwritten) from the
+ * longitudinal currents il; electrodes with |il| < DBL_EPSILON are skipped. */
+int magnetic_potential (const double *point, const Electrode *electrodes, size_t num_electrodes,
+                        const tags_cdouble *il, tags_cdouble gamma, double mur, size_t max_eval,
+                        double req_abs_error, double req_rel_error, tags_cdouble *va);
+
+/* Electric field -grad u - s A. As in the reference, ve is overwritten by
+ * -s A when |s| > DBL_EPSILON and the conservative part is then added; with
+ * |s| <= DBL_EPSILON only the conservative part is added to ve. */
+int electric_field (const double *point, const Electrode *electrodes, size_t num_electrodes,
+                    const tags_cdouble *il, const tags_cdouble *it, tags_cdouble gamma, tags_cdouble s, double mur,
+                    tags_cdouble kappa, size_t max_eval, double req_abs_error, double req_rel_error,
+                    tags_cdouble *ve);
+
+/* The reference's path voltage from point1 to point2: the integral over t in
+ * [0, 1] of E . (point2 - point1) / |point2 - point1| (the voltage along the
+ * straight path divided by its length). */
+tags_cdouble voltage (const double *point1, const double *point2, const Electrode *electrodes,
+                      size_t num_electrodes, const tags_cdouble *il, const tags_cdouble *it, tags_cdouble gamma,
+                      tags_cdouble s, double mur, tags_cdouble kappa, size_t max_eval, double req_abs_error,
+                      double req_rel_error);
+
+/* Batched post-processing (no counterpart function in the reference; it
+ * replaces the per-point, per-sample loops of examples/visacro57emc01.c:
+ * 406-460). Currents il/it are [sample][injection][electrode] (each sample's
+ * ne x nrhs column-major block, samples one after another); gamma and kappa
+ * per sample.
+ *   pot     [sample][point][injection]      electric_potential
+ *   vecpot  [sample][point][injection][3]   magnetic_potential
+ *   efield  [sample][point][injection][3]   conservative field -grad u (the
+ *           full field is efield - s vecpot), as electric_field with s = 0
+ * Any output may be NULL. Returns 0, TAGS_E_GEOMETRY when a point lies on an
+ * electrode (its outputs are NaN), or another TAGS_E_* code. */
+int tags_fields_batch (const double *points, size_t num_points, const Electrode *electrodes, size_t num_electrodes,
+                       const tags_cdouble *il, const tags_cdouble *it, size_t nrhs, size_t nsamples,
+                       const tags_cdouble *gamma, const tags_cdouble *kappa, double mur, tags_cdouble *pot,
+                       tags_cdouble *vecpot, tags_cdouble *efield);
+
+/* Ground potential by the examples' closed-form mHEM expression
+ * (examples/visacro57emc01.c:406-430): gpd[sample][point][injection] = sum_m
+ * it[m] e^{-gamma rbar} log((r1 + r2 + L) / (r1 + r2 - L)) / (L 4 pi kappa),
+ * rbar, r1, r2 the distances from the point to the midpoint and the ends of
+ * electrode m. it as above, already multiplied by (1 + ref_t) where the
+ * caller wants the images' effect at ground level (as the example does). */
+int tags_gpd_mhem_batch (const double *points, size_t num_points, const Electrode *electrodes,
+                         size_t num_electrodes, const tags_cdouble *it, size_t nrhs, size_t nsamples,
+                         const tags_cdouble *gamma, const tags_cdouble *kappa, tags_cdouble *gpd);
+
+/* Path voltages (the reference's voltage) for paths[6 * l] = (x1, y1, z1, x2,
+ * y2, z2): v[sample][path][injection]; s per sample. NaN for a path whose
+ * squared length is below DBL_EPSILON. */
+int tags_voltage_batch (const double *paths, size_t num_paths, const Electrode *electrodes, size_t num_electrodes,
+                        const tags_cdouble *il, const tags_cdouble *it, size_t nrhs, size_t nsamples,
+                        const tags_cdouble *gamma, const tags_cdouble *s, const tags_cdouble *kappa, double mur,
+                        tags_cdouble *v);
 
 /* ---- Part 2: batched extension -------------------------------------------- */
 

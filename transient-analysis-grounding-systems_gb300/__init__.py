@@ -57,6 +57,8 @@ EXPORTS = (
     "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
+    "tags_gpd_mhem_batch", "tags_voltage_batch",
     "tags_gpu_set_quiet",
 )
 
@@ -135,6 +137,16 @@ def lib() -> ctypes.CDLL:
             L.tags_inv_laplace_batch.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int, ctypes.c_int]
             L.tags_plan_tune.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int,
                                          ctypes.POINTER(TuneResult)]
+            d = ctypes.c_double
+            L.electric_potential.argtypes = [_vp, _vp, _sz, _vp, C, C, _sz, d, d]
+            L.electric_potential.restype = C
+            L.magnetic_potential.argtypes = [_vp, _vp, _sz, _vp, C, d, _sz, d, d, _vp]
+            L.electric_field.argtypes = [_vp, _vp, _sz, _vp, _vp, C, C, d, C, _sz, d, d, _vp]
+            L.voltage.argtypes = [_vp, _vp, _vp, _sz, _vp, _vp, C, C, d, C, _sz, d, d]
+            L.voltage.restype = C
+            L.tags_fields_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, _sz, _vp, _vp, d, _vp, _vp, _vp]
+            L.tags_gpd_mhem_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _sz, _sz, _vp, _vp, _vp]
+            L.tags_voltage_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, _sz, _vp, _vp, _vp, d, _vp]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
@@ -144,7 +156,9 @@ def lib() -> ctypes.CDLL:
                          "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
                          "inv_laplace_trans",
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
-                         "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch"):
+                         "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
+                         "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
+                         "tags_voltage_batch"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -412,6 +426,142 @@ def inv_laplace_batch(g, s, tmax: float, nt: int, filt: int = FILTER_NONE) -> np
     f = np.zeros((nt, nser))
     _ret(lib().tags_inv_laplace_batch(_addr(f), _addr(g), _addr(s), float(tmax), int(nt), int(nser), int(filt), 0))
     return f
+
+
+# post-processing: potentials, fields and path voltages (src/electrode.c:434-668)
+
+def _currents(c, ns: int, m: int, name: str) -> np.ndarray:
+    """Currents as [sample][injection][electrode] (complex128, contiguous) from
+    an array shaped (m,), (ns, m) or (ns, nrhs, m)."""
+    a = np.asarray(c, dtype=np.complex128)
+    if a.ndim == 1:
+        a = a[None, None, :]
+    elif a.ndim == 2:
+        a = a[:, None, :]
+    if a.ndim != 3 or a.shape[0] != ns or a.shape[2] != m:
+        raise ValueError(f"{name} must be (m,), (ns, m) or (ns, nrhs, m) with ns = {ns}, m = {m}")
+    return np.ascontiguousarray(a)
+
+
+def _per_sample(v, ns: int) -> np.ndarray:
+    return np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.complex128), (ns,)))
+
+
+def fields_batch(points, electrodes, il, it, gamma, kappa, mur: float = 1.0, want=("pot", "vecpot", "efield")):
+    """Potential, vector potential and conservative field at many points for
+    many samples and injections (tags_fields_batch). gamma/kappa: per sample
+    (ns,); il/it: (ns, nrhs, m) (or (ns, m), or (m,) for one sample). Returns a
+    dict with pot (ns, P, nrhs), vecpot and efield (ns, P, nrhs, 3) and the
+    return code under "status" (0 or E_GEOMETRY); the full field is efield -
+    s vecpot."""
+    pts = np.ascontiguousarray(np.atleast_2d(points), dtype=np.float64)
+    e = _elec(electrodes)
+    g = np.atleast_1d(np.asarray(gamma, dtype=np.complex128))
+    ns, m, P = g.shape[0], e.shape[0], pts.shape[0]
+    g = _per_sample(g, ns)
+    k = _per_sample(kappa, ns)
+    itc = _currents(it, ns, m, "it")
+    ilc = _currents(il, ns, m, "il")
+    R = itc.shape[1]
+    if ilc.shape[1] != R:
+        raise ValueError("il and it need the same number of injections")
+    out = {}
+    pot = np.zeros((ns, P, R), np.complex128) if "pot" in want else None
+    vec = np.zeros((ns, P, R, 3), np.complex128) if "vecpot" in want else None
+    ef = np.zeros((ns, P, R, 3), np.complex128) if "efield" in want else None
+    rc = lib().tags_fields_batch(_addr(pts), P, _addr(e), m, _addr(ilc), _addr(itc), R, ns, _addr(g), _addr(k),
+                                 float(mur), _addr(pot) if pot is not None else None,
+                                 _addr(vec) if vec is not None else None, _addr(ef) if ef is not None else None)
+    if rc not in (0, E_GEOMETRY):
+        _ret(rc)
+    for name, arr in (("pot", pot), ("vecpot", vec), ("efield", ef)):
+        if arr is not None:
+            out[name] = arr
+    out["status"] = rc
+    return out
+
+
+def gpd_mhem_batch(points, electrodes, it, gamma, kappa) -> np.ndarray:
+    """Closed-form mHEM ground potential (ns, P, nrhs) (tags_gpd_mhem_batch);
+    it (ns, nrhs, m) already multiplied by (1 + ref_t) where wanted."""
+    pts = np.ascontiguousarray(np.atleast_2d(points), dtype=np.float64)
+    e = _elec(electrodes)
+    g = np.atleast_1d(np.asarray(gamma, dtype=np.complex128))
+    ns, m, P = g.shape[0], e.shape[0], pts.shape[0]
+    g = _per_sample(g, ns)
+    k = _per_sample(kappa, ns)
+    itc = _currents(it, ns, m, "it")
+    R = itc.shape[1]
+    out = np.zeros((ns, P, R), np.complex128)
+    _ret(lib().tags_gpd_mhem_batch(_addr(pts), P, _addr(e), m, _addr(itc), R, ns, _addr(g), _addr(k), _addr(out)))
+    return out
+
+
+def voltage_batch(paths, electrodes, il, it, gamma, s, kappa, mur: float = 1.0) -> np.ndarray:
+    """The reference's path voltage for paths (L, 6) = (p1, p2), every sample
+    and injection: (ns, L, nrhs) (tags_voltage_batch)."""
+    pa = np.ascontiguousarray(np.atleast_2d(paths), dtype=np.float64)
+    if pa.shape[1] != 6:
+        raise ValueError("paths must be (L, 6)")
+    e = _elec(electrodes)
+    g = np.atleast_1d(np.asarray(gamma, dtype=np.complex128))
+    ns, m, NL = g.shape[0], e.shape[0], pa.shape[0]
+    g = _per_sample(g, ns)
+    sv = _per_sample(s, ns)
+    k = _per_sample(kappa, ns)
+    itc = _currents(it, ns, m, "it")
+    ilc = _currents(il, ns, m, "il")
+    R = itc.shape[1]
+    out = np.zeros((ns, NL, R), np.complex128)
+    rc = lib().tags_voltage_batch(_addr(pa), NL, _addr(e), m, _addr(ilc), _addr(itc), R, ns, _addr(g), _addr(sv),
+                                  _addr(k), float(mur), _addr(out))
+    if rc not in (0, E_GEOMETRY):
+        _ret(rc)
+    return out
+
+
+def electric_potential(point, electrodes, it, gamma, kappa) -> complex:
+    """Drop-in electric_potential (src/electrode.c:434-457) for one point."""
+    p = np.ascontiguousarray(point, dtype=np.float64)
+    e = _elec(electrodes)
+    itc = np.ascontiguousarray(it, dtype=np.complex128)
+    r = lib().electric_potential(_addr(p), _addr(e), e.shape[0], _addr(itc), c_complex.of(gamma),
+                                 c_complex.of(kappa), 0, 0.0, 0.0)
+    return complex(r.re, r.im)
+
+
+def magnetic_potential(point, electrodes, il, gamma, mur: float = 1.0) -> np.ndarray:
+    p = np.ascontiguousarray(point, dtype=np.float64)
+    e = _elec(electrodes)
+    ilc = np.ascontiguousarray(il, dtype=np.complex128)
+    va = np.zeros(3, np.complex128)
+    _ret(lib().magnetic_potential(_addr(p), _addr(e), e.shape[0], _addr(ilc), c_complex.of(gamma), float(mur), 0,
+                                  0.0, 0.0, _addr(va)))
+    return va
+
+
+def electric_field(point, electrodes, il, it, gamma, s, kappa, mur: float = 1.0, ve=None) -> np.ndarray:
+    """Drop-in electric_field: returns ve after the call (overwritten when |s|
+    > DBL_EPSILON, added to otherwise, as the reference)."""
+    p = np.ascontiguousarray(point, dtype=np.float64)
+    e = _elec(electrodes)
+    ilc = np.ascontiguousarray(il, dtype=np.complex128)
+    itc = np.ascontiguousarray(it, dtype=np.complex128)
+    out = np.zeros(3, np.complex128) if ve is None else np.array(ve, dtype=np.complex128)
+    _ret(lib().electric_field(_addr(p), _addr(e), e.shape[0], _addr(ilc), _addr(itc), c_complex.of(gamma),
+                              c_complex.of(s), float(mur), c_complex.of(kappa), 0, 0.0, 0.0, _addr(out)))
+    return out
+
+
+def voltage(p1, p2, electrodes, il, it, gamma, s, kappa, mur: float = 1.0) -> complex:
+    a = np.ascontiguousarray(p1, dtype=np.float64)
+    b = np.ascontiguousarray(p2, dtype=np.float64)
+    e = _elec(electrodes)
+    ilc = np.ascontiguousarray(il, dtype=np.complex128)
+    itc = np.ascontiguousarray(it, dtype=np.complex128)
+    r = lib().voltage(_addr(a), _addr(b), _addr(e), e.shape[0], _addr(ilc), _addr(itc), c_complex.of(gamma),
+                      c_complex.of(s), float(mur), c_complex.of(kappa), 0, 0.0, 0.0)
+    return complex(r.re, r.im)
 
 
 # nodal admittance formulation (src/linalg.c:142-350), used by the reference's mHEM examples

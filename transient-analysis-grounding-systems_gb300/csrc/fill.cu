@@ -354,6 +354,29 @@ __global__ void __launch_bounds__(128) k_fill_fp64(const double* __restrict__ el
     }
 }
 
+// Path/electrode double integrals for the path voltage: thread per
+// (electrode, path), grid.y over samples; jj[(smp * npaths + l) * m + e] =
+// \int_0^1 \int_0^1 e^{-gamma r}/r (the pair rule above, tight table).
+__global__ void __launch_bounds__(128) k_path_pairs(const double* __restrict__ elec, int m,
+                                                    const double* __restrict__ paths, int npaths,
+                                                    const SampleCoef* __restrict__ coef, double2* __restrict__ jj,
+                                                    int* status) {
+    __shared__ double sx[GL_TOTAL], sw[GL_TOTAL];
+    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) { sx[t] = g_glx[t]; sw[t] = g_glw[t]; }
+    __syncthreads();
+    GLTab gl{sx, sw};
+    const long long n = (long long)m * npaths;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int smp = blockIdx.y;
+    if (idx >= n) return;
+    const int e = (int)(idx % m), l = (int)(idx / m);
+    Seg S, R;
+    ld_seg(paths + 11LL * l, S);
+    ld_seg(elec + 11LL * e, R);
+    const double2 j = pair_integral(S, R, coef[smp].gamma, TAGS_INTG_DOUBLE, true, gl, status);
+    jj[((long long)smp * npaths + l) * m + e] = cscale(j, 1.0 / (S.len * R.len));
+}
+
 // ---- mixed form: plan-time pair classification + FP32 regular-pair fill --------
 
 // Pair code (geometry only, computed once per plan):
@@ -701,8 +724,10 @@ __global__ void k_seg_dirs(const double* __restrict__ elec, const double* __rest
     }
 }
 
+}  // namespace
+
 // Gauss-Legendre nodes/weights by Newton iteration on P_q (host side).
-void gauss_legendre(int q, double* x, double* w) {
+void tags_gauss_legendre(int q, double* x, double* w) {
     for (int i = 0; i < q; ++i) {
         double z = cos(TAGS_PI * (i + 0.75) / (q + 0.5)), dp = 1.0;
         for (int it = 0; it < 100; ++it) {
@@ -732,11 +757,10 @@ void gauss_legendre(int q, double* x, double* w) {
     }
 }
 
-}  // namespace
 
 int tags_fill_tables_init() {
     static double hx[GL_TOTAL], hw[GL_TOTAL];
-    for (int q = 1; q <= QMAX; ++q) gauss_legendre(q, hx + q * (q - 1) / 2, hw + q * (q - 1) / 2);
+    for (int q = 1; q <= QMAX; ++q) tags_gauss_legendre(q, hx + q * (q - 1) / 2, hw + q * (q - 1) / 2);
     TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glx, hx, sizeof(hx)));
     TAGS_CUDA_OK(cudaMemcpyToSymbol(g_glw, hw, sizeof(hw)));
     static float fx[GL_MIX], fw[GL_MIX];
@@ -985,6 +1009,19 @@ int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, cons
     int pf = tags_prof_begin(TAGS_PROF_FILL_FP64, st);
     k_fill_fp64<<<grid, 128, 0, st>>>(d_elec, d_img, m, d_coef, nsamp, out, mode, itype, tight, d_status);
     tags_prof_end(TAGS_PROF_FILL_FP64, pf, st, 0.0, 0.0);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    return 0;
+}
+
+int tags_launch_path_pairs(const double* d_elec, int m, const double* d_paths, int npaths, const SampleCoef* d_coef,
+                           int nsamp, double2* d_jj, int* d_status, cudaStream_t st) {
+    if (m <= 0 || npaths <= 0 || nsamp <= 0) return 0;
+    if (nsamp > 65535) return tags_fail_cuda(cudaErrorInvalidValue, "path_pairs: more than 65535 samples", __FILE__,
+                                             __LINE__);
+    const long long n = (long long)m * npaths;
+    k_path_pairs<<<dim3((unsigned)((n + 127) / 128), (unsigned)nsamp), 128, 0, st>>>(d_elec, m, d_paths, npaths,
+                                                                                       d_coef, d_jj, d_status);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

@@ -56,6 +56,14 @@ int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, cons
                           int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
                           cudaStream_t st);
 
+// Double integrals of e^{-gamma r}/r over [0,1]^2 between each path (a
+// segment record with radius 0) and each electrode, for every sample:
+// jj[(s * npaths + l) * m + e], unscaled (FP64, the plain fill's rule).
+int tags_launch_path_pairs(const double* d_elec, int m, const double* d_paths, int npaths, const SampleCoef* d_coef,
+                           int nsamp, double2* d_jj, int* d_status, cudaStream_t st);
+// Gauss-Legendre nodes (ascending) and weights on [0, 1] (host side).
+void tags_gauss_legendre(int q, double* x, double* w);
+
 // Bookkeeping of kernel launches (reported by tags_gpu_launch_count).
 void tags_note_launch(long long n = 1);
 
