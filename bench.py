@@ -9,6 +9,7 @@ samples, cycling through the 2048-sample set. Prints one JSON line.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|plain]
   python bench.py --impl reference      # the reference's CPU path on the host cores
+  python bench.py --workload fields     # post-processing: potentials and field along a line
 """
 from __future__ import annotations
 
@@ -130,7 +131,7 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1700.0, "bf16_kind": "sustained", "src": "fallback"}
 
 
-PROFILE_FAMILIES = 10
+PROFILE_FAMILIES = 11
 TENSOR_FAMILIES = {"ldl_trailing_gemm", "ldl_panel_gemm"}
 FP64_FAMILIES = {"lu_fp64_gemm"}
 FP64_PIPE_TFLOPS = 1.19   # DFMA throughput measured on this machine's GB300 (probe kernel, 8 FMA chains)
@@ -242,6 +243,144 @@ def run_reference(args):
     return 0
 
 
+# ---- post-processing workload -------------------------------------------------
+# The field line of examples/visacro57emc01.c:229-247 (direction atan(5/4),
+# starting 6 m outside the grid, four injections), here 251 points 0.3 m apart
+# across the benchmark grid at ground level; every Laplace sample of the set.
+FIELD_POINTS, FIELD_RHS, FIELD_STEP = 251, 4, 0.3
+# FP64 pipe operations one rule-node evaluation executes in k_fields
+# (potential, vector potential and field for four injections): (DFMA x 2 + DADD
+# + DMUL) per evaluation, from an ncu count of the kernel (see profiles/).
+FIELD_FP64_FLOPS_PER_EVAL = 196.9
+
+
+def field_points():
+    hyp = math.hypot(4.0, 5.0)
+    d = np.arange(FIELD_POINTS) * FIELD_STEP
+    return np.column_stack([-6.0 + d * 4.0 / hyp, -6.0 + d * 5.0 / hyp, np.zeros(FIELD_POINTS)])
+
+
+def field_currents(step, nb, m):
+    """Seeded synthetic currents of one step ([sample][injection][electrode]);
+    the cost of the kernels does not depend on their values."""
+    rng = np.random.default_rng(1000 + step)
+    il = rng.standard_normal((nb, FIELD_RHS, m)) + 1j * rng.standard_normal((nb, FIELD_RHS, m))
+    it = rng.standard_normal((nb, FIELD_RHS, m)) + 1j * rng.standard_normal((nb, FIELD_RHS, m))
+    return il, it
+
+
+def field_cpu_baseline(pkg, elec, pts, s, kappa, gamma, budget_s=12.0):
+    """The reference's per-point loop (examples/visacro57emc01.c:436-458:
+    electric_field with s = 0, then magnetic_potential, per injection) on the
+    oracle, at the example's tolerances (1e-6), on all host cores (ctypes
+    releases the GIL), for about budget_s seconds of wall time."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    port = O.get("port")
+    cores = os.cpu_count() or 1
+    m = elec.shape[0]
+    il, it = field_currents(0, 1, m)
+
+    def one(job):
+        k, p = job
+        for r in range(FIELD_RHS):
+            port.electric_field(pts[p], elec, il[0, r], it[0, r], gamma[k], 0.0, kappa[k], 1.0, 0, 1e-6, 1e-6)
+            port.magnetic_potential(pts[p], elec, il[0, r], gamma[k], 1.0, 0, 1e-6, 1e-6)
+        return 1
+
+    jobs = [(k, p) for k in np.linspace(0, len(s) - 1, 64).astype(int) for p in range(0, FIELD_POINTS, 10)]
+    done, t0 = 0, time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        for q in range(0, len(jobs), cores):
+            done += sum(ex.map(one, jobs[q:q + cores]))
+            if time.perf_counter() - t0 > budget_s:
+                break
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "point-samples/s", "cores": cores, "kind": "port",
+            "sample": f"{done} (sample, point) pairs of the workload, 4 injections each, the example's loop "
+                      f"(electric_field at s=0 + magnetic_potential per injection, cubature 1e-6) in {dt:.1f} s"}
+
+
+def run_fields(args):
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+    pkg = entry.load_package()
+    pkg.build()
+    elec, img, nodes, s, kappa, inj, centre = workload(pkg)
+    gamma = np.sqrt(s * pkg.MU0 * kappa)
+    m = elec.shape[0]
+    pts = field_points()
+    B = args.batch or 128
+    ns_total = len(s)
+    dev = torch.device("cuda", local)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > L2
+
+    def batch(step):
+        k0 = (step * B) % ns_total
+        nb = min(B, ns_total - k0)
+        il, it = field_currents(step, nb, m)
+        return k0, nb, il, it
+
+    for w in range(args.warmup):
+        k0, nb, il, it = batch(w)
+        pkg.fields_batch(pts, elec, il, it, gamma[k0:k0 + nb], kappa[k0:k0 + nb])
+    steps = [batch(args.warmup + q) for q in range(args.steps)]     # host inputs made before the timed region
+    torch.cuda.synchronize()
+    pkg.fields_evaluations(reset=True)
+    launches0 = pkg.launch_count()
+    pkg.lib().tags_gpu_profile(1)
+    wall, ps = 0.0, 0
+    with ClockSampler(local) as clk:
+        for k0, nb, il, it in steps:
+            flush.zero_()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            out = pkg.fields_batch(pts, elec, il, it, gamma[k0:k0 + nb], kappa[k0:k0 + nb])
+            wall += time.perf_counter() - t0
+            ps += nb * FIELD_POINTS
+            if out["status"] != 0:
+                raise RuntimeError("field evaluation flagged a point on an electrode")
+    prof = read_profile(pkg)
+    pkg.lib().tags_gpu_profile(0)
+    launches = pkg.launch_count() - launches0
+    evals = pkg.fields_evaluations()
+    f = prof.get("fields")
+    dev_s = f["ms"] * 1e-3
+    value = ps / dev_s
+    roof = {"bound": "fp64", "kernel": "fields", "launches": f["launches"], "avg_launch_ms": f["ms"] / f["launches"],
+            "evaluations_per_launch": evals / f["launches"], "evaluations_per_s": evals / dev_s,
+            "unit": "TFLOP/s", "peak": FP64_PIPE_TFLOPS, "traffic": None}
+    if FIELD_FP64_FLOPS_PER_EVAL:
+        ach = evals * FIELD_FP64_FLOPS_PER_EVAL / dev_s / 1e12
+        roof.update({"achieved": ach, "frac": ach / FP64_PIPE_TFLOPS,
+                     "note": "executed FP64 flops (ncu count per rule-node evaluation x evaluations counted on "
+                             "the device) over the measured DFMA throughput of this pool's GB300"})
+    else:
+        roof.update({"achieved": None, "frac": None, "note": "FP64 operations per evaluation not yet counted"})
+    B_h2d = sum(2 * nb * FIELD_RHS * m * 16 + 2 * nb * 16 for _, nb, _, _ in steps) / len(steps)
+    B_d2h = sum(7 * nb * FIELD_POINTS * FIELD_RHS * 16 for _, nb, _, _ in steps) / len(steps)
+    line = {"metric": "field point-samples/s (1560-segment grid, 251-point line, 4 injections, 2048 samples)",
+            "value": value, "unit": "point-samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_s / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic (reference grid generator, Alipio soil; "
+                                                          "seeded currents)",
+            "config": {"workload": "grid 60x60 m, 1560 segments; 251 ground-level points 0.3 m apart on the line "
+                                   "atan(5/4) from (-6, -6); potential, vector potential and field for 4 "
+                                   "injections; 2048 Laplace samples of the solve benchmark",
+                       "samples_per_step": B, "l2": "flushed between steps (256 MB write)"},
+            "roofline": roof, "gpu_launches": launches, "clocks": clk.summary(),
+            "e2e": {"value": ps / wall, "unit": "point-samples/s", "h2d_bytes_per_step": int(B_h2d),
+                    "d2h_bytes_per_step": int(B_d2h)}}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = field_cpu_baseline(pkg, elec, pts, s, kappa, gamma)
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -256,9 +395,13 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the 16-sample check against plain FP64")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
+    ap.add_argument("--workload", default="solves", choices=["solves", "fields"],
+                    help="solves: the per-sample HEM path (default); fields: post-processing along a line")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "fields":
+        return run_fields(args)
 
     import torch
     import torch.distributed as dist

@@ -231,6 +231,11 @@ int tags_voltage_batch (const double *paths, size_t num_paths, const Electrode *
                         const tags_cdouble *gamma, const tags_cdouble *s, const tags_cdouble *kappa, double mur,
                         tags_cdouble *v);
 
+/* Node evaluations (rule node x sample) made by the field kernels on the
+ * current device since the last reset: the unit of work of the post-processing
+ * rules, for throughput reports. reset != 0 zeroes the counter after reading. */
+int tags_fields_evaluations (unsigned long long *count, int reset);
+
 /* ---- Part 2: batched extension -------------------------------------------- */
 
 enum {
@@ -364,7 +369,7 @@ int tags_debug_ldl_solve (tags_cdouble *a, tags_cdouble *b, int N, int nb, int p
 /* Per-family kernel timing with CUDA events on the launching stream (0 = off,
  * the default). Enabling resets the counters. Families, in this order:
  * fill_fp64, fill_mixed, ldl_diag, ldl_panel_gemm, ldl_trailing_gemm,
- * ldl_solve, residual_fp64, build_fp32, lu_fp64_gemm, lu_fp64_other. */
+ * ldl_solve, residual_fp64, build_fp32, lu_fp64_gemm, lu_fp64_other, fields. */
 int tags_gpu_profile (int enable);
 /* launches, device milliseconds, algorithmic flops and bytes of one family. */
 int tags_gpu_profile_read (int family, long long *launches, double *ms, double *flops, double *bytes,

@@ -58,7 +58,7 @@ EXPORTS = (
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
-    "tags_gpd_mhem_batch", "tags_voltage_batch",
+    "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations",
     "tags_gpu_set_quiet",
 )
 
@@ -147,6 +147,7 @@ def lib() -> ctypes.CDLL:
             L.tags_fields_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, _sz, _vp, _vp, d, _vp, _vp, _vp]
             L.tags_gpd_mhem_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _sz, _sz, _vp, _vp, _vp]
             L.tags_voltage_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, _sz, _vp, _vp, _vp, d, _vp]
+            L.tags_fields_evaluations.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
@@ -158,7 +159,7 @@ def lib() -> ctypes.CDLL:
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
-                         "tags_voltage_batch"):
+                         "tags_voltage_batch", "tags_fields_evaluations"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -479,6 +480,13 @@ def fields_batch(points, electrodes, il, it, gamma, kappa, mur: float = 1.0, wan
             out[name] = arr
     out["status"] = rc
     return out
+
+
+def fields_evaluations(reset: bool = False) -> int:
+    """Rule-node x sample evaluations of the field kernels since the last reset."""
+    n = ctypes.c_ulonglong(0)
+    _ret(lib().tags_fields_evaluations(ctypes.byref(n), 1 if reset else 0))
+    return int(n.value)
 
 
 def gpd_mhem_batch(points, electrodes, it, gamma, kappa) -> np.ndarray:

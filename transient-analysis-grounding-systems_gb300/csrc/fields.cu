@@ -82,6 +82,9 @@ struct FieldArgs {
     double2* vec;           // [S][P][R][3]
     double2* ef;            // [S][P][R][3]
     int* status;
+    unsigned long long* evals;  // node x sample evaluations (work counter)
+    int nchunk;             // electrode chunks (warps per point and sample group)
+    double2* part;          // [nchunk][S][P][R][7] raw sums: pot, vec xyz, ef xyz
 };
 
 TAGS_D double warp_max(double v) {
@@ -94,18 +97,25 @@ TAGS_D double2 shfl_xor2(double2 v, int o) {
     return make_double2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
 }
 
-// One warp per (point, group of G samples); lanes are (sample si = lane % G,
-// node slice sub = lane / G). The rule's nodes of each electrode are built
-// once per warp into shared memory and reused by all samples of the group.
+// One warp per (electrode chunk, point, group of G samples); lanes are
+// (sample si = lane % G, node slice sub = lane / G). The rule's nodes of each
+// electrode are built once per warp into shared memory and reused by all
+// samples of the group. The electrode chunks spread one point's work over
+// several warps so the grid fills the GPU evenly; k_fields_reduce adds them.
 __global__ void __launch_bounds__(FW * 32) k_fields(FieldArgs a, int r0) {
     __shared__ WarpSmem sm_all[FW];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     WarpSmem& sm = sm_all[warp];
     const int G = a.G, NS = 32 / G;
     const int ngroups = (a.S + G - 1) / G;
-    const long long item = (long long)blockIdx.x * FW + warp;
-    if (item >= (long long)a.P * ngroups) return;     // whole warp leaves together
+    const long long per_chunk = (long long)a.P * ngroups;
+    const long long item_all = (long long)blockIdx.x * FW + warp;
+    if (item_all >= per_chunk * a.nchunk) return;     // whole warp leaves together
+    const int chunk = (int)(item_all / per_chunk);
+    const long long item = item_all - (long long)chunk * per_chunk;
     const int p = (int)(item / ngroups), grp = (int)(item % ngroups);
+    const int e_begin = (int)((long long)chunk * a.m / a.nchunk);
+    const int e_end = (int)((long long)(chunk + 1) * a.m / a.nchunk);
     const int si = lane % G, sub = lane / G;
     const int smp = grp * G + si;
     const bool valid = smp < a.S;
@@ -123,7 +133,7 @@ __global__ void __launch_bounds__(FW * 32) k_fields(FieldArgs a, int r0) {
         for (int c = 0; c < 3; ++c) { vec[r][c] = cz(0.0, 0.0); ef[r][c] = cz(0.0, 0.0); }
     }
 
-    for (int e = 0; e < a.m; ++e) {
+    for (int e = e_begin; e < e_end; ++e) {
         const Seg& S = a.elec[e];
         const double D[3] = {S.b[0] - S.a[0], S.b[1] - S.a[1], S.b[2] - S.a[2]};
         const double L2 = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
@@ -177,6 +187,7 @@ __global__ void __launch_bounds__(FW * 32) k_fields(FieldArgs a, int r0) {
         if (lane < nu) sm.pre[lane] = incl - kj;
         const int ksum = __shfl_sync(0xffffffffu, incl, 31);
         const int nodes = ksum * FQ;
+        if (lane == 0 && a.evals) atomicAdd(a.evals, (unsigned long long)nodes * (unsigned long long)min(G, a.S - grp * G));
         __syncwarp();
 
         double2 J1 = cz(0.0, 0.0), Ap = cz(0.0, 0.0), Bp = cz(0.0, 0.0);
@@ -268,19 +279,41 @@ __global__ void __launch_bounds__(FW * 32) k_fields(FieldArgs a, int r0) {
     }
 
     if (!valid || sub != 0) return;
-    const double2 kap = a.kappa[smp];
-    const double2 i4pk = cdiv(cz(1.0, 0.0), cscale(kap, TAGS_FOUR_PI));
-    const double u4pi = a.mur * TAGS_MU0 / TAGS_FOUR_PI;
 #pragma unroll
     for (int r = 0; r < RMAX; ++r) {
         if (r >= nr) break;
-        const long long o = ((long long)smp * a.P + p) * a.R + r0 + r;
-        if (a.pot && (a.want & WANT_POT)) a.pot[o] = cmul(pot[r], i4pk);
+        double2* o = a.part + ((((long long)chunk * a.S + smp) * a.P + p) * a.R + r0 + r) * 7;
+        o[0] = pot[r];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            if (a.vec && (a.want & WANT_VEC)) a.vec[3 * o + c] = cscale(vec[r][c], u4pi);
-            if (a.ef && (a.want & WANT_EF)) a.ef[3 * o + c] = cmul(ef[r][c], i4pk);
+            o[1 + c] = vec[r][c];
+            o[4 + c] = ef[r][c];
         }
+    }
+}
+
+// Sum of the electrode chunks and the scale factors: 1 / (4 pi kappa) for the
+// potential and field, mur mu0 / (4 pi) for the vector potential.
+__global__ void k_fields_reduce(FieldArgs a) {
+    const long long n = (long long)a.S * a.P * a.R;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int smp = (int)(i / ((long long)a.P * a.R));
+    double2 v[7];
+#pragma unroll
+    for (int c = 0; c < 7; ++c) v[c] = cz(0.0, 0.0);
+    for (int ch = 0; ch < a.nchunk; ++ch) {
+        const double2* q = a.part + ((long long)ch * n + i) * 7;
+#pragma unroll
+        for (int c = 0; c < 7; ++c) v[c] = cadd(v[c], q[c]);
+    }
+    const double2 i4pk = cdiv(cz(1.0, 0.0), cscale(a.kappa[smp], TAGS_FOUR_PI));
+    const double u4pi = a.mur * TAGS_MU0 / TAGS_FOUR_PI;
+    if (a.pot && (a.want & WANT_POT)) a.pot[i] = cmul(v[0], i4pk);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (a.vec && (a.want & WANT_VEC)) a.vec[3 * i + c] = cscale(v[1 + c], u4pi);
+        if (a.ef && (a.want & WANT_EF)) a.ef[3 * i + c] = cmul(v[4 + c], i4pk);
     }
 }
 
@@ -404,6 +437,7 @@ __global__ void k_voltage(const double* __restrict__ paths, int NL, const Seg* _
 }
 
 bool g_tables_ready[64] = {};
+unsigned long long* g_evals[64] = {};   // per-device work counter
 
 int fields_tables(int dev) {
     if (dev < 0 || dev >= 64) return TAGS_E_CUDA;
@@ -412,6 +446,8 @@ int fields_tables(int dev) {
     tags_gauss_legendre(FQ, x, w);
     TAGS_CUDA_OK(cudaMemcpyToSymbol(c_fx, x, sizeof(x)));
     TAGS_CUDA_OK(cudaMemcpyToSymbol(c_fw, w, sizeof(w)));
+    TAGS_CUDA_OK(cudaMalloc(&g_evals[dev], sizeof(unsigned long long)));
+    TAGS_CUDA_OK(cudaMemset(g_evals[dev], 0, sizeof(unsigned long long)));
     g_tables_ready[dev] = true;
     return 0;
 }
@@ -430,17 +466,38 @@ size_t chunk_samples(size_t S, size_t per_sample) {
 
 inline double2 D2(tags_cdouble v) { return make_double2(v.re, v.im); }
 
+// Electrode chunks per (point, sample group): enough warps for about six
+// waves of two 4-warp CTAs per SM (the register-limited residency), at least
+// 16 electrodes per chunk, and partial sums of at most `part_cap` bytes.
+int field_chunks(size_t P, size_t ns, size_t R, size_t m, size_t part_cap) {
+    const size_t G = (size_t)samples_per_warp(ns);
+    const size_t warps = P * ((ns + G - 1) / G);
+    const size_t target = 152 * 8 * 6;
+    size_t c = warps ? (target + warps - 1) / warps : 1;
+    c = std::min<size_t>(c, std::max<size_t>(1, m / 16));
+    c = std::min<size_t>(c, 64);
+    const size_t per = 7 * sizeof(double2) * P * R * ns;
+    if (per) c = std::min<size_t>(c, std::max<size_t>(1, part_cap / per));
+    return (int)std::max<size_t>(1, c);
+}
+
 int launch_fields(const FieldArgs& base, cudaStream_t st) {
     const int ngroups = (base.S + base.G - 1) / base.G;
-    const long long items = (long long)base.P * ngroups;
+    const long long items = (long long)base.P * ngroups * base.nchunk;
     if (items == 0 || base.m == 0) return 0;
     const long long blocks = (items + FW - 1) / FW;
     if (blocks > 0x7fffffffLL) return tags_fail(TAGS_E_ARG, "too many points x samples for one launch");
+    const int pf = tags_prof_begin(TAGS_PROF_FIELDS, st);
     for (int r0 = 0; r0 < base.R; r0 += RMAX) {
         k_fields<<<(unsigned)blocks, FW * 32, 0, st>>>(base, r0);
         tags_note_launch();
         TAGS_CUDA_OK(cudaGetLastError());
     }
+    const long long n = (long long)base.S * base.P * base.R;
+    k_fields_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(base);
+    tags_prof_end(TAGS_PROF_FIELDS, pf, st, 0.0, 0.0);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
     return 0;
 }
 
@@ -469,10 +526,11 @@ int fields_run(const FieldsIn& in) {
     const size_t P = in.P, m = in.m, R = in.R, S = in.S;
     const size_t per_sample = sizeof(double2) * (4 * R * m + P * R * 7 + 2);
     const size_t cs = chunk_samples(S, per_sample);
+    const int nchunk = field_chunks(P, cs, R, m, (size_t)1e9);
     double* d_pts = (double*)c->scratch(10, sizeof(double) * 3 * P + 16);
     Seg* d_el = (Seg*)c->scratch(11, sizeof(Seg) * m + 16);
     double2* d_cur = (double2*)c->scratch(12, sizeof(double2) * 4 * R * m * cs + 16);
-    double2* d_out = (double2*)c->scratch(13, sizeof(double2) * 7 * P * R * cs + 16);
+    double2* d_out = (double2*)c->scratch(13, sizeof(double2) * 7 * P * R * cs * (1 + (size_t)nchunk) + 16);
     double2* d_gk = (double2*)c->scratch(14, sizeof(double2) * 2 * cs + 16);
     if (!d_pts || !d_el || !d_cur || !d_out || !d_gk) return tags_fail(TAGS_E_NOMEM, "device allocation failed");
     TAGS_CUDA_OK(cudaMemcpyAsync(d_pts, in.points, sizeof(double) * 3 * P, cudaMemcpyHostToDevice, st));
@@ -520,6 +578,9 @@ int fields_run(const FieldsIn& in) {
         a.vec = d_out + P * R * ns;
         a.ef = d_out + 4 * P * R * ns;
         a.status = c->status;
+        a.evals = g_evals[c->device];
+        a.nchunk = nchunk;
+        a.part = d_out + 7 * P * R * ns;
         if (int e = launch_fields(a, st)) return e;
         if (in.pot && (in.want & WANT_POT))
             TAGS_CUDA_OK(cudaMemcpyAsync(in.pot + s0 * P * R, a.pot, sizeof(double2) * P * R * ns,
@@ -705,6 +766,19 @@ extern "C" int tags_voltage_batch(const double* paths, size_t num_paths, const E
         TAGS_CUDA_OK(cudaMemcpyAsync(v + s0 * NL * R, d_v, sizeof(double2) * n, cudaMemcpyDeviceToHost, st));
         TAGS_CUDA_OK(cudaStreamSynchronize(st));
     }
+    return 0;
+}
+
+extern "C" int tags_fields_evaluations(unsigned long long* count, int reset) {
+    if (!count) return tags_fail(TAGS_E_ARG, "null pointer argument");
+    std::lock_guard<std::mutex> lk(tags_dropin_mutex());
+    DeviceCtx* c = tags_ctx();
+    if (!c) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
+    if (int e = fields_tables(c->device)) return e;
+    TAGS_CUDA_OK(cudaMemcpyAsync(count, g_evals[c->device], sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                 c->stream));
+    if (reset) TAGS_CUDA_OK(cudaMemsetAsync(g_evals[c->device], 0, sizeof(unsigned long long), c->stream));
+    TAGS_CUDA_OK(cudaStreamSynchronize(c->stream));
     return 0;
 }
 

@@ -25,7 +25,8 @@ struct Family {
 };
 
 const char* kNames[TAGS_PROF_N] = {"fill_fp64", "fill_mixed", "ldl_diag", "ldl_panel_gemm", "ldl_trailing_gemm",
-                                   "ldl_solve", "residual_fp64", "build_fp32", "lu_fp64_gemm", "lu_fp64_other"};
+                                   "ldl_solve", "residual_fp64", "build_fp32", "lu_fp64_gemm", "lu_fp64_other",
+                                   "fields"};
 Family g_fam[TAGS_PROF_N];
 std::atomic<int> g_on{0};
 std::mutex g_pm;

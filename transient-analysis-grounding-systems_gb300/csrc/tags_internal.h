@@ -115,7 +115,8 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
 // profile.cu: optional CUDA-event timing of kernel families
 enum {
     TAGS_PROF_FILL_FP64 = 0, TAGS_PROF_FILL_MIXED, TAGS_PROF_LDL_DIAG, TAGS_PROF_LDL_PANEL, TAGS_PROF_LDL_TRAIL,
-    TAGS_PROF_LDL_SOLVE, TAGS_PROF_RESID, TAGS_PROF_BUILD, TAGS_PROF_LU64_GEMM, TAGS_PROF_LU64_OTHER, TAGS_PROF_N
+    TAGS_PROF_LDL_SOLVE, TAGS_PROF_RESID, TAGS_PROF_BUILD, TAGS_PROF_LU64_GEMM, TAGS_PROF_LU64_OTHER,
+    TAGS_PROF_FIELDS, TAGS_PROF_N
 };
 int tags_prof_begin(int fam, cudaStream_t st);
 void tags_prof_end(int fam, int slot, cudaStream_t st, double flops, double bytes);
