@@ -500,156 +500,223 @@ TAGS_D float2 anchor_df(float grh, float grl, float gih, float gil, float rh, fl
     return make_float2(mag * cs, -mag * sn);
 }
 
-constexpr int MIX_SG = 4;   // samples per thread (124 registers: four 128-thread CTAs per SM)
+constexpr int FILL_WARPS = 4;              // warps per CTA
+constexpr int FILL_SUB = 8;                // rows of one write sub-tile
+constexpr int FILL_GEO = QMIX * QMIX;      // points of one panel pair, at most
 
-// Mixed-form fill of the regular pairs, all in FP32: one thread per (pair,
-// group of MIX_SG samples), the group's constants in shared memory. Pairs that
-// share an endpoint (log-singular) are left to k_fill_touch. Z (ZL at zl, ZT at
-// zt, complex FP32) gets the lower element and its mirror.
-__global__ void __launch_bounds__(128) k_fill_mixed(const double* __restrict__ elec, const double* __restrict__ img,
-                                                    const float4* __restrict__ sdir, const float4* __restrict__ idir,
-                                                    const float* __restrict__ selfv, int m,
-                                                    const uint16_t* __restrict__ codes,
-                                                    const PairRec* __restrict__ recs,
-                                                    const SampleF32* __restrict__ coef, int nsamp, float2* zl0,
-                                                    float2* zt0, long long bstride, int has_img, int* status) {
+struct FillWarpSmem {
+    float2 geo[FILL_GEO];                  // (r_p - r_c, w_i w_j / r_p) of the current panel pair
+    float4 anc[32];                        // panel-pair anchors (midpoint vector, |.| high part) of a chunk
+    float ancl[32];                        // |.| low part
+    float2 zl[FILL_SUB][33], zt[FILL_SUB][33];   // a sub-tile of outputs, [row][sample]
+};
+
+// Lower-triangle tiles of 32 rows: tile t -> (row block kb, column i); block
+// rows kb < KB - 1 hold columns 0 .. 32 kb + 31, the last one all m columns.
+TAGS_D void fill_tile(long long t, int m, int& kb, int& i) {
+    const int KB = (m + 31) / 32;
+    const long long full = 16LL * (KB - 1) * KB;
+    if (t >= full) {
+        kb = KB - 1;
+        i = (int)(t - full);
+        return;
+    }
+    int b = (int)floor((sqrt(1.0 + (double)t / 4.0) - 1.0) * 0.5);
+    if (b < 0) b = 0;
+    while (b > 0 && 16LL * b * (b + 1) > t) --b;
+    while (16LL * (b + 1) * (b + 2) <= t) ++b;
+    kb = b;
+    i = (int)(t - 16LL * b * (b + 1));
+}
+
+// Mixed-form fill of the regular pairs, all in FP32, lower triangle only (the
+// mirror is k_zmirror's). One warp per (column i, 32 rows, 32 samples): the
+// lanes are the samples, so each quadrature point's geometry (offset from the
+// panel-pair anchor and weight / r) is computed once, by the warp's lanes in
+// parallel, into shared memory, and every sample applies its own
+// e^{-gamma (r_p - r_c)} to it. Panel-pair anchors of split pairs are formed
+// in FP64 once per warp (a lane per panel pair), never per sample. Outputs
+// pass through a [row][sample] sub-tile so each store instruction writes 64
+// contiguous bytes per sample. Pairs that share an endpoint (log-singular)
+// are left to k_fill_touch.
+__global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_mixed(
+    const double* __restrict__ elec, const double* __restrict__ img, const float4* __restrict__ sdir,
+    const float4* __restrict__ idir, const float* __restrict__ selfv, int m, const uint16_t* __restrict__ codes,
+    const PairRec* __restrict__ recs, const SampleF32* __restrict__ coef, int nsamp, float2* zl0, float2* zt0,
+    long long bstride, int has_img, long long ntiles, int* status) {
     __shared__ float sxm[GL_MIX], swf[GL_MIX];
-    __shared__ SampleF32 sc[MIX_SG];
-    __shared__ float s_gmax;
-    const int s0 = blockIdx.y * MIX_SG;
-    const int ns = min(MIX_SG, nsamp - s0);
+    __shared__ FillWarpSmem sw_all[FILL_WARPS];
     for (int t = threadIdx.x; t < GL_MIX; t += blockDim.x) {
         sxm[t] = g_glxm[t];
         swf[t] = g_glwm[t];
     }
-    if (threadIdx.x < MIX_SG) {
-        SampleF32 z{};
-        sc[threadIdx.x] = threadIdx.x < ns ? coef[s0 + threadIdx.x] : z;
-    }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        float gm = 0.f;
-        for (int q = 0; q < ns; ++q) gm = fmaxf(gm, sqrtf(sc[q].grh * sc[q].grh + sc[q].gih * sc[q].gih));
-        s_gmax = gm;
-    }
-    __syncthreads();
-    const float gmax = s_gmax;
-    const long long npairs = (long long)m * (m + 1) / 2;
-    const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npairs || ns <= 0) return;
-    int i, k;
-    pair_index(p, m, i, k);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    FillWarpSmem& W = sw_all[warp];
+    const long long tile = (long long)blockIdx.x * FILL_WARPS + warp;
+    if (tile >= ntiles) return;                      // whole warp leaves together
+    int kb, i;
+    fill_tile(tile, m, kb, i);
+    const int smp = blockIdx.y * 32 + lane;
+    const bool valid = smp < nsamp;
+    SampleF32 c{};
+    if (valid) c = coef[smp];
+    float gmax = valid ? sqrtf(c.grh * c.grh + c.gih * c.gih) : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gmax = fmaxf(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
     const float4 ds = sdir[i];
-    float2 zl[MIX_SG], zt[MIX_SG];
-#pragma unroll
-    for (int q = 0; q < MIX_SG; ++q) zl[q] = zt[q] = make_float2(0.f, 0.f);
-    if (k == i) {
-        // self term: the reference's static closed form (src/electrode.c:346-348)
-        const float v = selfv[i];
-#pragma unroll
-        for (int q = 0; q < MIX_SG; ++q) {
-            zl[q] = make_float2(sc[q].cL.x * v, sc[q].cL.y * v);
-            zt[q] = make_float2(sc[q].cT.x * v / (ds.w * ds.w), sc[q].cT.y * v / (ds.w * ds.w));
-        }
-    }
-    for (int kind = 0; kind < 2; ++kind) {
-        if (kind == 0 && k == i) continue;
-        if (kind == 1 && !has_img) break;
-        const uint16_t code = codes[2 * p + kind];
-        if (code & (PC_TOUCH | PC_DEGEN)) continue;      // k_fill_touch
-        const float4 dr = kind == 0 ? sdir[k] : idir[k];
-        const PairRec rec = recs[2 * p + kind];
-        const float lmax = fmaxf(ds.w, dr.w);
-        const int P = min(32, max(code & 63, (int)ceilf(gmax * lmax / 1.5f)));
-        const int qg = (code >> 6) & 63;
-        const int qq = min(QMIX, qg + (int)ceilf(gmax * lmax / P));
-        const float* x = sxm + gl_off(qq);
-        const float* w = swf + gl_off(qq);
-        const float h = 1.f / (float)P;
-        const float3 hr = make_float3(dr.x * h, dr.y * h, dr.z * h);
-        const float3 hs = make_float3(ds.x * h, ds.y * h, ds.z * h);
-        float2 acc[MIX_SG];
-#pragma unroll
-        for (int q = 0; q < MIX_SG; ++q) acc[q] = make_float2(0.f, 0.f);
-        for (int pi = 0; pi < P; ++pi) {
-            for (int pj = 0; pj < P; ++pj) {
-                // panel-pair anchor: midpoint vector and its length as a float pair
-                float3 D;
-                float rh, rl;
-                if (P == 1) {
-                    D = make_float3(rec.dx, rec.dy, rec.dz);
-                    rh = rec.rch;
-                    rl = rec.rcl;
-                } else {
-                    const double* SR = (kind == 0 ? elec : img) + 11LL * k;
-                    const double* SS = elec + 11LL * i;
-                    double fr = (pi + 0.5) / P, fs = (pj + 0.5) / P, dd[3];
-                    for (int c = 0; c < 3; ++c)
-                        dd[c] = (SR[c] + fr * (SR[3 + c] - SR[c])) - (SS[c] + fs * (SS[3 + c] - SS[c]));
-                    double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
-                    D = make_float3((float)dd[0], (float)dd[1], (float)dd[2]);
-                    rh = (float)r;
-                    rl = (float)(r - (double)rh);
-                }
-                const float rc2 = rh * rh;
-                float2 psum[MIX_SG];
-#pragma unroll
-                for (int q = 0; q < MIX_SG; ++q) psum[q] = make_float2(0.f, 0.f);
-                for (int qi = 0; qi < qq; ++qi) {
-                    const float a = x[qi], wi = w[qi];
-                    const float ax = a * hr.x, ay = a * hr.y, az = a * hr.z;
-                    for (int qj = 0; qj < qq; ++qj) {
-                        const float b = x[qj];
-                        // u = a hr - b hs: offset of the point pair from the panel centres
-                        const float ux = fmaf(-b, hs.x, ax), uy = fmaf(-b, hs.y, ay), uz = fmaf(-b, hs.z, az);
-                        const float e = fmaf(2.f, fmaf(D.x, ux, fmaf(D.y, uy, D.z * uz)),
-                                             fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
-                        const float t = rc2 + e;
-                        const float irp = rsqrtf(t);                          // 1 / r_p
-                        const float del = e * __frcp_rn(fmaf(t, irp, rh));    // r_p - r_c
-                        const float wt = wi * w[qj] * irp;
-#pragma unroll
-                        for (int q = 0; q < MIX_SG; ++q) {
-                            const float mg = wt * exp2f(-1.44269502f * sc[q].grh * del);
-                            float sn, cs;
-                            __sincosf(sc[q].gih * del, &sn, &cs);
-                            psum[q].x = fmaf(mg, cs, psum[q].x);
-                            psum[q].y = fmaf(-mg, sn, psum[q].y);
+    const float3 hs1 = make_float3(ds.x, ds.y, ds.z);
+    const long long pstart = (long long)i * (2LL * m - i + 1) / 2;     // pair index of (i, i)
+    const int k_lo = max(i, 32 * kb), k_hi = min(m, 32 * kb + 32);
+    const float kr = -1.44269502f * c.grh;
+    for (int k0 = k_lo; k0 < k_hi; k0 += FILL_SUB) {
+        const int kend = min(k_hi, k0 + FILL_SUB);
+        for (int k = k0; k < kend; ++k) {
+            const long long p = pstart + (k - i);
+            float2 zl = make_float2(0.f, 0.f), zt = make_float2(0.f, 0.f);
+            if (k == i) {
+                // self term: the reference's static closed form (src/electrode.c:346-348)
+                const float v = selfv[i];
+                zl = make_float2(c.cL.x * v, c.cL.y * v);
+                zt = make_float2(c.cT.x * v / (ds.w * ds.w), c.cT.y * v / (ds.w * ds.w));
+            }
+            for (int kind = 0; kind < 2; ++kind) {
+                if (kind == 0 && k == i) continue;
+                if (kind == 1 && !has_img) break;
+                const uint16_t code = codes[2 * p + kind];
+                if (code & (PC_TOUCH | PC_DEGEN)) continue;      // k_fill_touch
+                const float4 dr = kind == 0 ? sdir[k] : idir[k];
+                const PairRec rec = recs[2 * p + kind];
+                const float lmax = fmaxf(ds.w, dr.w);
+                const int P = min(32, max(code & 63, (int)ceilf(gmax * lmax / 1.5f)));
+                const int qg = (code >> 6) & 63;
+                const int qq = min(QMIX, qg + (int)ceilf(gmax * lmax / P));
+                const float* x = sxm + gl_off(qq);
+                const float* w = swf + gl_off(qq);
+                const float h = 1.f / (float)P;
+                const float3 hr = make_float3(dr.x * h, dr.y * h, dr.z * h);
+                const float3 hs = make_float3(hs1.x * h, hs1.y * h, hs1.z * h);
+                const int npts = qq * qq;
+                float2 acc = make_float2(0.f, 0.f);
+                const int npp = P * P;
+                for (int pp0 = 0; pp0 < npp; pp0 += 32) {
+                    const int cnt = min(32, npp - pp0);
+                    if (P > 1) {
+                        // panel-pair anchors of this chunk in FP64, one per lane
+                        // (the FP64 pipe is 1/64 of FP32 here: never per sample)
+                        if (lane < cnt) {
+                            const int pp = pp0 + lane, pi = pp / P, pj = pp - pi * P;
+                            const double* SR = (kind == 0 ? elec : img) + 11LL * k;
+                            const double* SS = elec + 11LL * i;
+                            const double fr = (pi + 0.5) / P, fs = (pj + 0.5) / P;
+                            double dd[3];
+                            for (int cc = 0; cc < 3; ++cc)
+                                dd[cc] = (SR[cc] + fr * (SR[3 + cc] - SR[cc])) - (SS[cc] + fs * (SS[3 + cc] - SS[cc]));
+                            const double r = sqrt(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+                            const float rhf = (float)r;
+                            W.anc[lane] = make_float4((float)dd[0], (float)dd[1], (float)dd[2], rhf);
+                            W.ancl[lane] = (float)(r - (double)rhf);
                         }
+                        __syncwarp();
                     }
+                    for (int u = 0; u < cnt; ++u) {
+                        // panel-pair anchor: midpoint vector and its length as a float pair
+                        float3 D;
+                        float rh, rl;
+                        if (P == 1) {
+                            D = make_float3(rec.dx, rec.dy, rec.dz);
+                            rh = rec.rch;
+                            rl = rec.rcl;
+                        } else {
+                            const float4 an4 = W.anc[u];
+                            D = make_float3(an4.x, an4.y, an4.z);
+                            rh = an4.w;
+                            rl = W.ancl[u];
+                        }
+                        const float rc2 = rh * rh;
+                        for (int t = lane; t < npts; t += 32) {
+                            const int qi = t / qq, qj = t - qi * qq;
+                            const float a = x[qi], b = x[qj];
+                            // u = a hr - b hs: offset of the point pair from the panel centres
+                            const float ux = fmaf(-b, hs.x, a * hr.x), uy = fmaf(-b, hs.y, a * hr.y),
+                                        uz = fmaf(-b, hs.z, a * hr.z);
+                            const float e = fmaf(2.f, fmaf(D.x, ux, fmaf(D.y, uy, D.z * uz)),
+                                                 fmaf(ux, ux, fmaf(uy, uy, uz * uz)));
+                            const float tt = rc2 + e;
+                            const float irp = rsqrtf(tt);                          // 1 / r_p
+                            const float del = e * __frcp_rn(fmaf(tt, irp, rh));    // r_p - r_c
+                            W.geo[t] = make_float2(del, w[qi] * w[qj] * irp);
+                        }
+                        __syncwarp();
+                        float2 ps = make_float2(0.f, 0.f);
+#pragma unroll 4
+                        for (int t = 0; t < npts; ++t) {
+                            const float2 g = W.geo[t];
+                            const float mg = g.y * exp2f(kr * g.x);
+                            float sn, cs;
+                            __sincosf(c.gih * g.x, &sn, &cs);
+                            ps.x = fmaf(mg, cs, ps.x);
+                            ps.y = fmaf(-mg, sn, ps.y);
+                        }
+                        __syncwarp();
+                        const float2 an = anchor_df(c.grh, c.grl, c.gih, c.gil, rh, rl);
+                        acc = ffmac(an, ps, acc);
+                    }
+                    __syncwarp();                     // the chunk's anchors are read: free for the next
                 }
-#pragma unroll
-                for (int q = 0; q < MIX_SG; ++q) {
-                    const float2 an = anchor_df(sc[q].grh, sc[q].grl, sc[q].gih, sc[q].gil, rh, rl);
-                    acc[q] = ffmac(an, psum[q], acc[q]);
-                }
+                const float h2 = h * h;
+                const float2 J = make_float2(acc.x * h2, acc.y * h2);
+                const float2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
+                zt = ffmac(cT, J, zt);
+                zl = ffmac(make_float2(cL.x * rec.fl, cL.y * rec.fl), J, zl);
+            }
+            W.zl[k - k0][lane] = zl;
+            W.zt[k - k0][lane] = zt;
+        }
+        __syncwarp();
+        const int nrow = kend - k0;
+        for (int idx = lane; idx < FILL_SUB * 32; idx += 32) {
+            const int j = idx % FILL_SUB, sl = idx / FILL_SUB;
+            const int ss = blockIdx.y * 32 + sl;
+            if (j < nrow && ss < nsamp) {
+                const float2 a = W.zl[j][sl], b = W.zt[j][sl];
+                if (!isfinite(a.x + a.y + b.x + b.y)) raise_status(status, TAGS_ST_NONFINITE);
+                const long long off = bstride * ss + (k0 + j) + (long long)m * i;
+                zl0[off] = a;
+                zt0[off] = b;
             }
         }
-        const float h2 = h * h;
-#pragma unroll
-        for (int q = 0; q < MIX_SG; ++q) {
-            const float2 J = make_float2(acc[q].x * h2, acc[q].y * h2);
-            const float2 cL = kind == 0 ? sc[q].cL : sc[q].cLi, cT = kind == 0 ? sc[q].cT : sc[q].cTi;
-            zt[q] = ffmac(cT, J, zt[q]);
-            zl[q] = ffmac(make_float2(cL.x * rec.fl, cL.y * rec.fl), J, zl[q]);
-        }
+        __syncwarp();
     }
-#pragma unroll
-    for (int q = 0; q < MIX_SG; ++q) {
-        if (q >= ns) break;
-        const long long bs = bstride * (s0 + q);
-        if (!isfinite(zl[q].x + zl[q].y + zt[q].x + zt[q].y)) raise_status(status, TAGS_ST_NONFINITE);
-        zl0[bs + k + (long long)m * i] = zl[q];
-        zt0[bs + k + (long long)m * i] = zt[q];
-        if (k != i) {
-            zl0[bs + i + (long long)m * k] = zl[q];
-            zt0[bs + i + (long long)m * k] = zt[q];
-        }
+}
+
+// Upper triangle of ZL and ZT from the lower one, 32 x 32 tiles through
+// shared memory (coalesced reads and writes); grid.y = 2 x samples.
+__global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long long bstride, int m) {
+    __shared__ float2 tile[32][33];
+    const long long t = blockIdx.x;
+    // lower tiles by block row: row block bk holds column blocks 0 .. bk
+    int bk = (int)floor((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    if (bk < 0) bk = 0;
+    while (bk > 0 && (long long)bk * (bk + 1) / 2 > t) --bk;
+    while ((long long)(bk + 1) * (bk + 2) / 2 <= t) ++bk;
+    const int bi = (int)(t - (long long)bk * (bk + 1) / 2);
+    const int smp = blockIdx.y >> 1;
+    float2* Z = ((blockIdx.y & 1) ? zt0 : zl0) + bstride * smp;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int j = ty; j < 32; j += 8) {
+        const int r = bk * 32 + tx, cc = bi * 32 + j;
+        if (r < m && cc < m && r > cc) tile[j][tx] = Z[r + (long long)m * cc];
+    }
+    __syncthreads();
+    for (int j = ty; j < 32; j += 8) {
+        const int cc = bi * 32 + tx, r = bk * 32 + j;     // element (row cc, column r) of the upper triangle
+        if (r < m && cc < m && r > cc) Z[cc + (long long)m * r] = tile[tx][j];
     }
 }
 
 // Pairs sharing an endpoint (log-singular): the Duffy rule in FP64, added to
-// what k_fill_mixed wrote. One thread per (listed pair, sample).
+// what k_fill_mixed wrote (lower triangle). One thread per (listed pair, sample).
 __global__ void __launch_bounds__(128) k_fill_touch(const double* __restrict__ elec, const double* __restrict__ img,
                                                     int m, const int* __restrict__ list, const int* __restrict__ nlist,
                                                     const PairRec* __restrict__ recs,
@@ -694,17 +761,12 @@ __global__ void __launch_bounds__(128) k_fill_touch(const double* __restrict__ e
         dl = cadd(dl, cscale(cmul(cL, J), (double)recs[2 * p + kind].fl));
     }
     if (!isfinite(dl.x + dl.y + dt.x + dt.y)) raise_status(status, TAGS_ST_NONFINITE);
-    const long long bs = bstride * smp;
-    const long long lo = bs + k + (long long)m * i, up = bs + i + (long long)m * k;
+    const long long lo = bstride * smp + k + (long long)m * i;      // lower triangle (k_zmirror copies it up)
     float2 a = zl0[lo], b = zt0[lo];
     a = make_float2(a.x + (float)dl.x, a.y + (float)dl.y);
     b = make_float2(b.x + (float)dt.x, b.y + (float)dt.y);
     zl0[lo] = a;
     zt0[lo] = b;
-    if (k != i) {
-        zl0[up] = a;
-        zt0[up] = b;
-    }
 }
 
 __global__ void k_seg_dirs(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
@@ -830,19 +892,22 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
     if (m <= 0 || nsamp <= 0) return 0;
     if (nsamp > 4096) return tags_fail_cuda(cudaErrorInvalidValue, "fill_mixed: batch above 4096", __FILE__, __LINE__);
     MixedFillWs w = carve(ws, m);
-    const long long npairs = (long long)m * (m + 1) / 2;
     int pf = tags_prof_begin(TAGS_PROF_FILL_MIXED, st);
     k_coef32<<<(nsamp + 127) / 128, 128, 0, st>>>(d_coef, nsamp, w.c32);
-    dim3 grid((unsigned)((npairs + 127) / 128), (unsigned)((nsamp + MIX_SG - 1) / MIX_SG));
-    k_fill_mixed<<<grid, 128, 0, st>>>(d_elec, d_img, w.sdir, w.idir, w.selfv, m, w.codes, w.recs, w.c32, nsamp, d_zl,
-                                       d_zt, bstride, has_img, d_status);
+    const int KB = (m + 31) / 32;
+    const long long ntiles = 16LL * (KB - 1) * KB + m;
+    dim3 grid((unsigned)((ntiles + FILL_WARPS - 1) / FILL_WARPS), (unsigned)((nsamp + 31) / 32));
+    k_fill_mixed<<<grid, FILL_WARPS * 32, 0, st>>>(d_elec, d_img, w.sdir, w.idir, w.selfv, m, w.codes, w.recs, w.c32,
+                                                   nsamp, d_zl, d_zt, bstride, has_img, ntiles, d_status);
     if (max_touch > 0) {
         dim3 gt((unsigned)((max_touch + 127) / 128), (unsigned)nsamp);
         k_fill_touch<<<gt, 128, 0, st>>>(d_elec, d_img, m, w.list, w.nlist, w.recs, d_coef, nsamp, d_zl, d_zt, bstride,
                                          d_status);
     }
+    k_zmirror<<<dim3((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)(2 * nsamp)), 256, 0, st>>>(d_zl, d_zt,
+                                                                                                      bstride, m);
     tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
-    tags_note_launch(max_touch > 0 ? 3 : 2);
+    tags_note_launch(max_touch > 0 ? 4 : 3);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
 }
@@ -901,6 +966,8 @@ __global__ void k_mhem_fp64(const double* __restrict__ elec, const double* __res
         store(out.zt + bs, (long long)(out.row0_t + i) + out.ld * (out.col0_t + k), zt, out.accumulate != 0);
     }
 }
+
+constexpr int MIX_SG = 4;   // samples per thread of the mHEM rescale
 
 // Mixed form: the exponentials from the pair plan's two-float midpoint
 // distances (anchor_df, exact range reduction), products in FP32; ZL at zl,
