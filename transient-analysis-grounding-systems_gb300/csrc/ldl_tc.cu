@@ -745,10 +745,11 @@ __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__
 // row index is contiguous across threads (the transpose of the one applied).
 __global__ void __launch_bounds__(512) k_blk_inv_apply(const float2* __restrict__ linv32, long long lstride, int blk,
                                                        int jb, float2* __restrict__ x0, long long xstride,
-                                                       int transpose) {
+                                                       int transpose, const int* __restrict__ active) {
     __shared__ float2 v[TB];
     __shared__ float2 part[4][TB];
     const int smp = blockIdx.x, tid = threadIdx.x, r = tid & (TB - 1), qt = tid >> 7;
+    if (active && !active[smp]) return;              // the sample has finished refining
     float2* x = x0 + xstride * smp + (long long)blk * TB;
     // M[r][k] is at Mt[k * TB + r]: Mt = Linv^T (row-major) for z = Linv r, Linv for z = Linv^T r
     const float2* Mt = linv32 + lstride * smp + (long long)blk * 2 * TB * TB + (transpose ? 0 : TB * TB);
@@ -776,9 +777,10 @@ __global__ void __launch_bounds__(512) k_blk_inv_apply(const float2* __restrict_
 // a thread per row, 16 loads in flight, the block's x in shared memory
 __global__ void __launch_bounds__(128) k_blk_fwd_update(const float2* __restrict__ A0, long long ld, long long mstride,
                                                         int N, int j0, int jb, float2* __restrict__ x0,
-                                                        long long xstride, int zl_m) {
+                                                        long long xstride, int zl_m, const int* __restrict__ active) {
     __shared__ float2 xs[TB];
     const int smp = blockIdx.y;
+    if (active && !active[smp]) return;
     float2* x = x0 + xstride * smp;
     if ((int)threadIdx.x < jb) xs[threadIdx.x] = x[j0 + threadIdx.x];
     __syncthreads();
@@ -804,9 +806,10 @@ __global__ void __launch_bounds__(128) k_blk_fwd_update(const float2* __restrict
 // (coalesced), 16 loads in flight per lane.
 __global__ void __launch_bounds__(256) k_blk_bwd_update(const float2* __restrict__ A0, long long ld, long long mstride,
                                                         int j0, int jb, float2* __restrict__ x0, long long xstride,
-                                                        int zl_m) {
+                                                        int zl_m, const int* __restrict__ active) {
     __shared__ float2 xs[TB];
     const int smp = blockIdx.y, lane = threadIdx.x & 31;
+    if (active && !active[smp]) return;
     float2* x = x0 + xstride * smp;
     // zero beyond jb: the products there have zero weights, and 0 * NaN would not vanish
     if ((int)threadIdx.x < TB) xs[threadIdx.x] = (int)threadIdx.x < jb ? x[j0 + threadIdx.x] : make_float2(0.f, 0.f);
@@ -851,8 +854,9 @@ __global__ void __launch_bounds__(256) k_blk_bwd_update(const float2* __restrict
 
 // x[i] /= D[i] (D on the diagonal of the factored matrix)
 __global__ void k_diag_scale(const float2* __restrict__ A0, long long ld, long long mstride, int N,
-                             float2* __restrict__ x0, long long xstride) {
+                             float2* __restrict__ x0, long long xstride, const int* __restrict__ active) {
     const int smp = blockIdx.y;
+    if (active && !active[smp]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
     const float2 d = A0[mstride * smp + i + ld * (long long)i];
@@ -982,24 +986,28 @@ static int launch_gemm(int NS, const CUtensorMap& mA, const CUtensorMap& mB, con
 }
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
-                     float2* x, long long xstride, int zl_m, cudaStream_t st) {
+                     float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active) {
     const float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
     const int nblk = (N + TB - 1) / TB;
     int pf = tags_prof_begin(TAGS_PROF_LDL_SOLVE, st);
     for (int b = 0; b < nblk; ++b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 0);
+        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 0, active);
         const int rest = N - j0 - jb;
-        if (rest > 0) k_blk_fwd_update<<<dim3((rest + 127) / 128, nb), 128, 0, st>>>(A, ld, mstride, N, j0, jb, x, xstride, zl_m);
+        if (rest > 0)
+            k_blk_fwd_update<<<dim3((rest + 127) / 128, nb), 128, 0, st>>>(A, ld, mstride, N, j0, jb, x, xstride, zl_m,
+                                                                         active);
         tags_note_launch(rest > 0 ? 2 : 1);
     }
-    k_diag_scale<<<dim3((N + 255) / 256, nb), 256, 0, st>>>(A, ld, mstride, N, x, xstride);
+    k_diag_scale<<<dim3((N + 255) / 256, nb), 256, 0, st>>>(A, ld, mstride, N, x, xstride, active);
     tags_note_launch();
     for (int b = nblk - 1; b >= 0; --b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 1);
-        if (j0 > 0) k_blk_bwd_update<<<dim3((j0 + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m);
+        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 1, active);
+        if (j0 > 0)
+            k_blk_bwd_update<<<dim3((j0 + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m,
+                                                                     active);
         tags_note_launch(j0 > 0 ? 2 : 1);
     }
     // two triangular sweeps over the factor: 8 N^2 real flops, 8 N^2 bytes read

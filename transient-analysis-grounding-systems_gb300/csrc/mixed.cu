@@ -509,7 +509,8 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     dim3 gv((N + 255) / 256, nb);
     k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf, p->d_norms);
     tags_note_launch();
-    int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st);
+    // samples that stopped refining skip the sweeps (their x is left alone)
+    int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st, s.active);
     if (err) return err;
     k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active);
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
