@@ -622,11 +622,11 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
             __syncthreads();
             float2 L[4], W[8];
 #pragma unroll
-            for (int p = 0; p < 4; ++p) L[p] = lv[buf][tx + 32 * p];
+            for (int p = kq >> 1; p < 4; ++p) L[p] = lv[buf][tx + 32 * p];
 #pragma unroll
             for (int q = 0; q < 8; ++q) W[q] = wv[buf][ty + 16 * q];
 #pragma unroll
-            for (int p = 0; p < 4; ++p)
+            for (int p = kq >> 1; p < 4; ++p)        // rows i <= k < 32 (kq / 2) need no update
 #pragma unroll
                 for (int q = kq; q < 8; ++q) {       // columns j < 16 kq are finished
                     const int i = tx + 32 * p, j = ty + 16 * q;
@@ -669,7 +669,7 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
 #pragma unroll
             for (int p = kp; p < 4; ++p)             // rows i < 32 kp are finished
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
+                for (int q = 0; q < 2 * kp + 2; ++q) {   // columns j > k < 32 kp + 32 stay zero
                     const int i = tx + 32 * p, j = ty + 16 * q;
                     if (i > k && j <= k) a[p][q] = fsub(a[p][q], fmulc(L[p], X[q]));
                 }
