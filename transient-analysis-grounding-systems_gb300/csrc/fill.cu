@@ -500,6 +500,15 @@ TAGS_D float2 anchor_df(float grh, float grl, float gih, float gil, float rh, fl
     return make_float2(mag * cs, -mag * sn);
 }
 
+// 2^x with the special-function unit's approximation (PTX ex2.approx.ftz:
+// a few ulp, results below 2^-126 flushed to zero, which only happens for
+// terms that are negligible against the panel's anchor).
+TAGS_D float ex2_approx(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
 constexpr int FILL_WARPS = 4;              // warps per CTA
 constexpr int FILL_SUB = 8;                // rows of one write sub-tile
 constexpr int FILL_GEO = QMIX * QMIX;      // points of one panel pair, at most
@@ -652,7 +661,7 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_mixed(
 #pragma unroll 4
                         for (int t = 0; t < npts; ++t) {
                             const float2 g = W.geo[t];
-                            const float mg = g.y * exp2f(kr * g.x);
+                            const float mg = g.y * ex2_approx(kr * g.x);
                             float sn, cs;
                             __sincosf(c.gih * g.x, &sn, &cs);
                             ps.x = fmaf(mg, cs, ps.x);
