@@ -395,6 +395,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the 16-sample check against plain FP64")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
+    ap.add_argument("--first-batch", type=int, default=0,
+                    help="batch of samples the warm-up and timed steps start from (0 = the whole job in order)")
     ap.add_argument("--workload", default="solves", choices=["solves", "fields"],
                     help="solves: the per-sample HEM path (default); fields: post-processing along a line")
     args = ap.parse_args()
@@ -433,7 +435,7 @@ def main():
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > L2
 
     def batch_index(step):
-        start = ((step * world + rank) * B) % ns_total
+        start = (((args.first_batch + step) * world + rank) * B) % ns_total
         return start, min(B, ns_total - start)
 
     def run_step(step):

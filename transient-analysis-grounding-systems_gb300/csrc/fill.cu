@@ -700,9 +700,12 @@ __global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_mixed(
 }
 
 // Upper triangle of ZL and ZT from the lower one, 32 x 32 tiles through
-// shared memory (coalesced reads and writes); grid.y = 2 x samples.
-__global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long long bstride, int m) {
-    __shared__ float2 tile[32][33];
+// shared memory (coalesced reads and writes). A CTA moves one tile position
+// of MIRROR_MATS matrices (ZL and ZT of consecutive samples), so each CTA
+// carries enough traffic to hide its start-up.
+constexpr int MIRROR_MATS = 8;
+__global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long long bstride, int m, int nmat) {
+    __shared__ float2 tile[2][32][33];
     const long long t = blockIdx.x;
     // lower tiles by block row: row block bk holds column blocks 0 .. bk
     int bk = (int)floor((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -710,17 +713,22 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
     while (bk > 0 && (long long)bk * (bk + 1) / 2 > t) --bk;
     while ((long long)(bk + 1) * (bk + 2) / 2 <= t) ++bk;
     const int bi = (int)(t - (long long)bk * (bk + 1) / 2);
-    const int smp = blockIdx.y >> 1;
-    float2* Z = ((blockIdx.y & 1) ? zt0 : zl0) + bstride * smp;
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
-    for (int j = ty; j < 32; j += 8) {
-        const int r = bk * 32 + tx, cc = bi * 32 + j;
-        if (r < m && cc < m && r > cc) tile[j][tx] = Z[r + (long long)m * cc];
-    }
-    __syncthreads();
-    for (int j = ty; j < 32; j += 8) {
-        const int cc = bi * 32 + tx, r = bk * 32 + j;     // element (row cc, column r) of the upper triangle
-        if (r < m && cc < m && r > cc) Z[cc + (long long)m * r] = tile[tx][j];
+    const int mat0 = blockIdx.y * MIRROR_MATS;
+    for (int q = 0; q < MIRROR_MATS; ++q) {
+        const int mat = mat0 + q;                      // 2 x sample + (0: ZL, 1: ZT)
+        if (mat >= nmat) break;
+        float2* Z = ((mat & 1) ? zt0 : zl0) + bstride * (mat >> 1);
+        float2 (*T)[33] = tile[q & 1];                 // two buffers: one barrier per matrix
+        for (int j = ty; j < 32; j += 8) {
+            const int r = bk * 32 + tx, cc = bi * 32 + j;
+            if (r < m && cc < m && r > cc) T[j][tx] = Z[r + (long long)m * cc];
+        }
+        __syncthreads();
+        for (int j = ty; j < 32; j += 8) {
+            const int cc = bi * 32 + tx, r = bk * 32 + j;     // element (row cc, column r) of the upper triangle
+            if (r < m && cc < m && r > cc) Z[cc + (long long)m * r] = T[tx][j];
+        }
     }
 }
 
@@ -913,8 +921,8 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
         k_fill_touch<<<gt, 128, 0, st>>>(d_elec, d_img, m, w.list, w.nlist, w.recs, d_coef, nsamp, d_zl, d_zt, bstride,
                                          d_status);
     }
-    k_zmirror<<<dim3((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)(2 * nsamp)), 256, 0, st>>>(d_zl, d_zt,
-                                                                                                      bstride, m);
+    k_zmirror<<<dim3((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS)),
+                256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
     tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
     tags_note_launch(max_touch > 0 ? 4 : 3);
     TAGS_CUDA_OK(cudaGetLastError());
