@@ -163,6 +163,9 @@ int inv_laplace_trans (double *f, tags_cdouble *g, tags_cdouble *s, double tmax,
  * flags: TAGS_RUN_DEVICE_PTRS for device pointers (declared below). */
 int tags_inv_laplace_batch (double *f, const tags_cdouble *g, const tags_cdouble *s, double tmax, size_t nt,
                             size_t nseries, int filter, int flags);
+/* The same transform under the name of the batched extension. */
+int tags_gpu_inlt (double *f, const tags_cdouble *g, const tags_cdouble *s, double tmax, size_t nt, size_t nseries,
+                   int filter, int flags);
 
 /* ---- post-processing: potentials, fields, path voltage --------------------- */
 /* The tolerance arguments (max_eval, req_abs_error, req_rel_error) are
@@ -283,6 +286,32 @@ int tags_plan_run (tags_plan plan, const tags_cdouble *s, const tags_cdouble *ka
                    int *info, int flags, tags_run_stats *stats);
 
 int tags_plan_destroy (tags_plan plan);
+
+/* One grid of a many-grid run (tags_gpu_solve_batch): geometry, its samples
+ * and injections as for tags_plan_create / tags_plan_run, and where its
+ * solutions go (sol ns x (n + 2m) and info ns, either may be NULL). */
+typedef struct {
+    const Electrode *electrodes;
+    const Electrode *images;           /* NULL: no images */
+    size_t num_electrodes;
+    const double *nodes;
+    size_t num_nodes;
+    const tags_cdouble *s;
+    const tags_cdouble *kappa;
+    size_t ns;
+    const tags_cdouble *ie;            /* ns x n injected currents, or NULL: unit current at inj_node */
+    size_t inj_node;
+    tags_cdouble *sol;
+    int *info;
+} tags_grid_job;
+
+/* No counterpart function in the reference: many grids x many Laplace samples
+ * in one call (host buffers). A plan per grid, run from `workers` host threads
+ * (0 = 4) on the calling thread's device, so that grids of uneven size share
+ * the GPU; max_batch = samples resident per plan (0 = min(ns, 256)). Returns
+ * 0 or the first error code of any grid (the other grids still run). */
+int tags_gpu_solve_batch (const tags_grid_job *jobs, size_t njobs, int precision, double mur, size_t max_batch,
+                          int workers);
 
 /* Passes as CUDA graphs (default on): each pass shape (samples in the pass,
  * mur, injection form) is captured once into an executable graph holding

@@ -72,3 +72,26 @@ def test_grid_with_rods_n17875(gpu_pkg):
     print(f"\nN = 17875: mixed 2 samples {t_mixed:.2f} s (refinement steps <= {sm.max_iterations}, "
           f"backward error {sm.max_backward_error:.1e}), plain 1 sample {t_plain:.2f} s, rel err {err:.1e}")
     assert err < 1e-6
+
+
+def test_solve_batch_many_grids_matches_plans(gpu_pkg):
+    """tags_gpu_solve_batch (many grids x many samples in one C call) gives the
+    per-grid plans' solutions: three uneven grids, 12 samples each, plain FP64
+    to rounding and the mixed form within 1e-6 of it."""
+    pkg = gpu_pkg
+    from oracle import oracle as O
+    jobs = []
+    for k, (nv, L, seg) in enumerate([(3, 10.0, 2), (4, 12.0, 1), (2, 6.0, 3)]):
+        e, nd = pkg.electrode_grid(nv, nv, L, L, seg, seg, 7e-3, -0.5)
+        f = np.logspace(2, 6.5, 12)
+        s = 2j * np.pi * f + 1e3
+        kappa = 1.0 / (100.0 * (k + 1)) + s * 10.0 * O.EPS0
+        jobs.append({"electrodes": e, "images": pkg.images(e), "nodes": nd, "s": s, "kappa": kappa,
+                     "inj_node": k})
+    for precision, tol in ((pkg.PLAIN_FP64, 1e-13), (pkg.MIXED, 1e-6)):
+        got = pkg.solve_batch(jobs, precision=precision, workers=3)
+        ref = pkg.hem_sweep_grids(jobs, precision=pkg.PLAIN_FP64, workers=1)
+        for (sol, info), (rsol, rinfo, _) in zip(got, ref):
+            assert not np.any(info) and not np.any(rinfo)
+            err = np.max(np.abs(sol - rsol)) / np.max(np.abs(rsol))
+            assert err <= tol, (precision, err)

@@ -58,7 +58,8 @@ EXPORTS = (
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
-    "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations",
+    "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
+    "tags_gpu_inlt",
     "tags_gpu_set_quiet",
 )
 
@@ -77,6 +78,15 @@ class c_complex(ctypes.Structure):
 class TuneResult(ctypes.Structure):
     _fields_ = [("samples_per_pass", ctypes.c_int), ("panels_per_update", ctypes.c_int), ("split", ctypes.c_int),
                 ("solves_per_second", ctypes.c_double), ("candidates", ctypes.c_int)]
+
+
+class GridJob(ctypes.Structure):
+    """tags_grid_job: one grid of a tags_gpu_solve_batch call (pointers as integers)."""
+
+    _fields_ = [("electrodes", ctypes.c_void_p), ("images", ctypes.c_void_p), ("num_electrodes", ctypes.c_size_t),
+                ("nodes", ctypes.c_void_p), ("num_nodes", ctypes.c_size_t), ("s", ctypes.c_void_p),
+                ("kappa", ctypes.c_void_p), ("ns", ctypes.c_size_t), ("ie", ctypes.c_void_p),
+                ("inj_node", ctypes.c_size_t), ("sol", ctypes.c_void_p), ("info", ctypes.c_void_p)]
 
 
 class RunStats(ctypes.Structure):
@@ -148,6 +158,8 @@ def lib() -> ctypes.CDLL:
             L.tags_gpd_mhem_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _sz, _sz, _vp, _vp, _vp]
             L.tags_voltage_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, _sz, _vp, _vp, _vp, d, _vp]
             L.tags_fields_evaluations.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
+            L.tags_gpu_solve_batch.argtypes = [ctypes.POINTER(GridJob), _sz, ctypes.c_int, d, _sz, ctypes.c_int]
+            L.tags_gpu_inlt.argtypes = [_vp, _vp, _vp, d, _sz, _sz, ctypes.c_int, ctypes.c_int]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
             L.tags_gpu_set_quiet.argtypes = [ctypes.c_int]
@@ -159,7 +171,7 @@ def lib() -> ctypes.CDLL:
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
-                         "tags_voltage_batch", "tags_fields_evaluations"):
+                         "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -786,6 +798,33 @@ def hem_sweep_grids(jobs, precision=MIXED, max_batch=0, workers=8, graphs=True, 
 
     with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
         return list(ex.map(one, jobs))
+
+
+def solve_batch(jobs, precision=MIXED, mur: float = 1.0, max_batch: int = 0, workers: int = 4):
+    """Many grids x many samples in one C call (tags_gpu_solve_batch). Jobs as
+    for hem_sweep_grids (dicts with electrodes, images, nodes, s, kappa and ie
+    or inj_node); returns [(solution ns x (n + 2m), info)] in job order."""
+    keep, out = [], []
+    arr = (GridJob * len(jobs))()
+    for q, job in enumerate(jobs):
+        e = _elec(job["electrodes"])
+        im = None if job.get("images") is None else _elec(job["images"])
+        nd = np.ascontiguousarray(job["nodes"], dtype=np.float64)
+        sv = np.ascontiguousarray(np.atleast_1d(job["s"]), dtype=np.complex128)
+        ns = sv.shape[0]
+        kv = np.ascontiguousarray(np.broadcast_to(job["kappa"], (ns,)), dtype=np.complex128)
+        ie = job.get("ie")
+        if ie is not None:
+            ie = np.ascontiguousarray(ie, dtype=np.complex128).reshape(ns, nd.shape[0])
+        sol = np.zeros((ns, nd.shape[0] + 2 * e.shape[0]), np.complex128)
+        info = np.zeros(ns, np.int32)
+        keep += [e, im, nd, sv, kv, ie]
+        out.append((sol, info))
+        arr[q] = GridJob(_addr(e), None if im is None else _addr(im), e.shape[0], _addr(nd), nd.shape[0], _addr(sv),
+                         _addr(kv), ns, None if ie is None else _addr(ie), int(job.get("inj_node", 0)), _addr(sol),
+                         _addr(info))
+    _ret(lib().tags_gpu_solve_batch(arr, len(jobs), int(precision), float(mur), int(max_batch), int(workers)))
+    return out
 
 
 # ---- multi-GPU helpers (host side) ------------------------------------------------------
