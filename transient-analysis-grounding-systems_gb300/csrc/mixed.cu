@@ -84,46 +84,53 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 // One CTA per (column j, sample) walks rows j .. N-1. Node rows of a segment
 // column hold its two incidence entries (start +1 / end -1 in the ZL columns,
 // 0.5 in the ZT columns), read once per CTA from the per-segment list.
+constexpr int BUILD_COLS = 4;      // columns of W'' per CTA (enough traffic per CTA to hide its start-up)
+
 __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const Incidence inc,
                                                const double* __restrict__ scale, int m, int n,
                                                float2* __restrict__ A) {
     const int N = n + 2 * m;
-    const int j = blockIdx.x, b = blockIdx.y;
+    const int b = blockIdx.y;
     const double* d = scale + (size_t)b * N;
     const float2* Zb = Z + (size_t)b * 2 * m * m;
-    float2* Aj = A + (size_t)b * N * N + (size_t)j * N;
-    const int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
-    const float dj = (float)d[j];
     // the segment's incidence entries (two for a well-formed grid)
     __shared__ int s_nd[8];
     __shared__ float s_a[8];
-    int q0 = 0, cnt = 0;
-    if (bj < 2) {
-        const int e = j - bj * m;
-        q0 = inc.seg_ptr[e];
-        cnt = inc.seg_ptr[e + 1] - q0;
-    }
-    if ((int)threadIdx.x < min(cnt, 8)) {
-        s_nd[threadIdx.x] = inc.seg_node[q0 + threadIdx.x];
-        s_a[threadIdx.x] = bj == 0 ? (float)inc.seg_a[q0 + threadIdx.x] : 0.5f;
-    }
-    __syncthreads();
-    for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
-        const int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
-        float vx = 0.f, vy = 0.f;
-        if (bi < 2 && bj == bi) {
-            const float2 z = Zb[(size_t)bi * m * m + (i - bi * m) + (size_t)m * (j - bj * m)];
-            vx = -z.x;
-            vy = -z.y;
-        } else if (bi == 2 && bj < 2) {
-            const int nd = i - 2 * m;
-            for (int q = 0; q < cnt; ++q) {
-                const int ndq = q < 8 ? s_nd[q] : inc.seg_node[q0 + q];
-                if (ndq == nd) vx = q < 8 ? s_a[q] : (bj == 0 ? (float)inc.seg_a[q0 + q] : 0.5f);
-            }
+    for (int c = 0; c < BUILD_COLS; ++c) {
+        const int j = blockIdx.x * BUILD_COLS + c;
+        if (j >= N) break;
+        float2* Aj = A + (size_t)b * N * N + (size_t)j * N;
+        const int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
+        const float dj = (float)d[j];
+        int q0 = 0, cnt = 0;
+        if (bj < 2) {
+            const int e = j - bj * m;
+            q0 = inc.seg_ptr[e];
+            cnt = inc.seg_ptr[e + 1] - q0;
         }
-        const float s = (float)d[i] * dj;
-        Aj[i] = make_float2(vx * s, vy * s);
+        __syncthreads();                          // the previous column's entries are read
+        if ((int)threadIdx.x < min(cnt, 8)) {
+            s_nd[threadIdx.x] = inc.seg_node[q0 + threadIdx.x];
+            s_a[threadIdx.x] = bj == 0 ? (float)inc.seg_a[q0 + threadIdx.x] : 0.5f;
+        }
+        __syncthreads();
+        for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
+            const int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
+            float vx = 0.f, vy = 0.f;
+            if (bi < 2 && bj == bi) {
+                const float2 z = Zb[(size_t)bi * m * m + (i - bi * m) + (size_t)m * (j - bj * m)];
+                vx = -z.x;
+                vy = -z.y;
+            } else if (bi == 2 && bj < 2) {
+                const int nd = i - 2 * m;
+                for (int q = 0; q < cnt; ++q) {
+                    const int ndq = q < 8 ? s_nd[q] : inc.seg_node[q0 + q];
+                    if (ndq == nd) vx = q < 8 ? s_a[q] : (bj == 0 ? (float)inc.seg_a[q0 + q] : 0.5f);
+                }
+            }
+            const float s = (float)d[i] * dj;
+            Aj[i] = make_float2(vx * s, vy * s);
+        }
     }
 }
 
@@ -211,7 +218,7 @@ TAGS_D F2 f2_mac(F2 a, float z, float xh, float xl) {
 // x is split into float pairs), so its result is accurate to ~2^-44 of
 // |Z| |x| without FP64 arithmetic in the m^2 loop.
 constexpr int RES_CHUNK = 1024;
-__global__ void __launch_bounds__(256) k_residual_z(const float2* __restrict__ Z, const Incidence inc, int m, int n,
+__global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z, const Incidence inc, int m, int n,
                                                     const double2* __restrict__ bvec, const double2* __restrict__ x,
                                                     double2* __restrict__ r, double* __restrict__ norms,
                                                     const int* __restrict__ active) {
@@ -477,7 +484,8 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     tags_note_launch(2);
     // 3. FP32 working matrix and its LDL^T (no pivoting)
     int pf = tags_prof_begin(TAGS_PROF_BUILD, st);
-    k_build<<<dim3((unsigned)N, nb), 256, 0, st>>>(p->d_Z, p->inc, p->d_scale, m, n, p->d_A);
+    k_build<<<dim3((unsigned)((N + BUILD_COLS - 1) / BUILD_COLS), nb), 256, 0, st>>>(p->d_Z, p->inc, p->d_scale, m, n,
+                                                                                  p->d_A);
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
@@ -516,7 +524,7 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
     k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);
-    k_residual_z<<<dim3((m + 255) / 256, 2 * nb), 256, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
+    k_residual_z<<<dim3((m + 127) / 128, 2 * nb), 128, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);
     // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
     tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
