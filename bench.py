@@ -219,7 +219,8 @@ def run_reference(args):
     from oracle import oracle as O
     port = O.get("port")
     times = []
-    steps = max(1, min(args.steps, args.ref_steps))     # each step is ~10-15 s of all host cores
+    # each step is ~10-15 s of all host cores
+    steps = args.ref_steps if args.steps <= 0 else max(1, min(args.steps, args.ref_steps))
     for step in range(steps):
         idx = (np.arange(nsamp) * 127 + step * 61) % len(s)
         t0 = time.perf_counter()
@@ -307,6 +308,8 @@ def run_fields(args):
     if rank != 0:
         return 0
     torch.cuda.set_device(local)
+    if args.steps <= 0:
+        args.steps = 8
     import __graft_entry__ as entry
     pkg = entry.load_package()
     pkg.build()
@@ -384,7 +387,9 @@ def run_fields(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=16, help="timed steps (16 x 128 samples = the whole 2048-sample job)")
+    ap.add_argument("--steps", type=int, default=0,
+                    help="timed steps (0: the whole 2048-sample job once, 8 steps of 2 x 128 samples)")
+    ap.add_argument("--pipelines", type=int, default=0, help="passes in flight per step (0: 2 mixed, 1 plain)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
@@ -418,11 +423,17 @@ def main():
     m, n = elec.shape[0], nodes.shape[0]
     N = n + 2 * m
     mixed = args.precision == "mixed"
-    B = args.batch or (128 if mixed else 8)
+    B = args.batch or (128 if mixed else 8)          # samples per pass
+    P = args.pipelines or (2 if mixed else 1)         # passes in flight per step
+    SB = B * P                                        # samples per step
     plan = pkg.Plan(elec, img, nodes, pkg.MIXED if mixed else pkg.PLAIN_FP64, max_batch=B)
     if mixed and args.split:
         plan.set_split(args.split)
+    if P > 1:
+        plan.set_pipelines(P)
     ns_total = len(s)
+    if args.steps <= 0:
+        args.steps = max(1, -(-ns_total // (SB * world)))
     dev = torch.device("cuda", local)
     # inputs resident in HBM; each rank takes its own strided share of samples
     s_d = torch.from_numpy(s).to(dev)
@@ -430,13 +441,13 @@ def main():
     ie_full = np.zeros((ns_total, n), np.complex128)
     ie_full[:, centre] = inj
     ie_d = torch.from_numpy(ie_full).to(dev)
-    sol_d = torch.empty((B, N), dtype=torch.complex128, device=dev)
-    info_d = torch.empty((B,), dtype=torch.int32, device=dev)
+    sol_d = torch.empty((SB, N), dtype=torch.complex128, device=dev)
+    info_d = torch.empty((SB,), dtype=torch.int32, device=dev)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)   # > L2
 
     def batch_index(step):
-        start = (((args.first_batch + step) * world + rank) * B) % ns_total
-        return start, min(B, ns_total - start)
+        start = (((args.first_batch + step) * world + rank) * SB) % ns_total
+        return start, min(SB, ns_total - start)
 
     def run_step(step):
         k0, nb = batch_index(step)
@@ -476,24 +487,27 @@ def main():
     # the measured pass: every batch one CUDA-graph launch (the default path)
     plan.set_graphs(not args.no_graphs)
     dev_time, stats_iter, stats_fb, launches, clk, wall, _, split = timed(False)
-    # the same steps kernel by kernel with per-family events: kernel shares and roofline
+    # the same steps kernel by kernel with per-family events, one pass in flight
+    # (kernels timed alone): kernel shares and roofline
     plan.set_graphs(False)
+    plan.set_pipelines(1)
     prof_time, _, _, _, _, _, prof, _ = timed(True)
     plan.set_graphs(not args.no_graphs)
+    plan.set_pipelines(P)
     if world > 1:
         t = torch.tensor([dev_time], device=dev, dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_time = float(t.item())
         dist.barrier()
-    samples = B * args.steps * world
+    samples = sum(batch_index(st_i)[1] for st_i in range(args.steps)) * world
     value = samples / dev_time
 
     # end to end through the public API with host (pinned) buffers
     s_h = torch.from_numpy(s).pin_memory()
     k_h = torch.from_numpy(kappa).pin_memory()
     ie_h = torch.from_numpy(ie_full).pin_memory()
-    sol_h = torch.empty((B, N), dtype=torch.complex128).pin_memory()
-    info_h = torch.empty((B,), dtype=torch.int32).pin_memory()
+    sol_h = torch.empty((SB, N), dtype=torch.complex128).pin_memory()
+    info_h = torch.empty((SB,), dtype=torch.int32).pin_memory()
     e2e_steps = max(1, args.steps)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -504,8 +518,9 @@ def main():
         if code != 0:
             raise RuntimeError(pkg.last_error())
     e2e_t = time.perf_counter() - t0
-    e2e = {"value": B * e2e_steps / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": B * 16 * (2 + n),
-           "d2h_bytes_per_step": B * (16 * N + 4)}
+    e2e_samples = sum(batch_index(st_i)[1] for st_i in range(e2e_steps))
+    e2e = {"value": e2e_samples / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": SB * 16 * (2 + n),
+           "d2h_bytes_per_step": SB * (16 * N + 4)}
 
     # accuracy of the measured form against the plain FP64 form: 16 strided
     # samples, node potentials for the injected current (outside the timed region)
@@ -534,8 +549,9 @@ def main():
             "data": "synthetic (reference grid generator, Alipio soil, 1.2/50 us current)",
             "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, 1417 nodes, N=4537, 2048 Laplace "
                                    "samples (nt=4094, 10 MHz), Alipio soil sigma0=1 mS/m, centre injection",
-                       "precision": args.precision, "samples_per_step": B, "l2": "flushed between steps (256 MB write)",
-                       "timed_samples": "batches in frequency order from the first sample (16 steps = all 2048)",
+                       "precision": args.precision, "samples_per_step": SB, "samples_per_pass": B,
+                       "passes_in_flight": P, "l2": "flushed between steps (256 MB write)",
+                       "timed_samples": "batches in frequency order from the first sample (the default steps cover all 2048 once)",
                        "cuda_graphs": not args.no_graphs},
             "roofline": roof, "kernel_families": fams,
             "profiled_pass": {"ms_per_step": 1e3 * prof_time / args.steps,

@@ -313,6 +313,15 @@ typedef struct {
 int tags_gpu_solve_batch (const tags_grid_job *jobs, size_t njobs, int precision, double mur, size_t max_batch,
                           int workers);
 
+/* Passes in flight (1 = default, or 2): with 2 the plan builds a twin of the
+ * same geometry and settings (twice the device memory) and a run of several
+ * passes gives every other pass to the twin, on its own stream from a second
+ * host thread, so that one pass's latency-bound phases (diagonal blocks,
+ * triangular sweeps, refinement steps) overlap the other's dense work. The
+ * run's statistics cover both; its device time spans both streams. Going
+ * back to 1 keeps the twin's memory until the plan is destroyed. */
+int tags_plan_set_pipelines (tags_plan plan, int pipelines);
+
 /* Passes as CUDA graphs (default on): each pass shape (samples in the pass,
  * mur, injection form) is captured once into an executable graph holding
  * the fill, the factorisation and, for TAGS_MIXED, a conditional while-node

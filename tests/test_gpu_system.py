@@ -241,3 +241,33 @@ def test_batched_inverse_laplace_matches_single_series(gpu_pkg):
             for q in range(G.shape[1]):
                 assert np.array_equal(F[:, q], pkg.inv_laplace_trans(G[:, q].copy(), s, 1e-4, nt, filt))
             assert rel_err(F[:, 0], gd[f"inv_{nt}_{filt}"]) < 4e-16 * nt * nt
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_two_pipelines_match_one(gpu_pkg, graphs):
+    """A plan with two passes in flight (a twin plan takes every other pass on
+    its own stream, from a second host thread) gives the single-pipeline
+    solutions and statistics: config 2 grid, 72 samples in passes of 16 (five
+    passes, the last ragged), with graphs and kernel by kernel, host buffers."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    img = pkg.images(e)
+    idx = np.linspace(0, len(gd["s"]) - 1, 72).astype(int)
+    s, kappa = gd["s"][idx], gd["kappa"][idx]
+    ie = np.zeros((len(idx), nodes.shape[0]), np.complex128)
+    ie[:, 0] = gd["inj_s"][idx]
+    plan = pkg.Plan(e, img, nodes, pkg.MIXED, max_batch=16, graphs=graphs)
+    try:
+        one, info1, st1 = plan.run(s, kappa, 1.0, ie)
+        plan.set_pipelines(2)
+        two, info2, st2 = plan.run(s, kappa, 1.0, ie)
+        plan.set_split(3)                       # settings follow to the twin
+        three, info3, _ = plan.run(s, kappa, 1.0, ie)
+    finally:
+        plan.close()
+    assert np.all(info1 == 0) and np.all(info2 == 0) and np.all(info3 == 0)
+    assert st1.max_iterations == st2.max_iterations and st1.fallbacks == st2.fallbacks == 0
+    assert np.max(np.abs(two - one)) <= 1e-12 * np.max(np.abs(one))
+    assert np.max(np.abs(three[:, 0] - gd["u0"][idx]) / np.abs(gd["u0"][idx])) < 1e-6
+    assert st2.seconds > 0

@@ -56,7 +56,7 @@ EXPORTS = (
     "solve_immittance", "fill_incidence_adm", "fill_impedance_adm", "calculate_yla_ytb", "fill_impedance_adm2",
     "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
-    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
     "tags_gpu_inlt",
@@ -142,6 +142,7 @@ def lib() -> ctypes.CDLL:
                                         ctypes.c_int, ctypes.POINTER(RunStats)]
             L.tags_plan_destroy.argtypes = [_vp]
             L.tags_plan_set_graphs.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_set_pipelines.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_fill.argtypes = [_vp, ctypes.c_int]
             L.tags_inv_laplace_batch.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int, ctypes.c_int]
@@ -169,6 +170,7 @@ def lib() -> ctypes.CDLL:
                          "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
                          "inv_laplace_trans",
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
+                         "tags_plan_set_pipelines",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
                          "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt"):
@@ -665,6 +667,10 @@ class Plan:
             raise RuntimeError(f"tags_plan_create failed ({code}): {last_error()}")
         self.handle = h
         self.set_graphs(graphs)
+
+    def set_pipelines(self, n):
+        """1 or 2 passes in flight (2: a twin plan takes every other pass)."""
+        _ret(lib().tags_plan_set_pipelines(self.handle, int(n)))
 
     def set_split(self, pieces):
         """Split form of the mixed form's tensor-core products: SPLIT_BF16_3,

@@ -9,6 +9,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <thread>
 #include <vector>
 
 #include "tags_common.cuh"
@@ -158,7 +159,9 @@ static void plan_free(tags_plan_s* p) {
     if (p->ev0) cudaEventDestroy(p->ev0);
     if (p->ev1) cudaEventDestroy(p->ev1);
     if (p->stream) cudaStreamDestroy(p->stream);
+    tags_plan_s* tw = p->twin;
     delete p;
+    plan_free(tw);
 }
 
 extern "C" int tags_plan_create(tags_plan* out, const Electrode* electrodes, const Electrode* images,
@@ -175,6 +178,15 @@ extern "C" int tags_plan_create(tags_plan* out, const Electrode* electrodes, con
     if (!ctx) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
     tags_plan_s* p = new tags_plan_s();
     p->device = ctx->device;
+    {
+        const double* e = reinterpret_cast<const double*>(electrodes);
+        p->h_elec.assign(e, e + 11 * num_electrodes);
+        if (images) {
+            const double* im = reinterpret_cast<const double*>(images);
+            p->h_img.assign(im, im + 11 * num_electrodes);
+        }
+        p->h_nodes.assign(nodes, nodes + 3 * num_nodes);
+    }
     p->precision = precision;
     p->m = (int)num_electrodes;
     p->n = (int)num_nodes;
@@ -483,19 +495,14 @@ extern "C" int tags_plan_set_graphs(tags_plan plan, int enable) {
     return 0;
 }
 
-extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
-                             const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags,
-                             tags_run_stats* stats) {
-    tags_plan_s* p = plan;
-    if (!p || !s || !kappa) return tags_fail(TAGS_E_ARG, "tags_plan_run: invalid argument");
-    if (!ie && inj_node >= (size_t)p->n) return tags_fail(TAGS_E_ARG, "tags_plan_run: inj_node out of range");
-    if (ns == 0) return 0;
-    TAGS_CUDA_OK(cudaSetDevice(p->device));
+// Passes first, first + stride, ... of a run (pass q covers samples q * per_pass
+// onwards) on plan p's stream; per-sample statistics folded into *acc.
+static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
+                      const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags, size_t per_pass,
+                      size_t first, size_t stride, tags_run_stats* acc) {
     cudaStream_t st = p->stream;
     const bool dev = (flags & TAGS_RUN_DEVICE_PTRS) != 0;
     const long long N = p->N;
-    DeviceCtx* ctx = tags_ctx();
-    if (!ctx) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
     // staging for host inputs
     double2* d_in = nullptr;
     if (!dev && !p->use_graphs) {
@@ -509,12 +516,7 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
         }
         d_in = p->d_stage;
     }
-    std::vector<int> h_info;
-    if (stats) memset(stats, 0, sizeof(*stats));
-    TAGS_CUDA_OK(cudaMemsetAsync(p->d_status, 0, sizeof(int) * 4, st));
-    TAGS_CUDA_OK(cudaEventRecord(p->ev0, st));
-    const size_t per_pass = p->pass_batch > 0 && p->pass_batch < p->batch ? p->pass_batch : p->batch;
-    for (size_t k0 = 0; k0 < ns; k0 += per_pass) {
+    for (size_t k0 = first * per_pass; k0 < ns; k0 += stride * per_pass) {
         const int nb = (int)std::min<size_t>(per_pass, ns - k0);
         const double2 *ds, *dk, *die = nullptr;
         if (p->use_graphs) {
@@ -568,12 +570,10 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
             if (err) return err;
         }
         if (p->precision != TAGS_PLAIN_FP64) {
-            if (stats) {
-                for (int q = 0; q < nb; ++q) {
-                    stats->max_iterations = std::max(stats->max_iterations, iters[q]);
-                    stats->max_backward_error = std::max(stats->max_backward_error, berr[q]);
-                    if (!conv[q]) stats->fallbacks++;
-                }
+            for (int q = 0; q < nb; ++q) {
+                acc->max_iterations = std::max(acc->max_iterations, iters[q]);
+                acc->max_backward_error = std::max(acc->max_backward_error, berr[q]);
+                if (!conv[q]) acc->fallbacks++;
             }
         }
         if (sol) {
@@ -586,18 +586,117 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
         }
         if (!dev) TAGS_CUDA_OK(cudaStreamSynchronize(st));   // staging buffer reused by the next pass
     }
+    return 0;
+}
+
+// The twin follows the plan's settings (split, panels per update, samples per
+// pass, graphs, fill model) before it takes passes.
+static int sync_twin(tags_plan_s* p) {
+    tags_plan_s* t = p->twin;
+    if (t->split_pieces != p->split_pieces || t->group_panels != p->group_panels || t->pass_batch != p->pass_batch) {
+        t->split_pieces = p->split_pieces;
+        t->group_panels = p->group_panels;
+        t->pass_batch = p->pass_batch;
+        tags_plan_drop_graphs(t);
+    }
+    t->use_graphs = p->use_graphs;
+    if (t->fill_model != p->fill_model) return tags_plan_set_fill(t, p->fill_model);
+    return 0;
+}
+
+extern "C" int tags_plan_set_pipelines(tags_plan plan, int pipelines) {
+    tags_plan_s* p = plan;
+    if (!p || p->twin == p) return tags_fail(TAGS_E_ARG, "tags_plan_set_pipelines: invalid plan");
+    if (pipelines != 1 && pipelines != 2) return tags_fail(TAGS_E_ARG, "tags_plan_set_pipelines: 1 or 2");
+    TAGS_CUDA_OK(cudaSetDevice(p->device));
+    if (pipelines == 1) {           // the twin (if any) is kept for a later switch back
+        p->pipelines = 1;
+        return 0;
+    }
+    if (!p->twin) {
+        tags_plan t = nullptr;
+        const size_t m = (size_t)p->m, n = (size_t)p->n;
+        int err = tags_plan_create(&t, reinterpret_cast<const Electrode*>(p->h_elec.data()),
+                                   p->h_img.empty() ? nullptr : reinterpret_cast<const Electrode*>(p->h_img.data()), m,
+                                   p->h_nodes.data(), n, p->precision, (size_t)p->batch);
+        if (err) return err;
+        if (t->batch != p->batch) {
+            plan_free(t);
+            return tags_fail(TAGS_E_NOMEM, "tags_plan_set_pipelines: no room for a second pipeline of the same batch");
+        }
+        p->twin = t;
+        err = sync_twin(p);
+        if (err) return err;
+    }
+    p->pipelines = 2;
+    return 0;
+}
+
+extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
+                             const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags,
+                             tags_run_stats* stats) {
+    tags_plan_s* p = plan;
+    if (!p || !s || !kappa) return tags_fail(TAGS_E_ARG, "tags_plan_run: invalid argument");
+    if (!ie && inj_node >= (size_t)p->n) return tags_fail(TAGS_E_ARG, "tags_plan_run: inj_node out of range");
+    if (ns == 0) return 0;
+    TAGS_CUDA_OK(cudaSetDevice(p->device));
+    cudaStream_t st = p->stream;
+    DeviceCtx* ctx = tags_ctx();
+    if (!ctx) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
+    if (stats) memset(stats, 0, sizeof(*stats));
+    tags_run_stats acc{}, acc2{};
+    TAGS_CUDA_OK(cudaMemsetAsync(p->d_status, 0, sizeof(int) * 4, st));
+    const size_t per_pass = p->pass_batch > 0 && p->pass_batch < p->batch ? p->pass_batch : p->batch;
+    const size_t passes = (ns + per_pass - 1) / per_pass;
+    const bool two = p->twin && p->pipelines == 2 && passes >= 2;
+    if (two) {
+        if (int e = sync_twin(p)) return e;
+        TAGS_CUDA_OK(cudaMemsetAsync(p->twin->d_status, 0, sizeof(int) * 4, p->twin->stream));
+    }
+    TAGS_CUDA_OK(cudaEventRecord(p->ev0, st));
+    int err = 0;
+    if (two) {
+        // every other pass on the twin's stream, from a second host thread; the
+        // twin starts after ev0 so the run's device time spans both
+        tags_plan_s* t = p->twin;
+        TAGS_CUDA_OK(cudaStreamWaitEvent(t->stream, p->ev0, 0));
+        int err2 = 0;
+        std::thread th([&] {
+            if (cudaSetDevice(t->device) != cudaSuccess) {
+                err2 = TAGS_E_CUDA;
+                return;
+            }
+            err2 = run_passes(t, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, 1, 2, &acc2);
+            if (!err2 && cudaEventRecord(t->ev1, t->stream) != cudaSuccess) err2 = TAGS_E_CUDA;
+        });
+        err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, 0, 2, &acc);
+        th.join();
+        if (!err) err = err2;
+        if (!err) {
+            TAGS_CUDA_OK(cudaStreamWaitEvent(st, t->ev1, 0));
+            acc.max_iterations = std::max(acc.max_iterations, acc2.max_iterations);
+            acc.max_backward_error = std::max(acc.max_backward_error, acc2.max_backward_error);
+            acc.fallbacks += acc2.fallbacks;
+        }
+    } else {
+        err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, 0, 1, &acc);
+    }
+    if (err) return err;
     TAGS_CUDA_OK(cudaEventRecord(p->ev1, st));
-    int status = 0;
-    TAGS_CUDA_OK(cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int status[2] = {0, 0};
+    TAGS_CUDA_OK(cudaMemcpyAsync(&status[0], p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    if (two) TAGS_CUDA_OK(cudaMemcpyAsync(&status[1], p->twin->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaStreamSynchronize(st));
     if (stats) {
+        *stats = acc;
         float ms = 0.f;
         cudaEventElapsedTime(&ms, p->ev0, p->ev1);
         stats->seconds = ms * 1e-3;
         stats->split = p->precision == TAGS_PLAIN_FP64 ? 0 : p->split_pieces;
     }
-    if (status & TAGS_ST_DEGENERATE_PAIR)
+    const int stt = status[0] | status[1];
+    if (stt & TAGS_ST_DEGENERATE_PAIR)
         return tags_fail(TAGS_E_GEOMETRY, "coincident or overlapping segments: the pair integral diverges");
-    if (status & TAGS_ST_NONFINITE) return tags_fail(TAGS_E_NONFINITE, "non-finite value in the impedance fill");
+    if (stt & TAGS_ST_NONFINITE) return tags_fail(TAGS_E_NONFINITE, "non-finite value in the impedance fill");
     return 0;
 }

@@ -94,6 +94,13 @@ struct tags_plan_s {
     size_t stage_bytes = 0;
     double2* d_fbW = nullptr;       // N x N (allocated on the first fallback)
     int* d_fbpiv = nullptr;         // N + 1
+    // host copy of the geometry (11 doubles per segment; nodes 3 per node), so
+    // a twin plan can be built from it
+    std::vector<double> h_elec, h_img, h_nodes;
+    // second pipeline (tags_plan_set_pipelines): a plan of the same geometry
+    // and settings on its own stream; runs take every other pass
+    tags_plan_s* twin = nullptr;
+    int pipelines = 1;
 };
 
 int tags_plan_run_plain(tags_plan_s* p, const double2* d_s_unused, int nb, cudaStream_t st);
