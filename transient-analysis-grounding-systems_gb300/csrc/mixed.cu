@@ -44,7 +44,7 @@ TAGS_D void atomic_max_nonneg(double* addr, double v) {
 // Row maxima (and row sums) of the impedance blocks: Z is symmetric, so row k
 // equals column k (contiguous). One warp per (row, block, sample).
 __global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restrict__ scale, double* __restrict__ rsum,
-                           int N) {
+                           float* __restrict__ scalef, int N) {
     int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     int blk = blockIdx.y;       // 0 = ZL, 1 = ZT
     int b = blockIdx.z;
@@ -64,7 +64,9 @@ __global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restri
     if (lane == 0) {
         double inc = blk == 0 ? 1.0 : 0.5;            // incidence entries of the row
         int row = blk * m + warp;                      // reordered index
-        scale[(size_t)b * N + row] = 1.0 / sqrt(fmax((double)mx, inc));
+        const double sc = 1.0 / sqrt(fmax((double)mx, inc));
+        scale[(size_t)b * N + row] = sc;
+        scalef[(size_t)b * N + row] = (float)sc;             // the build's copy (no FP64 per element there)
         rsum[(size_t)b * N + row] = (double)sm + 2.0 * inc;
     }
 }
@@ -72,11 +74,12 @@ __global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restri
 // Node rows: max |entry| = 1 (A) so the scale is 1; row sum = sum over
 // incident segments of (1 + 0.5).
 __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m, double* __restrict__ scale,
-                                 double* __restrict__ rsum, int N) {
+                                 double* __restrict__ rsum, float* __restrict__ scalef, int N) {
     int nd = blockIdx.x * blockDim.x + threadIdx.x;
     int b = blockIdx.y;
     if (nd >= n) return;
     scale[(size_t)b * N + 2 * m + nd] = 1.0;
+    scalef[(size_t)b * N + 2 * m + nd] = 1.f;
     rsum[(size_t)b * N + 2 * m + nd] = 1.5 * (double)(node_ptr[nd + 1] - node_ptr[nd]);
 }
 
@@ -87,11 +90,11 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 constexpr int BUILD_COLS = 4;      // columns of W'' per CTA (enough traffic per CTA to hide its start-up)
 
 __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const Incidence inc,
-                                               const double* __restrict__ scale, int m, int n,
+                                               const float* __restrict__ scale, int m, int n,
                                                float2* __restrict__ A) {
     const int N = n + 2 * m;
     const int b = blockIdx.y;
-    const double* d = scale + (size_t)b * N;
+    const float* d = scale + (size_t)b * N;
     const float2* Zb = Z + (size_t)b * 2 * m * m;
     // the segment's incidence entries (two for a well-formed grid)
     __shared__ int s_nd[8];
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, con
         if (j >= N) break;
         float2* Aj = A + (size_t)b * N * N + (size_t)j * N;
         const int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
-        const float dj = (float)d[j];
+        const float dj = d[j];
         int q0 = 0, cnt = 0;
         if (bj < 2) {
             const int e = j - bj * m;
@@ -128,7 +131,7 @@ __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, con
                     if (ndq == nd) vx = q < 8 ? s_a[q] : (bj == 0 ? (float)inc.seg_a[q0 + q] : 0.5f);
                 }
             }
-            const float s = (float)d[i] * dj;
+            const float s = d[i] * dj;
             Aj[i] = make_float2(vx * s, vy * s);
         }
     }
@@ -395,7 +398,8 @@ int tags_mixed_alloc(tags_plan_s* p) {
     if (err) return err;
     TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_A, sizeof(float2) * N * N * b));
-    TAGS_CUDA_OK(cudaMalloc(&p->d_scale, sizeof(double) * 2 * N * b));   // scale + row sums
+    // scale + row sums (FP64), then an FP32 copy of the scale
+    TAGS_CUDA_OK(cudaMalloc(&p->d_scale, sizeof(double) * 2 * N * b + sizeof(float) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_r, sizeof(double2) * 2 * N * b));      // residual + right-hand side
     TAGS_CUDA_OK(cudaMalloc(&p->d_rf, sizeof(float2) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_norms, sizeof(double) * 4 * b));
@@ -479,12 +483,14 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
                                            p->d_status, st);
     if (err) return err;
     // 2. scaling
-    k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, N);
-    k_rowstats_nodes<<<dim3((n + 127) / 128, nb), 128, 0, st>>>(p->inc.node_ptr, n, m, p->d_scale, d_rsum, N);
+    float* d_scalef = reinterpret_cast<float*>(p->d_scale + 2 * (size_t)p->batch * N);
+    k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, d_scalef, N);
+    k_rowstats_nodes<<<dim3((n + 127) / 128, nb), 128, 0, st>>>(p->inc.node_ptr, n, m, p->d_scale, d_rsum, d_scalef,
+                                                                N);
     tags_note_launch(2);
     // 3. FP32 working matrix and its LDL^T (no pivoting)
     int pf = tags_prof_begin(TAGS_PROF_BUILD, st);
-    k_build<<<dim3((unsigned)((N + BUILD_COLS - 1) / BUILD_COLS), nb), 256, 0, st>>>(p->d_Z, p->inc, p->d_scale, m, n,
+    k_build<<<dim3((unsigned)((N + BUILD_COLS - 1) / BUILD_COLS), nb), 256, 0, st>>>(p->d_Z, p->inc, d_scalef, m, n,
                                                                                   p->d_A);
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
