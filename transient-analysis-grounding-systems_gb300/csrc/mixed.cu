@@ -193,27 +193,24 @@ __global__ void k_residual_nodes(const Incidence inc, int m, int n, const double
     atomic_max_nonneg(norms + 4 * b + 2, fabs(rv.x) + fabs(rv.y));
 }
 
-// Two-float helpers: a value is hi + lo with |lo| <= ulp(hi)/2 (~2^-48 relative).
+// Two-float accumulator: the running FP32 sum hi of the products' leading
+// parts and, in lo, every rounding error (of the products, exact by FMA, and of
+// the additions to hi, exact by TwoSum). lo stays ~2^-24 of hi, so its own
+// rounding is negligible and no renormalisation is needed until the end.
 struct F2 {
     float hi, lo;
 };
-TAGS_D F2 f2_add(F2 a, float p, float e) {
-    // a + (p + e), p the leading part of a product, e its rounding error
-    float s = a.hi + p;
-    float v = s - a.hi;
-    float t = (a.hi - (s - v)) + (p - v);
-    t += a.lo + e;
-    F2 o;
-    o.hi = s + t;
-    o.lo = t - (o.hi - s);
-    return o;
-}
 // a += z * (xh + xl) for real z (exact in FP32) and a two-float x
 TAGS_D F2 f2_mac(F2 a, float z, float xh, float xl) {
-    float p = z * xh;
+    const float p = z * xh;
     float e = fmaf(z, xh, -p);
     e = fmaf(z, xl, e);
-    return f2_add(a, p, e);
+    const float s = a.hi + p;                 // TwoSum(a.hi, p)
+    const float v = s - a.hi;
+    const float t = (a.hi - (s - v)) + (p - v);
+    a.hi = s;
+    a.lo += t + e;
+    return a;
 }
 
 // Impedance rows: r_k = b_k - (incidence terms - sum_j Z_kj x_j). The dense
