@@ -10,6 +10,7 @@ samples, cycling through the 2048-sample set. Prints one JSON line.
   python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|plain]
   python bench.py --impl reference      # the reference's CPU path on the host cores
   python bench.py --workload fields     # post-processing: potentials and field along a line
+  python bench.py --workload grids      # 64 grids of uneven size x 256 samples in one call
 """
 from __future__ import annotations
 
@@ -384,6 +385,92 @@ def run_fields(args):
     return 0
 
 
+# ---- many uneven grids ---------------------------------------------------------------
+# 64 square grids of uneven size (side 5-40 m, 2-10 meshes, 1 m segmentation,
+# m = 36..880), each with its own soil, 256 Laplace samples each (nt = 510,
+# 10 MHz), unit current at the first node: all through one
+# tags_gpu_solve_batch call (a plan per grid, plans in flight together).
+GRIDS_COUNT, GRIDS_NT = 64, 510
+GRIDS_TMAX = (GRIDS_NT // 2) / 10e6
+
+
+def grid_jobs(pkg, count=GRIDS_COUNT):
+    s = pkg.laplace_samples(GRIDS_NT, GRIDS_TMAX)
+    jobs = []
+    for g in pkg.uneven_grids(count, seed=0):
+        kappa = 1.0 / g["rho"] + s * g["epsr"] * pkg.EPS0
+        jobs.append({"electrodes": g["electrodes"], "images": pkg.images(g["electrodes"]), "nodes": g["nodes"],
+                     "s": s, "kappa": kappa, "inj_node": 0})
+    return jobs
+
+
+def run_grids(args):
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+    pkg = entry.load_package()
+    pkg.build()
+    jobs = grid_jobs(pkg)
+    ms = [j["electrodes"].shape[0] for j in jobs]
+    ns = len(jobs[0]["s"])
+    workers = args.pipelines or 4
+    pkg.solve_batch(jobs[:4], precision=pkg.MIXED, workers=workers)          # warm-up: modules, tables
+    torch.cuda.synchronize()
+    launches0 = pkg.launch_count()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        out = pkg.solve_batch(jobs, precision=pkg.MIXED, workers=workers)
+        wall = time.perf_counter() - t0
+    launches = pkg.launch_count() - launches0
+    if any(np.any(info) for _, info in out):
+        raise RuntimeError("a grid reported a failed sample")
+    solves = len(jobs) * ns
+    # accuracy: mixed against plain FP64 on four grids, 16 strided samples each
+    idx = np.linspace(0, ns - 1, 16).astype(int)
+    sub = [dict(j, s=j["s"][idx], kappa=j["kappa"][idx]) for j in (jobs[0], jobs[21], jobs[42], jobs[63])]
+    mx = pkg.solve_batch(sub, precision=pkg.MIXED, workers=2)
+    pl = pkg.solve_batch(sub, precision=pkg.PLAIN_FP64, workers=2)
+    err = max(float(np.max(np.abs(a[0][:, 0] - b[0][:, 0]) / np.abs(b[0][:, 0]))) for a, b in zip(mx, pl))
+    line = {"metric": "Laplace-sample solves/s over 64 uneven grids (m = %d..%d), 256 samples each" % (min(ms), max(ms)),
+            "value": solves / wall, "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64+c128", "data": "synthetic (reference grid generator; per-grid soil)",
+            "config": {"workload": "64 square grids, side 5-40 m, 2-10 meshes, 1 m segmentation, depth 0.3-1 m, "
+                                   "rho 50-5000 ohm m, eps_r 5-40; 256 Laplace samples each (nt = 510, 10 MHz); "
+                                   "one tags_gpu_solve_batch call, %d host threads" % workers,
+                       "grids": len(jobs), "segments": [min(ms), max(ms)]},
+            "roofline": None, "gpu_launches": launches, "clocks": clk.summary(),
+            "e2e": {"value": solves / wall, "unit": "solves/s",
+                    "h2d_bytes_per_step": int(sum(16 * ns * 2 for _ in jobs)),
+                    "d2h_bytes_per_step": int(sum(ns * (16 * (j["nodes"].shape[0] + 2 * j["electrodes"].shape[0]) + 4)
+                                                  for j in jobs))},
+            "accuracy": {"grids": 4, "samples": 16, "reference": "plain FP64 form of this library",
+                         "max_rel_err_u_inj": err},
+            "note": "value is end to end: plan set-up (allocation, pair plan, graph capture) of every grid is inside "
+                    "the timed call; the kernels are those of the solves workload, whose line carries their roofline"}
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        port = O.get("port")
+        cores = os.cpu_count() or 1
+        sidx = np.linspace(0, ns - 1, cores).astype(int)
+        picked = (0, 21, 42, 63)
+        t0 = time.perf_counter()
+        for q in picked:
+            j = jobs[q]
+            port.hem_sweep(j["electrodes"], j["images"], j["nodes"], j["s"][sidx], j["kappa"][sidx], 0,
+                           np.ones(len(sidx)), req_abs=1e-6, req_rel=1e-6, threads=cores)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(picked) * len(sidx) / dt, "unit": "solves/s", "cores": cores,
+                                "kind": "port",
+                                "sample": f"grids {picked} (m = {[ms[q] for q in picked]}), {len(sidx)} strided samples "
+                                          f"each, path A at the reference's tolerances, {dt:.1f} s"}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,13 +489,16 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     ap.add_argument("--first-batch", type=int, default=0,
                     help="batch of samples the warm-up and timed steps start from (0 = the whole job in order)")
-    ap.add_argument("--workload", default="solves", choices=["solves", "fields"],
-                    help="solves: the per-sample HEM path (default); fields: post-processing along a line")
+    ap.add_argument("--workload", default="solves", choices=["solves", "fields", "grids"],
+                    help="solves: the per-sample HEM path (default); fields: post-processing along a line; "
+                         "grids: 64 uneven grids in one call")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "fields":
         return run_fields(args)
+    if args.workload == "grids":
+        return run_grids(args)
 
     import torch
     import torch.distributed as dist

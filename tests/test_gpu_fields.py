@@ -142,3 +142,22 @@ def test_empty_and_zero_currents(gpu_pkg):
     assert not np.any(out["pot"]) and not np.any(out["vecpot"]) and not np.any(out["efield"])
     out = pkg.fields_batch(d["points"], d["elec"][:0], z[:, :, :0], z[:, :, :0], d["gamma"], d["kappa"])
     assert out["pot"].shape == (3, d["points"].shape[0], 2) and not np.any(out["pot"])
+
+
+def test_more_injections_than_one_pass(gpu_pkg, port):
+    """Six injections (the kernel takes four per pass over the electrodes) and
+    a single sample: every injection against the oracle."""
+    pkg = gpu_pkg
+    d = _field_case()
+    rng = np.random.default_rng(8)
+    m = d["elec"].shape[0]
+    il = rng.normal(size=(1, 6, m)) + 1j * rng.normal(size=(1, 6, m))
+    it = rng.normal(size=(1, 6, m)) + 1j * rng.normal(size=(1, 6, m))
+    pts = d["points"][:4]
+    out = pkg.fields_batch(pts, d["elec"], il, it, d["gamma"][1:2], d["kappa"][1:2])
+    for r in range(6):
+        for p in range(pts.shape[0]):
+            u = port.electric_potential(pts[p], d["elec"], it[0, r], d["gamma"][1], d["kappa"][1], 0, 1e-14, 1e-12)
+            va = port.magnetic_potential(pts[p], d["elec"], il[0, r], d["gamma"][1], 1.0, 0, 1e-14, 1e-12)
+            assert abs(out["pot"][0, p, r] - u) <= TOL * abs(u)
+            assert _close(out["vecpot"][0, p, r], va) <= TOL

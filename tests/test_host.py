@@ -146,3 +146,23 @@ def test_soil_models_match_reference(pkg, orc_mod):
         out = np.zeros(2, np.complex128)
         pkg.lib().alipio_soil(out[:1].ctypes.data, out[1:].ctypes.data, 1e-3, C.of(s), 1.26, 0.54, 12.0)
         assert np.max(np.abs(out - want) / np.abs(want)) <= 1e-13
+
+
+def test_solve_batch_rejects_bad_jobs(pkg):
+    """tags_gpu_solve_batch checks its jobs before touching the GPU: a job
+    without electrodes, or an injection node beyond the grid, is TAGS_E_ARG."""
+    import ctypes
+    L = pkg.lib()
+    e, nd = pkg.segment_electrode([0.0, 0.0, 0.0], [0.0, 0.0, -2.0], 4, 7e-3)
+    s = np.array([2j * np.pi * 1e3])
+    k = np.array([0.01 + 0j])
+    good = pkg.GridJob(e.ctypes.data, None, e.shape[0], nd.ctypes.data, nd.shape[0], s.ctypes.data, k.ctypes.data,
+                       1, None, 0, None, None)
+    bad_node = pkg.GridJob(e.ctypes.data, None, e.shape[0], nd.ctypes.data, nd.shape[0], s.ctypes.data,
+                           k.ctypes.data, 1, None, nd.shape[0], None, None)
+    no_elec = pkg.GridJob(None, None, 0, nd.ctypes.data, nd.shape[0], s.ctypes.data, k.ctypes.data, 1, None, 0,
+                          None, None)
+    for job in (bad_node, no_elec):
+        arr = (pkg.GridJob * 2)(good, job)
+        assert L.tags_gpu_solve_batch(arr, 2, pkg.MIXED, 1.0, 0, 2) == pkg.E_ARG
+    assert L.tags_gpu_solve_batch(None, 0, pkg.MIXED, 1.0, 0, 2) == 0
