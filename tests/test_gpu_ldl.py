@@ -85,7 +85,7 @@ def _banded_sym(rng, N, zl_m, dominance):
 
 
 @pytest.mark.parametrize("pieces,group", [(3, 4), (16, 4), (16, 2), (16, 1)])
-@pytest.mark.parametrize("N,zl_m", [(300, 0), (517, 0), (700, 150), (1000, 300)])
+@pytest.mark.parametrize("N,zl_m", [(300, 0), (517, 0), (700, 150), (1000, 300), (1500, 400)])
 def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group):
     """One solve with the tensor-core factors (block-inverse sweeps, the
     diagonal, the zero ZL/ZT band skipped when zl_m > 0; 4, 2 or 1 panels per

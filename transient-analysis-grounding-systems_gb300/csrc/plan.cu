@@ -225,7 +225,7 @@ extern "C" int tags_plan_create(tags_plan* out, const Electrode* electrodes, con
     const double NN = (double)N * (double)N;
     double per = precision == TAGS_PLAIN_FP64
                      ? 16.0 * NN + 40.0 * N
-                     : 8.0 * NN + 32.0 * (double)p->m * p->m + 80.0 * N;
+                     : 8.0 * NN + 32.0 * (double)p->m * p->m + 80.0 * N + (double)tags_ldl_tc_workspace((int)N, 1);
     long long cap = (long long)(0.45 * (double)freeb / per);
     long long b = max_batch ? (long long)max_batch : std::min<long long>(cap, 64);
     if (b > cap) b = cap;
