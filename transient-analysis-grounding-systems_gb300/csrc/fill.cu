@@ -732,58 +732,118 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
     }
 }
 
-// Pairs sharing an endpoint (log-singular): the Duffy rule in FP64, added to
-// what k_fill_mixed wrote (lower triangle). One thread per (listed pair, sample).
-__global__ void __launch_bounds__(128) k_fill_touch(const double* __restrict__ elec, const double* __restrict__ img,
-                                                    int m, const int* __restrict__ list, const int* __restrict__ nlist,
-                                                    const PairRec* __restrict__ recs,
-                                                    const SampleCoef* __restrict__ coef, int nsamp, float2* zl0,
-                                                    float2* zt0, long long bstride, int* status) {
-    __shared__ double sx[GL_TOTAL], sw[GL_TOTAL];
-    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) { sx[t] = g_glx[t]; sw[t] = g_glw[t]; }
-    __syncthreads();
-    GLTab gl{sx, sw};
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    const int smp = blockIdx.y;
-    if (e >= *nlist || smp >= nsamp) return;
+// Pairs sharing an endpoint (log-singular): the Duffy rule of j_touch, added
+// to what k_fill_mixed wrote (lower triangle). One warp per listed pair and 32
+// samples (lanes): the rule's nodes (rho1, rho2 and w / rho of both Duffy
+// halves) are computed once per warp in FP64 and kept in shared memory as
+// float pairs; each lane then sums phi(gamma rho) w / rho in FP32, with
+// phi(x) = (1 - e^{-x}) / x from its series while |Re x| + |Im x| < 1, else
+// from the exactly reduced exponential (anchor_df). The order is the largest the
+// warp's samples ask for (10 + |gamma| L, at most QMAX).
+constexpr int TOUCH_WARPS = 4;
+
+struct TouchNode {
+    float rh, rl, wr;                      // rho = rh + rl, w / rho
+};
+
+TAGS_D float2 phi_touch(const SampleF32& c, float rh, float rl) {
+    const float xr = c.grh * rh, xi = c.gih * rh;
+    if (fabsf(xr) + fabsf(xi) < 1.f) {
+        // sum_k (-x)^k / (k+1)!, k <= 12: truncation below 1 / 14! ~ 1.1e-11
+        float2 term = make_float2(1.f, 0.f), acc = term;
+#pragma unroll
+        for (int k = 1; k <= 12; ++k) {
+            const float s = -1.f / (float)(k + 1);
+            term = make_float2(s * (term.x * xr - term.y * xi), s * (term.x * xi + term.y * xr));
+            acc.x += term.x;
+            acc.y += term.y;
+        }
+        return acc;
+    }
+    const float2 e = anchor_df(c.grh, c.grl, c.gih, c.gil, rh, rl);      // e^{-x}
+    const float nr = 1.f - e.x, ni = -e.y;
+    const float den = xr * xr + xi * xi;
+    return make_float2((nr * xr + ni * xi) / den, (ni * xr - nr * xi) / den);
+}
+
+__global__ void __launch_bounds__(TOUCH_WARPS * 32) k_fill_touch(
+    const double* __restrict__ elec, const double* __restrict__ img, int m, const int* __restrict__ list,
+    const int* __restrict__ nlist, const PairRec* __restrict__ recs, const SampleF32* __restrict__ coef, int nsamp,
+    float2* zl0, float2* zt0, long long bstride, int* status) {
+    __shared__ TouchNode nodes_all[TOUCH_WARPS][2 * QMAX];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    TouchNode* nodes = nodes_all[warp];
+    const int e = blockIdx.x * TOUCH_WARPS + warp;
+    if (e >= *nlist) return;                          // whole warp leaves together
+    const int smp = blockIdx.y * 32 + lane;
+    const bool valid = smp < nsamp;
+    SampleF32 c{};
+    if (valid) c = coef[smp];
     const long long p = list[2 * e];
     const int mask = list[2 * e + 1];
     int i, k;
     pair_index(p, m, i, k);
     Seg S, R;
     ld_seg(elec + 11LL * i, S);
-    const SampleCoef c = coef[smp];
-    double2 dl = cz(0.0, 0.0), dt = cz(0.0, 0.0);
-    for (int kind = 0; kind < 2; ++kind) {
+    float2 dl = make_float2(0.f, 0.f), dt = make_float2(0.f, 0.f);
+    bool bad = false;
+    for (int kind = 0; kind < 2 && !bad; ++kind) {
         if (!(mask & (1 << kind))) continue;
         ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
         const double lmax = fmax(S.len, R.len);
         int ia, ib;
-        if (!touching(R, S, 1e-9 * lmax, ia, ib)) {
-            raise_status(status, TAGS_ST_DEGENERATE_PAIR);      // coincident or overlapping
-            dl = dt = cz(nan(""), nan(""));
-            break;
+        bad = !touching(R, S, 1e-9 * lmax, ia, ib);       // coincident or overlapping
+        if (!bad) {
+            const double* ro = ia == 0 ? R.b : R.a;
+            const double* so = ib == 0 ? S.b : S.a;
+            bad = fmax(fabs(ro[0] - so[0]), fmax(fabs(ro[1] - so[1]), fabs(ro[2] - so[2]))) <= 1e-9 * lmax;
         }
-        const double* ro = ia == 0 ? R.b : R.a;
-        const double* so = ib == 0 ? S.b : S.a;
-        if (fmax(fabs(ro[0] - so[0]), fmax(fabs(ro[1] - so[1]), fabs(ro[2] - so[2]))) <= 1e-9 * lmax) {
-            raise_status(status, TAGS_ST_DEGENERATE_PAIR);
-            dl = dt = cz(nan(""), nan(""));
-            break;
+        if (bad) break;
+        const float gabs = sqrtf(c.grh * c.grh + c.gih * c.gih);
+        int q = valid ? min(QMAX, 10 + (int)ceilf(gabs * (float)lmax)) : 0;
+        q = __reduce_max_sync(0xffffffffu, q);
+        double a[3], b[3];
+        for (int d = 0; d < 3; ++d) {
+            a[d] = ia == 0 ? R.b[d] - R.a[d] : R.a[d] - R.b[d];
+            b[d] = ib == 0 ? S.b[d] - S.a[d] : S.a[d] - S.b[d];
         }
-        const int qt = min(QMAX, 10 + (int)ceil(sqrt(cabs2(c.gamma)) * lmax));
-        const double2 J = j_touch(R, S, ia, ib, c.gamma, false, qt, gl);
-        const double2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
-        dt = cadd(dt, cmul(cT, J));
-        dl = cadd(dl, cscale(cmul(cL, J), (double)recs[2 * p + kind].fl));
+        __syncwarp();
+        for (int qi = lane; qi < q; qi += 32) {
+            const double t = g_glx[gl_off(q) + qi], w = g_glw[gl_off(q) + qi];
+            const double u1[3] = {a[0] - t * b[0], a[1] - t * b[1], a[2] - t * b[2]};
+            const double u2[3] = {t * a[0] - b[0], t * a[1] - b[1], t * a[2] - b[2]};
+            const double r1 = sqrt(dot3(u1, u1)), r2 = sqrt(dot3(u2, u2));
+            const float r1h = (float)r1, r2h = (float)r2;
+            nodes[2 * qi] = TouchNode{r1h, (float)(r1 - (double)r1h), (float)(w / r1)};
+            nodes[2 * qi + 1] = TouchNode{r2h, (float)(r2 - (double)r2h), (float)(w / r2)};
+        }
+        __syncwarp();
+        float2 J = make_float2(0.f, 0.f);
+        if (valid) {
+            for (int j = 0; j < 2 * q; ++j) {
+                const TouchNode nd = nodes[j];
+                const float2 ph = phi_touch(c, nd.rh, nd.rl);
+                J.x = fmaf(nd.wr, ph.x, J.x);
+                J.y = fmaf(nd.wr, ph.y, J.y);
+            }
+        }
+        const float2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
+        const float fl = recs[2 * p + kind].fl;
+        dt.x += cT.x * J.x - cT.y * J.y;
+        dt.y += cT.x * J.y + cT.y * J.x;
+        dl.x += fl * (cL.x * J.x - cL.y * J.y);
+        dl.y += fl * (cL.x * J.y + cL.y * J.x);
     }
+    if (bad) {
+        if (lane == 0) raise_status(status, TAGS_ST_DEGENERATE_PAIR);
+        dl = dt = make_float2(nanf(""), nanf(""));
+    }
+    if (!valid) return;
     if (!isfinite(dl.x + dl.y + dt.x + dt.y)) raise_status(status, TAGS_ST_NONFINITE);
     const long long lo = bstride * smp + k + (long long)m * i;      // lower triangle (k_zmirror copies it up)
-    float2 a = zl0[lo], b = zt0[lo];
-    a = make_float2(a.x + (float)dl.x, a.y + (float)dl.y);
-    b = make_float2(b.x + (float)dt.x, b.y + (float)dt.y);
-    zl0[lo] = a;
-    zt0[lo] = b;
+    float2 za = zl0[lo], zb = zt0[lo];
+    zl0[lo] = make_float2(za.x + dl.x, za.y + dl.y);
+    zt0[lo] = make_float2(zb.x + dt.x, zb.y + dt.y);
 }
 
 __global__ void k_seg_dirs(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
@@ -917,9 +977,9 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
     k_fill_mixed<<<grid, FILL_WARPS * 32, 0, st>>>(d_elec, d_img, w.sdir, w.idir, w.selfv, m, w.codes, w.recs, w.c32,
                                                    nsamp, d_zl, d_zt, bstride, has_img, ntiles, d_status);
     if (max_touch > 0) {
-        dim3 gt((unsigned)((max_touch + 127) / 128), (unsigned)nsamp);
-        k_fill_touch<<<gt, 128, 0, st>>>(d_elec, d_img, m, w.list, w.nlist, w.recs, d_coef, nsamp, d_zl, d_zt, bstride,
-                                         d_status);
+        dim3 gt((unsigned)((max_touch + TOUCH_WARPS - 1) / TOUCH_WARPS), (unsigned)((nsamp + 31) / 32));
+        k_fill_touch<<<gt, TOUCH_WARPS * 32, 0, st>>>(d_elec, d_img, m, w.list, w.nlist, w.recs, w.c32, nsamp, d_zl, d_zt,
+                                                     bstride, d_status);
     }
     k_zmirror<<<dim3((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS)),
                 256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
