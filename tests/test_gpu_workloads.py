@@ -95,3 +95,30 @@ def test_solve_batch_many_grids_matches_plans(gpu_pkg):
             assert not np.any(info) and not np.any(rinfo)
             err = np.max(np.abs(sol - rsol)) / np.max(np.abs(rsol))
             assert err <= tol, (precision, err)
+
+
+@pytest.mark.parametrize("sigma", [1e-3, 0.05])
+def test_bent_wire_long_segments(gpu_pkg, sigma):
+    """A bent wire of 4 m segments (a 40 m horizontal run and a 20 m rod
+    down from its end): every neighbouring pair shares an endpoint, collinear
+    along each leg and at a right angle at the bend. From 1 kHz to 20 MHz
+    |gamma| L reaches ~5 (sigma = 1 mS/m) and ~12 (sigma = 50 mS/m), so the
+    touching-pair rule runs from its series branch to its reduced exponential
+    with up to 22 nodes per half. Mixed-form node potentials within 1e-6 of
+    the plain FP64 form's, and the longitudinal currents as well."""
+    pkg = gpu_pkg
+    eh, nh = pkg.segment_electrode([0.0, 0.0, -0.5], [40.0, 0.0, -0.5], 10, 7e-3)
+    ev, nv = pkg.segment_electrode([40.0, 0.0, -0.5], [40.0, 0.0, -20.5], 5, 7e-3)
+    e = np.vstack([eh, ev])
+    nodes = np.vstack([nh, nv[1:]])
+    img = pkg.images(e)
+    m, n = e.shape[0], nodes.shape[0]
+    f = np.array([1e3, 1e5, 1e6, 5e6, 1e7, 2e7])
+    s = 2e4 + 2j * np.pi * f
+    kappa = sigma + s * 10.0 * pkg.EPS0
+    xm, im, sm = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=0, precision=pkg.MIXED)
+    xp, ip, _ = pkg.hem_sweep(e, img, nodes, s, kappa, inj_node=0, precision=pkg.PLAIN_FP64)
+    assert np.all(im == 0) and np.all(ip == 0) and sm.fallbacks == 0
+    for k in range(len(s)):
+        assert _rel(xm[k, :n], xp[k, :n]) < 1e-6, (f[k], _rel(xm[k, :n], xp[k, :n]))
+        assert _rel(xm[k, n:n + m], xp[k, n:n + m]) < 1e-6, (f[k], _rel(xm[k, n:n + m], xp[k, n:n + m]))
