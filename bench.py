@@ -476,7 +476,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=0,
                     help="timed steps (0: the whole 2048-sample job once, 8 steps of 2 x 128 samples)")
-    ap.add_argument("--pipelines", type=int, default=0, help="passes in flight per step (0: 2 mixed, 1 plain)")
+    ap.add_argument("--pipelines", type=int, default=0, help="passes in flight (0: 2 mixed, 1 plain)")
+    ap.add_argument("--step-passes", type=int, default=0,
+                    help="passes per step, taken by the pipelines as they free up (0 = pipelines)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"])
@@ -515,7 +517,7 @@ def main():
     mixed = args.precision == "mixed"
     B = args.batch or (128 if mixed else 8)          # samples per pass
     P = args.pipelines or (2 if mixed else 1)         # passes in flight per step
-    SB = B * P                                        # samples per step
+    SB = B * (args.step_passes or P)                  # samples per step
     plan = pkg.Plan(elec, img, nodes, pkg.MIXED if mixed else pkg.PLAIN_FP64, max_batch=B)
     if mixed and args.split:
         plan.set_split(args.split)
@@ -551,11 +553,14 @@ def main():
         dist.barrier()
     # the timed steps walk the sample set from its first (lowest-frequency,
     # hardest-to-refine) batch: 16 steps of 128 samples are the whole job
+    step_ms = []
+
     def timed(profile):
         """K steps; each step's device time from the plan's events on its
         stream. profile=True: kernel by kernel with per-family events."""
         launches0 = pkg.launch_count()
         it_max, fb, dt, split = 0, 0, 0.0, 0
+        step_ms.clear()
         if profile:
             pkg.lib().tags_gpu_profile(1)      # per-family CUDA events on the launching stream
         with ClockSampler(local) as clk:
@@ -564,6 +569,7 @@ def main():
                 flush.zero_()
                 st = run_step(st_i)
                 dt += st.seconds
+                step_ms.append(round(st.seconds * 1e3, 3))
                 it_max = max(it_max, st.max_iterations)
                 fb += st.fallbacks
                 split = st.split
@@ -577,6 +583,7 @@ def main():
     # the measured pass: every batch one CUDA-graph launch (the default path)
     plan.set_graphs(not args.no_graphs)
     dev_time, stats_iter, stats_fb, launches, clk, wall, _, split = timed(False)
+    measured_step_ms = list(step_ms)
     # the same steps kernel by kernel with per-family events, one pass in flight
     # (kernels timed alone): kernel shares and roofline
     plan.set_graphs(False)
@@ -634,7 +641,8 @@ def main():
     roof, fams = roofline(prof, peaks, split)
     line = {"metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)", "value": value,
             "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * dev_time / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1e3 * dev_time / args.steps, "step_ms": measured_step_ms,
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128" if not mixed else "c64+c128",
             "data": "synthetic (reference grid generator, Alipio soil, 1.2/50 us current)",
             "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, 1417 nodes, N=4537, 2048 Laplace "

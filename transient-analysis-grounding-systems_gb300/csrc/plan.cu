@@ -7,6 +7,7 @@
 // (gamma = sqrt(s mur mu0 kappa), ref_t = (kappa - s eps0)/(kappa + s eps0),
 // ref_l = 1) and the right-hand side is [I_E; 0; 0] (src/linalg.h:61-68).
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <thread>
@@ -495,11 +496,12 @@ extern "C" int tags_plan_set_graphs(tags_plan plan, int enable) {
     return 0;
 }
 
-// Passes first, first + stride, ... of a run (pass q covers samples q * per_pass
-// onwards) on plan p's stream; per-sample statistics folded into *acc.
+// The passes of a run that plan p takes from the shared counter `next` (pass q
+// covers samples q * per_pass onwards), on p's stream; per-sample statistics
+// folded into *acc.
 static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
                       const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags, size_t per_pass,
-                      size_t first, size_t stride, tags_run_stats* acc) {
+                      std::atomic<size_t>* next, tags_run_stats* acc) {
     cudaStream_t st = p->stream;
     const bool dev = (flags & TAGS_RUN_DEVICE_PTRS) != 0;
     const long long N = p->N;
@@ -516,7 +518,9 @@ static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble*
         }
         d_in = p->d_stage;
     }
-    for (size_t k0 = first * per_pass; k0 < ns; k0 += stride * per_pass) {
+    // passes are taken in order from a counter shared with the other pipeline
+    // (if any): a pipeline takes the next pass once its last one has finished
+    for (size_t k0 = next->fetch_add(1) * per_pass; k0 < ns; k0 = next->fetch_add(1) * per_pass) {
         const int nb = (int)std::min<size_t>(per_pass, ns - k0);
         const double2 *ds, *dk, *die = nullptr;
         if (p->use_graphs) {
@@ -655,9 +659,10 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     }
     TAGS_CUDA_OK(cudaEventRecord(p->ev0, st));
     int err = 0;
+    std::atomic<size_t> next{0};
     if (two) {
-        // every other pass on the twin's stream, from a second host thread; the
-        // twin starts after ev0 so the run's device time spans both
+        // the twin takes passes on its own stream from a second host thread; it
+        // starts after ev0 so the run's device time spans both
         tags_plan_s* t = p->twin;
         TAGS_CUDA_OK(cudaStreamWaitEvent(t->stream, p->ev0, 0));
         int err2 = 0;
@@ -666,10 +671,10 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
                 err2 = TAGS_E_CUDA;
                 return;
             }
-            err2 = run_passes(t, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, 1, 2, &acc2);
+            err2 = run_passes(t, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &acc2);
             if (!err2 && cudaEventRecord(t->ev1, t->stream) != cudaSuccess) err2 = TAGS_E_CUDA;
         });
-        err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, 0, 2, &acc);
+        err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &acc);
         th.join();
         if (!err) err = err2;
         if (!err) {
@@ -679,7 +684,7 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
             acc.fallbacks += acc2.fallbacks;
         }
     } else {
-        err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, 0, 1, &acc);
+        err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &acc);
     }
     if (err) return err;
     TAGS_CUDA_OK(cudaEventRecord(p->ev1, st));
