@@ -145,31 +145,64 @@ TAGS_D int orig_of(int ip, int m, int n) {
 // rf = D P r (FP32)
 // (first kernel of a refinement step: also clears the step's reductions)
 __global__ void k_ir_rhs(const double2* __restrict__ r, const double* __restrict__ scale, int m, int n,
-                         float2* __restrict__ rf, double* __restrict__ norms) {
+                         float2* __restrict__ rf, double* __restrict__ norms, double* __restrict__ dots) {
     const int N = n + 2 * m;
     int ip = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (blockIdx.x == 0 && threadIdx.x < 3) norms[4 * b + threadIdx.x] = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x < 4) dots[4 * b + threadIdx.x] = 0.0;
     if (ip >= N) return;
     double2 v = r[(size_t)b * N + orig_of(ip, m, n)];
     double s = scale[(size_t)b * N + ip];
     rf[(size_t)b * N + ip] = make_float2((float)(v.x * s), (float)(v.y * s));
 }
 
-// x += P^T D y (FP64); norms[b*4 + 0] = max|dx|, [1] = max|x|
-__global__ void k_ir_update(const float2* __restrict__ y, const double* __restrict__ scale, int m, int n,
-                            double2* __restrict__ x, double* __restrict__ norms, const int* __restrict__ active) {
+// x += P^T D y (FP64); norms[b*4 + 0] = max|dx|, [1] = max|x|. From the
+// third step on also dots[b*4 + 0..3] = (Re, Im of sum conj(yp) y, sum |yp|^2,
+// sum |y|^2) against the previous step's correction yp, kept in yprev. 256
+// threads per CTA.
+__global__ void __launch_bounds__(256) k_ir_update(const float2* __restrict__ y, const double* __restrict__ scale,
+                                                   int m, int n, double2* __restrict__ x, double* __restrict__ norms,
+                                                   const int* __restrict__ active, float2* __restrict__ yprev,
+                                                   double* __restrict__ dots, const int* __restrict__ step) {
+    __shared__ double red[8][4];
     const int N = n + 2 * m;
     int ip = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (ip >= N || !active[b]) return;
-    double s = scale[(size_t)b * N + ip];
-    float2 yv = y[(size_t)b * N + ip];
-    double2 dx = make_double2((double)yv.x * s, (double)yv.y * s);
-    size_t o = (size_t)b * N + orig_of(ip, m, n);
-    double2 xv = cadd(x[o], dx);
-    x[o] = xv;
-    atomic_max_nonneg(norms + 4 * b + 0, fabs(dx.x) + fabs(dx.y));
-    atomic_max_nonneg(norms + 4 * b + 1, fabs(xv.x) + fabs(xv.y));
+    if (!active[b]) return;                                // the whole CTA
+    const bool dot = *step >= 2;
+    double a[4] = {0.0, 0.0, 0.0, 0.0};
+    if (ip < N) {
+        double s = scale[(size_t)b * N + ip];
+        float2 yv = y[(size_t)b * N + ip];
+        double2 dx = make_double2((double)yv.x * s, (double)yv.y * s);
+        size_t o = (size_t)b * N + orig_of(ip, m, n);
+        double2 xv = cadd(x[o], dx);
+        x[o] = xv;
+        atomic_max_nonneg(norms + 4 * b + 0, fabs(dx.x) + fabs(dx.y));
+        atomic_max_nonneg(norms + 4 * b + 1, fabs(xv.x) + fabs(xv.y));
+        float2* yp = yprev + (size_t)b * N + ip;
+        if (dot) {
+            const float2 pv = *yp;
+            a[0] = (double)pv.x * yv.x + (double)pv.y * yv.y;
+            a[1] = (double)pv.x * yv.y - (double)pv.y * yv.x;
+            a[2] = (double)pv.x * pv.x + (double)pv.y * pv.y;
+            a[3] = (double)yv.x * yv.x + (double)yv.y * yv.y;
+        }
+        *yp = yv;
+    }
+    if (!dot) return;                                      // the whole CTA
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_xor_sync(0xffffffffu, a[k], o);
+    if ((threadIdx.x & 31) == 0)
+        for (int k = 0; k < 4; ++k) red[threadIdx.x >> 5][k] = a[k];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += red[w][threadIdx.x];
+        atomicAdd(dots + 4 * b + threadIdx.x, t);
+    }
 }
+
 
 // r = b - W x with the structure of W_G; norms[2] = max|r|.
 // Node rows (sparse incidence, exact +-1 / 0.5) in FP64.
@@ -305,6 +338,7 @@ struct IrState {
     double* berr;
     int* step;       // steps done
     int* cont;       // 1 while another step is wanted
+    int* extr;       // per sample: the step of its last extrapolation (k_ir_extrap)
 };
 
 IrState ir_state(tags_plan_s* p) {
@@ -315,10 +349,45 @@ IrState ir_state(tags_plan_s* p) {
     s.iters = p->d_iri + 2 * b;
     s.step = p->d_iri + 3 * b;
     s.cont = p->d_iri + 3 * b + 1;
+    s.extr = p->d_iri + 3 * b + 2;
     s.prev_dx = p->d_ird;
     s.wnorm = p->d_ird + b;
     s.berr = p->d_ird + 2 * b;
     return s;
+}
+
+// Extrapolation against one slow mode. Near DC the scaled system keeps a mode
+// (the grid's common potential) that the FP32 factors reproduce poorly, and the
+// corrections then shrink by a nearly constant complex factor: y_k ~ lambda
+// y_{k-1}. When the last two corrections are that close to parallel (cosine
+// >= 0.9, 0.2 <= |lambda| <= 0.95), the error left in x is about
+// lambda / (1 - lambda) times the last correction, which is added (Aitken's
+// step, one vector). At most every other step, from the third on. The residual
+// that follows is computed from scratch, so a poor estimate costs a step, not
+// accuracy. Same grid as k_ir_update.
+__global__ void k_ir_extrap(const float2* __restrict__ y, const double* __restrict__ scale, int m, int n,
+                            double2* __restrict__ x, const double* __restrict__ dots, IrState s) {
+    const int N = n + 2 * m;
+    const int ip = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (!s.active[b]) return;
+    const int step = *s.step;
+    if (step < 2 || s.extr[b] == step - 1) return;
+    const double re = dots[4 * b], im = dots[4 * b + 1], pp = dots[4 * b + 2], yy = dots[4 * b + 3];
+    if (!(pp > 0.0) || !(yy > 0.0) || re * re + im * im < 0.81 * pp * yy) return;
+    const double lr = re / pp, li = im / pp, l2 = lr * lr + li * li;
+    if (!(l2 >= 0.04 && l2 <= 0.9025)) return;
+    const double dr = 1.0 - lr, di = -li, dd = dr * dr + di * di;
+    const double gr = (lr * dr + li * di) / dd, gi = (li * dr - lr * di) / dd;      // lambda / (1 - lambda)
+    if (ip == 0) s.extr[b] = step;
+    if (ip >= N) return;
+    const double sc = scale[(size_t)b * N + ip];
+    const float2 yv = y[(size_t)b * N + ip];
+    const double dxr = (double)yv.x * sc, dxi = (double)yv.y * sc;
+    const size_t o = (size_t)b * N + orig_of(ip, m, n);
+    double2 xv = x[o];
+    xv.x += gr * dxr - gi * dxi;
+    xv.y += gr * dxi + gi * dxr;
+    x[o] = xv;
 }
 
 // A sample refines unless its static-order factorisation hit a zero pivot
@@ -338,6 +407,7 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
     s.prev_dx[q] = INFINITY;
     s.wnorm[q] = norms[4 * q + 3];
     s.berr[q] = 0.0;
+    s.extr[q] = -10;
 }
 
 // After a refinement step: per sample, stop once the correction is below
@@ -358,16 +428,24 @@ __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ n
         const double be = rn / (s.wnorm[q] * xn + 1e-300);
         s.berr[q] = be;
         if (!(dx == dx) || !(xn == xn)) { s.active[q] = 0; continue; }
+        if (s.extr[q] == step) {
+            // extrapolated in this step: x moved by more than dx, and the next
+            // correction says nothing about the contraction
+            s.prev_dx[q] = -1.0;
+            any = 1;
+            continue;
+        }
         if (dx <= 1e-9 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
+        const double pdx = s.prev_dx[q];        // <= 0: no contraction estimate yet
         // contraction estimate rho = dx_k / dx_{k-1} (step 0 starts from x =
         // 0, so dx_0 = |x_0| and rho_1 is already one): the error left after
         // this correction is about rho dx_k; stop when four times that is
         // below 1e-8 |x|, a decade under the FP32 fill's own error
-        if (step >= 1) {
-            const double rho = dx / s.prev_dx[q];
+        if (step >= 1 && pdx > 0.0) {
+            const double rho = dx / pdx;
             if (rho <= 0.25 && 4.0 * rho * dx <= 1e-8 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
         }
-        if (step >= 2 && dx > 0.5 * s.prev_dx[q]) {
+        if (step >= 2 && pdx > 0.0 && dx > 0.5 * pdx) {
             s.conv[q] = be <= 1e-12;
             s.active[q] = 0;
             continue;
@@ -400,7 +478,9 @@ int tags_mixed_alloc(tags_plan_s* p) {
     TAGS_CUDA_OK(cudaMalloc(&p->d_r, sizeof(double2) * 2 * N * b));      // residual + right-hand side
     TAGS_CUDA_OK(cudaMalloc(&p->d_rf, sizeof(float2) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_norms, sizeof(double) * 4 * b));
-    TAGS_CUDA_OK(cudaMalloc(&p->d_iri, sizeof(int) * (3 * b + 2)));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_iri, sizeof(int) * (4 * b + 2)));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_yprev, sizeof(float2) * N * b));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_dots, sizeof(double) * 4 * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_ird, sizeof(double) * 3 * b));
     const size_t ws = tags_ldl_tc_workspace((int)N, (int)b);
     TAGS_CUDA_OK(cudaMalloc(&p->d_ldlws, ws));
@@ -413,11 +493,13 @@ int tags_mixed_alloc(tags_plan_s* p) {
 
 int tags_mixed_free(tags_plan_s* p) {
     void* ptrs[] = {p->d_Z,      p->d_A,      p->d_scale, p->d_r,      p->d_rf,  p->d_norms,
-                    p->d_fillws, p->d_ldlws, p->d_ldlerr, p->d_iri, p->d_ird};
+                    p->d_fillws, p->d_ldlws, p->d_ldlerr, p->d_iri, p->d_ird, p->d_yprev, p->d_dots};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     p->d_Z = nullptr;
     p->d_A = nullptr;
+    p->d_yprev = nullptr;
+    p->d_dots = nullptr;
     return 0;
 }
 
@@ -518,12 +600,14 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     double2* d_b = p->d_r + (size_t)p->batch * N;
     const IrState s = ir_state(p);
     dim3 gv((N + 255) / 256, nb);
-    k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf, p->d_norms);
+    k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf, p->d_norms, p->d_dots);
     tags_note_launch();
     // samples that stopped refining skip the sweeps (their x is left alone)
     int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st, s.active);
     if (err) return err;
-    k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active);
+    k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active, p->d_yprev, p->d_dots,
+                                    s.step);
+    k_ir_extrap<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_dots, s);
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
     k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);
@@ -532,7 +616,7 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
     tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
     k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, kMaxSteps, s, cond, set_cond);
-    tags_note_launch(4);
+    tags_note_launch(5);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
 }

@@ -62,6 +62,8 @@ struct tags_plan_s {
     double2* d_r = nullptr;         // batch x N residual (FP64)
     float2* d_rf = nullptr;         // batch x N correction right-hand side (FP32)
     double* d_norms = nullptr;      // batch x 4 reductions
+    float2* d_yprev = nullptr;      // batch x N previous refinement correction (FP32, as d_rf)
+    double* d_dots = nullptr;       // batch x 4 sums of the current against the previous correction
     void* d_fillws = nullptr;       // pair classes and geometry records of the mixed fill
     int n_touch = 0;                // pairs sharing an endpoint (FP64 Duffy rule)
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
@@ -72,7 +74,8 @@ struct tags_plan_s {
     SampleCoef* d_coef1 = nullptr;  // unit coefficients for the potentials
     int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
-    int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue
+    int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue,
+                                    // step of the last extrapolation (batch)
     double* d_ird = nullptr;        // refinement state: previous correction, max row sum, backward error
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // CUDA-graph passes: inputs staged in plan-owned buffers, one executable
