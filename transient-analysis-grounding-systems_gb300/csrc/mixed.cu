@@ -84,9 +84,11 @@ __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m,
 }
 
 // W'' (complex FP32, column-major N x N, reordered and scaled), lower triangle.
-// One CTA per (column j, sample) walks rows j .. N-1. Node rows of a segment
-// column hold its two incidence entries (start +1 / end -1 in the ZL columns,
-// 0.5 in the ZT columns), read once per CTA from the per-segment list.
+// A CTA writes BUILD_COLS columns of one sample, rows j .. N-1 of column j, in
+// at most three plain row ranges: the column's impedance block (-Z d_i d_j),
+// the zero ZT rows of a ZL column, and the node rows, which are zero but for
+// the segment's incidence entries (start +1 / end -1 in the ZL columns, 0.5 in
+// the ZT columns; node rows have scale 1), written after a barrier.
 constexpr int BUILD_COLS = 4;      // columns of W'' per CTA (enough traffic per CTA to hide its start-up)
 
 __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, const Incidence inc,
@@ -96,44 +98,33 @@ __global__ void __launch_bounds__(256) k_build(const float2* __restrict__ Z, con
     const int b = blockIdx.y;
     const float* d = scale + (size_t)b * N;
     const float2* Zb = Z + (size_t)b * 2 * m * m;
-    // the segment's incidence entries (two for a well-formed grid)
-    __shared__ int s_nd[8];
-    __shared__ float s_a[8];
+    const float2 zero = make_float2(0.f, 0.f);
     for (int c = 0; c < BUILD_COLS; ++c) {
         const int j = blockIdx.x * BUILD_COLS + c;
         if (j >= N) break;
         float2* Aj = A + (size_t)b * N * N + (size_t)j * N;
-        const int bj = j < m ? 0 : (j < 2 * m ? 1 : 2);
+        if (j >= 2 * m) {                                   // node columns: rows j .. N-1 are zero
+            for (int i = j + (int)threadIdx.x; i < N; i += blockDim.x) Aj[i] = zero;
+            continue;
+        }
         const float dj = d[j];
-        int q0 = 0, cnt = 0;
-        if (bj < 2) {
-            const int e = j - bj * m;
-            q0 = inc.seg_ptr[e];
-            cnt = inc.seg_ptr[e + 1] - q0;
+        const int bj = j < m ? 0 : 1, e = j - bj * m;
+        // zc[i] = Z_bj(i - bj m, e) for rows i of the column's impedance block
+        const float2* zc = Zb + (size_t)bj * m * m + (size_t)m * e - (size_t)bj * m;
+        for (int i = j + (int)threadIdx.x; i < (bj + 1) * m; i += blockDim.x) {
+            const float2 z = zc[i];
+            const float sc = d[i] * dj;
+            Aj[i] = make_float2(-z.x * sc, -z.y * sc);
         }
-        __syncthreads();                          // the previous column's entries are read
-        if ((int)threadIdx.x < min(cnt, 8)) {
-            s_nd[threadIdx.x] = inc.seg_node[q0 + threadIdx.x];
-            s_a[threadIdx.x] = bj == 0 ? (float)inc.seg_a[q0 + threadIdx.x] : 0.5f;
-        }
-        __syncthreads();
-        for (int i = j + threadIdx.x; i < N; i += blockDim.x) {
-            const int bi = i < m ? 0 : (i < 2 * m ? 1 : 2);
-            float vx = 0.f, vy = 0.f;
-            if (bi < 2 && bj == bi) {
-                const float2 z = Zb[(size_t)bi * m * m + (i - bi * m) + (size_t)m * (j - bj * m)];
-                vx = -z.x;
-                vy = -z.y;
-            } else if (bi == 2 && bj < 2) {
-                const int nd = i - 2 * m;
-                for (int q = 0; q < cnt; ++q) {
-                    const int ndq = q < 8 ? s_nd[q] : inc.seg_node[q0 + q];
-                    if (ndq == nd) vx = q < 8 ? s_a[q] : (bj == 0 ? (float)inc.seg_a[q0 + q] : 0.5f);
-                }
+        if (bj == 0)
+            for (int i = m + (int)threadIdx.x; i < 2 * m; i += blockDim.x) Aj[i] = zero;
+        for (int i = 2 * m + (int)threadIdx.x; i < N; i += blockDim.x) Aj[i] = zero;
+        __syncthreads();                                    // the zeros land before the entries
+        if (threadIdx.x == 0)
+            for (int q = inc.seg_ptr[e]; q < inc.seg_ptr[e + 1]; ++q) {
+                const float a = bj == 0 ? (float)inc.seg_a[q] : 0.5f;
+                Aj[2 * m + inc.seg_node[q]] = make_float2(a * dj, 0.f);
             }
-            const float s = d[i] * dj;
-            Aj[i] = make_float2(vx * s, vy * s);
-        }
     }
 }
 
