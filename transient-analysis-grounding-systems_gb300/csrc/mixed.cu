@@ -330,7 +330,28 @@ struct IrState {
     int* step;       // steps done
     int* cont;       // 1 while another step is wanted
     int* extr;       // per sample: the step of its last extrapolation (k_ir_extrap)
+    double* lam;     // per sample: |lambda| of that extrapolation
 };
+
+// Stopping test after a correction of max-norm dx, |x| = xn (max norm). pdx:
+// the previous correction's size (> 0; infinite before the first), or, after
+// an extrapolated step, minus the slow mode's |lambda|. The error left after
+// this correction is about rho dx for the measured contraction rho = dx / pdx
+// (rho <= 1/4), or the mode's tail |lambda| / (1 - |lambda|) dx; stop when four
+// times that is below 1e-8 |x|, a decade under the FP32 fill's own error. Step
+// 0 starts from x = 0 (dx_0 = |x_0|), so it never stops on the estimate.
+TAGS_D bool ir_converged(int step, double dx, double xn, double pdx) {
+    if (dx <= 1e-9 * xn) return true;
+    if (step >= 1 && pdx > 0.0) {
+        const double rho = dx / pdx;
+        return rho <= 0.25 && 4.0 * rho * dx <= 1e-8 * xn;
+    }
+    if (pdx < 0.0) {
+        const double l = -pdx;
+        return 4.0 * l / (1.0 - l) * dx <= 1e-8 * xn;
+    }
+    return false;
+}
 
 IrState ir_state(tags_plan_s* p) {
     const int b = p->batch;
@@ -344,32 +365,41 @@ IrState ir_state(tags_plan_s* p) {
     s.prev_dx = p->d_ird;
     s.wnorm = p->d_ird + b;
     s.berr = p->d_ird + 2 * b;
+    s.lam = p->d_ird + 3 * b;
     return s;
 }
 
-// Extrapolation against one slow mode. Near DC the scaled system keeps a mode
-// (the grid's common potential) that the FP32 factors reproduce poorly, and the
-// corrections then shrink by a nearly constant complex factor: y_k ~ lambda
-// y_{k-1}. When the last two corrections are that close to parallel (cosine
-// >= 0.9, 0.2 <= |lambda| <= 0.95), the error left in x is about
+// Extrapolation against one slow mode. At low frequencies the scaled system
+// keeps a mode (the grid's common potential) that the FP32 factors reproduce
+// poorly, and the corrections then shrink by a nearly constant complex factor:
+// y_k ~ lambda y_{k-1} (measured: cosine^2 = 1.000 between successive
+// corrections, |lambda| from 0.02 to 0.5). When the last two corrections are
+// that close to parallel (cosine >= 0.9, 0.01 <= |lambda| <= 0.95) and the
+// sample is not stopping at this step anyway, the error left in x is about
 // lambda / (1 - lambda) times the last correction, which is added (Aitken's
-// step, one vector). At most every other step, from the third on. The residual
-// that follows is computed from scratch, so a poor estimate costs a step, not
-// accuracy. Same grid as k_ir_update.
+// step, one vector). Never on two steps running (the correction after an
+// extrapolated step says nothing about lambda), and from the third step on.
+// The residual that follows is computed from scratch, so a poor estimate costs
+// a step, not accuracy. Same grid as k_ir_update.
 __global__ void k_ir_extrap(const float2* __restrict__ y, const double* __restrict__ scale, int m, int n,
-                            double2* __restrict__ x, const double* __restrict__ dots, IrState s) {
+                            double2* __restrict__ x, const double* __restrict__ norms, const double* __restrict__ dots,
+                            IrState s) {
     const int N = n + 2 * m;
     const int ip = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (!s.active[b]) return;
     const int step = *s.step;
     if (step < 2 || s.extr[b] == step - 1) return;
+    if (ir_converged(step, norms[4 * b + 0], norms[4 * b + 1], s.prev_dx[b])) return;
     const double re = dots[4 * b], im = dots[4 * b + 1], pp = dots[4 * b + 2], yy = dots[4 * b + 3];
     if (!(pp > 0.0) || !(yy > 0.0) || re * re + im * im < 0.81 * pp * yy) return;
     const double lr = re / pp, li = im / pp, l2 = lr * lr + li * li;
-    if (!(l2 >= 0.04 && l2 <= 0.9025)) return;
+    if (!(l2 >= 1e-4 && l2 <= 0.9025)) return;
     const double dr = 1.0 - lr, di = -li, dd = dr * dr + di * di;
     const double gr = (lr * dr + li * di) / dd, gi = (li * dr - lr * di) / dd;      // lambda / (1 - lambda)
-    if (ip == 0) s.extr[b] = step;
+    if (ip == 0) {
+        s.extr[b] = step;
+        s.lam[b] = sqrt(l2);
+    }
     if (ip >= N) return;
     const double sc = scale[(size_t)b * N + ip];
     const float2 yv = y[(size_t)b * N + ip];
@@ -420,22 +450,14 @@ __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ n
         s.berr[q] = be;
         if (!(dx == dx) || !(xn == xn)) { s.active[q] = 0; continue; }
         if (s.extr[q] == step) {
-            // extrapolated in this step: x moved by more than dx, and the next
-            // correction says nothing about the contraction
-            s.prev_dx[q] = -1.0;
+            // extrapolated in this step: x moved by more than dx; the next
+            // step measures its error against the mode's contraction
+            s.prev_dx[q] = -s.lam[q];
             any = 1;
             continue;
         }
-        if (dx <= 1e-9 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
-        const double pdx = s.prev_dx[q];        // <= 0: no contraction estimate yet
-        // contraction estimate rho = dx_k / dx_{k-1} (step 0 starts from x =
-        // 0, so dx_0 = |x_0| and rho_1 is already one): the error left after
-        // this correction is about rho dx_k; stop when four times that is
-        // below 1e-8 |x|, a decade under the FP32 fill's own error
-        if (step >= 1 && pdx > 0.0) {
-            const double rho = dx / pdx;
-            if (rho <= 0.25 && 4.0 * rho * dx <= 1e-8 * xn) { s.active[q] = 0; s.conv[q] = 1; continue; }
-        }
+        const double pdx = s.prev_dx[q];
+        if (ir_converged(step, dx, xn, pdx)) { s.active[q] = 0; s.conv[q] = 1; continue; }
         if (step >= 2 && pdx > 0.0 && dx > 0.5 * pdx) {
             s.conv[q] = be <= 1e-12;
             s.active[q] = 0;
@@ -472,7 +494,7 @@ int tags_mixed_alloc(tags_plan_s* p) {
     TAGS_CUDA_OK(cudaMalloc(&p->d_iri, sizeof(int) * (4 * b + 2)));
     TAGS_CUDA_OK(cudaMalloc(&p->d_yprev, sizeof(float2) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_dots, sizeof(double) * 4 * b));
-    TAGS_CUDA_OK(cudaMalloc(&p->d_ird, sizeof(double) * 3 * b));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_ird, sizeof(double) * 4 * b));
     const size_t ws = tags_ldl_tc_workspace((int)N, (int)b);
     TAGS_CUDA_OK(cudaMalloc(&p->d_ldlws, ws));
     TAGS_CUDA_OK(cudaMemset(p->d_ldlws, 0, ws));
@@ -598,7 +620,7 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     if (err) return err;
     k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active, p->d_yprev, p->d_dots,
                                     s.step);
-    k_ir_extrap<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_dots, s);
+    k_ir_extrap<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, p->d_dots, s);
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
     k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);

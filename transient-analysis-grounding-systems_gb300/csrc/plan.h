@@ -76,7 +76,8 @@ struct tags_plan_s {
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue,
                                     // step of the last extrapolation (batch)
-    double* d_ird = nullptr;        // refinement state: previous correction, max row sum, backward error
+    double* d_ird = nullptr;        // refinement state: previous correction, max row sum, backward error,
+                                    // |lambda| of the last extrapolation (batch each)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     // CUDA-graph passes: inputs staged in plan-owned buffers, one executable
     // graph per pass shape (samples, mu_r, injection form)
