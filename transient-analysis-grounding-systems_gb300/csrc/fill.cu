@@ -547,8 +547,10 @@ TAGS_D void fill_tile(long long t, int m, int& kb, int& i) {
 // in FP64 once per warp (a lane per panel pair), never per sample. Outputs
 // pass through a [row][sample] sub-tile so each store instruction writes 64
 // contiguous bytes per sample. Pairs that share an endpoint (log-singular)
-// are left to k_fill_touch.
-__global__ void __launch_bounds__(FILL_WARPS * 32) k_fill_mixed(
+// are left to k_fill_touch. Five CTAs per SM (their shared memory allows five;
+// 96 registers instead of 122): the point loop is latency-bound, so the extra
+// warps pay for the few spilled values outside it.
+__global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
     const double* __restrict__ elec, const double* __restrict__ img, const float4* __restrict__ sdir,
     const float4* __restrict__ idir, const float* __restrict__ selfv, int m, const uint16_t* __restrict__ codes,
     const PairRec* __restrict__ recs, const SampleF32* __restrict__ coef, int nsamp, float2* zl0, float2* zt0,
