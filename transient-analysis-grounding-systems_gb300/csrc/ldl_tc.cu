@@ -513,6 +513,11 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                     vi[j] *= unscale;
                 }
                 if (MODE == 0) {
+                    // rows of the next panel's block column below its diagonal
+                    // block go on as split planes only: the panel GEMM reads them
+                    // from the planes and then writes L21 over them in FP32, so
+                    // their FP32 store would be dead
+                    const bool planes_only = g.Np && J == 0 && I >= 1 && gr - TB < g.Mn;
                     // all loads of the chunk first, then the stores
                     float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + TB * J + cc * 16);
                     float2 cv[16];
@@ -522,9 +527,9 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         cv[j] = make_float2(cv[j].x - vr[j], cv[j].y - vi[j]);
-                        if (TB * J + cc * 16 + j < g.Nn) base_p[g.ld * j] = cv[j];
+                        if (!planes_only && TB * J + cc * 16 + j < g.Nn) base_p[g.ld * j] = cv[j];
                     }
-                    if (g.Np && J == 0 && I >= 1 && gr - TB < g.Mn) {
+                    if (planes_only) {
                         // the next panel's block column, as split planes
 #pragma unroll
                         for (int j = 0; j < 16; ++j)
