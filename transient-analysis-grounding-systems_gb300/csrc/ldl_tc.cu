@@ -518,16 +518,20 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                     // from the planes and then writes L21 over them in FP32, so
                     // their FP32 store would be dead
                     const bool planes_only = g.Np && J == 0 && I >= 1 && gr - TB < g.Mn;
+                    // in a diagonal tile (the updates' rows and columns share
+                    // their origin) only the lower triangle is live: the
+                    // diagonal-block kernel reads nothing above it
+                    const int cend = I == J ? min(g.Nn, gr + 1) : g.Nn;
                     // all loads of the chunk first, then the stores
                     float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + TB * J + cc * 16);
                     float2 cv[16];
 #pragma unroll
                     for (int j = 0; j < 16; ++j)
-                        if (TB * J + cc * 16 + j < g.Nn) cv[j] = base_p[g.ld * j];
+                        if (TB * J + cc * 16 + j < cend) cv[j] = base_p[g.ld * j];
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         cv[j] = make_float2(cv[j].x - vr[j], cv[j].y - vi[j]);
-                        if (!planes_only && TB * J + cc * 16 + j < g.Nn) base_p[g.ld * j] = cv[j];
+                        if (!planes_only && TB * J + cc * 16 + j < cend) base_p[g.ld * j] = cv[j];
                     }
                     if (planes_only) {
                         // the next panel's block column, as split planes
