@@ -8,8 +8,10 @@
 //                      shared memory, complex FP32);
 //   2. k_panel_planes: the block column A21 below it -> bf16 split planes;
 //   3. k_gemm_tc     : W21 = A21 L11^{-T} (the triangular solve as a GEMM),
-//                      L21 = W21 D1^{-1}, both written as split planes;
-//   4. k_gemm_tc     : A22 -= L21 W21^T on the lower 128 x 128 tiles.
+//                      L21 = W21 D1^{-1} in FP32 (for the solves) and
+//                      V21 = W21 D1^{-1/2} = L21 D1^{1/2} as split planes;
+//   4. k_gemm_tc     : A22 -= V21 V21^T (= L21 D1 L21^T) on the lower 128 x
+//                      128 tiles: one plane set feeds both operands.
 // The GEMMs run on the 5th-generation tensor cores: operands are staged in
 // shared memory by TMA (128-byte swizzle), tcgen05.mma (kind::f16, bf16 in,
 // FP32 accumulate) is issued by one thread, the two accumulators (real and
@@ -146,6 +148,17 @@ TAGS_D float2 crecip_f(float2 d) {
     return make_float2(a / den, -b / den);
 }
 
+// Principal square root of complex FP32 z, in the cancellation-free form:
+// with r = |z|, t = sqrt((r + |Re z|) / 2) is the larger part and the other is
+// |Im z| / (2 t). sqrt(0) = 0. Any fixed branch serves: only s * s = z is used.
+TAGS_D float2 csqrt_f(float2 z) {
+    const float r = hypotf(z.x, z.y);
+    if (r == 0.f) return make_float2(0.f, 0.f);
+    const float t = sqrtf(0.5f * (r + fabsf(z.x)));
+    const float u = 0.5f * fabsf(z.y) / t;
+    return z.x >= 0.f ? make_float2(t, copysignf(u, z.y)) : make_float2(u, copysignf(t, z.y));
+}
+
 // Split forms of an FP32 value, as 16-bit patterns (each piece the rounded
 // remainder of the previous ones):
 //   bf16: x = p[0] + ... + p[S-1], S = 2 or 3 (3 pieces keep FP32 precision);
@@ -195,7 +208,7 @@ template <int S> struct GemmCfg {
     static constexpr int STAGE = 2 * NPL * PST;      // A and B planes of one K block
     static constexpr int STAGES = S == 2 ? 3 : 2;
     static constexpr int BARS = 512;                  // mbarriers and the TMEM slot
-    static constexpr int DINV = 8 * 64 * 8;           // mode 1: 64 values of D^{-1} per epilogue warp
+    static constexpr int DINV = 2 * 8 * 64 * 8;       // mode 1: 64 values of D^{-1} and of D^{-1/2} per epilogue warp
     static constexpr int SMEM = STAGES * STAGE + 1024 + BARS + DINV;
 };
 
@@ -221,12 +234,12 @@ struct GemmArgs {
     long long ld, mstride;
     int row0, col0;            // matrix coordinates of output element (0, 0)
     const float2* dinv;        // per sample 128 values (mode 1)
-    uint16_t* Lp;              // planes written in mode 1: [sample][2S][R][KG] (a group's buffers)
-    uint16_t* Wp;
+    const float2* dsq;         // per sample 128 values of D^{-1/2} (mode 1)
+    uint16_t* Lp;              // V planes written in mode 1: [sample][2S][R][KG] (a group's buffer)
     int prow0;                 // mode 1: buffer row of output row 0
     int kcol0;                 // mode 1: buffer column of output column 0 (128 x panel index in the group)
     int band_planes;           // mode 1: skipped band tiles still write (zero) planes
-    long long pstride;         // elements per sample of the group buffers (Lp, Wp)
+    long long pstride;         // elements per sample of the group buffer (Lp)
     long long npstride;        // elements per sample of the block-column buffer (Np), rows of 128
     int R;                     // rows of a plane buffer
     int* err;                  // err[0]: a wait ran out (all CTAs stop); err[1]: fp16 range
@@ -464,7 +477,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
             if (skip) {
                 const int gr = TB * I + r;
                 if (MODE == 1 && g.band_planes && gr < g.M) {
-                    // rows of the zero band: L21 = W21 = 0 there; their planes are
+                    // rows of the zero band: L21 = V21 = 0 there; their planes are
                     // written (as zeros) so that a later update that no longer
                     // skips the band reads zeros, not another panel's values
                     float2 zv[16];
@@ -472,7 +485,6 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                     for (int j = 0; j < 16; ++j) zv[j] = make_float2(0.f, 0.f);
                     for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
                         store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, zv, f16, ovf);
-                        store_planes16<S>(g.Wp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, zv, f16, ovf);
                     }
                 }
                 // no update of this tile; if it holds rows of the next panel's
@@ -491,10 +503,12 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                 continue;
             }
             if (MODE == 1) {
-                // this warp's 64 columns of D^{-1}, staged before the wait
+                // this warp's 64 columns of D^{-1} and D^{-1/2}, staged before the wait
                 __syncwarp();
                 dinv_w[lane] = g.dinv[(long long)TB * smp + half * 64 + lane];
                 dinv_w[32 + lane] = g.dinv[(long long)TB * smp + half * 64 + 32 + lane];
+                dinv_w[8 * 64 + lane] = g.dsq[(long long)TB * smp + half * 64 + lane];
+                dinv_w[8 * 64 + 32 + lane] = g.dsq[(long long)TB * smp + half * 64 + 32 + lane];
                 __syncwarp();
             }
             if (!mbar_wait(tfull(acc), aphase, g.err)) break;
@@ -542,16 +556,16 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                     }
                 } else {
                     const float2* dv = dinv_w - half * 64;      // indexed by the tile column
-                    float2 lv[16], wv[16];
+                    const float2* sq = dv + 8 * 64;
+                    float2 vv[16];
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
                         const int c = cc * 16 + j;
-                        wv[j] = make_float2(vr[j], vi[j]);
-                        lv[j] = fmulc(wv[j], dv[c]);
-                        if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = lv[j];
+                        const float2 wv = make_float2(vr[j], vi[j]);
+                        vv[j] = fmulc(wv, sq[c]);
+                        if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = fmulc(wv, dv[c]);
                     }
-                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, lv, f16, ovf);
-                    store_planes16<S>(g.Wp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, wv, f16, ovf);
+                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, vv, f16, ovf);
                 }
             }
             tc_fence_before();
@@ -581,7 +595,8 @@ constexpr int DIAG_LD = TB + 1;        // padded row stride of the output stagin
 
 __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, long long ld, long long mstride, int j0,
                                                      int jb, uint16_t* __restrict__ linv_planes,
-                                                     float2* __restrict__ dinv, int* __restrict__ info,
+                                                     float2* __restrict__ dinv, float2* __restrict__ dsq,
+                                                     int* __restrict__ info,
                                                      float2* __restrict__ linv32, long long lstride, int NS, int f16,
                                                      int* __restrict__ err) {
     extern __shared__ __align__(16) float2 S[];        // L columns S[k * TB + i]; later X staged S[i * DIAG_LD + j]
@@ -653,7 +668,11 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
         }
     __syncthreads();
     if (tid == 0 && zero_at < jb && info[smp] == 0) info[smp] = j0 + zero_at + 1;
-    if (tid < TB) dinv[(long long)TB * smp + tid] = tid < jb ? crecip_f(dsh[tid]) : make_float2(0.f, 0.f);
+    if (tid < TB) {
+        const float2 di = tid < jb ? crecip_f(dsh[tid]) : make_float2(0.f, 0.f);
+        dinv[(long long)TB * smp + tid] = di;
+        dsq[(long long)TB * smp + tid] = csqrt_f(di);
+    }
     // ---- X = L11^{-1}: for k = 0..126, X[i, j] -= L[i, k] X[k, j] (i > k, j <= k);
     // row k of X is final once step k - 1 is done. Reuse a[][] for X.
 #pragma unroll
@@ -922,25 +941,25 @@ int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samp
 
 static long long linv32_stride(int N) { return (long long)((N + TB - 1) / TB) * 2 * TB * TB; }
 
-// Workspace layout (sized for SMAX pieces): A21 planes, L planes, W planes
-// (2 SMAX planes of N x 128 each per sample), L11^{-1} planes, D^{-1}, FP32
+// Workspace layout (sized for SMAX pieces): A21 planes, V planes (2 SMAX
+// planes of N x 128 each per sample), L11^{-1} planes, D^{-1}, D^{-1/2}, FP32
 // inverses of all diagonal blocks (and their transposes).
 static long long plane_stride(int N) { return (long long)2 * SMAX * N * TB; }
 
-// Workspace per sample: the block-column planes (rows of 128), the L and W
-// planes of a group of up to GMAX panels (rows of KG), the L11^{-1} planes,
-// D^{-1}, and the FP32 inverses of all diagonal blocks.
+// Workspace per sample: the block-column planes (rows of 128), the V planes
+// of a group of up to GMAX panels (rows of KG), the L11^{-1} planes, D^{-1},
+// D^{-1/2}, and the FP32 inverses of all diagonal blocks.
 size_t tags_ldl_tc_workspace(int N, int batch) {
     size_t plane = (size_t)plane_stride(N) * 2;
-    return (size_t)batch * ((1 + 2 * GMAX) * plane + (size_t)2 * SMAX * TB * TB * 2 + TB * sizeof(float2) +
+    return (size_t)batch * ((1 + GMAX) * plane + (size_t)2 * SMAX * TB * TB * 2 + 2 * TB * sizeof(float2) +
                             (size_t)linv32_stride(N) * sizeof(float2)) + 1024;
 }
 
 static float2* linv32_of(void* ws, int N, int batch_cap) {
     const long long pstride = plane_stride(N);
-    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + (1 + 2 * GMAX) * pstride * batch_cap;
+    uint16_t* Lin = reinterpret_cast<uint16_t*>(ws) + (1 + GMAX) * pstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
-    return dinv + (long long)TB * batch_cap;
+    return dinv + 2LL * TB * batch_cap;
 }
 
 static int num_sms() {
@@ -1038,17 +1057,16 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
     const long long pstride = plane_stride(N);           // block-column buffer, rows of 128
     const long long gstride = pstride * GMAX;             // group buffers, rows of KG
     uint16_t* A21p = reinterpret_cast<uint16_t*>(ws);
-    uint16_t* Lg = A21p + pstride * batch_cap;            // L and W planes of the current group of panels
-    uint16_t* Wg = Lg + gstride * batch_cap;
-    uint16_t* Lin = Wg + gstride * batch_cap;
+    uint16_t* Lg = A21p + pstride * batch_cap;            // V planes of the current group of panels
+    uint16_t* Lin = Lg + gstride * batch_cap;
     float2* dinv = reinterpret_cast<float2*>(Lin + (long long)2 * SMAX * TB * TB * batch_cap);
+    float2* dsq = dinv + (long long)TB * batch_cap;
     float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
     // the maps see a sample stride of 2 SMAX planes: declare that many planes
-    CUtensorMap mA21, mLg, mWg, mLin;
+    CUtensorMap mA21, mLg, mLin;
     int e = make_plane_map(&mA21, A21p, N, 2 * SMAX, batch_cap);
     if (!e) e = make_plane_map(&mLg, Lg, N, 2 * SMAX, batch_cap, KG);
-    if (!e) e = make_plane_map(&mWg, Wg, N, 2 * SMAX, batch_cap, KG);
     if (!e) e = make_plane_map(&mLin, Lin, TB, 2 * SMAX, batch_cap);
     if (e) return e;
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * nb, st));
@@ -1061,6 +1079,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.ld = ld;
         g.mstride = mstride;
         g.dinv = dinv;
+        g.dsq = dsq;
         g.pstride = gstride;
         g.npstride = pstride;
         g.R = N;
@@ -1082,8 +1101,8 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
     };
     auto diag = [&](int j0, int jb) {
         int pf = tags_prof_begin(TAGS_PROF_LDL_DIAG, st);
-        k_ldl_diag<<<nb, 512, TB * DIAG_LD * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, info, L32, ls,
-                                                              NS, f16, err);
+        k_ldl_diag<<<nb, 512, TB * DIAG_LD * sizeof(float2), st>>>(A, ld, mstride, j0, jb, Lin, dinv, dsq, info, L32,
+                                                              ls, NS, f16, err);
         tags_prof_end(TAGS_PROF_LDL_DIAG, pf, st, 4.0 / 3.0 * jb * (double)jb * jb * nb, 16.0 * jb * jb * nb);
         tags_note_launch();
     };
@@ -1102,7 +1121,6 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.row0 = jp + jb;
         g.col0 = jp;
         g.Lp = Lg;
-        g.Wp = Wg;
         g.prow0 = jp + jb - jg;
         g.kcol0 = TB * p;
         int pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
@@ -1132,7 +1150,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.Mn = Mn;
         g.Np = Mn > 0 ? A21p : nullptr;
         int pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
-        int e1 = launch_gemm(NS, mLg, mWg, g, st);
+        int e1 = launch_gemm(NS, mLg, mLg, g, st);
         // rank-K update outside the zero band: 8 K cells flops (cells: the triangle or the block column)
         const double r = M - (double)(g.zhi - g.zlo);
         const double K = g.kblocks * BK;
