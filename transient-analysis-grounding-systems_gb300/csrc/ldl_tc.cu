@@ -1131,7 +1131,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
                       (8.0 * rp * jb + 16.0 * rp * 128 * 2) * nb);
         return e1;
     };
-    // C -= L W^T over the first `np` panels of the group starting at jg, on
+    // C -= V V^T over the first `np` panels of the group starting at jg, on
     // rows (and, tri, columns) row0 .. row0 + M; the first tile column's new
     // values also become the next panel's block-column planes (Mn rows).
     auto update = [&](int jg, int np, int row0, int M, int Nn, bool tri, int Mn) {
