@@ -1106,9 +1106,10 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         tags_prof_end(TAGS_PROF_LDL_DIAG, pf, st, 4.0 / 3.0 * jb * (double)jb * jb * nb, 16.0 * jb * jb * nb);
         tags_note_launch();
     };
-    // W21 = A21 L11^{-T}, L21 = W21 D^{-1} for panel p of the group starting at
-    // jg (columns jp = jg + 128 p .. jp + jb): FP32 L21 into A, both as split
-    // planes into the group buffers at rows (row - jg) and columns 128 p ...
+    // W21 = A21 L11^{-T}, L21 = W21 D^{-1}, V21 = W21 D^{-1/2} for panel p of
+    // the group starting at jg (columns jp = jg + 128 p .. jp + jb): FP32 L21
+    // into A, V21 as split planes into the group buffer at rows (row - jg) and
+    // columns 128 p ...
     auto panel = [&](int jg, int p, int jb, int rest, bool band_planes) {
         const int jp = jg + TB * p;
         GemmArgs g = base();
