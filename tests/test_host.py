@@ -166,3 +166,23 @@ def test_solve_batch_rejects_bad_jobs(pkg):
         arr = (pkg.GridJob * 2)(good, job)
         assert L.tags_gpu_solve_batch(arr, 2, pkg.MIXED, 1.0, 0, 2) == pkg.E_ARG
     assert L.tags_gpu_solve_batch(None, 0, pkg.MIXED, 1.0, 0, 2) == 0
+
+
+def test_bench_reference_arm_contract():
+    """`bench.py --impl reference` (the CPU implementation of the path on the
+    host cores) prints one JSON line carrying the bench contract's keys, with
+    its own cpu_baseline and an e2e object without host-device traffic."""
+    import json
+    import subprocess
+    import sys
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0"], cwd=ROOT, capture_output=True, text=True, timeout=900)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    for key in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["metric"].startswith("Laplace-sample solves/s")
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    assert line["cpu_baseline"]["value"] == line["value"] and line["cpu_baseline"]["cores"] >= 1
