@@ -86,9 +86,16 @@ _lock = threading.Lock()
 _libs: dict[str, "Oracle"] = {}
 
 
+def reference_dir() -> str:
+    """Where the reference's sources are read from to build ``ref``: the
+    TAGS_REFERENCE_DIR environment variable, else a checkout named
+    ``reference`` beside this repository."""
+    return os.environ.get("TAGS_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
+
+
 def build(ref: bool = False) -> None:
     """Compile the restatement (and, with ``ref``, the reference) via oracle/Makefile."""
-    target = ["ref"] if ref else []
+    target = ["ref", "REF=" + reference_dir()] if ref else []
     subprocess.run(["make", "-s", "-C", HERE] + target, check=True)
 
 

@@ -13,7 +13,10 @@
 // calls on a device share it and it keeps the previous call's contents, so
 // calls that overlap on the GPU (other host threads, other streams) race.
 // The first call on each device looks up the array's device address; make that
-// first call before any stream capture.
+// first call before any stream capture. The address is kept for the life of
+// the process, so after cudaDeviceReset on a device the entry point must not
+// be called on that device again (the cached address belongs to the context
+// the reset destroyed).
 #include <cstdio>
 #include <mutex>
 
