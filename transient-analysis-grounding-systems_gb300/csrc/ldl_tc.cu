@@ -50,6 +50,10 @@ TAGS_HD long long plane_elem(int p, int R, int K, int row, int col) {
 }
 constexpr int SMAX = 3;                 // most bf16 pieces per real value (split products)
 constexpr uint64_t WAIT_NS = 50ull * 1000 * 1000;   // 50 ms per wait
+// Limit of the waits in the main loops of the tensor-core kernels (WAIT_NS
+// unless a test lowered it through tags_debug_tc_wait_limit). The waits that
+// let issued work finish after a failure always use WAIT_NS.
+__device__ unsigned long long g_tc_wait_ns = WAIT_NS;
 
 // ---- PTX wrappers ----------------------------------------------------------------
 
@@ -70,6 +74,8 @@ TAGS_D uint64_t globaltimer_ns() {
 // WAIT_NS of wall time; gives up early once any CTA raised `err`. Returns
 // false (and raises `err`) when the bound ran out.
 TAGS_D bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
+    const uint64_t lim = g_tc_wait_ns;
+    const unsigned mask = lim < WAIT_NS ? 0u : 255u;     // a lowered limit is checked at every try
     const uint64_t t0 = globaltimer_ns();
     for (unsigned it = 0;; ++it) {
         uint32_t ok;
@@ -79,12 +85,32 @@ TAGS_D bool mbar_wait(uint32_t bar, uint32_t parity, int* err) {
             : "r"(bar), "r"(parity)
             : "memory");
         if (ok) return true;
-        if ((it & 255) == 255) {
+        if ((it & mask) == mask) {
             if (*(volatile int*)err != 0) return false;
-            if (globaltimer_ns() - t0 > WAIT_NS) {
+            if (globaltimer_ns() - t0 > lim) {
                 atomicOr(err, 8);
                 return false;
             }
+        }
+    }
+}
+// Wait for the phase with parity `parity` of `bar` regardless of `err` (used
+// after a wait ran out, to let work already issued finish before the CTA
+// releases its resources), bounded by WAIT_NS; raises `err` if even that
+// bound runs out.
+TAGS_D bool mbar_wait_drain(uint32_t bar, uint32_t parity, int* err) {
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (ok) return true;
+        if (globaltimer_ns() - t0 > WAIT_NS) {
+            atomicOr(err, 8);
+            return false;
         }
     }
 }
@@ -360,6 +386,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
         uint32_t phase = 0;
         bool alive = true;
         int issued[4] = {0, 0, 0, 0};     // stages with a load whose completion nobody waited for yet
+        uint32_t ipar[4] = {0, 0, 0, 0};  // parity of the full-barrier phase each such load completes
         for (int t = blockIdx.x; t < total && alive; t += gridDim.x) {
             int smp, I, J;
             bool skip;
@@ -377,31 +404,18 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                         tma_load_5d(sb + (C::NPL + p) * PST, &tmB, 0, rb, kb, p, smp, full(stage));
                     }
                     issued[stage] = 1;
+                    ipar[stage] = phase;
                     if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
                 }
             }
             alive = __shfl_sync(0xffffffffu, alive ? 1 : 0, 0) != 0;
         }
-        if (lane == 0 && !alive) {
-            // let the copies in flight land before the CTA exits
-            const uint64_t t0 = globaltimer_ns();
-            for (int q = 0; q < C::STAGES; ++q) {
-                if (!issued[q]) continue;
-                uint32_t okq = 0;
-                while (!okq && globaltimer_ns() - t0 < WAIT_NS) {
-                    asm volatile(
-                        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                        : "=r"(okq)
-                        : "r"(full(q)), "r"(0u)
-                        : "memory");
-                    if (!okq)
-                        asm volatile(
-                            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                            : "=r"(okq)
-                            : "r"(full(q)), "r"(1u)
-                            : "memory");
-                }
-            }
+        if (lane == 0) {
+            // let the copies in flight land before the CTA exits (after a wait
+            // ran out anywhere in the CTA some may be unconsumed): each waits
+            // on the phase its stage was issued under
+            for (int q = 0; q < C::STAGES; ++q)
+                if (issued[q]) mbar_wait_drain(full(q), ipar[q], g.err);
         }
     } else if (warp == 1) {
         // ---- MMA issuer
@@ -448,15 +462,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
             }
             // every product issued is complete before tensor memory is released
             mma_commit(drain);
-            const uint64_t t0 = globaltimer_ns();
-            uint32_t okd = 0;
-            while (!okd && globaltimer_ns() - t0 < WAIT_NS) {
-                asm volatile(
-                    "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-                    : "=r"(okd)
-                    : "r"(drain), "r"(0u)
-                    : "memory");
-            }
+            mbar_wait_drain(drain, 0u, g.err);
         }
     } else {
         // ---- epilogue warps 2..9: warp w reads tensor-memory lanes 32 (w % 4) ...
@@ -1213,6 +1219,15 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
 // ---- diagnostic entry points (declared in include/tags_gpu.h) -----------------------
 
 static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m, int group);
+
+extern "C" int tags_debug_tc_wait_limit(long long ns) {
+    const unsigned long long v = ns > 0 ? (unsigned long long)ns : WAIT_NS;
+    DeviceCtx* c = tags_ctx();
+    if (!c) return tags_fail(TAGS_E_CUDA, "no usable CUDA device");
+    TAGS_CUDA_OK(cudaDeviceSynchronize());          // no tensor-core kernel of this device is running
+    TAGS_CUDA_OK(cudaMemcpyToSymbol(g_tc_wait_ns, &v, sizeof(v)));
+    return 0;
+}
 
 extern "C" int tags_debug_ldl(tags_cdouble* a, int N, int nb, int pieces) {
     return debug_ldl_impl(a, nullptr, N, nb, pieces, 0, GMAX);
