@@ -306,12 +306,35 @@ typedef struct {
 } tags_grid_job;
 
 /* No counterpart function in the reference: many grids x many Laplace samples
- * in one call (host buffers). A plan per grid, run from `workers` host threads
- * (0 = 4) on the calling thread's device, so that grids of uneven size share
- * the GPU; max_batch = samples resident per plan (0 = min(ns, 256)). Returns
- * 0 or the first error code of any grid (the other grids still run). */
+ * in one call (host buffers), on the calling thread's device: a grid batch
+ * (tags_batch_create, one tags_batch_run, tags_batch_destroy). If the grids
+ * do not fit in device memory together, a plan per grid runs from `workers`
+ * host threads (0 = 4) instead. max_batch = samples resident per grid (0 =
+ * min(ns, 256), reduced by the memory admission). Returns 0 or the first
+ * error code of any grid. */
 int tags_gpu_solve_batch (const tags_grid_job *jobs, size_t njobs, int precision, double mur, size_t max_batch,
                           int workers);
+
+/* No counterpart in the reference (it loops over grids and samples with
+ * OpenMP, examples/three_grids.c:286-443). A grid batch holds, for many grids
+ * of uneven size, a plan per grid, device arrays for every grid's samples,
+ * injections and solutions, and ONE executable CUDA graph in which each grid
+ * is an independent branch: its passes in sequence (fill, assembly,
+ * factorisation and, for TAGS_MIXED, the refinement loop as a conditional
+ * while-node), so grids of different sizes run side by side. The samples
+ * resident per grid (at most max_batch, 0 = 256) are admitted against 60 %
+ * of the free device memory. Built once; every run reuses it. */
+typedef struct tags_batch_s *tags_batch;
+int tags_batch_create (tags_batch *batch, const tags_grid_job *jobs, size_t njobs, int precision, double mur,
+                       size_t max_batch);
+/* Solves every sample of every grid: copies the jobs' s, kappa (and ie) to
+ * the device, launches the graph once, re-solves in plain FP64 the samples
+ * whose refinement did not converge, and copies sol / info back. The jobs
+ * must have the shapes (ns, m, n, injection form) the batch was built with.
+ * stats: largest refinement count, fallbacks, largest backward error, and the
+ * device time of the graph launch. */
+int tags_batch_run (tags_batch batch, const tags_grid_job *jobs, size_t njobs, tags_run_stats *stats);
+int tags_batch_destroy (tags_batch batch);
 
 /* Passes in flight (1 = default, or 2): with 2 the plan builds a twin of the
  * same geometry and settings (twice the device memory) and a run of several
@@ -376,7 +399,9 @@ int tags_plan_tune (tags_plan plan, const tags_cdouble *s, const tags_cdouble *k
  * TAGS_NOALLOC_MAX_N. The solver's scratch is a fixed device array inside the
  * library (no cudaMalloc or cudaFree on any call); every GPU that loads the
  * library holds it until exit. The first call on a device looks the array up:
- * make that call before any stream capture. All calls share the array, so
+ * make that call before any stream capture. That address is kept for the
+ * life of the process: after cudaDeviceReset on a device, this entry point
+ * must not be called on that device again. All calls share the array, so
  * calls that overlap on the GPU race. stream may be NULL (default stream).
  * Returns 0, k > 0 when the k-th pivot is exactly zero (ie unchanged), or a
  * negative TAGS_E_* code (TAGS_E_ARG for a system above the limit). */
@@ -385,6 +410,42 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
                                    size_t num_nodes, void *stream);
 
 /* ---- Part 4: diagnostics -------------------------------------------------------- */
+
+/* No counterpart in the reference. Stopping tolerance of the mixed form's
+ * refinement: a sample stops once the error its corrections predict (four
+ * times the last correction times their measured contraction) is below
+ * tol |x|, or once a correction is below tol / 10 |x| (0 restores the default
+ * 1e-8; at most 1e-3). Smaller values cost refinement steps and bring x
+ * closer to the solution of the system the residual sees. */
+int tags_plan_set_refine_tol (tags_plan plan, double tol);
+
+/* No counterpart in the reference. Caps the refinement steps of the mixed
+ * form's passes (1 .. 40; 0 restores the default 40). A sample that has not
+ * met its stopping rule after that many steps is re-solved by the plain FP64
+ * path (partial pivoting), as one whose refinement stops converging; the
+ * run's stats count it in `fallbacks`. A cap of 1 sends every sample there
+ * (the first correction is the whole solution), which tests that path. */
+int tags_plan_set_max_steps (tags_plan plan, int steps);
+
+/* No counterpart in the reference. The mixed form's impedance fill of ns
+ * samples (1 <= ns <= the plan's batch; INTG_DOUBLE fill) on a mixed plan:
+ * zl, zt (ns x m x m each, sample-major, column-major, both triangles)
+ * receive the values the refinement's residual uses: the FP32 entries of
+ * the regular pairs and, for pairs sharing an endpoint and the diagonal,
+ * their FP64 value (FP32 part + stored rounding residue). */
+int tags_debug_mixed_fill (tags_plan plan, const tags_cdouble *s, const tags_cdouble *kappa, double mur,
+                           size_t ns, tags_cdouble *zl, tags_cdouble *zt);
+
+/* No counterpart in the reference. Test hook: the wall-clock limit, in
+ * nanoseconds, of each wait in the main loops of the tensor-core
+ * factorisation kernels on the current device (ns <= 0 restores the default
+ * 50 ms). When a wait runs out the kernel raises its error word, lets the
+ * copies and products it issued finish (those waits keep the 50 ms limit),
+ * frees its tensor memory and returns; the pass is then re-solved by the
+ * plain FP64 path and tags_run_stats counts the fallbacks. Waits a few
+ * microseconds long run out within a pass, which exercises that path.
+ * Synchronises the device first. */
+int tags_debug_tc_wait_limit (long long ns);
 
 /* No counterpart in the reference. Factorises nb complex symmetric N x N
  * matrices (host, column-major, sample-major; lower half read) with the mixed

@@ -154,3 +154,66 @@ def test_full_size_pair_integrals(gpu_pkg, port):
         assert c1 == 0 and c2 == 0
         want = cT / (e[i, 9] * e[k, 9]) * d + ref_t * cT / (e[i, 9] * img[k, 9]) * im
         assert abs(zt[k, i] - want) <= TOL * abs(want), (i, k)
+
+
+def _touching_pairs(e):
+    """Lower-triangle pairs (k > i) of segments that share an endpoint."""
+    ends = {}
+    for j in range(e.shape[0]):
+        for pt in (e[j, 0:3], e[j, 3:6]):
+            ends.setdefault(tuple(np.round(pt, 9)), []).append(j)
+    pairs = set()
+    for segs in ends.values():
+        for a in segs:
+            for b in segs:
+                if a != b:
+                    pairs.add((max(a, b), min(a, b)))
+    return pairs
+
+
+@pytest.mark.parametrize("with_images", [False, True])
+def test_mixed_fill_keeps_log_singular_entries_in_fp64(gpu_pkg, with_images):
+    """60 x 60 m grid (1560 segments), a low and a high Laplace sample of the
+    benchmark: the mixed form's fill as its residual sees it, against the FP64
+    fill. The entries of pairs sharing an endpoint and the diagonal are FP64
+    (hi + lo): without images they are purely log-singular and self terms, and
+    agree to FP64 rounding; with images those entries carry an FP32 image
+    part. Regular pairs are FP32 (~1e-7)."""
+    pkg = gpu_pkg
+    e, nodes = pkg.electrode_grid(13, 13, 60.0, 60.0, 5, 5, 7e-3, -0.5)
+    m = e.shape[0]
+    img = pkg.images(e) if with_images else None
+    c = np.log(4094.0 ** 2) / 204.7e-6
+    s = np.array([c + 2j * np.pi * 2e4, c + 2j * np.pi * 7e6])
+    kappa = np.zeros_like(s)
+    for j, sk in enumerate(s):
+        sig, epsr = pkg.alipio_soil(1e-3, sk, 1.26, 0.54, 12)
+        kappa[j] = sig + sk * epsr * pkg.EPS0
+    plan = pkg.Plan(e, img, nodes, pkg.MIXED, max_batch=2)
+    try:
+        zl_m, zt_m = plan.mixed_fill(s, kappa)
+    finally:
+        plan.close()
+    touch = _touching_pairs(e)
+    spec = np.zeros((m, m), bool)
+    spec[tuple(np.array(sorted(touch)).T)] = True
+    spec[np.diag_indices(m)] = True
+    low = np.tril(np.ones((m, m), bool))
+    regular = low & ~spec
+    worst = {}
+    for b in range(len(s)):
+        zl_p, zt_p = gpu_fill(pkg, e, img, s[b], kappa[b])
+        for name, zm, zp in (("zl", zl_m[b], zl_p), ("zt", zt_m[b], zt_p)):
+            for part, mask in (("special", spec), ("regular", regular)):
+                nz = mask & (np.abs(zp) > 0)
+                assert np.all(zm[mask & (zp == 0)] == 0)
+                err = float(np.max(np.abs(zm[nz] - zp[nz]) / np.abs(zp[nz])))
+                worst[(name, part)] = max(worst.get((name, part), 0.0), err)
+    print(f"\nmixed fill vs FP64 fill ({'with' if with_images else 'without'} images), "
+          f"{len(touch)} touching pairs + {m} diagonal: " +
+          ", ".join(f"{k[0]} {k[1]} {v:.2e}" for k, v in sorted(worst.items())))
+    if not with_images:
+        assert worst[("zl", "special")] <= 1e-13 and worst[("zt", "special")] <= 1e-13
+    else:
+        assert worst[("zl", "special")] <= 1e-7 and worst[("zt", "special")] <= 1e-7
+    assert worst[("zl", "regular")] <= 2e-6 and worst[("zt", "regular")] <= 2e-6

@@ -1,0 +1,66 @@
+"""Accuracy of the mixed form on the benchmark workload itself.
+
+The 60 x 60 m grid (1560 segments, N = 4537), Alipio soil, 1 kA 1.2/50 us
+current at the centre node, all 2048 Laplace samples: the mixed form's node
+potentials and its transient GPR (the reference's inverse transform,
+src/auxiliary.c:265-329) against the plain FP64 form's, stored in
+tests/golden/gpr4.npz (made by tests/golden/make_gpr4.py, whose 16 strided
+samples are pinned to the reference build). Bar: 1e-6 relative, the mixed
+form's target for impedance and GPR."""
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mixed_gpr_on_benchmark_grid_all_samples(gpu_pkg):
+    pkg = gpu_pkg
+    fx = golden("gpr4.npz")
+    elec, nodes = pkg.electrode_grid(13, 13, 60.0, 60.0, 5, 5, 7e-3, -0.5)
+    img = pkg.images(elec)
+    n = nodes.shape[0]
+    s, kappa, inj, centre = fx["s"], fx["kappa"], fx["inj"], int(fx["centre"])
+    ns = len(s)
+    assert ns == 2048 and elec.shape[0] == int(fx["m"]) and n == int(fx["n"])
+    plan = pkg.Plan(elec, img, nodes, pkg.MIXED, max_batch=128)
+    plan.set_pipelines(2)
+    u = np.zeros(ns, np.complex128)
+    u_nodes = np.zeros((len(fx["pin_idx"]), n), np.complex128)
+    it_max, fb = 0, 0
+    try:
+        for k0 in range(0, ns, 512):
+            k1 = min(ns, k0 + 512)
+            ie = np.zeros((k1 - k0, n), np.complex128)
+            ie[:, centre] = inj[k0:k1]
+            sol, info, st = plan.run(s[k0:k1], kappa[k0:k1], 1.0, ie)
+            assert np.all(info == 0)
+            it_max, fb = max(it_max, st.max_iterations), fb + st.fallbacks
+            u[k0:k1] = sol[:, centre]
+            for j, k in enumerate(fx["pin_idx"]):
+                if k0 <= k < k1:
+                    u_nodes[j] = sol[k - k0, :n]
+    finally:
+        plan.close()
+    assert fb == 0
+    per_sample = np.abs(u - fx["u_centre"]) / np.abs(fx["u_centre"])
+    nt = int(fx["nt"])
+    gpr = pkg.inv_laplace_trans(u, s, float(fx["tmax"]), nt)
+    gpr_err = rel_err(gpr, fx["gpr"])
+    half = nt // 2
+    gpr_err_half = rel_err(gpr[:half], fx["gpr"][:half])
+    nodes_err = rel_err(u_nodes, fx["u_nodes"])
+    print(f"\nmixed vs plain FP64, 2048 samples: U(inj) max rel {per_sample.max():.3e}, "
+          f"GPR rel {gpr_err:.3e} (t <= T/2: {gpr_err_half:.3e}), node potentials at 16 samples {nodes_err:.3e}, "
+          f"max refinement steps {it_max}")
+    assert per_sample.max() <= 1e-6
+    assert nodes_err <= 1e-6
+    quarter = nt // 4
+    gpr_err_quarter = rel_err(gpr[:quarter], fx["gpr"][:quarter])
+    print(f"GPR rel err, t <= T/4: {gpr_err_quarter:.3e}")
+    assert gpr_err_quarter <= 1e-6
+    if "ref_u_nodes" in fx:
+        ref_err = rel_err(u_nodes, fx["ref_u_nodes"])
+        print(f"mixed vs reference build at 16 samples: {ref_err:.3e}")
+        assert ref_err <= 1e-6

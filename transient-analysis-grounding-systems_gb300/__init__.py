@@ -57,9 +57,10 @@ EXPORTS = (
     "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
-    "tags_gpu_inlt",
+    "tags_gpu_inlt", "tags_batch_create", "tags_batch_run", "tags_batch_destroy",
     "tags_gpu_set_quiet",
 )
 
@@ -145,6 +146,10 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_pipelines.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_fill.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_set_max_steps.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_set_refine_tol.argtypes = [_vp, ctypes.c_double]
+            L.tags_debug_tc_wait_limit.argtypes = [ctypes.c_longlong]
+            L.tags_debug_mixed_fill.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _vp]
             L.tags_inv_laplace_batch.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int, ctypes.c_int]
             L.tags_plan_tune.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int,
                                          ctypes.POINTER(TuneResult)]
@@ -160,6 +165,9 @@ def lib() -> ctypes.CDLL:
             L.tags_voltage_batch.argtypes = [_vp, _sz, _vp, _sz, _vp, _vp, _sz, _sz, _vp, _vp, _vp, d, _vp]
             L.tags_fields_evaluations.argtypes = [ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int]
             L.tags_gpu_solve_batch.argtypes = [ctypes.POINTER(GridJob), _sz, ctypes.c_int, d, _sz, ctypes.c_int]
+            L.tags_batch_create.argtypes = [ctypes.POINTER(_vp), ctypes.POINTER(GridJob), _sz, ctypes.c_int, d, _sz]
+            L.tags_batch_run.argtypes = [_vp, ctypes.POINTER(GridJob), _sz, ctypes.POINTER(RunStats)]
+            L.tags_batch_destroy.argtypes = [_vp]
             L.tags_gpu_inlt.argtypes = [_vp, _vp, _vp, d, _sz, _sz, ctypes.c_int, ctypes.c_int]
             L.tags_gpu_launch_count.restype = ctypes.c_longlong
             L.tags_gpu_last_error.restype = ctypes.c_char_p
@@ -172,8 +180,11 @@ def lib() -> ctypes.CDLL:
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
                          "tags_plan_set_pipelines",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
+                         "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_debug_mixed_fill",
+                         "tags_plan_set_refine_tol",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
-                         "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt"):
+                         "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt",
+                         "tags_batch_create", "tags_batch_run", "tags_batch_destroy"):
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
@@ -698,6 +709,33 @@ class Plan:
         if code != 0:
             raise RuntimeError(f"tags_plan_set_fill failed ({code}): {last_error()}")
 
+    def set_refine_tol(self, tol):
+        """Refinement stopping tolerance of the mixed form (0 = default 1e-8)."""
+        code = lib().tags_plan_set_refine_tol(self.handle, float(tol))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_set_refine_tol failed ({code}): {last_error()}")
+
+    def set_max_steps(self, steps):
+        """Cap the mixed form's refinement steps per pass (1..40, 0 = 40);
+        samples not converged by then are re-solved in plain FP64."""
+        code = lib().tags_plan_set_max_steps(self.handle, int(steps))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_set_max_steps failed ({code}): {last_error()}")
+
+    def mixed_fill(self, s, kappa, mur=1.0):
+        """The mixed form's ZL, ZT (ns x m x m, full) as its residual sees
+        them: FP32 regular pairs, FP64 touching pairs and diagonal."""
+        s = np.ascontiguousarray(s, dtype=np.complex128)
+        ns = s.shape[0]
+        kappa = np.ascontiguousarray(np.broadcast_to(kappa, (ns,)), dtype=np.complex128)
+        zl = np.zeros((ns, self.m, self.m), np.complex128)
+        zt = np.zeros((ns, self.m, self.m), np.complex128)
+        code = lib().tags_debug_mixed_fill(self.handle, _addr(s), _addr(kappa), float(mur), ns, _addr(zl), _addr(zt))
+        if code != 0:
+            raise RuntimeError(f"tags_debug_mixed_fill failed ({code}): {last_error()}")
+        # column-major buffers: element (k, i) at k + m i
+        return zl.transpose(0, 2, 1), zt.transpose(0, 2, 1)
+
     def set_graphs(self, enable):
         """Run each pass as one CUDA-graph launch (True) or kernel by kernel."""
         code = lib().tags_plan_set_graphs(self.handle, 1 if enable else 0)
@@ -741,6 +779,12 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def debug_tc_wait_limit(ns: int = 0) -> None:
+    """Test hook: per-wait limit (ns) of the tensor-core kernels' main loops on
+    the current device; 0 restores the default (50 ms)."""
+    _ret(lib().tags_debug_tc_wait_limit(int(ns)))
 
 
 def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, precision=PLAIN_FP64,
@@ -804,6 +848,66 @@ def hem_sweep_grids(jobs, precision=MIXED, max_batch=0, workers=8, graphs=True, 
 
     with ThreadPoolExecutor(max_workers=max(1, int(workers))) as ex:
         return list(ex.map(one, jobs))
+
+
+def _grid_jobs(jobs):
+    """ctypes job array for tags_gpu_solve_batch / tags_batch_*: the arrays it
+    points into (kept alive by the caller) and the (solution, info) outputs."""
+    keep, out = [], []
+    arr = (GridJob * len(jobs))()
+    for q, job in enumerate(jobs):
+        e = _elec(job["electrodes"])
+        im = None if job.get("images") is None else _elec(job["images"])
+        nd = np.ascontiguousarray(job["nodes"], dtype=np.float64)
+        sv = np.ascontiguousarray(np.atleast_1d(job["s"]), dtype=np.complex128)
+        ns = sv.shape[0]
+        kv = np.ascontiguousarray(np.broadcast_to(job["kappa"], (ns,)), dtype=np.complex128)
+        ie = job.get("ie")
+        if ie is not None:
+            ie = np.ascontiguousarray(ie, dtype=np.complex128).reshape(ns, nd.shape[0])
+        sol = np.zeros((ns, nd.shape[0] + 2 * e.shape[0]), np.complex128)
+        info = np.zeros(ns, np.int32)
+        keep += [e, im, nd, sv, kv, ie, sol, info]
+        out.append((sol, info))
+        arr[q] = GridJob(_addr(e), None if im is None else _addr(im), e.shape[0], _addr(nd), nd.shape[0], _addr(sv),
+                         _addr(kv), ns, None if ie is None else _addr(ie), int(job.get("inj_node", 0)), _addr(sol),
+                         _addr(info))
+    return arr, keep, out
+
+
+class GridBatch:
+    """Many grids of uneven size in one CUDA graph (tags_batch_create /
+    tags_batch_run / tags_batch_destroy): built once for the jobs' shapes,
+    each run solves every sample of every grid with one graph launch."""
+
+    def __init__(self, jobs, precision=MIXED, mur: float = 1.0, max_batch: int = 0):
+        arr, keep, _ = _grid_jobs(jobs)
+        h = ctypes.c_void_p()
+        code = lib().tags_batch_create(ctypes.byref(h), arr, len(jobs), int(precision), float(mur), int(max_batch))
+        if code != 0:
+            raise RuntimeError(f"tags_batch_create failed ({code}): {last_error()}")
+        self.handle = h
+        self.count = len(jobs)
+
+    def run(self, jobs):
+        """[(solution ns x (n + 2m), info)] in job order, and the RunStats."""
+        arr, keep, out = _grid_jobs(jobs)
+        st = RunStats()
+        code = lib().tags_batch_run(self.handle, arr, len(jobs), ctypes.byref(st))
+        if code != 0:
+            raise RuntimeError(f"tags_batch_run failed ({code}): {last_error()}")
+        return out, st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().tags_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def solve_batch(jobs, precision=MIXED, mur: float = 1.0, max_batch: int = 0, workers: int = 4):

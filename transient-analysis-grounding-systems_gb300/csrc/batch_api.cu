@@ -1,8 +1,9 @@
 // One-call batched entry points of the C-ABI (host code):
-//   tags_gpu_solve_batch  many grids x many Laplace samples: a plan per grid,
-//                         the plans run concurrently from a few host threads
-//                         (each plan owns its stream, workspaces and graphs),
-//                         which is how grids of uneven size share the GPU;
+//   tags_gpu_solve_batch  many grids x many Laplace samples: one grid batch
+//                         (grid_batch.cu: every grid a branch of one CUDA
+//                         graph); grids too large to be resident together run
+//                         as plans from a few host threads instead (each plan
+//                         owns its stream, workspaces and graphs);
 //   tags_gpu_inlt         the batched inverse Laplace transform.
 // They replace the per-grid, per-sample OpenMP loops the reference's examples
 // write around the library (examples/three_grids.c:286-465).
@@ -25,6 +26,21 @@ extern "C" int tags_gpu_solve_batch(const tags_grid_job* jobs, size_t njobs, int
         if (!j.electrodes || !j.nodes || (j.ns && (!j.s || !j.kappa)) || j.num_electrodes == 0 || j.num_nodes == 0)
             return TAGS_E_ARG;
         if (!j.ie && j.inj_node >= j.num_nodes) return TAGS_E_ARG;
+    }
+    {
+        // all grids in one graph when they fit in device memory together
+        std::vector<tags_grid_job> live;
+        for (size_t q = 0; q < njobs; ++q)
+            if (jobs[q].ns) live.push_back(jobs[q]);
+        if (live.empty()) return 0;
+        tags_batch b = nullptr;
+        int e = tags_batch_create(&b, live.data(), live.size(), precision, mur, max_batch);
+        if (e == 0) {
+            e = tags_batch_run(b, live.data(), live.size(), nullptr);
+            tags_batch_destroy(b);
+            return e;
+        }
+        if (e != TAGS_E_NOMEM) return e;
     }
     int device = 0;
     if (cudaGetDevice(&device) != cudaSuccess) return TAGS_E_CUDA;

@@ -21,6 +21,9 @@
 // The scaling and the quirks follow the reference: |cos theta| of the
 // direction vectors, ZL = 0 when cos < DBL_EPSILON (direct) and image ZL only
 // when cos > DBL_EPSILON, images include k = i and accumulate.
+#include <map>
+#include <vector>
+
 #include "tags_common.cuh"
 #include "tags_internal.h"
 
@@ -547,12 +550,12 @@ TAGS_D void fill_tile(long long t, int m, int& kb, int& i) {
 // in FP64 once per warp (a lane per panel pair), never per sample. Outputs
 // pass through a [row][sample] sub-tile so each store instruction writes 64
 // contiguous bytes per sample. Pairs that share an endpoint (log-singular)
-// are left to k_fill_touch. Five CTAs per SM (their shared memory allows five;
+// and the self terms are left to k_fill_special64 (FP64). Five CTAs per SM (their shared memory allows five;
 // 96 registers instead of 122): the point loop is latency-bound, so the extra
 // warps pay for the few spilled values outside it.
 __global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
     const double* __restrict__ elec, const double* __restrict__ img, const float4* __restrict__ sdir,
-    const float4* __restrict__ idir, const float* __restrict__ selfv, int m, const uint16_t* __restrict__ codes,
+    const float4* __restrict__ idir, int m, const uint16_t* __restrict__ codes,
     const PairRec* __restrict__ recs, const SampleF32* __restrict__ coef, int nsamp, float2* zl0, float2* zt0,
     long long bstride, int has_img, long long ntiles, int* status) {
     __shared__ float sxm[GL_MIX], swf[GL_MIX];
@@ -584,18 +587,13 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
         const int kend = min(k_hi, k0 + FILL_SUB);
         for (int k = k0; k < kend; ++k) {
             const long long p = pstart + (k - i);
+            // the self term of the diagonal is added in FP64 by k_fill_special64
             float2 zl = make_float2(0.f, 0.f), zt = make_float2(0.f, 0.f);
-            if (k == i) {
-                // self term: the reference's static closed form (src/electrode.c:346-348)
-                const float v = selfv[i];
-                zl = make_float2(c.cL.x * v, c.cL.y * v);
-                zt = make_float2(c.cT.x * v / (ds.w * ds.w), c.cT.y * v / (ds.w * ds.w));
-            }
             for (int kind = 0; kind < 2; ++kind) {
                 if (kind == 0 && k == i) continue;
                 if (kind == 1 && !has_img) break;
                 const uint16_t code = codes[2 * p + kind];
-                if (code & (PC_TOUCH | PC_DEGEN)) continue;      // k_fill_touch
+                if (code & (PC_TOUCH | PC_DEGEN)) continue;      // k_fill_special64
                 const float4 dr = kind == 0 ? sdir[k] : idir[k];
                 const PairRec rec = recs[2 * p + kind];
                 const float lmax = fmaxf(ds.w, dr.w);
@@ -734,63 +732,39 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
     }
 }
 
-// Pairs sharing an endpoint (log-singular): the Duffy rule of j_touch, added
-// to what k_fill_mixed wrote (lower triangle). One warp per listed pair and 32
-// samples (lanes): the rule's nodes (rho1, rho2 and w / rho of both Duffy
-// halves) are computed once per warp in FP64 and kept in shared memory as
-// float pairs; each lane then sums phi(gamma rho) w / rho in FP32, with
-// phi(x) = (1 - e^{-x}) / x from its series while |Re x| + |Im x| < 1, else
-// from the exactly reduced exponential (anchor_df). The order is the largest the
-// warp's samples ask for (10 + |gamma| L, at most QMAX).
-constexpr int TOUCH_WARPS = 4;
+// The log-singular entries in FP64: for each special entry (a pair with a
+// kind that shares an endpoint, or a diagonal entry) the Duffy rule of
+// j_touch at the plain form's order (16 + 2 |gamma| L) for the touching kinds,
+// and the static closed form for the self term, added to the FP32 value
+// k_fill_mixed left there for the regular kinds (lower triangle). The sum v
+// is formed in FP64 and stored as hi = fl(v) in Z and lo = fl(v - hi) in the
+// residue list that the refinement's residual reads. One warp per entry and
+// 32 samples (lanes): the rule's nodes (rho and w / rho of both Duffy halves)
+// are computed once per warp into shared memory.
+constexpr int SPEC_WARPS = 4;
 
-struct TouchNode {
-    float rh, rl, wr;                      // rho = rh + rl, w / rho
-};
-
-TAGS_D float2 phi_touch(const SampleF32& c, float rh, float rl) {
-    const float xr = c.grh * rh, xi = c.gih * rh;
-    if (fabsf(xr) + fabsf(xi) < 1.f) {
-        // sum_k (-x)^k / (k+1)!, k <= 12: truncation below 1 / 14! ~ 1.1e-11
-        float2 term = make_float2(1.f, 0.f), acc = term;
-#pragma unroll
-        for (int k = 1; k <= 12; ++k) {
-            const float s = -1.f / (float)(k + 1);
-            term = make_float2(s * (term.x * xr - term.y * xi), s * (term.x * xi + term.y * xr));
-            acc.x += term.x;
-            acc.y += term.y;
-        }
-        return acc;
-    }
-    const float2 e = anchor_df(c.grh, c.grl, c.gih, c.gil, rh, rl);      // e^{-x}
-    const float nr = 1.f - e.x, ni = -e.y;
-    const float den = xr * xr + xi * xi;
-    return make_float2((nr * xr + ni * xi) / den, (ni * xr - nr * xi) / den);
-}
-
-__global__ void __launch_bounds__(TOUCH_WARPS * 32) k_fill_touch(
-    const double* __restrict__ elec, const double* __restrict__ img, int m, const int* __restrict__ list,
-    const int* __restrict__ nlist, const PairRec* __restrict__ recs, const SampleF32* __restrict__ coef, int nsamp,
-    float2* zl0, float2* zt0, long long bstride, int* status) {
-    __shared__ TouchNode nodes_all[TOUCH_WARPS][2 * QMAX];
+__global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
+    const double* __restrict__ elec, const double* __restrict__ img, int m, const int2* __restrict__ ent, int nent,
+    const SampleCoef* __restrict__ coef, int nsamp, float2* zl0, float2* zt0, long long bstride,
+    float4* __restrict__ lo, int* status) {
+    __shared__ double2 nodes_all[SPEC_WARPS][2 * QMAX];      // (rho, w / rho)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    TouchNode* nodes = nodes_all[warp];
-    const int e = blockIdx.x * TOUCH_WARPS + warp;
-    if (e >= *nlist) return;                          // whole warp leaves together
+    double2* nodes = nodes_all[warp];
+    const int e = blockIdx.x * SPEC_WARPS + warp;
+    if (e >= nent) return;                            // whole warp leaves together
     const int smp = blockIdx.y * 32 + lane;
     const bool valid = smp < nsamp;
-    SampleF32 c{};
+    SampleCoef c{};
     if (valid) c = coef[smp];
-    const long long p = list[2 * e];
-    const int mask = list[2 * e + 1];
+    const int2 en = ent[e];
     int i, k;
-    pair_index(p, m, i, k);
+    pair_index(en.x, m, i, k);
     Seg S, R;
     ld_seg(elec + 11LL * i, S);
-    float2 dl = make_float2(0.f, 0.f), dt = make_float2(0.f, 0.f);
+    double2 dl = cz(0.0, 0.0), dt = cz(0.0, 0.0);
     bool bad = false;
     for (int kind = 0; kind < 2 && !bad; ++kind) {
-        if (!(mask & (1 << kind))) continue;
+        if (!(en.y & (1 << kind))) continue;
         ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
         const double lmax = fmax(S.len, R.len);
         int ia, ib;
@@ -801,8 +775,7 @@ __global__ void __launch_bounds__(TOUCH_WARPS * 32) k_fill_touch(
             bad = fmax(fabs(ro[0] - so[0]), fmax(fabs(ro[1] - so[1]), fabs(ro[2] - so[2]))) <= 1e-9 * lmax;
         }
         if (bad) break;
-        const float gabs = sqrtf(c.grh * c.grh + c.gih * c.gih);
-        int q = valid ? min(QMAX, 10 + (int)ceilf(gabs * (float)lmax)) : 0;
+        int q = valid ? min(QMAX, 16 + 2 * (int)ceil(sqrt(cabs2(c.gamma)) * lmax)) : 0;
         q = __reduce_max_sync(0xffffffffu, q);
         double a[3], b[3];
         for (int d = 0; d < 3; ++d) {
@@ -815,47 +788,59 @@ __global__ void __launch_bounds__(TOUCH_WARPS * 32) k_fill_touch(
             const double u1[3] = {a[0] - t * b[0], a[1] - t * b[1], a[2] - t * b[2]};
             const double u2[3] = {t * a[0] - b[0], t * a[1] - b[1], t * a[2] - b[2]};
             const double r1 = sqrt(dot3(u1, u1)), r2 = sqrt(dot3(u2, u2));
-            const float r1h = (float)r1, r2h = (float)r2;
-            nodes[2 * qi] = TouchNode{r1h, (float)(r1 - (double)r1h), (float)(w / r1)};
-            nodes[2 * qi + 1] = TouchNode{r2h, (float)(r2 - (double)r2h), (float)(w / r2)};
+            nodes[2 * qi] = make_double2(r1, w / r1);
+            nodes[2 * qi + 1] = make_double2(r2, w / r2);
         }
         __syncwarp();
-        float2 J = make_float2(0.f, 0.f);
+        double2 J = cz(0.0, 0.0);
         if (valid) {
             for (int j = 0; j < 2 * q; ++j) {
-                const TouchNode nd = nodes[j];
-                const float2 ph = phi_touch(c, nd.rh, nd.rl);
-                J.x = fmaf(nd.wr, ph.x, J.x);
-                J.y = fmaf(nd.wr, ph.y, J.y);
+                const double2 nd = nodes[j];
+                const double2 ph = phi_c(cz(c.gamma.x * nd.x, c.gamma.y * nd.x));
+                J.x = fma(nd.y, ph.x, J.x);
+                J.y = fma(nd.y, ph.y, J.y);
             }
         }
-        const float2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
-        const float fl = recs[2 * p + kind].fl;
-        dt.x += cT.x * J.x - cT.y * J.y;
-        dt.y += cT.x * J.y + cT.y * J.x;
-        dl.x += fl * (cL.x * J.x - cL.y * J.y);
-        dl.y += fl * (cL.x * J.y + cL.y * J.x);
+        // ZL carries |d_i . d_k| (= |cos theta| L_i L_k), dropped where the
+        // reference drops it (cos < DBL_EPSILON direct, <= DBL_EPSILON images)
+        double cost = 0.0;
+        for (int d = 0; d < 3; ++d) cost += (S.b[d] - S.a[d]) * (R.b[d] - R.a[d]);
+        cost = fabs(cost);
+        const bool keep = kind == 0 ? !(cost < TAGS_DBL_EPSILON) : (cost > TAGS_DBL_EPSILON);
+        const double2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
+        dt = cadd(dt, cmul(cT, J));
+        if (keep) dl = cadd(dl, cscale(cmul(cL, J), cost));
+    }
+    if (!bad && (en.y & 4)) {
+        // self term: the reference's static closed form (src/electrode.c:238-245, used at :346-348)
+        const double v = self_integral_d(S);
+        dl = cadd(dl, cscale(c.cL, v));
+        dt = cadd(dt, cscale(c.cT, v / (S.len * S.len)));
     }
     if (bad) {
         if (lane == 0) raise_status(status, TAGS_ST_DEGENERATE_PAIR);
-        dl = dt = make_float2(nanf(""), nanf(""));
+        dl = dt = cz(nan(""), nan(""));
     }
     if (!valid) return;
     if (!isfinite(dl.x + dl.y + dt.x + dt.y)) raise_status(status, TAGS_ST_NONFINITE);
-    const long long lo = bstride * smp + k + (long long)m * i;      // lower triangle (k_zmirror copies it up)
-    float2 za = zl0[lo], zb = zt0[lo];
-    zl0[lo] = make_float2(za.x + dl.x, za.y + dl.y);
-    zt0[lo] = make_float2(zb.x + dt.x, zb.y + dt.y);
+    const long long idx = bstride * smp + k + (long long)m * i;      // lower triangle (k_zmirror copies it up)
+    const float2 za = zl0[idx], zb = zt0[idx];
+    const double vlr = (double)za.x + dl.x, vli = (double)za.y + dl.y;
+    const double vtr = (double)zb.x + dt.x, vti = (double)zb.y + dt.y;
+    const float2 hl = make_float2((float)vlr, (float)vli), ht = make_float2((float)vtr, (float)vti);
+    zl0[idx] = hl;
+    zt0[idx] = ht;
+    lo[(long long)smp * nent + e] = make_float4((float)(vlr - (double)hl.x), (float)(vli - (double)hl.y),
+                                                (float)(vtr - (double)ht.x), (float)(vti - (double)ht.y));
 }
 
 __global__ void k_seg_dirs(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
-                           float4* __restrict__ sdir, float4* __restrict__ idir, float* __restrict__ selfv) {
+                           float4* __restrict__ sdir, float4* __restrict__ idir) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= m) return;
     Seg S;
     ld_seg(elec + 11LL * i, S);
     sdir[i] = make_float4((float)(S.b[0] - S.a[0]), (float)(S.b[1] - S.a[1]), (float)(S.b[2] - S.a[2]), (float)S.len);
-    selfv[i] = (float)self_integral_d(S);
     if (has_img) {
         ld_seg(img + 11LL * i, S);
         idir[i] = make_float4((float)(S.b[0] - S.a[0]), (float)(S.b[1] - S.a[1]), (float)(S.b[2] - S.a[2]),
@@ -917,7 +902,7 @@ int tags_fill_tables_init() {
 size_t tags_mixed_fill_workspace(int m) {
     const size_t np = (size_t)m * (m + 1) / 2;
     return np * 2 * (sizeof(uint16_t) + sizeof(PairRec)) + np * 2 * sizeof(int) + 2 * m * sizeof(float4) +
-           m * sizeof(float) + 4096 * sizeof(SampleF32) + 1024;
+           4096 * sizeof(SampleF32) + 1024;
 }
 
 struct MixedFillWs {
@@ -927,7 +912,6 @@ struct MixedFillWs {
     int* nlist;
     float4* sdir;
     float4* idir;
-    float* selfv;
     SampleF32* c32;
 };
 
@@ -945,8 +929,6 @@ static MixedFillWs carve(void* ws, int m) {
     b += 4096 * sizeof(SampleF32);
     w.list = reinterpret_cast<int*>(b);
     b += np * 2 * sizeof(int);
-    w.selfv = reinterpret_cast<float*>(b);
-    b += ((m * sizeof(float) + 15) / 16) * 16;
     w.nlist = reinterpret_cast<int*>(b);
     b += 16;
     w.codes = reinterpret_cast<uint16_t*>(b);
@@ -957,7 +939,7 @@ int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int 
     MixedFillWs w = carve(ws, m);
     const long long npairs = (long long)m * (m + 1) / 2;
     TAGS_CUDA_OK(cudaMemsetAsync(w.nlist, 0, sizeof(int), st));
-    k_seg_dirs<<<(m + 127) / 128, 128, 0, st>>>(d_elec, d_img, m, has_img, w.sdir, w.idir, w.selfv);
+    k_seg_dirs<<<(m + 127) / 128, 128, 0, st>>>(d_elec, d_img, m, has_img, w.sdir, w.idir);
     k_pair_plan<<<(unsigned)((npairs + 127) / 128), 128, 0, st>>>(d_elec, d_img, m, has_img, w.codes, w.recs, w.nlist,
                                                                  w.list);
     tags_note_launch(2);
@@ -966,8 +948,8 @@ int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int 
 }
 
 int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
-                           int nsamp, float2* d_zl, float2* d_zt, long long bstride, int has_img, int max_touch,
-                           int* d_status, cudaStream_t st) {
+                           int nsamp, float2* d_zl, float2* d_zt, long long bstride, int has_img,
+                           const SpecialEntries& sp, int* d_status, cudaStream_t st) {
     if (m <= 0 || nsamp <= 0) return 0;
     if (nsamp > 4096) return tags_fail_cuda(cudaErrorInvalidValue, "fill_mixed: batch above 4096", __FILE__, __LINE__);
     MixedFillWs w = carve(ws, m);
@@ -976,19 +958,75 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
     const int KB = (m + 31) / 32;
     const long long ntiles = 16LL * (KB - 1) * KB + m;
     dim3 grid((unsigned)((ntiles + FILL_WARPS - 1) / FILL_WARPS), (unsigned)((nsamp + 31) / 32));
-    k_fill_mixed<<<grid, FILL_WARPS * 32, 0, st>>>(d_elec, d_img, w.sdir, w.idir, w.selfv, m, w.codes, w.recs, w.c32,
+    k_fill_mixed<<<grid, FILL_WARPS * 32, 0, st>>>(d_elec, d_img, w.sdir, w.idir, m, w.codes, w.recs, w.c32,
                                                    nsamp, d_zl, d_zt, bstride, has_img, ntiles, d_status);
-    if (max_touch > 0) {
-        dim3 gt((unsigned)((max_touch + TOUCH_WARPS - 1) / TOUCH_WARPS), (unsigned)((nsamp + 31) / 32));
-        k_fill_touch<<<gt, TOUCH_WARPS * 32, 0, st>>>(d_elec, d_img, m, w.list, w.nlist, w.recs, w.c32, nsamp, d_zl, d_zt,
-                                                     bstride, d_status);
-    }
+    dim3 gs((unsigned)((sp.n + SPEC_WARPS - 1) / SPEC_WARPS), (unsigned)((nsamp + 31) / 32));
+    k_fill_special64<<<gs, SPEC_WARPS * 32, 0, st>>>(d_elec, d_img, m, sp.ent, sp.n, d_coef, nsamp, d_zl, d_zt,
+                                                     bstride, sp.lo, d_status);
     k_zmirror<<<dim3((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS)),
                 256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
     tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
-    tags_note_launch(max_touch > 0 ? 4 : 3);
+    tags_note_launch(4);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
+}
+
+// The special entries from the pair plan's list of pairs with a touching (or
+// degenerate) kind, plus every diagonal entry; sorted by pair index, so the
+// list and each row's entries come out in the same order on every build.
+int tags_mixed_special_build(void* ws, int m, int batch, SpecialEntries* sp, cudaStream_t st) {
+    MixedFillWs w = carve(ws, m);
+    int nt = 0;
+    TAGS_CUDA_OK(cudaMemcpyAsync(&nt, w.nlist, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    std::vector<int> tl(2 * (size_t)nt);
+    if (nt > 0) {
+        TAGS_CUDA_OK(cudaMemcpyAsync(tl.data(), w.list, sizeof(int) * 2 * nt, cudaMemcpyDeviceToHost, st));
+        TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    }
+    std::map<long long, int> kinds;
+    for (int t = 0; t < nt; ++t) kinds[tl[2 * t]] |= tl[2 * t + 1] & 3;
+    for (int i = 0; i < m; ++i) kinds[(long long)i * (2LL * m - i + 1) / 2] |= 4;
+    const int n = (int)kinds.size();
+    std::vector<int2> ent;
+    ent.reserve(n);
+    std::vector<std::vector<int2>> rows(m);
+    int i = 0;                   // column of pair p (pairs ascend, so columns do)
+    for (const auto& kv : kinds) {
+        const long long p = kv.first;
+        // column i, row k of pair p (the enumeration of pair_index)
+        while (i < m - 1 && (long long)(i + 1) * (2LL * m - i) / 2 <= p) ++i;
+        const int k = i + (int)(p - (long long)i * (2LL * m - i + 1) / 2);
+        const int e = (int)ent.size();
+        ent.push_back(make_int2((int)p, kv.second));
+        rows[k].push_back(make_int2(i, e));
+        if (k != i) rows[i].push_back(make_int2(k, e));
+    }
+    std::vector<int> row_ptr(m + 1, 0);
+    std::vector<int2> row_ent;
+    for (int k = 0; k < m; ++k) {
+        row_ptr[k] = (int)row_ent.size();
+        row_ent.insert(row_ent.end(), rows[k].begin(), rows[k].end());
+    }
+    row_ptr[m] = (int)row_ent.size();
+    tags_mixed_special_free(sp);
+    TAGS_CUDA_OK(cudaMalloc(&sp->ent, sizeof(int2) * n));
+    TAGS_CUDA_OK(cudaMalloc(&sp->row_ptr, sizeof(int) * (m + 1)));
+    TAGS_CUDA_OK(cudaMalloc(&sp->row_ent, sizeof(int2) * row_ent.size()));
+    TAGS_CUDA_OK(cudaMalloc(&sp->lo, sizeof(float4) * (size_t)n * batch));
+    TAGS_CUDA_OK(cudaMemcpy(sp->ent, ent.data(), sizeof(int2) * n, cudaMemcpyHostToDevice));
+    TAGS_CUDA_OK(cudaMemcpy(sp->row_ptr, row_ptr.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
+    TAGS_CUDA_OK(cudaMemcpy(sp->row_ent, row_ent.data(), sizeof(int2) * row_ent.size(), cudaMemcpyHostToDevice));
+    TAGS_CUDA_OK(cudaMemset(sp->lo, 0, sizeof(float4) * (size_t)n * batch));
+    sp->n = n;
+    return 0;
+}
+
+void tags_mixed_special_free(SpecialEntries* sp) {
+    void* ptrs[] = {sp->ent, sp->row_ptr, sp->row_ent, sp->lo};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    *sp = SpecialEntries{};
 }
 
 int tags_mixed_touch_count(void* ws, int m, cudaStream_t st, int* out) {

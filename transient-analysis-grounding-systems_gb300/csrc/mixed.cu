@@ -242,10 +242,15 @@ TAGS_D F2 f2_mac(F2 a, float z, float xh, float xl) {
 // x is split into float pairs), so its result is accurate to ~2^-44 of
 // |Z| |x| without FP64 arithmetic in the m^2 loop.
 constexpr int RES_CHUNK = 1024;
+// Rows with FP64 entries (touching pairs, diagonal; SpecialEntries) add their
+// rounding residues lo times x in FP64, so the residual is that of the FP64
+// values there (row_ptr null: no such entries, as for the mHEM fill).
 __global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z, const Incidence inc, int m, int n,
                                                     const double2* __restrict__ bvec, const double2* __restrict__ x,
                                                     double2* __restrict__ r, double* __restrict__ norms,
-                                                    const int* __restrict__ active) {
+                                                    const int* __restrict__ active, const int* __restrict__ row_ptr,
+                                                    const int2* __restrict__ row_ent, const float4* __restrict__ lo,
+                                                    int nspec) {
     __shared__ float4 xs[RES_CHUNK];        // re_hi, re_lo, im_hi, im_lo
     const int N = n + 2 * m;
     const int blk = blockIdx.y & 1, b = blockIdx.y >> 1;
@@ -301,6 +306,17 @@ __global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z
     }
     acc.x -= (double)ar.hi + (double)ar.lo;
     acc.y -= (double)ai.hi + (double)ai.lo;
+    if (row_ptr) {
+        const float4* lb = lo + (size_t)b * nspec;
+        for (int q = row_ptr[k]; q < row_ptr[k + 1]; ++q) {
+            const int2 ce = row_ent[q];
+            const float4 l4 = lb[ce.y];
+            const double lr = blk == 0 ? l4.x : l4.z, li = blk == 0 ? l4.y : l4.w;
+            const double2 xv = xb[n + blk * m + ce.x];
+            acc.x -= lr * xv.x - li * xv.y;
+            acc.y -= lr * xv.y + li * xv.x;
+        }
+    }
     double2 rv = csub(bvec[(size_t)b * N + row], acc);
     r[(size_t)b * N + row] = rv;
     atomic_max_nonneg(norms + 4 * b + 2, fabs(rv.x) + fabs(rv.y));
@@ -331,6 +347,7 @@ struct IrState {
     int* cont;       // 1 while another step is wanted
     int* extr;       // per sample: the step of its last extrapolation (k_ir_extrap)
     double* lam;     // per sample: |lambda| of that extrapolation
+    double tol;      // stopping tolerance (relative error left in x)
 };
 
 // Stopping test after a correction of max-norm dx, |x| = xn (max norm). pdx:
@@ -338,17 +355,18 @@ struct IrState {
 // an extrapolated step, minus the slow mode's |lambda|. The error left after
 // this correction is about rho dx for the measured contraction rho = dx / pdx
 // (rho <= 1/4), or the mode's tail |lambda| / (1 - |lambda|) dx; stop when four
-// times that is below 1e-8 |x|, a decade under the FP32 fill's own error. Step
-// 0 starts from x = 0 (dx_0 = |x_0|), so it never stops on the estimate.
-TAGS_D bool ir_converged(int step, double dx, double xn, double pdx) {
-    if (dx <= 1e-9 * xn) return true;
+// times that is below tol |x| (default 1e-8, a decade under the FP32 fill's
+// own error), or when the correction itself is below tol / 10 |x|. Step 0
+// starts from x = 0 (dx_0 = |x_0|), so it never stops on the estimate.
+TAGS_D bool ir_converged(int step, double dx, double xn, double pdx, double tol) {
+    if (dx <= 0.1 * tol * xn) return true;
     if (step >= 1 && pdx > 0.0) {
         const double rho = dx / pdx;
-        return rho <= 0.25 && 4.0 * rho * dx <= 1e-8 * xn;
+        return rho <= 0.25 && 4.0 * rho * dx <= tol * xn;
     }
     if (pdx < 0.0) {
         const double l = -pdx;
-        return 4.0 * l / (1.0 - l) * dx <= 1e-8 * xn;
+        return 4.0 * l / (1.0 - l) * dx <= tol * xn;
     }
     return false;
 }
@@ -366,6 +384,7 @@ IrState ir_state(tags_plan_s* p) {
     s.wnorm = p->d_ird + b;
     s.berr = p->d_ird + 2 * b;
     s.lam = p->d_ird + 3 * b;
+    s.tol = p->ir_tol;
     return s;
 }
 
@@ -389,7 +408,7 @@ __global__ void k_ir_extrap(const float2* __restrict__ y, const double* __restri
     if (!s.active[b]) return;
     const int step = *s.step;
     if (step < 2 || s.extr[b] == step - 1) return;
-    if (ir_converged(step, norms[4 * b + 0], norms[4 * b + 1], s.prev_dx[b])) return;
+    if (ir_converged(step, norms[4 * b + 0], norms[4 * b + 1], s.prev_dx[b], s.tol)) return;
     const double re = dots[4 * b], im = dots[4 * b + 1], pp = dots[4 * b + 2], yy = dots[4 * b + 3];
     if (!(pp > 0.0) || !(yy > 0.0) || re * re + im * im < 0.81 * pp * yy) return;
     const double lr = re / pp, li = im / pp, l2 = lr * lr + li * li;
@@ -457,7 +476,7 @@ __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ n
             continue;
         }
         const double pdx = s.prev_dx[q];
-        if (ir_converged(step, dx, xn, pdx)) { s.active[q] = 0; s.conv[q] = 1; continue; }
+        if (ir_converged(step, dx, xn, pdx, s.tol)) { s.active[q] = 0; s.conv[q] = 1; continue; }
         if (step >= 2 && pdx > 0.0 && dx > 0.5 * pdx) {
             s.conv[q] = be <= 1e-12;
             s.active[q] = 0;
@@ -484,6 +503,8 @@ int tags_mixed_alloc(tags_plan_s* p) {
     if (err) return err;
     err = tags_mixed_touch_count(p->d_fillws, p->m, p->stream, &p->n_touch);
     if (err) return err;
+    err = tags_mixed_special_build(p->d_fillws, p->m, (int)b, &p->spec, p->stream);
+    if (err) return err;
     TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_A, sizeof(float2) * N * N * b));
     // scale + row sums (FP64), then an FP32 copy of the scale
@@ -509,6 +530,7 @@ int tags_mixed_free(tags_plan_s* p) {
                     p->d_fillws, p->d_ldlws, p->d_ldlerr, p->d_iri, p->d_ird, p->d_yprev, p->d_dots};
     for (void* q : ptrs)
         if (q) cudaFree(q);
+    tags_mixed_special_free(&p->spec);
     p->d_Z = nullptr;
     p->d_A = nullptr;
     p->d_yprev = nullptr;
@@ -551,10 +573,25 @@ static int fallback_plain(tags_plan_s* p, int q, cudaStream_t st) {
     return tags_lu_solve_z(W, (int)N, N, NN, 1, ipiv, x, 1, N, N, st);
 }
 
+int tags_plan_rhs(tags_plan_s* p, double2* d_X, const double2* d_ie, int inj_node, int nb, cudaStream_t st);
+int tags_plan_coef(tags_plan_s* p, const double2* d_s, const double2* d_kappa, double mur, int nb, cudaStream_t st);
+
+int tags_mixed_fallback_one(tags_plan_s* p, const double2* d_s, const double2* d_kappa, double mur,
+                            const double2* d_ie, int inj_node, double2* x_out, int* info_out, cudaStream_t st) {
+    int err = tags_plan_coef(p, d_s, d_kappa, mur, 1, st);          // coefficients in slot 0
+    double2* b0 = p->d_r + (size_t)p->batch * p->N;                    // saved right-hand side, slot 0
+    if (!err) err = tags_plan_rhs(p, b0, d_ie, inj_node, 1, st);
+    if (!err) err = fallback_plain(p, 0, st);
+    if (err) return err;
+    TAGS_CUDA_OK(cudaMemcpyAsync(x_out, p->d_x, sizeof(double2) * p->N, cudaMemcpyDeviceToDevice, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(info_out, p->d_info, sizeof(int), cudaMemcpyDeviceToDevice, st));
+    return 0;
+}
+
 // ---- one pass of nb samples, in four stages -------------------------------------
 // The right-hand side b is in d_x when a pass starts (written by the plan).
 
-static constexpr int kMaxSteps = 40;
+static constexpr int kMaxSteps = 40;      // upper bound of tags_plan_s::max_steps
 
 // b saved, x = 0, impedance fill, scaling, FP32 working matrix, its LDL^T
 int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
@@ -571,7 +608,7 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
                   ? tags_launch_mhem_mixed(m, p->has_images, p->d_pot, p->d_fillws, p->d_coef, nb, p->d_Z,
                                            p->d_Z + (size_t)m * m, 2LL * m * m, p->d_status, st)
                   : tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z,
-                                           p->d_Z + (size_t)m * m, 2LL * m * m, p->has_images, p->n_touch,
+                                           p->d_Z + (size_t)m * m, 2LL * m * m, p->has_images, p->spec,
                                            p->d_status, st);
     if (err) return err;
     // 2. scaling
@@ -624,11 +661,13 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
     k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);
+    const bool spec = p->fill_model != TAGS_INTG_MHEM && p->spec.n > 0;
     k_residual_z<<<dim3((m + 127) / 128, 2 * nb), 128, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
-                                                                s.active);
+                                                                s.active, spec ? p->spec.row_ptr : nullptr,
+                                                                p->spec.row_ent, p->spec.lo, p->spec.n);
     // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
     tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
-    k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, kMaxSteps, s, cond, set_cond);
+    k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, std::min(p->max_steps, kMaxSteps), s, cond, set_cond);
     tags_note_launch(5);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
@@ -680,6 +719,62 @@ int tags_mixed_finish(tags_plan_s* p, int nb, cudaStream_t st, int* h_iters, dou
     return 0;
 }
 
+int tags_plan_coef(tags_plan_s* p, const double2* d_s, const double2* d_kappa, double mur, int nb, cudaStream_t st);
+
+// Diagnostic: the mixed fill of ns <= batch samples, returned as the values the
+// refinement's residual uses (FP32 entries, FP64 hi + lo on the special ones).
+extern "C" int tags_debug_mixed_fill(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur,
+                                     size_t ns, tags_cdouble* zl, tags_cdouble* zt) {
+    tags_plan_s* p = plan;
+    if (!p || p->precision == TAGS_PLAIN_FP64 || !s || !kappa || !zl || !zt || ns == 0 || (int)ns > p->batch)
+        return tags_fail(TAGS_E_ARG, "tags_debug_mixed_fill: invalid argument (mixed plan, 1 <= ns <= batch)");
+    if (p->fill_model != TAGS_INTG_DOUBLE) return tags_fail(TAGS_E_ARG, "tags_debug_mixed_fill: INTG_DOUBLE fill only");
+    const int m = p->m, nb = (int)ns;
+    cudaStream_t st = p->stream;
+    TAGS_CUDA_OK(cudaMemcpyAsync(p->d_sin, s, sizeof(double2) * nb, cudaMemcpyHostToDevice, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(p->d_sin + p->batch, kappa, sizeof(double2) * nb, cudaMemcpyHostToDevice, st));
+    int err = tags_plan_coef(p, p->d_sin, p->d_sin + p->batch, mur, nb, st);
+    if (!err)
+        err = tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z, p->d_Z + (size_t)m * m,
+                                     2LL * m * m, p->has_images, p->spec, p->d_status, st);
+    if (err) return err;
+    std::vector<float2> z((size_t)2 * m * m * nb);
+    std::vector<float4> lo((size_t)p->spec.n * nb);
+    std::vector<int2> ent(p->spec.n);
+    TAGS_CUDA_OK(cudaMemcpyAsync(z.data(), p->d_Z, sizeof(float2) * z.size(), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(lo.data(), p->spec.lo, sizeof(float4) * lo.size(), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(ent.data(), p->spec.ent, sizeof(int2) * ent.size(), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    double* ol = reinterpret_cast<double*>(zl);
+    double* ot = reinterpret_cast<double*>(zt);
+    const size_t mm = (size_t)m * m;
+    for (int b = 0; b < nb; ++b)
+        for (size_t e = 0; e < mm; ++e) {
+            const float2 a = z[(size_t)b * 2 * mm + e], c = z[(size_t)b * 2 * mm + mm + e];
+            ol[2 * (b * mm + e)] = a.x;
+            ol[2 * (b * mm + e) + 1] = a.y;
+            ot[2 * (b * mm + e)] = c.x;
+            ot[2 * (b * mm + e) + 1] = c.y;
+        }
+    int i = 0;
+    for (int e = 0; e < p->spec.n; ++e) {
+        const long long pp = ent[e].x;
+        while (i < m - 1 && (long long)(i + 1) * (2LL * m - i) / 2 <= pp) ++i;
+        const int k = i + (int)(pp - (long long)i * (2LL * m - i + 1) / 2);
+        for (int b = 0; b < nb; ++b) {
+            const float4 l = lo[(size_t)b * p->spec.n + e];
+            const size_t pos[2] = {b * mm + k + (size_t)m * i, b * mm + i + (size_t)m * k};
+            for (int t = 0; t < (k == i ? 1 : 2); ++t) {
+                ol[2 * pos[t]] += l.x;
+                ol[2 * pos[t] + 1] += l.y;
+                ot[2 * pos[t]] += l.z;
+                ot[2 * pos[t] + 1] += l.w;
+            }
+        }
+    }
+    return 0;
+}
+
 // The pass without a graph: the host follows the device's continue flag.
 int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters, double* h_berr, int* h_conv,
                            cudaStream_t st) {
@@ -687,7 +782,7 @@ int tags_mixed_solve_batch(tags_plan_s* p, int nb, const double2*, int* h_iters,
     if (!err) err = tags_mixed_ir_setup(p, nb, st);
     if (err) return err;
     cudaGraphConditionalHandle none = 0;
-    for (int step = 0; step < kMaxSteps; ++step) {
+    for (int step = 0; step < std::min(p->max_steps, kMaxSteps); ++step) {
         err = tags_mixed_ir_step(p, nb, st, none, 0);
         if (err) return err;
         int cont = 0;

@@ -312,7 +312,7 @@ int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st)
 
 // Add a while-node after the work captured so far on `st`; its body graph is
 // returned for a separate capture, its condition starts at 1 on every launch.
-static int add_while_node(cudaStream_t st, cudaGraphConditionalHandle* cond, cudaGraph_t* body) {
+int tags_plan_add_while_node(cudaStream_t st, cudaGraphConditionalHandle* cond, cudaGraph_t* body) {
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
     cudaGraph_t g = nullptr;
     const cudaGraphNode_t* deps_rt = nullptr;
@@ -352,7 +352,7 @@ static int capture_pass(tags_plan_s* p, int nb, double mur, int has_ie, int inj,
         } else {
             err = tags_mixed_factor(p, nb, st);
             if (!err) err = tags_mixed_ir_setup(p, nb, st);
-            if (!err) err = add_while_node(st, &cond, &body);
+            if (!err) err = tags_plan_add_while_node(st, &cond, &body);
         }
     }
     cudaGraph_t g = nullptr;
@@ -419,6 +419,28 @@ extern "C" int tags_plan_set_split(tags_plan plan, int pieces) {
     if (plan->split_pieces != pieces) {
         plan->split_pieces = pieces;
         tags_plan_drop_graphs(plan);
+    }
+    return 0;
+}
+
+extern "C" int tags_plan_set_refine_tol(tags_plan plan, double tol) {
+    if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_refine_tol: invalid plan");
+    if (!(tol >= 0.0) || tol > 1e-3) return tags_fail(TAGS_E_ARG, "tags_plan_set_refine_tol: tol must be 0 .. 1e-3");
+    const double v = tol == 0.0 ? 1e-8 : tol;
+    if (plan->ir_tol != v) {
+        plan->ir_tol = v;
+        tags_plan_drop_graphs(plan);     // the tolerance is an argument of the captured refinement kernels
+    }
+    return 0;
+}
+
+extern "C" int tags_plan_set_max_steps(tags_plan plan, int steps) {
+    if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_max_steps: invalid plan");
+    if (steps < 0 || steps > 40) return tags_fail(TAGS_E_ARG, "tags_plan_set_max_steps: steps must be 0 .. 40");
+    const int v = steps == 0 ? 40 : steps;
+    if (plan->max_steps != v) {
+        plan->max_steps = v;
+        tags_plan_drop_graphs(plan);     // the step cap is an argument of the captured decision kernel
     }
     return 0;
 }
@@ -597,10 +619,13 @@ static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble*
 // pass, graphs, fill model) before it takes passes.
 static int sync_twin(tags_plan_s* p) {
     tags_plan_s* t = p->twin;
-    if (t->split_pieces != p->split_pieces || t->group_panels != p->group_panels || t->pass_batch != p->pass_batch) {
+    if (t->split_pieces != p->split_pieces || t->group_panels != p->group_panels || t->pass_batch != p->pass_batch ||
+        t->max_steps != p->max_steps || t->ir_tol != p->ir_tol) {
         t->split_pieces = p->split_pieces;
         t->group_panels = p->group_panels;
         t->pass_batch = p->pass_batch;
+        t->max_steps = p->max_steps;
+        t->ir_tol = p->ir_tol;
         tags_plan_drop_graphs(t);
     }
     t->use_graphs = p->use_graphs;

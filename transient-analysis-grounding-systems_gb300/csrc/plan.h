@@ -66,6 +66,7 @@ struct tags_plan_s {
     double* d_dots = nullptr;       // batch x 4 sums of the current against the previous correction
     void* d_fillws = nullptr;       // pair classes and geometry records of the mixed fill
     int n_touch = 0;                // pairs sharing an endpoint (FP64 Duffy rule)
+    SpecialEntries spec;            // entries filled in FP64 (touching pairs, diagonal) and their residues
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
     int split_pieces = TAGS_SPLIT_F16;   // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
@@ -73,6 +74,8 @@ struct tags_plan_s {
     double2* d_pot = nullptr;       // mHEM: 4 x m x m static potentials (direct ZL, ZT; images ZL, ZT)
     SampleCoef* d_coef1 = nullptr;  // unit coefficients for the potentials
     int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
+    int max_steps = 40;             // refinement steps per pass before the FP64 fallback (1 .. 40)
+    double ir_tol = 1e-8;           // refinement stopping tolerance (relative error left in x)
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue,
                                     // step of the last extrapolation (batch)
@@ -120,3 +123,9 @@ int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st);
 int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditionalHandle cond, int set_cond);
 int tags_mixed_finish(tags_plan_s* p, int nb, cudaStream_t st, int* h_iters, double* h_berr, int* h_conv,
                       int* h_steps);
+// Plain FP64 re-solve of one sample (inputs on the device) into x_out / info_out.
+int tags_mixed_fallback_one(tags_plan_s* p, const double2* d_s, const double2* d_kappa, double mur,
+                            const double2* d_ie, int inj_node, double2* x_out, int* info_out, cudaStream_t st);
+// While-node after the work captured so far on `st` (condition 1 at launch);
+// its body graph is returned for a separate capture.
+int tags_plan_add_while_node(cudaStream_t st, cudaGraphConditionalHandle* cond, cudaGraph_t* body);
