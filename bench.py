@@ -11,6 +11,7 @@ samples, cycling through the 2048-sample set. Prints one JSON line.
   python bench.py --impl reference      # the reference's CPU path on the host cores
   python bench.py --workload fields     # post-processing: potentials and field along a line
   python bench.py --workload grids      # 64 grids of uneven size x 256 samples in one call
+  python bench.py --workload mhem       # the examples' mHEM impedance model, same grid and samples
 """
 from __future__ import annotations
 
@@ -385,6 +386,158 @@ def run_fields(args):
     return 0
 
 
+# ---- mHEM + nodal admittance: what the reference's examples run ---------------------
+# The same grid, soil, current and samples; the impedances from the mHEM model
+# (static potentials once per geometry, rescaled per sample by e^{-gamma r}
+# of the midpoint distances, examples/three_grids.c:270-350) and the node
+# potentials of the nodal-admittance system (src/linalg.c:142-350), which is
+# the node-block Schur complement of the immittance system the plan solves.
+
+def mhem_cpu_baseline(elec, img, nodes, s, kappa, inj, centre, cores):
+    """Path B on the host cores: the oracle's restatement of the examples'
+    loop (INTG_MHEM potentials once, then per sample the rescale,
+    calculate_yla_ytb, fill_impedance_adm2 and zsysv on n x n; OpenMP over
+    samples, OpenBLAS on one thread). Two runs separate the once-per-geometry
+    potentials from the per-sample cost; the value is the whole 2048-sample
+    job's rate with the potentials amortised over it."""
+    from oracle import oracle as O
+    port = O.get("port")
+    idx1 = np.linspace(0, len(s) - 1, cores).astype(int)
+    idx2 = np.linspace(0, len(s) - 1, 2 * cores).astype(int)
+    t0 = time.perf_counter()
+    port.mhem_sweep(elec, img, nodes, s[idx1], kappa[idx1], centre, inj[idx1], threads=cores)
+    t1 = time.perf_counter()
+    port.mhem_sweep(elec, img, nodes, s[idx2], kappa[idx2], centre, inj[idx2], threads=cores)
+    t2 = time.perf_counter()
+    per_sample = max((t2 - t1) - (t1 - t0), 1e-9) / cores          # wall s per sample at `cores` threads
+    setup = max((t1 - t0) - cores * per_sample, 0.0)
+    ns = len(s)
+    return {"value": ns / (setup + ns * per_sample), "unit": "solves/s", "cores": cores, "kind": "port",
+            "per_sample_rate": 1.0 / per_sample, "potentials_s": setup,
+            "sample": f"path B (mHEM potentials at cubature 1e-6, per-sample rescale + calculate_yla_ytb + "
+                      f"fill_impedance_adm2 + zsysv n x n), {cores} and {2 * cores} strided samples in "
+                      f"{t1 - t0:.1f} s and {t2 - t1:.1f} s; value = 2048 samples with the once-per-geometry "
+                      f"potentials amortised"}
+
+
+def run_mhem(args):
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+    pkg = entry.load_package()
+    pkg.build()
+    elec, img, nodes, s, kappa, inj, centre = workload(pkg)
+    m, n = elec.shape[0], nodes.shape[0]
+    N = n + 2 * m
+    B = args.batch or 128
+    P = args.pipelines or 2
+    SB = B * (args.step_passes or P)
+    plan = pkg.Plan(elec, img, nodes, pkg.MIXED, max_batch=B)
+    plan.set_fill(pkg.INTG_MHEM)
+    if P > 1:
+        plan.set_pipelines(P)
+    ns_total = len(s)
+    steps = args.steps if args.steps > 0 else -(-ns_total // SB)
+    dev = torch.device("cuda", local)
+    s_d = torch.from_numpy(s).to(dev)
+    k_d = torch.from_numpy(kappa).to(dev)
+    ie_full = np.zeros((ns_total, n), np.complex128)
+    ie_full[:, centre] = inj
+    ie_d = torch.from_numpy(ie_full).to(dev)
+    sol_d = torch.empty((SB, N), dtype=torch.complex128, device=dev)
+    info_d = torch.empty((SB,), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+
+    def batch_index(step):
+        start = (step * SB) % ns_total
+        return start, min(SB, ns_total - start)
+
+    def run_step(step):
+        k0, nb = batch_index(step)
+        return plan.run_device(s_d[k0:].data_ptr(), k_d[k0:].data_ptr(), nb, 1.0, ie_d[k0:].data_ptr(), centre,
+                               sol_d.data_ptr(), info_d.data_ptr())
+
+    for w in range(args.warmup):
+        run_step(w)
+    torch.cuda.synchronize()
+    launches0 = pkg.launch_count()
+    dev_time, it_max, fb, step_ms = 0.0, 0, 0, []
+    with ClockSampler(local) as clk:
+        for st_i in range(steps):
+            flush.zero_()
+            st = run_step(st_i)
+            dev_time += st.seconds
+            step_ms.append(round(st.seconds * 1e3, 3))
+            it_max, fb = max(it_max, st.max_iterations), fb + st.fallbacks
+        torch.cuda.synchronize()
+    launches = pkg.launch_count() - launches0
+    samples = sum(batch_index(q)[1] for q in range(steps))
+    value = samples / dev_time
+    # kernel families, one pass in flight, kernel by kernel
+    plan.set_graphs(False)
+    plan.set_pipelines(1)
+    pkg.lib().tags_gpu_profile(1)
+    for st_i in range(steps):
+        flush.zero_()
+        run_step(st_i)
+    torch.cuda.synchronize()
+    prof = read_profile(pkg)
+    pkg.lib().tags_gpu_profile(0)
+    plan.set_graphs(True)
+    plan.set_pipelines(P)
+    # end to end through tags_plan_run with pinned host buffers
+    s_h = torch.from_numpy(s).pin_memory()
+    k_h = torch.from_numpy(kappa).pin_memory()
+    ie_h = torch.from_numpy(ie_full).pin_memory()
+    sol_h = torch.empty((SB, N), dtype=torch.complex128).pin_memory()
+    info_h = torch.empty((SB,), dtype=torch.int32).pin_memory()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for st_i in range(steps):
+        k0, nb = batch_index(st_i)
+        code = pkg.lib().tags_plan_run(plan.handle, s_h[k0:].data_ptr(), k_h[k0:].data_ptr(), 1.0, nb,
+                                       ie_h[k0:].data_ptr(), centre, sol_h.data_ptr(), info_h.data_ptr(), 0, None)
+        if code != 0:
+            raise RuntimeError(pkg.last_error())
+    e2e_t = time.perf_counter() - t0
+    # accuracy: mixed mHEM against plain-FP64 mHEM, 8 strided samples
+    idx = np.linspace(0, ns_total - 1, 8).astype(int)
+    um, _, _ = plan.run(s[idx], kappa[idx], 1.0, ie_full[idx])
+    ref = pkg.Plan(elec, img, nodes, pkg.PLAIN_FP64, max_batch=8)
+    try:
+        ref.set_fill(pkg.INTG_MHEM)
+        up, _, _ = ref.run(s[idx], kappa[idx], 1.0, ie_full[idx])
+    finally:
+        ref.close()
+    plan.close()
+    peaks = measured_peaks()
+    roof, fams = roofline(prof, peaks, 16)
+    line = {"metric": "Laplace-sample solves/s, mHEM model (1560-segment grid, 2048 samples)", "value": value,
+            "unit": "solves/s", "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dev_time / steps, "step_ms": step_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64+c128",
+            "data": "synthetic (reference grid generator, Alipio soil, 1.2/50 us current)",
+            "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, N=4537, 2048 Laplace samples, mHEM "
+                                   "impedances (tags_plan_set_fill(INTG_MHEM)), mixed-precision solve",
+                       "samples_per_step": SB, "samples_per_pass": B, "passes_in_flight": P,
+                       "l2": "flushed between steps (256 MB write)"},
+            "roofline": roof, "kernel_families": fams, "gpu_launches": launches, "clocks": clk.summary(),
+            "e2e": {"value": samples / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": SB * 16 * (2 + n),
+                    "d2h_bytes_per_step": SB * (16 * N + 4)},
+            "refinement": {"max_iterations": it_max, "fallbacks": fb},
+            "accuracy": {"samples": int(len(idx)), "reference": "plain FP64 form of this library, mHEM fill",
+                         "max_rel_err_u_inj": float(np.max(np.abs(um[:, centre] - up[:, centre]) /
+                                                           np.abs(up[:, centre]))),
+                         "max_rel_err_u_all": float(np.max(np.abs(um[:, :n] - up[:, :n])) / np.max(np.abs(up[:, :n])))}}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = mhem_cpu_baseline(elec, img, nodes, s, kappa, inj, centre, os.cpu_count() or 1)
+    print(json.dumps(line))
+    return 0
+
+
 # ---- many uneven grids ---------------------------------------------------------------
 # 64 square grids of uneven size (side 5-40 m, 2-10 meshes, 1 m segmentation,
 # m = 36..880), each with its own soil, 256 Laplace samples each (nt = 510,
@@ -416,41 +569,57 @@ def run_grids(args):
     jobs = grid_jobs(pkg)
     ms = [j["electrodes"].shape[0] for j in jobs]
     ns = len(jobs[0]["s"])
-    workers = args.pipelines or 4
-    pkg.solve_batch(jobs[:4], precision=pkg.MIXED, workers=workers)          # warm-up: modules, tables
+    steps = args.steps if args.steps > 0 else 3
+    # the grid batch: a plan per grid and one CUDA graph over all of them,
+    # built once (outside the timed region, like a plan)
+    t0 = time.perf_counter()
+    batch = pkg.GridBatch(jobs, precision=pkg.MIXED)
+    setup_s = time.perf_counter() - t0
+    for _ in range(max(1, args.warmup)):
+        batch.run(jobs)
     torch.cuda.synchronize()
     launches0 = pkg.launch_count()
+    dev_s, wall, it_max, fb = 0.0, 0.0, 0, 0
     with ClockSampler(local) as clk:
-        t0 = time.perf_counter()
-        out = pkg.solve_batch(jobs, precision=pkg.MIXED, workers=workers)
-        wall = time.perf_counter() - t0
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            out, st = batch.run(jobs)
+            wall += time.perf_counter() - t0
+            dev_s += st.seconds
+            it_max, fb = max(it_max, st.max_iterations), fb + st.fallbacks
+            if any(np.any(info) for _, info in out):
+                raise RuntimeError("a grid reported a failed sample")
     launches = pkg.launch_count() - launches0
-    if any(np.any(info) for _, info in out):
-        raise RuntimeError("a grid reported a failed sample")
-    solves = len(jobs) * ns
-    # accuracy: mixed against plain FP64 on four grids, 16 strided samples each
-    idx = np.linspace(0, ns - 1, 16).astype(int)
-    sub = [dict(j, s=j["s"][idx], kappa=j["kappa"][idx]) for j in (jobs[0], jobs[21], jobs[42], jobs[63])]
-    mx = pkg.solve_batch(sub, precision=pkg.MIXED, workers=2)
-    pl = pkg.solve_batch(sub, precision=pkg.PLAIN_FP64, workers=2)
-    err = max(float(np.max(np.abs(a[0][:, 0] - b[0][:, 0]) / np.abs(b[0][:, 0]))) for a, b in zip(mx, pl))
+    batch.close()
+    solves = len(jobs) * ns * steps
+    # accuracy: mixed against plain FP64 on every grid, 8 strided samples each
+    idx = np.linspace(0, ns - 1, 8).astype(int)
+    sub = [dict(j, s=j["s"][idx], kappa=j["kappa"][idx]) for j in jobs]
+    mx = pkg.solve_batch(sub, precision=pkg.MIXED)
+    pl = pkg.solve_batch(sub, precision=pkg.PLAIN_FP64)
+    per_grid = [float(np.max(np.abs(a[0][:, :j["nodes"].shape[0]] - b[0][:, :j["nodes"].shape[0]])) /
+                      np.max(np.abs(b[0][:, :j["nodes"].shape[0]]))) for a, b, j in zip(mx, pl, jobs)]
     line = {"metric": "Laplace-sample solves/s over 64 uneven grids (m = %d..%d), 256 samples each" % (min(ms), max(ms)),
-            "value": solves / wall, "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1,
-            "ms_per_step": 1e3 * wall, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "value": solves / dev_s, "unit": "solves/s", "n_gpus": 1, "steps": steps, "warmup": max(1, args.warmup),
+            "ms_per_step": 1e3 * dev_s / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c64+c128", "data": "synthetic (reference grid generator; per-grid soil)",
             "config": {"workload": "64 square grids, side 5-40 m, 2-10 meshes, 1 m segmentation, depth 0.3-1 m, "
                                    "rho 50-5000 ohm m, eps_r 5-40; 256 Laplace samples each (nt = 510, 10 MHz); "
-                                   "one tags_gpu_solve_batch call, %d host threads" % workers,
-                       "grids": len(jobs), "segments": [min(ms), max(ms)]},
+                                   "one grid batch (tags_batch_*): every grid a branch of one CUDA graph, one "
+                                   "graph launch per step",
+                       "grids": len(jobs), "segments": [min(ms), max(ms)], "setup_s": setup_s},
             "roofline": None, "gpu_launches": launches, "clocks": clk.summary(),
             "e2e": {"value": solves / wall, "unit": "solves/s",
                     "h2d_bytes_per_step": int(sum(16 * ns * 2 for _ in jobs)),
                     "d2h_bytes_per_step": int(sum(ns * (16 * (j["nodes"].shape[0] + 2 * j["electrodes"].shape[0]) + 4)
                                                   for j in jobs))},
-            "accuracy": {"grids": 4, "samples": 16, "reference": "plain FP64 form of this library",
-                         "max_rel_err_u_inj": err},
-            "note": "value is end to end: plan set-up (allocation, pair plan, graph capture) of every grid is inside "
-                    "the timed call; the kernels are those of the solves workload, whose line carries their roofline"}
+            "refinement": {"max_iterations": it_max, "fallbacks": fb},
+            "accuracy": {"grids": len(jobs), "samples": len(idx),
+                         "reference": "plain FP64 form of this library (node potentials)",
+                         "max_rel_err": max(per_grid), "per_grid_max_rel_err": [float("%.3g" % e) for e in per_grid]},
+            "note": "value = samples / device time of the graph launches (tags_batch_run stats); e2e = the same "
+                    "runs' wall time with the host copies; setup_s = building the 64 plans and capturing the graph "
+                    "once; the kernels are those of the solves workload, whose line carries their roofline"}
     if not args.no_cpu_baseline:
         from oracle import oracle as O
         port = O.get("port")
@@ -471,6 +640,86 @@ def run_grids(args):
     return 0
 
 
+GPR_FIXTURE = os.path.join(ROOT, "tests", "golden", "gpr4.npz")
+
+
+def plain_fp64_record(pkg, elec, img, nodes, s_d, k_d, ie_d, centre, local, flush, steps=3, batch=8):
+    """The plain FP64 form (FP64 fill, LU with partial pivoting) timed the way
+    the mixed form is: device time from the plan's CUDA events, inputs in
+    HBM, L2 flushed between steps; `steps` steps of `batch` samples spread
+    over the band after one warm-up step (its cost does not depend on the
+    sample: no refinement)."""
+    import torch
+    n = nodes.shape[0]
+    N = n + 2 * elec.shape[0]
+    ns = s_d.shape[0]
+    plan = pkg.Plan(elec, img, nodes, pkg.PLAIN_FP64, max_batch=batch)
+    sol = torch.empty((batch, N), dtype=torch.complex128, device=s_d.device)
+    info = torch.empty((batch,), dtype=torch.int32, device=s_d.device)
+    starts = np.linspace(0, ns - batch, steps).astype(int)
+
+    def one(k0):
+        return plan.run_device(s_d[k0:].data_ptr(), k_d[k0:].data_ptr(), batch, 1.0, ie_d[k0:].data_ptr(), centre,
+                               sol.data_ptr(), info.data_ptr())
+    try:
+        one(int(starts[-1]))
+        torch.cuda.synchronize()
+        dt, step_ms = 0.0, []
+        with ClockSampler(local) as clk:
+            for k0 in starts:
+                flush.zero_()
+                st = one(int(k0))
+                dt += st.seconds
+                step_ms.append(round(st.seconds * 1e3, 1))
+            torch.cuda.synchronize()
+        if int(info.abs().max().item()) != 0:
+            raise RuntimeError("plain FP64 solve reported a singular pivot")
+    finally:
+        plan.close()
+    return {"value": steps * batch / dt, "unit": "solves/s", "steps": steps, "samples_per_step": batch,
+            "ms_per_step": 1e3 * dt / steps, "step_ms": step_ms, "clocks": clk.summary(),
+            "note": "plain FP64 form of this library on the same workload: FP64 fill, FP64 LU with partial "
+                    "pivoting, device time from the plan's events, L2 flushed between steps"}
+
+
+def gpr_accuracy(pkg, plan, s_d, k_d, ie_d, centre, n, SB, sol_d, info_d, s, tmax, nt):
+    """The mixed form over every sample of the workload (outside the timed
+    region): U at the injection node per sample, its GPR through the
+    inverse Laplace transform, and both against the plain FP64 form's
+    (tests/golden/gpr4.npz, made by tests/golden/make_gpr4.py, its 16
+    strided samples pinned to the reference's own C code)."""
+    if not os.path.exists(GPR_FIXTURE):
+        return None
+    fx = np.load(GPR_FIXTURE)
+    if not np.array_equal(fx["s"], s):
+        return None
+    ns = len(s)
+    u = np.zeros(ns, np.complex128)
+    pin = {int(k): j for j, k in enumerate(fx["pin_idx"])}
+    u_nodes = np.zeros((len(pin), n), np.complex128)
+    for k0 in range(0, ns, SB):
+        nb = min(SB, ns - k0)
+        plan.run_device(s_d[k0:].data_ptr(), k_d[k0:].data_ptr(), nb, 1.0, ie_d[k0:].data_ptr(), centre,
+                        sol_d.data_ptr(), info_d.data_ptr())
+        u[k0:k0 + nb] = sol_d[:nb, centre].cpu().numpy()
+        for k in range(k0, k0 + nb):
+            if k in pin:
+                u_nodes[pin[k]] = sol_d[k - k0, :n].cpu().numpy()
+    gpr = pkg.inv_laplace_trans(u, s, tmax, nt)
+    per = np.abs(u - fx["u_centre"]) / np.abs(fx["u_centre"])
+    out = {"samples": ns, "reference": "plain FP64 form of this library over all samples (tests/golden/gpr4.npz)",
+           "gpr_rel_err": float(np.max(np.abs(gpr - fx["gpr"])) / np.max(np.abs(fx["gpr"]))),
+           "max_rel_err_u_inj": float(per.max()),
+           "max_rel_err_u_all": float(np.max(np.abs(u_nodes - fx["u_nodes"])) / np.max(np.abs(fx["u_nodes"]))),
+           "gpr_peak_v": float(np.max(np.abs(fx["gpr"])))}
+    if "ref_u_nodes" in fx:
+        ref = fx["ref_u_nodes"]
+        out["plain_vs_reference_build"] = float(np.max(np.abs(fx["u_nodes"] - ref)) / np.max(np.abs(ref)))
+        out["mixed_vs_reference_build"] = float(np.max(np.abs(u_nodes - ref)) / np.max(np.abs(ref)))
+        out["reference_samples"] = int(ref.shape[0])
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -486,14 +735,15 @@ def main():
     ap.add_argument("--cpu-samples", type=int, default=0, help="CPU-baseline samples (0 = host cores)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-graphs", action="store_true", help="launch kernel by kernel in the measured pass")
-    ap.add_argument("--no-accuracy", action="store_true", help="skip the 16-sample check against plain FP64")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the all-sample GPR check against plain FP64")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 sub-record")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     ap.add_argument("--first-batch", type=int, default=0,
                     help="batch of samples the warm-up and timed steps start from (0 = the whole job in order)")
-    ap.add_argument("--workload", default="solves", choices=["solves", "fields", "grids"],
+    ap.add_argument("--workload", default="solves", choices=["solves", "fields", "grids", "mhem"],
                     help="solves: the per-sample HEM path (default); fields: post-processing along a line; "
-                         "grids: 64 uneven grids in one call")
+                         "grids: 64 uneven grids in one call; mhem: the examples' mHEM model on the same grid")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -501,6 +751,8 @@ def main():
         return run_fields(args)
     if args.workload == "grids":
         return run_grids(args)
+    if args.workload == "mhem":
+        return run_mhem(args)
 
     import torch
     import torch.distributed as dist
@@ -524,6 +776,9 @@ def main():
     if P > 1:
         plan.set_pipelines(P)
     ns_total = len(s)
+    # default steps: the 2048-sample job split over the ranks (total work
+    # fixed: strong scaling); --steps K: K steps per rank (weak scaling)
+    scaling = "strong" if args.steps <= 0 and world > 1 else "weak"
     if args.steps <= 0:
         args.steps = max(1, -(-ns_total // (SB * world)))
     dev = torch.device("cuda", local)
@@ -619,21 +874,13 @@ def main():
     e2e = {"value": e2e_samples / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": SB * 16 * (2 + n),
            "d2h_bytes_per_step": SB * (16 * N + 4)}
 
-    # accuracy of the measured form against the plain FP64 form: 16 strided
-    # samples, node potentials for the injected current (outside the timed region)
-    accuracy = None
+    # accuracy of the measured form: every sample, GPR included, against the
+    # plain FP64 form (outside the timed region)
+    accuracy, plain = None, None
     if mixed and rank == 0 and not args.no_accuracy:
-        idx = np.arange(0, ns_total, max(1, ns_total // 16))[:16]
-        sol_m, _, _ = plan.run(s[idx], kappa[idx], 1.0, ie_full[idx])
-        ref = pkg.Plan(elec, img, nodes, pkg.PLAIN_FP64, max_batch=8)
-        try:
-            sol_p, _, _ = ref.run(s[idx], kappa[idx], 1.0, ie_full[idx])
-        finally:
-            ref.close()
-        um, up = sol_m[:, :n], sol_p[:, :n]
-        accuracy = {"samples": int(len(idx)), "reference": "plain FP64 form of this library",
-                    "max_rel_err_u_inj": float(np.max(np.abs(um[:, centre] - up[:, centre]) / np.abs(up[:, centre]))),
-                    "max_rel_err_u_all": float(np.max(np.abs(um - up)) / np.max(np.abs(up)))}
+        accuracy = gpr_accuracy(pkg, plan, s_d, k_d, ie_d, centre, n, SB, sol_d, info_d, s, TMAX, NT)
+    if mixed and rank == 0 and not args.no_plain:
+        plain = plain_fp64_record(pkg, elec, img, nodes, s_d, k_d, ie_d, centre, local, flush)
 
     if rank != 0:
         return 0
@@ -642,7 +889,7 @@ def main():
     line = {"metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)", "value": value,
             "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dev_time / args.steps, "step_ms": measured_step_ms,
-            "higher_is_better": True, "scaling": "weak",
+            "higher_is_better": True, "scaling": scaling,
             "vs_baseline": None, "dtype": "c128" if not mixed else "c64+c128",
             "data": "synthetic (reference grid generator, Alipio soil, 1.2/50 us current)",
             "config": {"workload": "grid 60x60 m, 12x12 meshes, 1560 segments, 1417 nodes, N=4537, 2048 Laplace "
@@ -658,6 +905,9 @@ def main():
             "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e,
             "refinement": {"max_iterations": stats_iter, "fallbacks": stats_fb, "split": split},
             "accuracy": accuracy, "wall_s": wall}
+    if plain is not None:
+        line["plain_fp64"] = plain
+        line["mixed_over_plain"] = value / plain["value"]
     if not args.no_cpu_baseline:
         nsamp = args.cpu_samples or (os.cpu_count() or 1)
         line["cpu_baseline"] = cpu_baseline(args, elec, img, nodes, s, kappa, inj, centre, nsamp)[0]
