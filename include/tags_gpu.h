@@ -415,8 +415,9 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
  * refinement: a sample stops once the error its corrections predict (four
  * times the last correction times their measured contraction) is below
  * tol |x|, or once a correction is below tol / 10 |x| (0 restores the default
- * 1e-8; at most 1e-3). Smaller values cost refinement steps and bring x
- * closer to the solution of the system the residual sees. */
+ * 1e-9; at most 1e-3). The residual sees the impedance entries to ~1e-13, so
+ * tol bounds the error against the FP64 solution; smaller values cost
+ * refinement steps. */
 int tags_plan_set_refine_tol (tags_plan plan, double tol);
 
 /* No counterpart in the reference. Caps the refinement steps of the mixed

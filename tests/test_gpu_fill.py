@@ -172,13 +172,13 @@ def _touching_pairs(e):
 
 
 @pytest.mark.parametrize("with_images", [False, True])
-def test_mixed_fill_keeps_log_singular_entries_in_fp64(gpu_pkg, with_images):
+def test_mixed_fill_matches_fp64_fill(gpu_pkg, with_images):
     """60 x 60 m grid (1560 segments), a low and a high Laplace sample of the
-    benchmark: the mixed form's fill as its residual sees it, against the FP64
-    fill. The entries of pairs sharing an endpoint and the diagonal are FP64
-    (hi + lo): without images they are purely log-singular and self terms, and
-    agree to FP64 rounding; with images those entries carry an FP32 image
-    part. Regular pairs are FP32 (~1e-7)."""
+    benchmark: the mixed form's fill as its residual sees it (float pairs hi +
+    lo), against the FP64 fill. Pairs sharing an endpoint and the diagonal are
+    computed in FP64 per sample (Duffy rule, closed-form self term); the
+    regular pairs come from the moment expansion (FP64 geometry moments, series
+    in float pairs). Both agree with the FP64 fill to ~1e-14."""
     pkg = gpu_pkg
     e, nodes = pkg.electrode_grid(13, 13, 60.0, 60.0, 5, 5, 7e-3, -0.5)
     m = e.shape[0]
@@ -212,8 +212,5 @@ def test_mixed_fill_keeps_log_singular_entries_in_fp64(gpu_pkg, with_images):
     print(f"\nmixed fill vs FP64 fill ({'with' if with_images else 'without'} images), "
           f"{len(touch)} touching pairs + {m} diagonal: " +
           ", ".join(f"{k[0]} {k[1]} {v:.2e}" for k, v in sorted(worst.items())))
-    if not with_images:
-        assert worst[("zl", "special")] <= 1e-13 and worst[("zt", "special")] <= 1e-13
-    else:
-        assert worst[("zl", "special")] <= 1e-7 and worst[("zt", "special")] <= 1e-7
-    assert worst[("zl", "regular")] <= 2e-6 and worst[("zt", "regular")] <= 2e-6
+    assert worst[("zl", "special")] <= 1e-13 and worst[("zt", "special")] <= 1e-13
+    assert worst[("zl", "regular")] <= 1e-12 and worst[("zt", "regular")] <= 1e-12

@@ -6,7 +6,15 @@ potentials and its transient GPR (the reference's inverse transform,
 src/auxiliary.c:265-329) against the plain FP64 form's, stored in
 tests/golden/gpr4.npz (made by tests/golden/make_gpr4.py, whose 16 strided
 samples are pinned to the reference build). Bar: 1e-6 relative, the mixed
-form's target for impedance and GPR."""
+form's target for impedance and GPR; the node potentials come out within
+1e-8 (measured ~1e-10).
+
+The inverse transform multiplies each time point by e^{c t} (up to nt^2 =
+1.7e7 at t = T), so sample-to-sample differences of the potentials reach the
+GPR amplified: a 1e-8 noise-like error per sample becomes ~1e-6 of the GPR's
+peak by t = T/2. The mixed form's impedance entries are float pairs good to
+~1e-13 and its refinement stops at 1e-9, which keeps the GPR within 1e-6
+over the whole window."""
 import numpy as np
 import pytest
 
@@ -54,12 +62,12 @@ def test_mixed_gpr_on_benchmark_grid_all_samples(gpu_pkg):
     print(f"\nmixed vs plain FP64, 2048 samples: U(inj) max rel {per_sample.max():.3e}, "
           f"GPR rel {gpr_err:.3e} (t <= T/2: {gpr_err_half:.3e}), node potentials at 16 samples {nodes_err:.3e}, "
           f"max refinement steps {it_max}")
-    assert per_sample.max() <= 1e-6
-    assert nodes_err <= 1e-6
-    quarter = nt // 4
-    gpr_err_quarter = rel_err(gpr[:quarter], fx["gpr"][:quarter])
-    print(f"GPR rel err, t <= T/4: {gpr_err_quarter:.3e}")
-    assert gpr_err_quarter <= 1e-6
+    assert per_sample.max() <= 1e-8
+    assert nodes_err <= 1e-8
+    # the whole window, and its first half against the physical peak there
+    # (the transform's late-time values grow as e^{c t} in both forms)
+    assert gpr_err <= 1e-6
+    assert gpr_err_half <= 1e-6
     if "ref_u_nodes" in fx:
         ref_err = rel_err(u_nodes, fx["ref_u_nodes"])
         print(f"mixed vs reference build at 16 samples: {ref_err:.3e}")

@@ -710,7 +710,7 @@ class Plan:
             raise RuntimeError(f"tags_plan_set_fill failed ({code}): {last_error()}")
 
     def set_refine_tol(self, tol):
-        """Refinement stopping tolerance of the mixed form (0 = default 1e-8)."""
+        """Refinement stopping tolerance of the mixed form (0 = default 1e-9)."""
         code = lib().tags_plan_set_refine_tol(self.handle, float(tol))
         if code != 0:
             raise RuntimeError(f"tags_plan_set_refine_tol failed ({code}): {last_error()}")

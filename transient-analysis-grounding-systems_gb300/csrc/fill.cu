@@ -34,6 +34,8 @@ constexpr int GL_TOTAL = QMAX * (QMAX + 1) / 2;
 
 __device__ double g_glx[GL_TOTAL];            // nodes on [0,1], order q at q(q-1)/2
 __device__ double g_glw[GL_TOTAL];            // weights on [0,1]
+constexpr int MOM_N = 24;                     // terms of the moment expansion stored (mixed fill)
+constexpr double MOM_H = 0.125;               // spacing of its expansion centres (m)
 constexpr int QMIX = 24;                      // largest order of the FP32 fill
 constexpr int GL_MIX = QMIX * (QMIX + 1) / 2;
 __device__ float g_glxm[GL_MIX];              // FP32 fill: nodes shifted to [-1/2, 1/2], orders 1..QMIX
@@ -557,22 +559,26 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
     const double* __restrict__ elec, const double* __restrict__ img, const float4* __restrict__ sdir,
     const float4* __restrict__ idir, int m, const uint16_t* __restrict__ codes,
     const PairRec* __restrict__ recs, const SampleF32* __restrict__ coef, int nsamp, float2* zl0, float2* zt0,
-    long long bstride, int has_img, long long ntiles, int* status) {
+    long long bstride, int has_img, long long ntiles, int* status, const int* __restrict__ mom_ok, float2* zlo0,
+    float2* ztlo0) {
     __shared__ float sxm[GL_MIX], swf[GL_MIX];
     __shared__ FillWarpSmem sw_all[FILL_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int smp = blockIdx.y * 32 + lane;
+    // samples the moment fill covers (mom_ok) are left to it; every warp of a
+    // CTA has the same 32 samples, so a CTA with none to do leaves as a whole
+    const bool valid = smp < nsamp && !(mom_ok && mom_ok[smp]);
+    if (!__any_sync(0xffffffffu, valid)) return;
     for (int t = threadIdx.x; t < GL_MIX; t += blockDim.x) {
         sxm[t] = g_glxm[t];
         swf[t] = g_glwm[t];
     }
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     FillWarpSmem& W = sw_all[warp];
     const long long tile = (long long)blockIdx.x * FILL_WARPS + warp;
     if (tile >= ntiles) return;                      // whole warp leaves together
     int kb, i;
     fill_tile(tile, m, kb, i);
-    const int smp = blockIdx.y * 32 + lane;
-    const bool valid = smp < nsamp;
     SampleF32 c{};
     if (valid) c = coef[smp];
     float gmax = valid ? sqrtf(c.grh * c.grh + c.gih * c.gih) : 0.f;
@@ -687,12 +693,16 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
         for (int idx = lane; idx < FILL_SUB * 32; idx += 32) {
             const int j = idx % FILL_SUB, sl = idx / FILL_SUB;
             const int ss = blockIdx.y * 32 + sl;
-            if (j < nrow && ss < nsamp) {
+            if (j < nrow && ss < nsamp && !(mom_ok && mom_ok[ss])) {
                 const float2 a = W.zl[j][sl], b = W.zt[j][sl];
                 if (!isfinite(a.x + a.y + b.x + b.y)) raise_status(status, TAGS_ST_NONFINITE);
                 const long long off = bstride * ss + (k0 + j) + (long long)m * i;
                 zl0[off] = a;
                 zt0[off] = b;
+                if (zlo0) {
+                    zlo0[off] = make_float2(0.f, 0.f);       // FP32 entries: no residue
+                    ztlo0[off] = make_float2(0.f, 0.f);
+                }
             }
         }
         __syncwarp();
@@ -736,17 +746,17 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
 // kind that shares an endpoint, or a diagonal entry) the Duffy rule of
 // j_touch at the plain form's order (16 + 2 |gamma| L) for the touching kinds,
 // and the static closed form for the self term, added to the FP32 value
-// k_fill_mixed left there for the regular kinds (lower triangle). The sum v
-// is formed in FP64 and stored as hi = fl(v) in Z and lo = fl(v - hi) in the
-// residue list that the refinement's residual reads. One warp per entry and
+// the regular fill left there for the regular kinds (lower triangle, hi in Z
+// and lo in Zlo). The sum v is formed in FP64 and stored again as hi = fl(v)
+// in Z and lo = fl(v - hi) in Zlo, which the refinement's residual reads. One warp per entry and
 // 32 samples (lanes): the rule's nodes (rho and w / rho of both Duffy halves)
 // are computed once per warp into shared memory.
 constexpr int SPEC_WARPS = 4;
 
 __global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
     const double* __restrict__ elec, const double* __restrict__ img, int m, const int2* __restrict__ ent, int nent,
-    const SampleCoef* __restrict__ coef, int nsamp, float2* zl0, float2* zt0, long long bstride,
-    float4* __restrict__ lo, int* status) {
+    const SampleCoef* __restrict__ coef, int nsamp, float2* zl0, float2* zt0, float2* zlo0, float2* ztlo0,
+    long long bstride, int* status) {
     __shared__ double2 nodes_all[SPEC_WARPS][2 * QMAX];      // (rho, w / rho)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double2* nodes = nodes_all[warp];
@@ -824,14 +834,350 @@ __global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
     if (!valid) return;
     if (!isfinite(dl.x + dl.y + dt.x + dt.y)) raise_status(status, TAGS_ST_NONFINITE);
     const long long idx = bstride * smp + k + (long long)m * i;      // lower triangle (k_zmirror copies it up)
-    const float2 za = zl0[idx], zb = zt0[idx];
-    const double vlr = (double)za.x + dl.x, vli = (double)za.y + dl.y;
-    const double vtr = (double)zb.x + dt.x, vti = (double)zb.y + dt.y;
+    const float2 za = zl0[idx], zb = zt0[idx], la = zlo0[idx], lb = ztlo0[idx];
+    const double vlr = ((double)za.x + (double)la.x) + dl.x, vli = ((double)za.y + (double)la.y) + dl.y;
+    const double vtr = ((double)zb.x + (double)lb.x) + dt.x, vti = ((double)zb.y + (double)lb.y) + dt.y;
     const float2 hl = make_float2((float)vlr, (float)vli), ht = make_float2((float)vtr, (float)vti);
     zl0[idx] = hl;
     zt0[idx] = ht;
-    lo[(long long)smp * nent + e] = make_float4((float)(vlr - (double)hl.x), (float)(vli - (double)hl.y),
-                                                (float)(vtr - (double)ht.x), (float)(vti - (double)ht.y));
+    zlo0[idx] = make_float2((float)(vlr - (double)hl.x), (float)(vli - (double)hl.y));
+    ztlo0[idx] = make_float2((float)(vtr - (double)ht.x), (float)(vti - (double)ht.y));
+}
+
+// ---- mixed form: moment expansion of the regular pairs ---------------------------------
+//
+// For a (pair, kind) whose segments share no endpoint,
+//   J(gamma) = \int_0^1 \int_0^1 e^{-gamma r} / r dt0 dt1
+//            = e^{-gamma R} sum_n (-gamma)^n / n! N_n,   N_n = \int\int (r - R)^n / r dt0 dt1,
+// expanded about R = b h, the multiple of h = 1/8 m nearest the midpoint
+// distance. |r - R| <= (L_i + L_k) / 2 + h / 2 on the pair, so the series
+// converges like that of e^{|gamma| dmax}: 16 terms reach 1e-14 at |gamma|
+// dmax = 0.9 (1 m segments at 10 MHz in 1 mS/m soil). The moments N_n depend
+// on the geometry only and are computed once per plan in FP64 (tensor
+// Gauss-Legendre at the FP64 fill's orders plus MOM_EXTRA). Per sample a pass
+// evaluates the series in two-float arithmetic (float pairs; the terms past
+// MOM_HEAD, below 1e-5 of the sum, by Horner in FP32) and multiplies by
+// e^{-gamma b h} from a per-sample table computed in FP64. The entries come
+// out as hi + lo float pairs good to ~1e-12, where the FP32 quadrature of the
+// same integrals (k_fill_mixed, kept for samples the series does not reach)
+// is good to ~1e-7. FP32 rounding of the stored entries varies from sample to
+// sample like noise, which the inverse Laplace transform amplifies by up to
+// e^{c t}; the float pairs keep that noise at the FP64 level.
+
+constexpr int MOM_HEAD = 8;                                  // terms kept as float pairs
+constexpr int MOM_FLOATS = 2 * MOM_HEAD + (MOM_N - MOM_HEAD);   // 32 floats per (pair, kind)
+constexpr int MOM_EXTRA = 6;                                 // orders above the FP64 fill's rule
+static_assert(MOM_FLOATS == 32, "a (pair, kind) record is one 128-byte line");
+
+struct MomRec {
+    int b;            // expansion centre R = b h
+    int regular;      // 1: the kind exists and shares no endpoint
+    float fl_hi, fl_lo;   // ZL factor |d_i . d_k| as a float pair (0 where the reference drops ZL)
+};
+
+// Warp per (pair, kind): the lanes share the tensor rule's points; each lane
+// accumulates all MOM_N moments of its points in FP64, then a butterfly sums
+// them. Lane n writes term n (head terms as hi, lo float pairs).
+__global__ void __launch_bounds__(128) k_moments(const double* __restrict__ elec, const double* __restrict__ img,
+                                                 int m, int has_img, float* __restrict__ mom,
+                                                 MomRec* __restrict__ rec) {
+    __shared__ double sx[GL_TOTAL], sw[GL_TOTAL];
+    for (int t = threadIdx.x; t < GL_TOTAL; t += blockDim.x) {
+        sx[t] = g_glx[t];
+        sw[t] = g_glw[t];
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long npk = (long long)m * (m + 1);              // (pair, kind) records
+    const long long pk = (long long)blockIdx.x * 4 + warp;
+    if (pk >= npk) return;                                      // whole warp leaves together
+    const long long p = pk >> 1;
+    const int kind = (int)(pk & 1);
+    int i, k;
+    pair_index(p, m, i, k);
+    Seg S, R;
+    ld_seg(elec + 11LL * i, S);
+    bool regular = (kind == 0 && k != i) || (kind == 1 && has_img);
+    if (regular) {
+        ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
+        regular = (classify_pair(S, R) & (PC_TOUCH | PC_DEGEN)) == 0;
+    }
+    float* out = mom + pk * MOM_FLOATS;
+    if (!regular) {
+        out[lane] = 0.f;
+        if (lane == 0) rec[pk] = MomRec{0, 0, 0.f, 0.f};
+        return;
+    }
+    double dm[3] = {R.mid[0] - S.mid[0], R.mid[1] - S.mid[1], R.mid[2] - S.mid[2]};
+    const double rc = sqrt(dot3(dm, dm));
+    const int b = (int)rint(rc / MOM_H);
+    const double Rb = b * MOM_H;
+    const double lmax = fmax(S.len, R.len);
+    const double ratio = seg_seg_dist(R.a, R.b, S.a, S.b) / lmax;
+    const int P = ratio >= 2.0 ? 1 : (int)fmin(32.0, ceil(2.0 / ratio));
+    const int q = min(QMAX, order_for(ratio * P, 0.0, true) + MOM_EXTRA);
+    const double* x = sx + gl_off(q);
+    const double* w = sw + gl_off(q);
+    double dr[3], ds[3];
+    for (int c = 0; c < 3; ++c) {
+        dr[c] = R.b[c] - R.a[c];
+        ds[c] = S.b[c] - S.a[c];
+    }
+    const double h = 1.0 / P;
+    double acc[MOM_N];
+#pragma unroll
+    for (int n = 0; n < MOM_N; ++n) acc[n] = 0.0;
+    const int qq = q * q, npts = P * P * qq;
+    for (int t = lane; t < npts; t += 32) {
+        const int pp = t / qq, u = t - pp * qq;
+        const int pi = pp / P, pj = pp - pi * P, qi = u / q, qj = u - qi * q;
+        const double t0 = (pi + x[qi]) * h, t1 = (pj + x[qj]) * h;
+        const double dx = (R.a[0] + t0 * dr[0]) - (S.a[0] + t1 * ds[0]);
+        const double dy = (R.a[1] + t0 * dr[1]) - (S.a[1] + t1 * ds[1]);
+        const double dz = (R.a[2] + t0 * dr[2]) - (S.a[2] + t1 * ds[2]);
+        const double r = sqrt(dx * dx + dy * dy + dz * dz);
+        const double d = r - Rb;
+        double v = w[qi] * w[qj] * h * h / r;
+#pragma unroll
+        for (int n = 0; n < MOM_N; ++n) {
+            acc[n] += v;
+            v *= d;
+        }
+    }
+#pragma unroll
+    for (int n = 0; n < MOM_N; ++n)
+        for (int o = 16; o > 0; o >>= 1) acc[n] += __shfl_xor_sync(0xffffffffu, acc[n], o);
+    double mine = 0.0;
+#pragma unroll
+    for (int n = 0; n < MOM_N; ++n)
+        if ((lane < 2 * MOM_HEAD ? lane >> 1 : lane - MOM_HEAD) == n) mine = acc[n];
+    if (lane < 2 * MOM_HEAD) {
+        const float hi = (float)mine;
+        out[lane] = (lane & 1) ? (float)(mine - (double)hi) : hi;
+    } else {
+        out[lane] = (float)mine;
+    }
+    if (lane == 0) {
+        double cost = fabs(dot3(ds, dr));
+        const bool keep = kind == 0 ? !(cost < TAGS_DBL_EPSILON) : (cost > TAGS_DBL_EPSILON);
+        if (!keep) cost = 0.0;
+        const float fh = (float)cost;
+        rec[pk] = MomRec{b, 1, fh, (float)(cost - (double)fh)};
+    }
+}
+
+// ---- two-float (float pair) arithmetic --------------------------------------------
+struct DF {
+    float h, l;
+};
+TAGS_HD DF df_of(double v) {
+    const float h = (float)v;
+    return DF{h, (float)(v - (double)h)};
+}
+// a * b, the head product exact (FMA), the cross terms added to the tail
+TAGS_D DF df_mul(DF a, DF b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, e);
+    e = fmaf(a.l, b.h, e);
+    return DF{p, e};
+}
+TAGS_D DF df_add(DF a, DF b) {
+    const float s = a.h + b.h;
+    const float z = s - a.h;
+    const float e = (a.h - (s - z)) + (b.h - z);
+    return DF{s, e + a.l + b.l};
+}
+TAGS_D DF df_neg(DF a) { return DF{-a.h, -a.l}; }
+TAGS_D DF df_norm(DF a) {
+    const float s = a.h + a.l;
+    return DF{s, a.l - (s - a.h)};
+}
+struct CDF {
+    DF re, im;
+};
+TAGS_D CDF cdf_mul(CDF a, CDF b) {
+    return CDF{df_norm(df_add(df_mul(a.re, b.re), df_neg(df_mul(a.im, b.im)))),
+               df_norm(df_add(df_mul(a.re, b.im), df_mul(a.im, b.re)))};
+}
+TAGS_D CDF cdf_add(CDF a, CDF b) { return CDF{df_add(a.re, b.re), df_add(a.im, b.im)}; }
+TAGS_HD CDF cdf_of(double2 v) { return CDF{df_of(v.x), df_of(v.y)}; }
+
+// Per-sample constants of the moment fill.
+struct MomCoef {
+    float a[MOM_HEAD][4];      // (-gamma)^n / n!, n < MOM_HEAD: re (hi, lo), im (hi, lo)
+    float2 g;                  // gamma (FP32), for the Horner tail
+    float2 a8;                 // (-gamma)^MOM_HEAD / MOM_HEAD! (FP32)
+    float cT[4], cTi[4], cL[4];   // scale factors (re hi, re lo, im hi, im lo); cLi = cL (ref_l = 1)
+    int nt;                    // terms this sample needs (<= MOM_N)
+    int ok;                    // 1: the series reaches 1e-14 within MOM_N terms
+};
+
+// Terms of the series for 1e-14 at x = |gamma| dmax: the first n with
+// x^n / n! <= 1e-14 e^{-x} (the sum is at least e^{-x} times its leading term's
+// scale), at least MOM_HEAD + 1.
+__global__ void k_mom_coef(const SampleCoef* __restrict__ coef, int nsamp, double dmax, MomCoef* __restrict__ out,
+                           int* __restrict__ ok) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nsamp) return;
+    const SampleCoef c = coef[q];
+    MomCoef o;
+    double2 an = make_double2(1.0, 0.0);
+    const double2 mg = make_double2(-c.gamma.x, -c.gamma.y);
+    for (int n = 0; n < MOM_HEAD; ++n) {
+        const DF r = df_of(an.x), im = df_of(an.y);
+        o.a[n][0] = r.h;
+        o.a[n][1] = r.l;
+        o.a[n][2] = im.h;
+        o.a[n][3] = im.l;
+        an = cscale(cmul(an, mg), 1.0 / (n + 1));
+    }
+    o.a8 = make_float2((float)an.x, (float)an.y);
+    o.g = make_float2((float)c.gamma.x, (float)c.gamma.y);
+    const double2 cc[3] = {c.cT, c.cTi, c.cL};
+    float* dst[3] = {o.cT, o.cTi, o.cL};
+    for (int j = 0; j < 3; ++j) {
+        const DF r = df_of(cc[j].x), im = df_of(cc[j].y);
+        dst[j][0] = r.h;
+        dst[j][1] = r.l;
+        dst[j][2] = im.h;
+        dst[j][3] = im.l;
+    }
+    const double xg = sqrt(cabs2(c.gamma)) * dmax;
+    double term = 1.0;
+    int nt = 0;
+    const double lim = 1e-14 * exp(-xg);
+    while (nt < 64 && !(term <= lim && nt > MOM_HEAD)) {
+        term *= xg / (nt + 1);
+        ++nt;
+    }
+    o.nt = nt;
+    o.ok = nt <= MOM_N ? 1 : 0;
+    out[q] = o;
+    ok[q] = o.ok;
+}
+
+// e^{-gamma b h} per bucket b and sample (FP64, stored as complex float pairs
+// [b][sample]).
+__global__ void k_mom_table(const SampleCoef* __restrict__ coef, int nsamp, int nb, int bstride,
+                            float4* __restrict__ tab) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (q >= nsamp || b >= nb) return;
+    const double2 g = coef[q].gamma;
+    const double2 e = cexp_d(make_double2(-g.x * b * MOM_H, -g.y * b * MOM_H));
+    const DF r = df_of(e.x), im = df_of(e.y);
+    tab[(long long)b * bstride + q] = make_float4(r.h, r.l, im.h, im.l);
+}
+
+// J of one (pair, kind) for this lane's sample from the staged record and
+// moments (shared memory, read by all lanes alike).
+TAGS_D CDF mom_series(const float* __restrict__ mv, int nt, const MomCoef& c) {
+    // tail: H = N_8 + (-gamma/9)(N_9 + (-gamma/10)(N_10 + ...)) by Horner in
+    // FP32 (a term of the tail is a_n N_n = a_8 (a_n / a_8) N_n), times a_8
+    float hr = 0.f, hi = 0.f;
+    for (int n = nt - 1; n >= MOM_HEAD; --n) {
+        const float f = -1.f / (float)(n + 1);
+        const float tr = f * (c.g.x * hr - c.g.y * hi), ti = f * (c.g.x * hi + c.g.y * hr);
+        hr = mv[2 * MOM_HEAD + n - MOM_HEAD] + tr;
+        hi = ti;
+    }
+    const float tr = c.a8.x * hr - c.a8.y * hi, ti = c.a8.x * hi + c.a8.y * hr;
+    DF sr{0.f, tr}, si{0.f, ti};
+#pragma unroll
+    for (int n = 0; n < MOM_HEAD; ++n) {
+        const DF N{mv[2 * n], mv[2 * n + 1]};
+        sr = df_add(sr, df_mul(DF{c.a[n][0], c.a[n][1]}, N));
+        si = df_add(si, df_mul(DF{c.a[n][2], c.a[n][3]}, N));
+    }
+    return CDF{df_norm(sr), df_norm(si)};
+}
+
+constexpr int MOM_WARPS = 4;
+struct MomWarpSmem {
+    float mv[2][MOM_FLOATS];                      // moments of the row's two kinds
+    MomRec rc[2];
+    float2 zl[FILL_SUB][33], zt[FILL_SUB][33];    // outputs hi, [row][sample]
+    float2 ll[FILL_SUB][33], lt[FILL_SUB][33];    // outputs lo
+};
+
+// Moment fill of the regular kinds, lower triangle, float pairs: Z gets hi,
+// Zlo gets lo. Warp per (column i, 32 rows, 32 samples) as k_fill_mixed;
+// samples whose series needs more than MOM_N terms are skipped (ok = 0) and
+// left to k_fill_mixed. The diagonal's self term and the touching kinds are
+// added afterwards by k_fill_special64.
+__global__ void __launch_bounds__(MOM_WARPS * 32) k_fill_moment(
+    int m, const float* __restrict__ mom, const MomRec* __restrict__ rec, const MomCoef* __restrict__ coef,
+    const float4* __restrict__ tab, int tstride, int nsamp, float2* zl0, float2* zt0, float2* zlo0, float2* ztlo0,
+    long long bstride, long long ntiles, int* status) {
+    __shared__ MomWarpSmem sw_all[MOM_WARPS];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    MomWarpSmem& W = sw_all[warp];
+    const long long tile = (long long)blockIdx.x * MOM_WARPS + warp;
+    if (tile >= ntiles) return;                      // whole warp leaves together
+    int kb, i;
+    fill_tile(tile, m, kb, i);
+    const int smp = blockIdx.y * 32 + lane;
+    bool valid = smp < nsamp;
+    MomCoef c{};
+    if (valid) c = coef[smp];
+    valid = valid && c.ok;
+    if (!__any_sync(0xffffffffu, valid)) return;
+    int ntw = valid ? c.nt : 0;
+    ntw = __reduce_max_sync(0xffffffffu, ntw);
+    const long long pstart = (long long)i * (2LL * m - i + 1) / 2;
+    const int k_lo = max(i, 32 * kb), k_hi = min(m, 32 * kb + 32);
+    const CDF cT{DF{c.cT[0], c.cT[1]}, DF{c.cT[2], c.cT[3]}};
+    const CDF cTi{DF{c.cTi[0], c.cTi[1]}, DF{c.cTi[2], c.cTi[3]}};
+    const CDF cL{DF{c.cL[0], c.cL[1]}, DF{c.cL[2], c.cL[3]}};
+    for (int k0 = k_lo; k0 < k_hi; k0 += FILL_SUB) {
+        const int kend = min(k_hi, k0 + FILL_SUB);
+        for (int k = k0; k < kend; ++k) {
+            const long long p = pstart + (k - i);
+            __syncwarp();
+            W.mv[0][lane] = mom[(2 * p) * MOM_FLOATS + lane];
+            W.mv[1][lane] = mom[(2 * p + 1) * MOM_FLOATS + lane];
+            if (lane < 2) W.rc[lane] = rec[2 * p + lane];
+            __syncwarp();
+            CDF zt{DF{0.f, 0.f}, DF{0.f, 0.f}}, zl = zt;
+#pragma unroll
+            for (int kind = 0; kind < 2; ++kind) {
+                const MomRec rc = W.rc[kind];
+                if (!rc.regular) continue;
+                const CDF S = mom_series(W.mv[kind], ntw, c);
+                const float4 t4 = valid ? tab[(long long)rc.b * tstride + smp] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const CDF J = cdf_mul(CDF{DF{t4.x, t4.y}, DF{t4.z, t4.w}}, S);
+                zt = cdf_add(zt, cdf_mul(kind == 0 ? cT : cTi, J));
+                const DF fl{rc.fl_hi, rc.fl_lo};
+                if (fl.h != 0.f) {
+                    const CDF lj = cdf_mul(cL, J);
+                    zl = cdf_add(zl, CDF{df_mul(lj.re, fl), df_mul(lj.im, fl)});
+                }
+            }
+            zl = CDF{df_norm(zl.re), df_norm(zl.im)};
+            zt = CDF{df_norm(zt.re), df_norm(zt.im)};
+            W.zl[k - k0][lane] = make_float2(zl.re.h, zl.im.h);
+            W.zt[k - k0][lane] = make_float2(zt.re.h, zt.im.h);
+            W.ll[k - k0][lane] = make_float2(zl.re.l, zl.im.l);
+            W.lt[k - k0][lane] = make_float2(zt.re.l, zt.im.l);
+        }
+        __syncwarp();
+        const int nrow = kend - k0;
+        for (int idx = lane; idx < FILL_SUB * 32; idx += 32) {
+            const int j = idx % FILL_SUB, sl = idx / FILL_SUB;
+            const int ss = blockIdx.y * 32 + sl;
+            const int ok_sl = __shfl_sync(0xffffffffu, valid ? 1 : 0, sl);     // every lane takes part
+            if (j < nrow && ss < nsamp && ok_sl) {
+                const float2 a = W.zl[j][sl], b = W.zt[j][sl];
+                if (!isfinite(a.x + a.y + b.x + b.y)) raise_status(status, TAGS_ST_NONFINITE);
+                const long long off = bstride * ss + (k0 + j) + (long long)m * i;
+                zl0[off] = a;
+                zt0[off] = b;
+                zlo0[off] = W.ll[j][sl];
+                ztlo0[off] = W.lt[j][sl];
+            }
+        }
+        __syncwarp();
+    }
 }
 
 __global__ void k_seg_dirs(const double* __restrict__ elec, const double* __restrict__ img, int m, int has_img,
@@ -948,32 +1294,90 @@ int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int 
 }
 
 int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
-                           int nsamp, float2* d_zl, float2* d_zt, long long bstride, int has_img,
-                           const SpecialEntries& sp, int* d_status, cudaStream_t st) {
+                           int nsamp, float2* d_zl, float2* d_zt, float2* d_zlo, float2* d_ztlo, long long bstride,
+                           int has_img, const SpecialEntries& sp, const MomentFill& mf, int* d_status,
+                           cudaStream_t st) {
     if (m <= 0 || nsamp <= 0) return 0;
-    if (nsamp > 4096) return tags_fail_cuda(cudaErrorInvalidValue, "fill_mixed: batch above 4096", __FILE__, __LINE__);
+    if (nsamp > 4096 || nsamp > mf.batch)
+        return tags_fail_cuda(cudaErrorInvalidValue, "fill_mixed: batch above capacity", __FILE__, __LINE__);
     MixedFillWs w = carve(ws, m);
     int pf = tags_prof_begin(TAGS_PROF_FILL_MIXED, st);
+    MomCoef* mc = reinterpret_cast<MomCoef*>(mf.coef);
+    k_mom_coef<<<(nsamp + 127) / 128, 128, 0, st>>>(d_coef, nsamp, mf.dmax, mc, mf.ok);
+    k_mom_table<<<dim3((nsamp + 127) / 128, mf.nb), 128, 0, st>>>(d_coef, nsamp, mf.nb, mf.batch, mf.tab);
     k_coef32<<<(nsamp + 127) / 128, 128, 0, st>>>(d_coef, nsamp, w.c32);
     const int KB = (m + 31) / 32;
     const long long ntiles = 16LL * (KB - 1) * KB + m;
-    dim3 grid((unsigned)((ntiles + FILL_WARPS - 1) / FILL_WARPS), (unsigned)((nsamp + 31) / 32));
-    k_fill_mixed<<<grid, FILL_WARPS * 32, 0, st>>>(d_elec, d_img, w.sdir, w.idir, m, w.codes, w.recs, w.c32,
-                                                   nsamp, d_zl, d_zt, bstride, has_img, ntiles, d_status);
+    dim3 grid((unsigned)((ntiles + MOM_WARPS - 1) / MOM_WARPS), (unsigned)((nsamp + 31) / 32));
+    k_fill_moment<<<grid, MOM_WARPS * 32, 0, st>>>(m, mf.mom, reinterpret_cast<const MomRec*>(mf.rec), mc, mf.tab,
+                                                   mf.batch, nsamp, d_zl, d_zt, d_zlo, d_ztlo, bstride, ntiles,
+                                                   d_status);
+    // samples the series does not reach: FP32 quadrature (warps with none leave at once)
+    dim3 gq((unsigned)((ntiles + FILL_WARPS - 1) / FILL_WARPS), (unsigned)((nsamp + 31) / 32));
+    k_fill_mixed<<<gq, FILL_WARPS * 32, 0, st>>>(d_elec, d_img, w.sdir, w.idir, m, w.codes, w.recs, w.c32, nsamp,
+                                                 d_zl, d_zt, bstride, has_img, ntiles, d_status, mf.ok, d_zlo,
+                                                 d_ztlo);
     dim3 gs((unsigned)((sp.n + SPEC_WARPS - 1) / SPEC_WARPS), (unsigned)((nsamp + 31) / 32));
-    k_fill_special64<<<gs, SPEC_WARPS * 32, 0, st>>>(d_elec, d_img, m, sp.ent, sp.n, d_coef, nsamp, d_zl, d_zt,
-                                                     bstride, sp.lo, d_status);
-    k_zmirror<<<dim3((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS)),
-                256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
+    k_fill_special64<<<gs, SPEC_WARPS * 32, 0, st>>>(d_elec, d_img, m, sp.ent, sp.n, d_coef, nsamp, d_zl, d_zt, d_zlo,
+                                                     d_ztlo, bstride, d_status);
+    const dim3 gm((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS));
+    k_zmirror<<<gm, 256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
+    k_zmirror<<<gm, 256, 0, st>>>(d_zlo, d_ztlo, bstride, m, 2 * nsamp);
     tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
-    tags_note_launch(4);
+    tags_note_launch(8);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
 }
 
+// Moments of every (pair, kind), once per plan, and the per-pass tables.
+int tags_moment_fill_build(const double* d_elec, const double* d_img, int m, int has_img, const double* h_elec,
+                           const double* h_img, int batch, MomentFill* mf, cudaStream_t st) {
+    tags_moment_fill_free(mf);
+    const long long npk = (long long)m * (m + 1);
+    // |r - R| <= (L_i + L_k) / 2 + h / 2 <= Lmax + h / 2; buckets up to the
+    // largest midpoint distance (bounding box of the midpoints and images)
+    double lmax = 0.0, lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int e = 0; e < m; ++e) {
+        lmax = fmax(lmax, h_elec[11 * e + 9]);
+        for (int c = 0; c < 3; ++c) {
+            const double v = h_elec[11 * e + 6 + c];
+            lo[c] = fmin(lo[c], v);
+            hi[c] = fmax(hi[c], v);
+            if (has_img) {
+                const double u = h_img[11 * e + 6 + c];
+                lo[c] = fmin(lo[c], u);
+                hi[c] = fmax(hi[c], u);
+            }
+        }
+    }
+    const double diag = sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                             (hi[2] - lo[2]) * (hi[2] - lo[2]));
+    mf->dmax = lmax + 0.5 * MOM_H;
+    mf->nb = (int)ceil(diag / MOM_H) + 2;
+    mf->batch = batch;
+    TAGS_CUDA_OK(cudaMalloc(&mf->mom, sizeof(float) * MOM_FLOATS * npk));
+    TAGS_CUDA_OK(cudaMalloc(&mf->rec, sizeof(MomRec) * npk));
+    TAGS_CUDA_OK(cudaMalloc(&mf->coef, sizeof(MomCoef) * batch));
+    TAGS_CUDA_OK(cudaMalloc(&mf->ok, sizeof(int) * batch));
+    TAGS_CUDA_OK(cudaMalloc(&mf->tab, sizeof(float4) * (size_t)mf->nb * batch));
+    k_moments<<<(unsigned)((npk + 3) / 4), 128, 0, st>>>(d_elec, d_img, m, has_img, mf->mom,
+                                                          reinterpret_cast<MomRec*>(mf->rec));
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    return 0;
+}
+
+void tags_moment_fill_free(MomentFill* mf) {
+    void* ptrs[] = {mf->mom, mf->rec, mf->coef, mf->ok, mf->tab};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    *mf = MomentFill{};
+}
+
 // The special entries from the pair plan's list of pairs with a touching (or
 // degenerate) kind, plus every diagonal entry; sorted by pair index, so the
-// list and each row's entries come out in the same order on every build.
+// list comes out in the same order on every build.
 int tags_mixed_special_build(void* ws, int m, int batch, SpecialEntries* sp, cudaStream_t st) {
     MixedFillWs w = carve(ws, m);
     int nt = 0;
@@ -990,40 +1394,17 @@ int tags_mixed_special_build(void* ws, int m, int batch, SpecialEntries* sp, cud
     const int n = (int)kinds.size();
     std::vector<int2> ent;
     ent.reserve(n);
-    std::vector<std::vector<int2>> rows(m);
-    int i = 0;                   // column of pair p (pairs ascend, so columns do)
-    for (const auto& kv : kinds) {
-        const long long p = kv.first;
-        // column i, row k of pair p (the enumeration of pair_index)
-        while (i < m - 1 && (long long)(i + 1) * (2LL * m - i) / 2 <= p) ++i;
-        const int k = i + (int)(p - (long long)i * (2LL * m - i + 1) / 2);
-        const int e = (int)ent.size();
-        ent.push_back(make_int2((int)p, kv.second));
-        rows[k].push_back(make_int2(i, e));
-        if (k != i) rows[i].push_back(make_int2(k, e));
-    }
-    std::vector<int> row_ptr(m + 1, 0);
-    std::vector<int2> row_ent;
-    for (int k = 0; k < m; ++k) {
-        row_ptr[k] = (int)row_ent.size();
-        row_ent.insert(row_ent.end(), rows[k].begin(), rows[k].end());
-    }
-    row_ptr[m] = (int)row_ent.size();
+    for (const auto& kv : kinds) ent.push_back(make_int2((int)kv.first, kv.second));
     tags_mixed_special_free(sp);
     TAGS_CUDA_OK(cudaMalloc(&sp->ent, sizeof(int2) * n));
-    TAGS_CUDA_OK(cudaMalloc(&sp->row_ptr, sizeof(int) * (m + 1)));
-    TAGS_CUDA_OK(cudaMalloc(&sp->row_ent, sizeof(int2) * row_ent.size()));
-    TAGS_CUDA_OK(cudaMalloc(&sp->lo, sizeof(float4) * (size_t)n * batch));
     TAGS_CUDA_OK(cudaMemcpy(sp->ent, ent.data(), sizeof(int2) * n, cudaMemcpyHostToDevice));
-    TAGS_CUDA_OK(cudaMemcpy(sp->row_ptr, row_ptr.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
-    TAGS_CUDA_OK(cudaMemcpy(sp->row_ent, row_ent.data(), sizeof(int2) * row_ent.size(), cudaMemcpyHostToDevice));
-    TAGS_CUDA_OK(cudaMemset(sp->lo, 0, sizeof(float4) * (size_t)n * batch));
     sp->n = n;
+    (void)batch;
     return 0;
 }
 
 void tags_mixed_special_free(SpecialEntries* sp) {
-    void* ptrs[] = {sp->ent, sp->row_ptr, sp->row_ent, sp->lo};
+    void* ptrs[] = {sp->ent};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     *sp = SpecialEntries{};

@@ -5,10 +5,11 @@
 //           [ A  -ZL   0   ]
 //           [ B   0   -ZT  ]
 // solved here as follows:
-//   0. impedance blocks: regular pairs in FP32 (anchors from two-float
-//      products), pairs sharing an endpoint (log-singular) in FP64, the
-//      diagonal in its closed form; stored as complex FP32, which is the
-//      matrix the refinement solves (its entries carry the fill's ~1e-7 error);
+//   0. impedance blocks as float pairs (hi in Z, lo in Zlo), good to ~1e-13:
+//      regular pairs from the moment expansion (FP64 geometry moments, series
+//      in float pairs), pairs sharing an endpoint (log-singular) and the
+//      diagonal's closed form in FP64 per sample; the refinement solves this
+//      matrix, the factorisation uses its FP32 high parts;
 //   1. static symmetric ordering P: ZL rows, ZT rows, then node rows, so that
 //      the elimination meets the impedance blocks (large diagonals) before the
 //      zero Y_E block and needs no pivot search;
@@ -18,8 +19,8 @@
 //   4. iterative refinement: x in FP64, r = b - W x with the exact incidence
 //      (sparse, +-1 / 0.5) in FP64 and the impedance blocks times x in
 //      two-float arithmetic (about 2^-44 relative), the correction from the
-//      FP32 factors; a sample stops once the correction is below 1e-9 |x|
-//      or stops shrinking. The stopping decision runs on the device
+//      FP32 factors; a sample stops once its predicted error is below the
+//      tolerance (1e-9 |x|) or its corrections stop shrinking. The stopping decision runs on the device
 //      (k_ir_decide), so one refinement step is a fixed launch sequence that a
 //      CUDA graph repeats under a conditional while-node;
 //   5. samples that do not converge are re-solved by the plain FP64 path
@@ -242,15 +243,14 @@ TAGS_D F2 f2_mac(F2 a, float z, float xh, float xl) {
 // x is split into float pairs), so its result is accurate to ~2^-44 of
 // |Z| |x| without FP64 arithmetic in the m^2 loop.
 constexpr int RES_CHUNK = 1024;
-// Rows with FP64 entries (touching pairs, diagonal; SpecialEntries) add their
-// rounding residues lo times x in FP64, so the residual is that of the FP64
-// values there (row_ptr null: no such entries, as for the mHEM fill).
-__global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z, const Incidence inc, int m, int n,
+// Zlo (may be null, as for the mHEM fill): the low parts of the entries, which
+// are float pairs (hi in Z): their products with x's high parts go into the
+// low accumulator, so the residual is that of the float-pair values.
+__global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z, const float2* __restrict__ Zlo,
+                                                    const Incidence inc, int m, int n,
                                                     const double2* __restrict__ bvec, const double2* __restrict__ x,
                                                     double2* __restrict__ r, double* __restrict__ norms,
-                                                    const int* __restrict__ active, const int* __restrict__ row_ptr,
-                                                    const int2* __restrict__ row_ent, const float4* __restrict__ lo,
-                                                    int nspec) {
+                                                    const int* __restrict__ active) {
     __shared__ float4 xs[RES_CHUNK];        // re_hi, re_lo, im_hi, im_lo
     const int N = n + 2 * m;
     const int blk = blockIdx.y & 1, b = blockIdx.y >> 1;
@@ -258,6 +258,7 @@ __global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     const double2* xb = x + (size_t)b * N;
     const float2* Zb = Z + (size_t)b * 2 * m * m + (size_t)blk * m * m;
+    const float2* Lb = Zlo ? Zlo + (size_t)b * 2 * m * m + (size_t)blk * m * m : nullptr;
     F2 ar{0.f, 0.f}, ai{0.f, 0.f};
     for (int j0 = 0; j0 < m; j0 += RES_CHUNK) {
         const int nj = min(RES_CHUNK, m - j0);
@@ -271,6 +272,38 @@ __global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z
         if (k < m) {
             const float2* zc = Zb + k + (size_t)m * j0;
             int j = 0;
+            if (Lb) {
+                const float2* lc = Lb + k + (size_t)m * j0;
+                for (; j + 8 <= nj; j += 8) {
+                    float2 z[8], l[8];                     // sixteen loads in flight
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        z[q] = zc[(size_t)m * (j + q)];
+                        l[q] = lc[(size_t)m * (j + q)];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const float4 xv = xs[j + q];
+                        ar = f2_mac(ar, z[q].x, xv.x, xv.y);
+                        ar = f2_mac(ar, -z[q].y, xv.z, xv.w);
+                        ai = f2_mac(ai, z[q].x, xv.z, xv.w);
+                        ai = f2_mac(ai, z[q].y, xv.x, xv.y);
+                        // low parts (|lo| <= 2^-24 |hi|): FP32 products into the low sums
+                        ar.lo = fmaf(l[q].x, xv.x, fmaf(-l[q].y, xv.z, ar.lo));
+                        ai.lo = fmaf(l[q].x, xv.z, fmaf(l[q].y, xv.x, ai.lo));
+                    }
+                }
+                for (; j < nj; ++j) {
+                    const float2 z = zc[(size_t)m * j], l = lc[(size_t)m * j];
+                    const float4 xv = xs[j];
+                    ar = f2_mac(ar, z.x, xv.x, xv.y);
+                    ar = f2_mac(ar, -z.y, xv.z, xv.w);
+                    ai = f2_mac(ai, z.x, xv.z, xv.w);
+                    ai = f2_mac(ai, z.y, xv.x, xv.y);
+                    ar.lo = fmaf(l.x, xv.x, fmaf(-l.y, xv.z, ar.lo));
+                    ai.lo = fmaf(l.x, xv.z, fmaf(l.y, xv.x, ai.lo));
+                }
+            }
             for (; j + 8 <= nj; j += 8) {
                 float2 z[8];                               // eight loads in flight
 #pragma unroll
@@ -306,17 +339,6 @@ __global__ void __launch_bounds__(128) k_residual_z(const float2* __restrict__ Z
     }
     acc.x -= (double)ar.hi + (double)ar.lo;
     acc.y -= (double)ai.hi + (double)ai.lo;
-    if (row_ptr) {
-        const float4* lb = lo + (size_t)b * nspec;
-        for (int q = row_ptr[k]; q < row_ptr[k + 1]; ++q) {
-            const int2 ce = row_ent[q];
-            const float4 l4 = lb[ce.y];
-            const double lr = blk == 0 ? l4.x : l4.z, li = blk == 0 ? l4.y : l4.w;
-            const double2 xv = xb[n + blk * m + ce.x];
-            acc.x -= lr * xv.x - li * xv.y;
-            acc.y -= lr * xv.y + li * xv.x;
-        }
-    }
     double2 rv = csub(bvec[(size_t)b * N + row], acc);
     r[(size_t)b * N + row] = rv;
     atomic_max_nonneg(norms + 4 * b + 2, fabs(rv.x) + fabs(rv.y));
@@ -355,9 +377,13 @@ struct IrState {
 // an extrapolated step, minus the slow mode's |lambda|. The error left after
 // this correction is about rho dx for the measured contraction rho = dx / pdx
 // (rho <= 1/4), or the mode's tail |lambda| / (1 - |lambda|) dx; stop when four
-// times that is below tol |x| (default 1e-8, a decade under the FP32 fill's
-// own error), or when the correction itself is below tol / 10 |x|. Step 0
-// starts from x = 0 (dx_0 = |x_0|), so it never stops on the estimate.
+// times that is below tol |x| (default 1e-9: the residual sees the impedance
+// entries as float pairs good to ~1e-13, so what refinement leaves is the
+// solution's error against FP64; the inverse Laplace transform amplifies
+// sample-to-sample errors by up to e^{c t}; with the fp16-pair factors'
+// contraction of ~1e-5, two steps already predict ~4e-10), or when the
+// correction itself is below tol / 10 |x|. Step 0 starts from x = 0 (dx_0 = |x_0|), so it never
+// stops on the estimate.
 TAGS_D bool ir_converged(int step, double dx, double xn, double pdx, double tol) {
     if (dx <= 0.1 * tol * xn) return true;
     if (step >= 1 && pdx > 0.0) {
@@ -450,12 +476,10 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
     s.extr[q] = -10;
 }
 
-// After a refinement step: per sample, stop once the correction is below
-// 1e-9 |x|, or once the correction times the measured contraction predicts an
-// error under 1e-8 |x| (each step contracts the error by about kappa *
-// eps_factor, a few 1e-3 here; the FP32 impedance fill itself is good to
-// ~1e-7), or once it stops shrinking (accepted when the backward error is
-// below 1e-12); NaN goes to the fallback. One CTA. Sets the continue
+// After a refinement step: per sample, stop on ir_converged (the correction
+// times the measured contraction predicts an error under the tolerance), or
+// once it stops shrinking (accepted when the backward error is below 1e-12);
+// NaN goes to the fallback. One CTA. Sets the continue
 // flag and, inside a graph, the while-node condition.
 __global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ norms, int nb, int max_steps, IrState s,
                                                     cudaGraphConditionalHandle cond, int set_cond) {
@@ -505,6 +529,12 @@ int tags_mixed_alloc(tags_plan_s* p) {
     if (err) return err;
     err = tags_mixed_special_build(p->d_fillws, p->m, (int)b, &p->spec, p->stream);
     if (err) return err;
+    err = tags_moment_fill_build(p->d_elec, p->has_images ? p->d_img : p->d_elec, p->m, p->has_images,
+                                 p->h_elec.data(), p->has_images ? p->h_img.data() : p->h_elec.data(), (int)b, &p->mom,
+                                 p->stream);
+    if (err) return err;
+    TAGS_CUDA_OK(cudaMalloc(&p->d_Zlo, sizeof(float2) * 2 * m * m * b));
+    TAGS_CUDA_OK(cudaMemset(p->d_Zlo, 0, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_A, sizeof(float2) * N * N * b));
     // scale + row sums (FP64), then an FP32 copy of the scale
@@ -531,6 +561,9 @@ int tags_mixed_free(tags_plan_s* p) {
     for (void* q : ptrs)
         if (q) cudaFree(q);
     tags_mixed_special_free(&p->spec);
+    tags_moment_fill_free(&p->mom);
+    if (p->d_Zlo) cudaFree(p->d_Zlo);
+    p->d_Zlo = nullptr;
     p->d_Z = nullptr;
     p->d_A = nullptr;
     p->d_yprev = nullptr;
@@ -608,8 +641,8 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
                   ? tags_launch_mhem_mixed(m, p->has_images, p->d_pot, p->d_fillws, p->d_coef, nb, p->d_Z,
                                            p->d_Z + (size_t)m * m, 2LL * m * m, p->d_status, st)
                   : tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z,
-                                           p->d_Z + (size_t)m * m, 2LL * m * m, p->has_images, p->spec,
-                                           p->d_status, st);
+                                           p->d_Z + (size_t)m * m, p->d_Zlo, p->d_Zlo + (size_t)m * m, 2LL * m * m,
+                                           p->has_images, p->spec, p->mom, p->d_status, st);
     if (err) return err;
     // 2. scaling
     float* d_scalef = reinterpret_cast<float*>(p->d_scale + 2 * (size_t)p->batch * N);
@@ -661,10 +694,9 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
     k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);
-    const bool spec = p->fill_model != TAGS_INTG_MHEM && p->spec.n > 0;
-    k_residual_z<<<dim3((m + 127) / 128, 2 * nb), 128, 0, st>>>(p->d_Z, p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
-                                                                s.active, spec ? p->spec.row_ptr : nullptr,
-                                                                p->spec.row_ent, p->spec.lo, p->spec.n);
+    const float2* zlo = p->fill_model == TAGS_INTG_MHEM ? nullptr : p->d_Zlo;
+    k_residual_z<<<dim3((m + 127) / 128, 2 * nb), 128, 0, st>>>(p->d_Z, zlo, p->inc, m, n, d_b, p->d_x, p->d_r,
+                                                                p->d_norms, s.active);
     // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
     tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
     k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, std::min(p->max_steps, kMaxSteps), s, cond, set_cond);
@@ -736,42 +768,24 @@ extern "C" int tags_debug_mixed_fill(tags_plan plan, const tags_cdouble* s, cons
     int err = tags_plan_coef(p, p->d_sin, p->d_sin + p->batch, mur, nb, st);
     if (!err)
         err = tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z, p->d_Z + (size_t)m * m,
-                                     2LL * m * m, p->has_images, p->spec, p->d_status, st);
+                                     p->d_Zlo, p->d_Zlo + (size_t)m * m, 2LL * m * m, p->has_images, p->spec, p->mom,
+                                     p->d_status, st);
     if (err) return err;
-    std::vector<float2> z((size_t)2 * m * m * nb);
-    std::vector<float4> lo((size_t)p->spec.n * nb);
-    std::vector<int2> ent(p->spec.n);
+    const size_t mm = (size_t)m * m;
+    std::vector<float2> z(2 * mm * nb), lo(2 * mm * nb);
     TAGS_CUDA_OK(cudaMemcpyAsync(z.data(), p->d_Z, sizeof(float2) * z.size(), cudaMemcpyDeviceToHost, st));
-    TAGS_CUDA_OK(cudaMemcpyAsync(lo.data(), p->spec.lo, sizeof(float4) * lo.size(), cudaMemcpyDeviceToHost, st));
-    TAGS_CUDA_OK(cudaMemcpyAsync(ent.data(), p->spec.ent, sizeof(int2) * ent.size(), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(lo.data(), p->d_Zlo, sizeof(float2) * lo.size(), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaStreamSynchronize(st));
     double* ol = reinterpret_cast<double*>(zl);
     double* ot = reinterpret_cast<double*>(zt);
-    const size_t mm = (size_t)m * m;
     for (int b = 0; b < nb; ++b)
         for (size_t e = 0; e < mm; ++e) {
-            const float2 a = z[(size_t)b * 2 * mm + e], c = z[(size_t)b * 2 * mm + mm + e];
-            ol[2 * (b * mm + e)] = a.x;
-            ol[2 * (b * mm + e) + 1] = a.y;
-            ot[2 * (b * mm + e)] = c.x;
-            ot[2 * (b * mm + e) + 1] = c.y;
+            const size_t a = (size_t)b * 2 * mm + e, c = a + mm, o = (size_t)b * mm + e;
+            ol[2 * o] = (double)z[a].x + (double)lo[a].x;
+            ol[2 * o + 1] = (double)z[a].y + (double)lo[a].y;
+            ot[2 * o] = (double)z[c].x + (double)lo[c].x;
+            ot[2 * o + 1] = (double)z[c].y + (double)lo[c].y;
         }
-    int i = 0;
-    for (int e = 0; e < p->spec.n; ++e) {
-        const long long pp = ent[e].x;
-        while (i < m - 1 && (long long)(i + 1) * (2LL * m - i) / 2 <= pp) ++i;
-        const int k = i + (int)(pp - (long long)i * (2LL * m - i + 1) / 2);
-        for (int b = 0; b < nb; ++b) {
-            const float4 l = lo[(size_t)b * p->spec.n + e];
-            const size_t pos[2] = {b * mm + k + (size_t)m * i, b * mm + i + (size_t)m * k};
-            for (int t = 0; t < (k == i ? 1 : 2); ++t) {
-                ol[2 * pos[t]] += l.x;
-                ol[2 * pos[t] + 1] += l.y;
-                ot[2 * pos[t]] += l.z;
-                ot[2 * pos[t] + 1] += l.w;
-            }
-        }
-    }
     return 0;
 }
 

@@ -426,7 +426,7 @@ extern "C" int tags_plan_set_split(tags_plan plan, int pieces) {
 extern "C" int tags_plan_set_refine_tol(tags_plan plan, double tol) {
     if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_refine_tol: invalid plan");
     if (!(tol >= 0.0) || tol > 1e-3) return tags_fail(TAGS_E_ARG, "tags_plan_set_refine_tol: tol must be 0 .. 1e-3");
-    const double v = tol == 0.0 ? 1e-8 : tol;
+    const double v = tol == 0.0 ? 1e-9 : tol;
     if (plan->ir_tol != v) {
         plan->ir_tol = v;
         tags_plan_drop_graphs(plan);     // the tolerance is an argument of the captured refinement kernels

@@ -66,7 +66,9 @@ struct tags_plan_s {
     double* d_dots = nullptr;       // batch x 4 sums of the current against the previous correction
     void* d_fillws = nullptr;       // pair classes and geometry records of the mixed fill
     int n_touch = 0;                // pairs sharing an endpoint (FP64 Duffy rule)
-    SpecialEntries spec;            // entries filled in FP64 (touching pairs, diagonal) and their residues
+    SpecialEntries spec;            // entries filled in FP64 per sample (touching pairs, diagonal)
+    MomentFill mom;                 // moment expansion of the regular pairs (geometry moments, per-pass tables)
+    float2* d_Zlo = nullptr;        // batch x 2 x m x m: low parts of ZL, ZT (Z holds the high parts)
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
     int split_pieces = TAGS_SPLIT_F16;   // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)
@@ -75,7 +77,7 @@ struct tags_plan_s {
     SampleCoef* d_coef1 = nullptr;  // unit coefficients for the potentials
     int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
     int max_steps = 40;             // refinement steps per pass before the FP64 fallback (1 .. 40)
-    double ir_tol = 1e-8;           // refinement stopping tolerance (relative error left in x)
+    double ir_tol = 1e-9;           // refinement stopping tolerance (relative error left in x)
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue,
                                     // step of the last extrapolation (batch)

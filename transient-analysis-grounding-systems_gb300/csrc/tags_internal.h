@@ -49,23 +49,38 @@ int tags_launch_mhem_mixed(int m, int has_img, const double2* d_pot, void* ws, c
 size_t tags_mixed_fill_workspace(int m);
 int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int has_img, void* ws, cudaStream_t st);
 int tags_mixed_touch_count(void* ws, int m, cudaStream_t st, int* out);
-// The entries of ZL/ZT the mixed fill computes in FP64: pairs with a kind
-// (direct or image) that shares an endpoint (log-singular) and the diagonal
-// (the self term). Their FP64 value v is stored as hi = fl(v) in the FP32
-// matrices and lo = fl(v - hi) here, so the FP64 residual of the refinement
-// sees v to ~2^-48 while the factorisation uses hi.
+// The entries of ZL/ZT the mixed fill computes in FP64 per sample: pairs with
+// a kind (direct or image) that shares an endpoint (log-singular) and the
+// diagonal (the self term), added to the regular kinds' value in FP64 and
+// stored as a float pair (hi in Z, lo in Zlo).
 struct SpecialEntries {
     int n = 0;                   // entries
     int2* ent = nullptr;         // (pair index p of (k, i), k >= i; kinds mask: bit 0 direct, 1 image, 2 self)
-    int* row_ptr = nullptr;      // m + 1: entries of row k at row_ent[row_ptr[k] .. row_ptr[k + 1])
-    int2* row_ent = nullptr;     // (column, entry) of each row's entries (both triangles)
-    float4* lo = nullptr;        // [sample][entry]: rounding residues (ZL re, ZL im, ZT re, ZT im)
 };
 int tags_mixed_special_build(void* ws, int m, int batch, SpecialEntries* sp, cudaStream_t st);
 void tags_mixed_special_free(SpecialEntries* sp);
+// The moment expansion of the regular kinds (fill.cu): moments of every
+// (pair, kind) once per plan; per pass the samples' constants and the table
+// e^{-gamma b h} of the expansion centres.
+struct MomentFill {
+    float* mom = nullptr;        // (pair, kind) moments, 32 floats each
+    void* rec = nullptr;         // (pair, kind) records
+    void* coef = nullptr;        // per-sample constants, batch
+    int* ok = nullptr;           // per sample: 1 where the series reaches FP64 accuracy (else the FP32 quadrature)
+    float4* tab = nullptr;       // e^{-gamma b h}: [bucket][sample], complex float pairs
+    int nb = 0;                  // buckets
+    double dmax = 0.0;           // bound of |r - R| over the pairs (m)
+    int batch = 0;
+};
+int tags_moment_fill_build(const double* d_elec, const double* d_img, int m, int has_img, const double* h_elec,
+                           const double* h_img, int batch, MomentFill* mf, cudaStream_t st);
+void tags_moment_fill_free(MomentFill* mf);
+// The mixed fill of a pass: ZL, ZT as float pairs (hi in d_zl / d_zt, lo in
+// d_zlo / d_ztlo), full symmetric.
 int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
-                           int nsamp, float2* d_zl, float2* d_zt, long long bstride, int has_img,
-                           const SpecialEntries& sp, int* d_status, cudaStream_t st);
+                           int nsamp, float2* d_zl, float2* d_zt, float2* d_zlo, float2* d_ztlo, long long bstride,
+                           int has_img, const SpecialEntries& sp, const MomentFill& mf, int* d_status,
+                           cudaStream_t st);
 int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, const SampleCoef* d_coef,
                           int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
                           cudaStream_t st);
