@@ -737,6 +737,8 @@ def main():
     ap.add_argument("--no-graphs", action="store_true", help="launch kernel by kernel in the measured pass")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the all-sample GPR check against plain FP64")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 sub-record")
+    ap.add_argument("--tc-pairs", type=int, default=-1,
+                    help="trailing updates on two-SM clusters: 1 on, 0 off (-1 = the plan's default)")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     ap.add_argument("--first-batch", type=int, default=0,
@@ -773,6 +775,8 @@ def main():
     plan = pkg.Plan(elec, img, nodes, pkg.MIXED if mixed else pkg.PLAIN_FP64, max_batch=B)
     if mixed and args.split:
         plan.set_split(args.split)
+    if mixed and args.tc_pairs >= 0:
+        plan.set_tc_pairs(args.tc_pairs)
     if P > 1:
         plan.set_pipelines(P)
     ns_total = len(s)

@@ -420,6 +420,17 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
  * refinement steps. */
 int tags_plan_set_refine_tol (tags_plan plan, double tol);
 
+/* No counterpart in the reference. 1: the mixed form's trailing updates run
+ * on clusters of two SMs (tcgen05.mma.cta_group::2, 256 x 128 products, each
+ * SM staging its own 128 rows of A and half of B); 0 (default): one SM per
+ * 128 x 128 tile. Where the device cannot host such clusters the single-SM
+ * kernel runs. */
+int tags_plan_set_tc_pairs (tags_plan plan, int on);
+
+/* No counterpart in the reference. The same switch for the diagnostic entry
+ * points tags_debug_ldl and tags_debug_ldl_solve (process-wide). */
+int tags_debug_tc_pairs (int on);
+
 /* No counterpart in the reference. Caps the refinement steps of the mixed
  * form's passes (1 .. 40; 0 restores the default 40). A sample that has not
  * met its stopping rule after that many steps is re-solved by the plain FP64

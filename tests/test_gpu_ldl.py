@@ -1,6 +1,6 @@
 """GPU checks of the mixed form's tensor-core LDL^T (tcgen05 GEMMs on split
-products: bf16 pieces or scaled fp16 pairs, FP32 storage) through its
-diagnostic entry point."""
+products: bf16 pieces or scaled fp16 pairs, FP32 storage; trailing updates on
+one SM per tile or on two-SM clusters) through its diagnostic entry points."""
 import ctypes
 
 import numpy as np
@@ -16,25 +16,29 @@ def _sym_matrix(rng, N, dominance):
     return a
 
 
-def _ldl(pkg, mats, pieces=3):
+def _ldl(pkg, mats, pieces=3, pairs=False):
+    pkg.lib().tags_debug_tc_pairs(1 if pairs else 0)
     fn = pkg.lib().tags_debug_ldl
     fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     fn.restype = ctypes.c_int
     nb, N = mats.shape[0], mats.shape[1]
     buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)   # column-major
     code = fn(buf.ctypes.data, N, nb, pieces)
+    pkg.lib().tags_debug_tc_pairs(0)
     return code, np.transpose(buf, (0, 2, 1))
 
 
+@pytest.mark.parametrize("pairs", [False, True])
 @pytest.mark.parametrize("pieces,tol", [(2, 2e-5), (3, 2e-6), (16, 4e-6)])
 @pytest.mark.parametrize("N", [128, 300, 517])
-def test_tensor_core_ldl_reconstructs(gpu_pkg, N, pieces, tol):
+def test_tensor_core_ldl_reconstructs(gpu_pkg, N, pieces, tol, pairs):
     """L D L^T reproduces A to the accuracy of the split products: ~1e-5 with
     two bf16 pieces per value (three products), FP32 level with three (six),
-    near FP32 level with two fp16 pieces of 2^8 x (three products)."""
+    near FP32 level with two fp16 pieces of 2^8 x (three products); the
+    trailing updates on one SM per tile or on two-SM clusters (pairs)."""
     rng = np.random.default_rng(N)
     mats = np.stack([_sym_matrix(rng, N, 4.0), _sym_matrix(rng, N, 2.0), _sym_matrix(rng, N, 3.0)])
-    code, fac = _ldl(gpu_pkg, mats, pieces)
+    code, fac = _ldl(gpu_pkg, mats, pieces, pairs)
     assert code == 0, gpu_pkg.last_error()
     for q in range(3):
         L = np.tril(fac[q], -1) + np.eye(N)
@@ -84,9 +88,10 @@ def _banded_sym(rng, N, zl_m, dominance):
     return a
 
 
+@pytest.mark.parametrize("pairs", [False, True])
 @pytest.mark.parametrize("pieces,group", [(3, 4), (16, 4), (16, 2), (16, 1)])
 @pytest.mark.parametrize("N,zl_m", [(300, 0), (517, 0), (700, 150), (1000, 300), (1500, 400)])
-def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group):
+def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group, pairs):
     """One solve with the tensor-core factors (block-inverse sweeps, the
     diagonal, the zero ZL/ZT band skipped when zl_m > 0; 4, 2 or 1 panels per
     trailing update) against numpy's solve of the same matrices: FP32-level
@@ -100,7 +105,11 @@ def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group):
     rhs = rng.standard_normal((2, N)) + 1j * rng.standard_normal((2, N))
     buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)
     x = rhs.copy()
-    code = fn(buf.ctypes.data, x.ctypes.data, N, 2, pieces, zl_m, group)
+    gpu_pkg.lib().tags_debug_tc_pairs(1 if pairs else 0)
+    try:
+        code = fn(buf.ctypes.data, x.ctypes.data, N, 2, pieces, zl_m, group)
+    finally:
+        gpu_pkg.lib().tags_debug_tc_pairs(0)
     assert code == 0, gpu_pkg.last_error()
     for q in range(2):
         ref = np.linalg.solve(mats[q], rhs[q])

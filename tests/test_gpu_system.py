@@ -271,3 +271,31 @@ def test_two_pipelines_match_one(gpu_pkg, graphs):
     assert np.max(np.abs(two - one)) <= 1e-12 * np.max(np.abs(one))
     assert np.max(np.abs(three[:, 0] - gd["u0"][idx]) / np.abs(gd["u0"][idx])) < 1e-6
     assert st2.seconds > 0
+
+
+def test_two_sm_updates_match_single_sm(gpu_pkg):
+    """The trailing updates on two-SM clusters (tcgen05 cta_group::2, 256 x
+    128 products) give the single-SM results: config 2 grid, 40 samples, and
+    two samples of the 60 x 60 m grid (N = 4537)."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    idx = np.linspace(0, len(gd["s"]) - 1, 40).astype(int)
+    cases = [(e, nodes, gd["s"][idx], gd["kappa"][idx], 0)]
+    e4, n4 = pkg.electrode_grid(13, 13, 60.0, 60.0, 5, 5, 7e-3, -0.5)
+    c = np.log(4094.0 ** 2) / 204.7e-6
+    s4 = np.array([c + 2j * np.pi * 2e4, c + 2j * np.pi * 7e6])
+    k4 = np.array([1e-3 + sk * 12 * pkg.EPS0 for sk in s4])
+    cases.append((e4, n4, s4, k4, int(np.argmin(np.linalg.norm(n4 - [30.0, 30.0, -0.5], axis=1)))))
+    for elec, nd, s, kappa, inj in cases:
+        out = []
+        for pairs in (False, True):
+            plan = pkg.Plan(elec, pkg.images(elec), nd, pkg.MIXED, max_batch=len(s))
+            try:
+                plan.set_tc_pairs(pairs)
+                sol, info, st = plan.run(s, kappa, 1.0, None, inj)
+            finally:
+                plan.close()
+            assert np.all(info == 0) and st.fallbacks == 0
+            out.append(sol)
+        assert rel_err(out[1], out[0]) < 1e-12

@@ -57,7 +57,8 @@ EXPORTS = (
     "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
-    "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol",
+    "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
+    "tags_debug_tc_pairs",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
     "tags_gpu_inlt", "tags_batch_create", "tags_batch_run", "tags_batch_destroy",
@@ -148,6 +149,8 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_fill.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_max_steps.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_refine_tol.argtypes = [_vp, ctypes.c_double]
+            L.tags_plan_set_tc_pairs.argtypes = [_vp, ctypes.c_int]
+            L.tags_debug_tc_pairs.argtypes = [ctypes.c_int]
             L.tags_debug_tc_wait_limit.argtypes = [ctypes.c_longlong]
             L.tags_debug_mixed_fill.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _vp]
             L.tags_inv_laplace_batch.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int, ctypes.c_int]
@@ -180,8 +183,9 @@ def lib() -> ctypes.CDLL:
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
                          "tags_plan_set_pipelines",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
-                         "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_debug_mixed_fill",
-                         "tags_plan_set_refine_tol",
+                         "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
+    "tags_debug_tc_pairs", "tags_debug_mixed_fill",
+                         "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs", "tags_debug_tc_pairs",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
                          "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt",
                          "tags_batch_create", "tags_batch_run", "tags_batch_destroy"):
@@ -708,6 +712,10 @@ class Plan:
         code = lib().tags_plan_set_fill(self.handle, int(integration_type))
         if code != 0:
             raise RuntimeError(f"tags_plan_set_fill failed ({code}): {last_error()}")
+
+    def set_tc_pairs(self, on):
+        """Trailing updates on two-SM clusters (tcgen05 cta_group::2) or not."""
+        _ret(lib().tags_plan_set_tc_pairs(self.handle, 1 if on else 0))
 
     def set_refine_tol(self, tol):
         """Refinement stopping tolerance of the mixed form (0 = default 1e-9)."""

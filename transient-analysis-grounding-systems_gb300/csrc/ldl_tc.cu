@@ -586,6 +586,364 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
     if (warp == 1) tmem_dealloc(tmem, 512);
 }
 
+// ---- two-SM GEMM (tcgen05 cta_group::2) for the mode-0 updates -----------------------
+//
+// A cluster of two CTAs on two SMs computes a pair of vertically adjacent
+// tiles, rows (I0, I0 + 1) x column J, as tcgen05.mma.cta_group::2 products
+// with M = 256, N = 128. Each CTA stages its own 128 rows of A and one half
+// (64 rows) of B in its shared memory; the products, issued by one thread of
+// the even CTA, read A from each CTA's own shared memory and B from both, so
+// each SM streams 4 KiB of A and 2 KiB of B per 64-clock product instead of
+// 4 + 4 KiB (the single-CTA kernel's shared-memory bound). Each CTA's tensor
+// memory holds the accumulators of its own 128 rows; its epilogue warps do
+// the read-modify-write of its own tile exactly as in k_gemm_tc (mode 0).
+// Barriers: the even CTA's full[s] takes two arrivals (one per CTA, each with
+// its own byte count) and both CTAs' copies complete on it; the products'
+// commits are multicast to both CTAs' empty[s] (stage free) and tfull[a]
+// (accumulators ready); the epilogue warps of both CTAs arrive on the even
+// CTA's tempty[a]. Every wait is bounded as in k_gemm_tc; at the end the even
+// CTA waits for its products and copies, then both CTAs meet at a cluster
+// barrier before the tensor memory is released.
+
+constexpr int PSTB = (TB / 2) * BK * 2;              // one plane of a B half in one stage: 4 KiB
+
+template <int S> struct Gemm2Cfg {
+    static constexpr int NPL = 2 * S;
+    static constexpr int ABYTES = NPL * PST;          // A planes of one stage
+    static constexpr int STAGE = NPL * (PST + PSTB);  // A planes, then the B half's planes
+    static constexpr int STAGES = S == 2 ? 4 : 3;
+    static constexpr int BARS = 512;
+    static constexpr int SMEM = STAGES * STAGE + 1024 + BARS;
+};
+
+TAGS_D uint32_t cluster_rank() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+TAGS_D uint32_t cluster_idx() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+    return r;
+}
+TAGS_D uint32_t cluster_count() {
+    uint32_t r;
+    asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+    return r;
+}
+// Address in the shared::cluster window of the same variable in CTA `rank`.
+TAGS_D uint32_t mapa_cta(uint32_t addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+TAGS_D void mbar_arrive_expect_tx_cluster(uint32_t cbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cluster.shared::cluster.b64 _, [%0], %1;" ::"r"(cbar), "r"(bytes)
+                 : "memory");
+}
+TAGS_D void mbar_arrive_cluster(uint32_t cbar) {
+    asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(cbar) : "memory");
+}
+TAGS_D void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+}
+// Copy into this CTA's shared memory; completion is signalled on the mbarrier
+// at cluster address `cbar` (the even CTA's).
+TAGS_D void tma_load_5d_pair(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3, int c4,
+                             uint32_t cbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%2, "
+        "%3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(cbar)
+        : "memory");
+}
+TAGS_D void tmem_alloc_pair(uint32_t slot, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(slot), "r"(ncols) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+}
+TAGS_D void tmem_dealloc_pair(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+TAGS_D void mma_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t accumulate) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+// Arrive on the mbarrier at this shared offset in both CTAs of the pair once
+// the products issued so far are complete.
+TAGS_D void mma_pair_commit_both(uint32_t bar) {
+    const uint16_t mask = 3;
+    asm volatile(
+        "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(bar),
+        "h"(mask)
+        : "memory");
+}
+TAGS_D void mma_pair_commit_local(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// Instruction descriptor of the pair products: M = 256, N = 128.
+TAGS_D uint32_t idesc_mma_pair(bool negate_a, bool f16) {
+    uint32_t d = idesc_mma(negate_a, f16);
+    d &= ~(31u << 24);
+    d |= (uint32_t)(2 * TB >> 4) << 24;                 // M = 256
+    return d;
+}
+
+TAGS_D bool tile_in_band(const GemmArgs& g, int I, int J) {
+    if (g.zhi <= g.zlo) return false;
+    const bool row_zero = TB * I >= g.zlo && TB * I + TB <= g.zhi;
+    const bool col_zero = TB * J >= g.zlo && TB * J + TB <= g.zhi;
+    return row_zero || col_zero;
+}
+// Tile rows of the update, and pair tiles per sample: tile rows I0, I0 + 1 of
+// column J (lower triangle: I0 = J, J + 2, ...; block column: J = 0).
+TAGS_HD int pair_rows(const GemmArgs& g) { return g.tri ? (g.M + TB - 1) / TB : g.tiles; }
+TAGS_HD int pair_count(const GemmArgs& g, int T) {
+    if (!g.tri) return (T + 1) / 2;
+    int c = 0;
+    for (int j = 0; j < T; ++j) c += (T - j + 1) / 2;
+    return c;
+}
+TAGS_D void pair_of(const GemmArgs& g, int T, int l, int& I0, int& J) {
+    if (!g.tri) {
+        J = 0;
+        I0 = 2 * l;
+        return;
+    }
+    int j = 0;
+    for (; j < T - 1; ++j) {
+        const int c = (T - j + 1) / 2;
+        if (l < c) break;
+        l -= c;
+    }
+    J = j;
+    I0 = j + 2 * l;
+}
+
+// Mode 0, a tile outside the products (zero band, or past the last tile
+// row): if it holds rows of the next panel's block column, their current
+// values become that block column's split planes.
+template <int S>
+TAGS_D void skipped_tile_planes(const GemmArgs& g, int smp, int I, int J, int r, int half, int& ovf) {
+    const int gr = TB * I + r;
+    if (!(g.Np && J == 0 && I >= 1 && gr < g.M && gr - TB < g.Mn)) return;
+    const bool f16 = S == 2 && g.f16 != 0;
+    const float2* Cb = g.Amat + g.mstride * smp;
+    for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
+        const float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + cc * 16);
+        float2 cv[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) cv[j] = cc * 16 + j < g.Nn ? base_p[g.ld * j] : make_float2(0.f, 0.f);
+        store_planes16<S>(g.Np + g.npstride * smp, g.R, TB, gr - TB, cc * 16, cv, f16, ovf);
+    }
+}
+
+template <int S>
+__global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc2(const __grid_constant__ CUtensorMap tmA,
+                                                              const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+    using C = Gemm2Cfg<S>;
+    extern __shared__ uint8_t smem_raw[];
+    const uint32_t base_u32 = (smem_u32(smem_raw) + 1023u) & ~1023u;
+    uint8_t* base = smem_raw + (base_u32 - smem_u32(smem_raw));
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base + C::STAGES * C::STAGE);
+    // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], drain
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 2 * C::STAGES + 5);
+    auto full = [&](int q) { return smem_u32(&bars[q]); };
+    auto empty = [&](int q) { return smem_u32(&bars[C::STAGES + q]); };
+    auto tfull = [&](int a) { return smem_u32(&bars[2 * C::STAGES + a]); };
+    auto tempty = [&](int a) { return smem_u32(&bars[2 * C::STAGES + 2 + a]); };
+    const uint32_t drain = smem_u32(&bars[2 * C::STAGES + 4]);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const uint32_t rank = cluster_rank();
+    const int T = pair_rows(g);
+    const int P = pair_count(g, T);
+    const long long total = (long long)P * g.nb;
+    const long long first = cluster_idx(), stride = cluster_count();
+    if (tid == 0) {
+        for (int q = 0; q < C::STAGES; ++q) {
+            mbar_init(full(q), 2);            // one arrival (with its bytes) per CTA of the pair
+            mbar_init(empty(q), 1);
+        }
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(tfull(a), 1);
+            mbar_init(tempty(a), 2 * EPI_WARPS);
+        }
+        mbar_init(drain, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    // both CTAs' barriers are initialised before either arrives remotely
+    cluster_sync_all();
+    if (warp == 1) tmem_alloc_pair(smem_u32(tslot), 512);
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tslot;
+
+    if (warp == 0) {
+        // ---- producer (both CTAs): own A rows, own half of B; completion on the even CTA's full[s]
+        int stage = 0;
+        uint32_t phase = 0;
+        bool alive = true;
+        int issued[4] = {0, 0, 0, 0};
+        uint32_t ipar[4] = {0, 0, 0, 0};
+        for (long long t = first; t < total && alive; t += stride) {
+            const int smp = (int)(t / P);
+            int I0, J;
+            pair_of(g, T, (int)(t - (long long)smp * P), I0, J);
+            const bool skip0 = tile_in_band(g, I0, J), skip1 = I0 + 1 >= T || tile_in_band(g, I0 + 1, J);
+            if (skip0 && skip1) continue;
+            if (lane == 0) {
+                const int I = I0 + (int)rank;
+                for (int kb = 0; kb < g.kblocks; ++kb) {
+                    if (!mbar_wait(empty(stage), phase ^ 1, g.err)) { alive = false; break; }
+                    issued[stage] = 0;
+                    const uint32_t sa = base_u32 + stage * C::STAGE, sb = sa + C::ABYTES;
+                    const uint32_t cfull = mapa_cta(full(stage), 0);
+                    mbar_arrive_expect_tx_cluster(cfull, C::STAGE);
+                    const int ra = TB * I + g.off, rb = TB * J + g.off + (TB / 2) * (int)rank;
+                    for (int p = 0; p < C::NPL; ++p) {
+                        tma_load_5d_pair(sa + p * PST, &tmA, 0, ra, kb, p, smp, cfull);
+                        tma_load_5d_pair(sb + p * PSTB, &tmB, 0, rb, kb, p, smp, cfull);
+                    }
+                    issued[stage] = 1;
+                    ipar[stage] = phase;
+                    if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+                }
+            }
+            alive = __shfl_sync(0xffffffffu, alive ? 1 : 0, 0) != 0;
+        }
+        if (lane == 0) {
+            // let this CTA's copies land before the pair releases its memory: the
+            // even CTA on its full barriers (both CTAs' bytes), the odd CTA on the
+            // products' release of each stage it filled
+            for (int q = 0; q < C::STAGES; ++q)
+                if (issued[q]) mbar_wait_drain(rank == 0 ? full(q) : empty(q), ipar[q], g.err);
+        }
+    } else if (warp == 1) {
+        // ---- MMA issuer: one thread of the even CTA
+        if (rank == 0 && lane == 0) {
+            const uint32_t idp = idesc_mma_pair(false, g.f16 != 0), idn = idesc_mma_pair(true, g.f16 != 0);
+            int stage = 0, acc = 0;
+            uint32_t phase = 0, aphase = 0;
+            bool alive = true;
+            for (long long t = first; t < total && alive; t += stride) {
+                const int smp = (int)(t / P);
+                int I0, J;
+                pair_of(g, T, (int)(t - (long long)smp * P), I0, J);
+                const bool skip0 = tile_in_band(g, I0, J), skip1 = I0 + 1 >= T || tile_in_band(g, I0 + 1, J);
+                if (skip0 && skip1) continue;
+                if (!mbar_wait(tempty(acc), aphase ^ 1, g.err)) { alive = false; break; }
+                tc_fence_after();
+                const uint32_t accR = tmem + acc * 256, accI = accR + 128;
+                for (int kb = 0; kb < g.kblocks && alive; ++kb) {
+                    if (!mbar_wait(full(stage), phase, g.err)) { alive = false; break; }
+                    tc_fence_after();
+                    const uint32_t sa = base_u32 + stage * C::STAGE, sbb = sa + C::ABYTES;
+                    for (int kk = 0; kk < BK / 16; ++kk) {
+                        const uint32_t off = kk * 32;
+                        bool firstR = kb == 0 && kk == 0, firstI = firstR;
+                        for (int i = 0; i < S; ++i) {
+                            for (int j = 0; i + j < S; ++j) {
+                                const uint64_t ar = sdesc64(sa + i * PST + off), ai = sdesc64(sa + (S + i) * PST + off);
+                                const uint64_t br = sdesc64(sbb + j * PSTB + off),
+                                               bi = sdesc64(sbb + (S + j) * PSTB + off);
+                                mma_pair(accR, ar, br, idp, firstR ? 0u : 1u);   // + Ar Br
+                                firstR = false;
+                                mma_pair(accR, ai, bi, idn, 1u);                 // - Ai Bi
+                                mma_pair(accI, ar, bi, idp, firstI ? 0u : 1u);   // + Ar Bi
+                                firstI = false;
+                                mma_pair(accI, ai, br, idp, 1u);                 // + Ai Br
+                            }
+                        }
+                    }
+                    mma_pair_commit_both(empty(stage));      // stage reusable in both CTAs
+                    if (++stage == C::STAGES) { stage = 0; phase ^= 1; }
+                }
+                if (!alive) break;
+                mma_pair_commit_both(tfull(acc));            // both CTAs' accumulators ready
+                if (++acc == 2) { acc = 0; aphase ^= 1; }
+            }
+            // every product issued is complete before tensor memory is released
+            mma_pair_commit_local(drain);
+            mbar_wait_drain(drain, 0u, g.err);
+        }
+    } else {
+        // ---- epilogue warps 2..9 of both CTAs: this CTA's tile row I0 + rank
+        const int quarter = warp & 3, half = (warp - 2) >> 2;
+        const int r = 32 * quarter + lane;
+        const uint32_t lane_off = (uint32_t)(32 * quarter) << 16;
+        const bool f16 = S == 2 && g.f16 != 0;
+        const float unscale = f16 ? kF16Unscale : 1.f;
+        int ovf = 0;
+        int acc = 0;
+        uint32_t aphase = 0;
+        for (long long t = first; t < total; t += stride) {
+            const int smp = (int)(t / P);
+            int I0, J;
+            pair_of(g, T, (int)(t - (long long)smp * P), I0, J);
+            const bool skip0 = tile_in_band(g, I0, J), skip1 = I0 + 1 >= T || tile_in_band(g, I0 + 1, J);
+            const int I = I0 + (int)rank;
+            const bool mine_valid = I < T;
+            const bool mine_skip = rank == 0 ? skip0 : skip1;
+            if (skip0 && skip1) {
+                if (mine_valid) skipped_tile_planes<S>(g, smp, I, J, r, half, ovf);
+                continue;
+            }
+            if (!mbar_wait(tfull(acc), aphase, g.err)) break;
+            tc_fence_after();
+            if (mine_skip) {
+                if (mine_valid) skipped_tile_planes<S>(g, smp, I, J, r, half, ovf);
+            } else {
+                const uint32_t accR = tmem + acc * 256, accI = accR + 128;
+                const int gr = TB * I + r;
+                float2* Cb = g.Amat + g.mstride * smp;
+                for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
+                    float vr[16], vi[16];
+                    tmem_ld16(accR + lane_off + cc * 16, vr);
+                    tmem_ld16(accI + lane_off + cc * 16, vi);
+                    if (gr >= g.M) continue;
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        vr[j] *= unscale;
+                        vi[j] *= unscale;
+                    }
+                    const bool planes_only = g.Np && J == 0 && I >= 1 && gr - TB < g.Mn;
+                    const int cend = I == J ? min(g.Nn, gr + 1) : g.Nn;
+                    float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + TB * J + cc * 16);
+                    float2 cv[16];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j)
+                        if (TB * J + cc * 16 + j < cend) cv[j] = base_p[g.ld * j];
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        cv[j] = make_float2(cv[j].x - vr[j], cv[j].y - vi[j]);
+                        if (!planes_only && TB * J + cc * 16 + j < cend) base_p[g.ld * j] = cv[j];
+                    }
+                    if (planes_only) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j)
+                            if (cc * 16 + j >= g.Nn) cv[j] = make_float2(0.f, 0.f);
+                        store_planes16<S>(g.Np + g.npstride * smp, g.R, TB, gr - TB, cc * 16, cv, f16, ovf);
+                    }
+                }
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_cluster(mapa_cta(tempty(acc), 0));
+            if (++acc == 2) { acc = 0; aphase ^= 1; }
+        }
+        if (ovf) atomicOr(g.err + kErrRange, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    // the even CTA arrives here only after its products and copies are done
+    cluster_sync_all();
+    if (warp == 1) tmem_dealloc_pair(tmem, 512);
+}
+
 // ---- diagonal block: LDL^T, L11^{-1} -------------------------------------------------
 
 // One CTA of 512 threads per sample. The block lives in registers: thread
@@ -923,14 +1281,15 @@ EncodeTiledFn encode_fn() {
 // (64-byte rows, 64-byte swizzle: the K block of one pipeline stage).
 // 5-D map over K-block-major planes [sample][plane][K / 32][rows][32] (16-bit),
 // box {32, 128, 1, 1, 1}: one K block of 128 rows (64-byte rows, 64-byte swizzle).
-int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samples, int klen = TB) {
+int make_plane_map(CUtensorMap* map, void* base, int rows, int nplanes, int samples, int klen = TB,
+                   int box_rows = TB) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t kblk = (cuuint64_t)klen / BK;
     cuuint64_t dims[5] = {(cuuint64_t)BK, (cuuint64_t)rows, kblk, (cuuint64_t)nplanes, (cuuint64_t)samples};
     cuuint64_t strides[4] = {(cuuint64_t)BK * 2, (cuuint64_t)BK * 2 * rows, (cuuint64_t)BK * 2 * rows * kblk,
                              (cuuint64_t)BK * 2 * rows * kblk * nplanes};
-    cuuint32_t box[5] = {(cuuint32_t)BK, (cuuint32_t)TB, 1, 1, 1};
+    cuuint32_t box[5] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1, 1, 1};
     cuuint32_t estr[5] = {1, 1, 1, 1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 5, base, dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -985,6 +1344,33 @@ static int set_gemm_attr() {
     return 0;
 }
 
+// Two-SM GEMM: shared-memory size and the most clusters of two that can be
+// resident at once (the persistent grid), per split form.
+static int g_pair_clusters[4] = {0, 0, 0, 0};
+
+template <int S>
+static int set_gemm2_attr() {
+    TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc2<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, Gemm2Cfg<S>::SMEM));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * 76);
+    cfg.blockDim = dim3(GEMM_THREADS);
+    cfg.dynamicSmemBytes = Gemm2Cfg<S>::SMEM;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, (void*)k_gemm_tc2<S>, &cfg) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 0;                        // two-SM products unavailable: the single-SM kernel is used
+    }
+    g_pair_clusters[S] = n;
+    return 0;
+}
+
 // Kernel attributes and the tensor-map encoder, set once per process before
 // any launch (and so before any graph capture).
 int tags_ldl_tc_prepare() {
@@ -995,6 +1381,8 @@ int tags_ldl_tc_prepare() {
         if (!rc) rc = set_gemm_attr<2, 1>();
         if (!rc) rc = set_gemm_attr<3, 0>();
         if (!rc) rc = set_gemm_attr<3, 1>();
+        if (!rc) rc = set_gemm2_attr<2>();
+        if (!rc) rc = set_gemm2_attr<3>();
         if (!rc && cudaFuncSetAttribute(k_ldl_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(TB * DIAG_LD * sizeof(float2))) != cudaSuccess)
             rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_ldl_diag) failed");
@@ -1011,6 +1399,37 @@ static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const Gem
     k_gemm_tc<S, MODE><<<grid, GEMM_THREADS, GemmCfg<S>::SMEM, st>>>(mA, mB, g);
     tags_note_launch();
     return 0;
+}
+
+// Mode-0 update on the two-SM kernel: clusters of two CTAs walk the pair
+// tiles (mB64: the operand map with 64-row boxes, each CTA's half of B).
+template <int S>
+static int launch_gemm2_m(const CUtensorMap& mA, const CUtensorMap& mB64, const GemmArgs& g, cudaStream_t st) {
+    const int T = pair_rows(g);
+    const long long total = (long long)pair_count(g, T) * g.nb;
+    if (total <= 0) return 0;
+    const int clusters = (int)std::min<long long>(total, g_pair_clusters[S]);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(2 * clusters);
+    cfg.blockDim = dim3(GEMM_THREADS);
+    cfg.dynamicSmemBytes = Gemm2Cfg<S>::SMEM;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    TAGS_CUDA_OK(cudaLaunchKernelEx(&cfg, k_gemm_tc2<S>, mA, mB64, g));
+    tags_note_launch();
+    return 0;
+}
+
+static bool pair_ready(int NS) { return g_pair_clusters[NS == 3 ? 3 : 2] > 0; }
+
+static int launch_gemm2(int NS, const CUtensorMap& mA, const CUtensorMap& mB64, const GemmArgs& g, cudaStream_t st) {
+    return NS == 3 ? launch_gemm2_m<3>(mA, mB64, g, st) : launch_gemm2_m<2>(mA, mB64, g, st);
 }
 
 // One GEMM launch: K = 32 g.kblocks from the operand maps (mA, mB).
@@ -1053,7 +1472,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
 // LDL^T of `nb` matrices A (N x N complex FP32, column-major, lower triangle
 // used) in place: L strictly below the diagonal, D on it.
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
-                int* err, int zl_m, int pieces, int group_panels, cudaStream_t st) {
+                int* err, int zl_m, int pieces, int group_panels, cudaStream_t st, int pairs) {
     if (int e0 = tags_ldl_tc_prepare()) return e0;
     // split forms: 3 = bf16 x 3 pieces (6 products), 2 = bf16 x 2 (3 products),
     // TAGS_SPLIT_F16 = scaled fp16 x 2 (3 products, range-checked)
@@ -1070,11 +1489,13 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
     float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
     // the maps see a sample stride of 2 SMAX planes: declare that many planes
-    CUtensorMap mA21, mLg, mLin;
+    CUtensorMap mA21, mLg, mLin, mLg64;
     int e = make_plane_map(&mA21, A21p, N, 2 * SMAX, batch_cap);
     if (!e) e = make_plane_map(&mLg, Lg, N, 2 * SMAX, batch_cap, KG);
     if (!e) e = make_plane_map(&mLin, Lin, TB, 2 * SMAX, batch_cap);
+    if (!e) e = make_plane_map(&mLg64, Lg, N, 2 * SMAX, batch_cap, KG, TB / 2);
     if (e) return e;
+    const bool use_pairs = pairs != 0 && pair_ready(NS);
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * nb, st));
     const int G = group_panels < 1 ? 1 : (group_panels > GMAX ? GMAX : group_panels);
 
@@ -1157,7 +1578,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.Mn = Mn;
         g.Np = Mn > 0 ? A21p : nullptr;
         int pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
-        int e1 = launch_gemm(NS, mLg, mLg, g, st);
+        int e1 = use_pairs ? launch_gemm2(NS, mLg, mLg64, g, st) : launch_gemm(NS, mLg, mLg, g, st);
         // rank-K update outside the zero band: 8 K cells flops (cells: the triangle or the block column)
         const double r = M - (double)(g.zhi - g.zlo);
         const double K = g.kblocks * BK;
@@ -1220,6 +1641,13 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
 
 static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int pieces, int zl_m, int group);
 
+static int g_debug_pairs = 0;     // tags_debug_ldl*: mode-0 updates on two-SM clusters
+
+extern "C" int tags_debug_tc_pairs(int on) {
+    g_debug_pairs = on ? 1 : 0;
+    return 0;
+}
+
 extern "C" int tags_debug_tc_wait_limit(long long ns) {
     const unsigned long long v = ns > 0 ? (unsigned long long)ns : WAIT_NS;
     DeviceCtx* c = tags_ctx();
@@ -1272,7 +1700,7 @@ static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int p
         // plane buffers start as NaN patterns: a read of a row no kernel wrote shows
         cudaMemsetAsync(ws, 0xFF, wsb, st);
         cudaMemsetAsync(err, 0, 2 * sizeof(int), st);
-        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, zl_m, pieces, group, st);
+        rc = tags_ldl_tc(A, N, N, NN, nb, nb, ws, info, err, zl_m, pieces, group, st, g_debug_pairs);
         if (!rc && b) {
             cudaMemcpyAsync(X, hx.data(), sizeof(float2) * N * nb, cudaMemcpyHostToDevice, st);
             rc = tags_ldl_solve_c(A, N, N, NN, nb, nb, ws, X, N, zl_m, st);

@@ -658,7 +658,7 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m,
-                       p->split_pieces, p->group_panels, st);
+                       p->split_pieces, p->group_panels, st, p->tc_pairs);
 }
 
 // r = b, max row sum of W per sample, refinement state

@@ -434,6 +434,16 @@ extern "C" int tags_plan_set_refine_tol(tags_plan plan, double tol) {
     return 0;
 }
 
+extern "C" int tags_plan_set_tc_pairs(tags_plan plan, int on) {
+    if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_tc_pairs: invalid plan");
+    const int v = on ? 1 : 0;
+    if (plan->tc_pairs != v) {
+        plan->tc_pairs = v;
+        tags_plan_drop_graphs(plan);
+    }
+    return 0;
+}
+
 extern "C" int tags_plan_set_max_steps(tags_plan plan, int steps) {
     if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_max_steps: invalid plan");
     if (steps < 0 || steps > 40) return tags_fail(TAGS_E_ARG, "tags_plan_set_max_steps: steps must be 0 .. 40");
@@ -620,12 +630,13 @@ static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble*
 static int sync_twin(tags_plan_s* p) {
     tags_plan_s* t = p->twin;
     if (t->split_pieces != p->split_pieces || t->group_panels != p->group_panels || t->pass_batch != p->pass_batch ||
-        t->max_steps != p->max_steps || t->ir_tol != p->ir_tol) {
+        t->max_steps != p->max_steps || t->ir_tol != p->ir_tol || t->tc_pairs != p->tc_pairs) {
         t->split_pieces = p->split_pieces;
         t->group_panels = p->group_panels;
         t->pass_batch = p->pass_batch;
         t->max_steps = p->max_steps;
         t->ir_tol = p->ir_tol;
+        t->tc_pairs = p->tc_pairs;
         tags_plan_drop_graphs(t);
     }
     t->use_graphs = p->use_graphs;

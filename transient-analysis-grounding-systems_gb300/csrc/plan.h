@@ -77,6 +77,7 @@ struct tags_plan_s {
     SampleCoef* d_coef1 = nullptr;  // unit coefficients for the potentials
     int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
     int max_steps = 40;             // refinement steps per pass before the FP64 fallback (1 .. 40)
+    int tc_pairs = 0;               // trailing updates on two-SM clusters (tcgen05 cta_group::2)
     double ir_tol = 1e-9;           // refinement stopping tolerance (relative error left in x)
     int pass_batch = 0;             // samples per pass (<= batch; 0 = batch)
     int* d_iri = nullptr;           // refinement state: active, converged, iterations (batch each), step, continue,

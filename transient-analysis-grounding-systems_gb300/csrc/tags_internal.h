@@ -136,8 +136,9 @@ size_t tags_ldl_tc_workspace(int N, int batch);
 // coupling block, which the factorisation and the solves skip.
 // pieces: bf16 pieces per real value in the split products (2: three
 // products per real product, ~2^-16; 3: six products, ~2^-23).
+// pairs: the mode-0 updates on two-SM clusters (tcgen05 cta_group::2) where available.
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
-                int* err, int zl_m, int pieces, int group_panels, cudaStream_t st);
+                int* err, int zl_m, int pieces, int group_panels, cudaStream_t st, int pairs);
 // active (optional, per sample): samples whose flag is 0 are skipped.
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
                      float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active = nullptr);
