@@ -136,7 +136,16 @@ def measured_peaks():
 PROFILE_FAMILIES = 11
 TENSOR_FAMILIES = {"ldl_trailing_gemm", "ldl_panel_gemm"}
 FP64_FAMILIES = {"lu_fp64_gemm"}
-FP64_PIPE_TFLOPS = 1.19   # DFMA throughput measured on this machine's GB300 (probe kernel, 8 FMA chains)
+
+
+def fp64_peak(pkg):
+    """FP64 throughput of this GPU, measured here (tags_probe_fp64): DFMA on
+    the CUDA cores and DMMA (mma.sync m8n8k4 f64) on the FP64 tensor path.
+    The plain form's FP64 kernels run on DFMA."""
+    dfma, dmma = pkg.probe_fp64()
+    return {"dfma_tflops": dfma, "dmma_tflops": dmma, "peak": max(dfma, dmma),
+            "note": "measured in this run by tags_probe_fp64 (8 FMA chains per thread; 4 m8n8k4 f64 "
+                    "accumulators per warp), best of three launches each"}
 
 
 def read_profile(pkg):
@@ -154,7 +163,22 @@ def read_profile(pkg):
     return out
 
 
-def roofline(prof, peaks, pieces=3):
+# DRAM bytes of the trailing-update family (k_gemm_tc<2, 0>), one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) of all 35 launches of
+# one 128-sample pass of this workload: 73.83 GB, i.e. 16.5 MB per launch per
+# sample (profiles/k_gemm_tc_trailing_dram_grid1560_batch128.md). The traffic
+# grows in proportion to the samples in the pass.
+TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 73.83e9 / 35 / 128
+# Pipe use of the mixed form's fill kernel (k_fill_moment), from an ncu capture
+# at 16 samples (profiles/k_fill_moment_grid1560_batch16.md).
+FILL_PIPES = {"kernel": "k_fill_moment", "issue_active": 0.775, "fma_pipe": 0.613, "alu_pipe": 0.139,
+              "fp64_pipe": 0.023, "xu_pipe": 0.014, "dram_frac": 0.106,
+              "source": "ncu --set full, 16 samples (profiles/k_fill_moment_grid1560_batch16.md)",
+              "note": "FP32 ALU-bound (float-pair series); the log-singular entries run on the FP64 pipe in "
+                      "k_fill_special64 (82.5 % of its pipe)"}
+
+
+def roofline(prof, peaks, pieces=3, fp64=None, samples_per_pass=None):
     """Roofline of the family with the largest device time.
 
     Tensor families: `achieved` counts the algorithmic complex flops of the
@@ -169,8 +193,12 @@ def roofline(prof, peaks, pieces=3):
         ach = f["flops"] / sec / 1e12
         products = 6 if pieces == 3 else 3
         form = {3: "three bf16 pieces", 2: "two bf16 pieces", 16: "two fp16 pieces of 2^8 x"}.get(pieces, str(pieces))
+        traffic = (TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE * samples_per_pass
+                   if name == "ldl_trailing_gemm" and samples_per_pass else None)
         roof = {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": ach / peaks["bf16_tflops"], "traffic": None,
+                "frac": ach / peaks["bf16_tflops"], "traffic": traffic,
+                "traffic_note": "DRAM bytes per average launch (ncu capture of one pass, scaled by samples per "
+                                "pass); algorithmic C traffic is 16 B per updated element per group of panels",
                 "kernel": name, "launches": f["launches"], "avg_launch_ms": f["ms"] / f["launches"],
                 "executed_tflops": ach * products, "executed_frac": ach * products / peaks["bf16_tflops"],
                 "note": f"achieved = algorithmic complex LDL^T flops outside the zero ZL/ZT band; the "
@@ -178,10 +206,11 @@ def roofline(prof, peaks, pieces=3):
                         f"(executed_*); peak = {peaks['src']} dense bf16, {peaks['bf16_kind']}"}
     elif name in FP64_FAMILIES:
         ach = f["flops"] / sec / 1e12
-        roof = {"bound": "fp64", "achieved": ach, "peak": FP64_PIPE_TFLOPS, "unit": "TFLOP/s",
-                "frac": ach / FP64_PIPE_TFLOPS, "traffic": None, "kernel": name, "launches": f["launches"],
+        pk = fp64["peak"] if fp64 else None
+        roof = {"bound": "fp64", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                "frac": ach / pk if pk else None, "traffic": None, "kernel": name, "launches": f["launches"],
                 "avg_launch_ms": f["ms"] / f["launches"],
-                "note": "FP64 CUDA-core pipe; peak = DFMA throughput of a probe kernel on this pool's GB300"}
+                "note": "FP64 pipe; peak = the faster of DFMA and DMMA measured in this run (tags_probe_fp64)"}
     else:
         ach = f["bytes"] / sec / 1e9
         roof = {"bound": "hbm", "achieved": ach, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -337,6 +366,7 @@ def run_fields(args):
     torch.cuda.synchronize()
     pkg.fields_evaluations(reset=True)
     launches0 = pkg.launch_count()
+    fp64 = fp64_peak(pkg)
     pkg.lib().tags_gpu_profile(1)
     wall, ps = 0.0, 0
     with ClockSampler(local) as clk:
@@ -358,10 +388,10 @@ def run_fields(args):
     value = ps / dev_s
     roof = {"bound": "fp64", "kernel": "fields", "launches": f["launches"], "avg_launch_ms": f["ms"] / f["launches"],
             "evaluations_per_launch": evals / f["launches"], "evaluations_per_s": evals / dev_s,
-            "unit": "TFLOP/s", "peak": FP64_PIPE_TFLOPS, "traffic": None}
+            "unit": "TFLOP/s", "peak": fp64["peak"], "traffic": None}
     if FIELD_FP64_FLOPS_PER_EVAL:
         ach = evals * FIELD_FP64_FLOPS_PER_EVAL / dev_s / 1e12
-        roof.update({"achieved": ach, "frac": ach / FP64_PIPE_TFLOPS,
+        roof.update({"achieved": ach, "frac": ach / fp64["peak"],
                      "note": "executed FP64 flops (ncu count per rule-node evaluation x evaluations counted on "
                              "the device) over the measured DFMA throughput of this pool's GB300"})
     else:
@@ -674,12 +704,23 @@ def plain_fp64_record(pkg, elec, img, nodes, s_d, k_d, ie_d, centre, local, flus
             torch.cuda.synchronize()
         if int(info.abs().max().item()) != 0:
             raise RuntimeError("plain FP64 solve reported a singular pivot")
+        # one more step kernel by kernel with per-family events: where the time goes
+        plan.set_graphs(False)
+        pkg.lib().tags_gpu_profile(1)
+        one(int(starts[0]))
+        torch.cuda.synchronize()
+        prof = read_profile(pkg)
+        pkg.lib().tags_gpu_profile(0)
     finally:
         plan.close()
+    fp64 = fp64_peak(pkg)
+    roof, fams = roofline(prof, measured_peaks(), fp64=fp64)
     return {"value": steps * batch / dt, "unit": "solves/s", "steps": steps, "samples_per_step": batch,
             "ms_per_step": 1e3 * dt / steps, "step_ms": step_ms, "clocks": clk.summary(),
+            "roofline": roof, "kernel_families": fams, "fp64_peak": fp64,
             "note": "plain FP64 form of this library on the same workload: FP64 fill, FP64 LU with partial "
-                    "pivoting, device time from the plan's events, L2 flushed between steps"}
+                    "pivoting, device time from the plan's events, L2 flushed between steps; roofline and "
+                    "kernel_families from one more step launched kernel by kernel"}
 
 
 def gpr_accuracy(pkg, plan, s_d, k_d, ie_d, centre, n, SB, sol_d, info_d, s, tmax, nt):
@@ -889,7 +930,7 @@ def main():
     if rank != 0:
         return 0
     peaks = measured_peaks()
-    roof, fams = roofline(prof, peaks, split)
+    roof, fams = roofline(prof, peaks, split, samples_per_pass=B)
     line = {"metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)", "value": value,
             "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dev_time / args.steps, "step_ms": measured_step_ms,
@@ -908,6 +949,7 @@ def main():
                                       "roofline and kernel_families come from this pass"},
             "gpu_launches": launches, "clocks": clk.summary(), "e2e": e2e,
             "refinement": {"max_iterations": stats_iter, "fallbacks": stats_fb, "split": split},
+            "fill_pipes": FILL_PIPES if mixed else None,
             "accuracy": accuracy, "wall_s": wall}
     if plain is not None:
         line["plain_fp64"] = plain

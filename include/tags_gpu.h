@@ -477,6 +477,12 @@ int tags_debug_ldl (tags_cdouble *a, int N, int nb, int pieces);
  * update (1, 2 or 4). */
 int tags_debug_ldl_solve (tags_cdouble *a, tags_cdouble *b, int N, int nb, int pieces, int zl_m, int group);
 
+/* No counterpart in the reference. FP64 throughput of the current device, in
+ * TFLOP/s: dfma from eight independent FMA chains per thread on the CUDA
+ * cores, dmma from mma.sync m8n8k4 f64 on the FP64 tensor path (best of three
+ * timed launches each). The plain form's roofline is reported against these. */
+int tags_probe_fp64 (double *dfma_tflops, double *dmma_tflops);
+
 /* Per-family kernel timing with CUDA events on the launching stream (0 = off,
  * the default). Enabling resets the counters. Families, in this order:
  * fill_fp64, fill_mixed, ldl_diag, ldl_panel_gemm, ldl_trailing_gemm,

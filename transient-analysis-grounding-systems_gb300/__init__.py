@@ -58,7 +58,7 @@ EXPORTS = (
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
-    "tags_debug_tc_pairs",
+    "tags_debug_tc_pairs", "tags_debug_mixed_fill", "tags_probe_fp64",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
     "tags_gpu_inlt", "tags_batch_create", "tags_batch_run", "tags_batch_destroy",
@@ -151,6 +151,7 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_refine_tol.argtypes = [_vp, ctypes.c_double]
             L.tags_plan_set_tc_pairs.argtypes = [_vp, ctypes.c_int]
             L.tags_debug_tc_pairs.argtypes = [ctypes.c_int]
+            L.tags_probe_fp64.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.tags_debug_tc_wait_limit.argtypes = [ctypes.c_longlong]
             L.tags_debug_mixed_fill.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _vp]
             L.tags_inv_laplace_batch.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _sz, ctypes.c_int, ctypes.c_int]
@@ -183,9 +184,8 @@ def lib() -> ctypes.CDLL:
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
                          "tags_plan_set_pipelines",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
-                         "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
-    "tags_debug_tc_pairs", "tags_debug_mixed_fill",
-                         "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs", "tags_debug_tc_pairs",
+                         "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol",
+                         "tags_plan_set_tc_pairs", "tags_debug_tc_pairs", "tags_debug_mixed_fill", "tags_probe_fp64",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
                          "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt",
                          "tags_batch_create", "tags_batch_run", "tags_batch_destroy"):
@@ -787,6 +787,13 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+def probe_fp64():
+    """(DFMA, DMMA) FP64 throughput of the current device in TFLOP/s."""
+    a, b = ctypes.c_double(), ctypes.c_double()
+    _ret(lib().tags_probe_fp64(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def debug_tc_wait_limit(ns: int = 0) -> None:
