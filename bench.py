@@ -12,6 +12,7 @@ samples, cycling through the 2048-sample set. Prints one JSON line.
   python bench.py --workload fields     # post-processing: potentials and field along a line
   python bench.py --workload grids      # 64 grids of uneven size x 256 samples in one call
   python bench.py --workload mhem       # the examples' mHEM impedance model, same grid and samples
+  python bench.py --workload rods       # 120 x 120 m grid with 50 rods (N = 17875), 512 samples
 """
 from __future__ import annotations
 
@@ -568,6 +569,80 @@ def run_mhem(args):
     return 0
 
 
+# ---- the 120 x 120 m grid with 50 rods (N = 17875) ------------------------------------
+# 24 x 24 meshes, 1 m segmentation (m = 6000) plus 50 vertical rods of 3 m (3
+# segments each) at seeded grid vertices: m = 6150, n = 5575, N = 17875;
+# soil 100 ohm m, eps_r 10; unit current at the centre; 512 Laplace samples
+# (nt = 1022, 10 MHz), streamed through the plan's memory-admitted passes.
+RODS_NT = 1022
+RODS_TMAX = 511 / 10e6
+
+
+def run_rods(args):
+    import torch
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    import __graft_entry__ as entry
+    pkg = entry.load_package()
+    pkg.build()
+    elec, nodes = pkg.grid_with_rods()
+    img = pkg.images(elec)
+    m, n = elec.shape[0], nodes.shape[0]
+    N = n + 2 * m
+    s = pkg.laplace_samples(RODS_NT, RODS_TMAX)
+    kappa = 1.0 / 100.0 + s * 10.0 * pkg.EPS0
+    centre = int(np.argmin(np.linalg.norm(nodes - [60.0, 60.0, -0.5], axis=1)))
+    t0 = time.perf_counter()
+    plan = pkg.Plan(elec, img, nodes, pkg.MIXED, max_batch=args.batch or 0)
+    setup_s = time.perf_counter() - t0
+    ns = len(s)
+    dev = torch.device("cuda", local)
+    s_d = torch.from_numpy(s).to(dev)
+    k_d = torch.from_numpy(kappa).to(dev)
+    sol_d = torch.empty((ns, N), dtype=torch.complex128, device=dev)
+    info_d = torch.empty((ns,), dtype=torch.int32, device=dev)
+    # warm-up: one small run (graph capture of the first pass shape, tables)
+    plan.run_device(s_d.data_ptr(), k_d.data_ptr(), 2, 1.0, None, centre, sol_d.data_ptr(), info_d.data_ptr())
+    torch.cuda.synchronize()
+    launches0 = pkg.launch_count()
+    with ClockSampler(local) as clk:
+        st = plan.run_device(s_d.data_ptr(), k_d.data_ptr(), ns, 1.0, None, centre, sol_d.data_ptr(),
+                             info_d.data_ptr())
+        torch.cuda.synchronize()
+    launches = pkg.launch_count() - launches0
+    if int(info_d.abs().max().item()) != 0:
+        raise RuntimeError("a sample reported a failed solve")
+    # end to end: host buffers through tags_plan_run
+    t0 = time.perf_counter()
+    sol_h, info_h, st_h = plan.run(s, kappa, 1.0, None, centre)
+    e2e_t = time.perf_counter() - t0
+    # accuracy against the plain FP64 form on two samples (lowest and 6 MHz)
+    idx = np.array([0, 306])
+    xp, ip, _ = pkg.hem_sweep(elec, img, nodes, s[idx], kappa[idx], inj_node=centre, precision=pkg.PLAIN_FP64,
+                              max_batch=2)
+    err = float(max(np.max(np.abs(sol_h[k, :n] - xp[j, :n])) / np.max(np.abs(xp[j, :n])) for j, k in enumerate(idx)))
+    plan.close()
+    line = {"metric": "Laplace-sample solves/s, 120 x 120 m grid with 50 rods (N = 17875), 512 samples",
+            "value": ns / st.seconds, "unit": "solves/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "ms_per_step": 1e3 * st.seconds, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64+c128", "data": "synthetic (reference grid generator plus seeded rods)",
+            "config": {"workload": "grid 120x120 m, 24x24 meshes, 1 m segments, 50 rods of 3 m; m=6150, n=5575, "
+                                   "N=17875; 512 Laplace samples (nt=1022, 10 MHz); soil 100 ohm m, eps_r 10",
+                       "samples": ns, "plan_setup_s": setup_s,
+                       "passes": "memory-admitted: the plan's samples per pass are sized from free device memory"},
+            "gpu_launches": launches, "clocks": clk.summary(),
+            "e2e": {"value": ns / e2e_t, "unit": "solves/s", "h2d_bytes_per_step": ns * 32,
+                    "d2h_bytes_per_step": ns * (16 * N + 4)},
+            "refinement": {"max_iterations": st.max_iterations, "fallbacks": st.fallbacks,
+                           "max_backward_error": st.max_backward_error},
+            "accuracy": {"samples": len(idx), "reference": "plain FP64 form of this library",
+                         "max_rel_err_u_all": err}}
+    print(json.dumps(line))
+    return 0
+
+
 # ---- many uneven grids ---------------------------------------------------------------
 # 64 square grids of uneven size (side 5-40 m, 2-10 meshes, 1 m segmentation,
 # m = 36..880), each with its own soil, 256 Laplace samples each (nt = 510,
@@ -784,9 +859,10 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     ap.add_argument("--first-batch", type=int, default=0,
                     help="batch of samples the warm-up and timed steps start from (0 = the whole job in order)")
-    ap.add_argument("--workload", default="solves", choices=["solves", "fields", "grids", "mhem"],
+    ap.add_argument("--workload", default="solves", choices=["solves", "fields", "grids", "mhem", "rods"],
                     help="solves: the per-sample HEM path (default); fields: post-processing along a line; "
-                         "grids: 64 uneven grids in one call; mhem: the examples' mHEM model on the same grid")
+                         "grids: 64 uneven grids in one call; mhem: the examples' mHEM model on the same grid; "
+                         "rods: the 120 x 120 m grid with 50 rods, N = 17875, 512 samples")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -796,6 +872,8 @@ def main():
         return run_grids(args)
     if args.workload == "mhem":
         return run_mhem(args)
+    if args.workload == "rods":
+        return run_rods(args)
 
     import torch
     import torch.distributed as dist
