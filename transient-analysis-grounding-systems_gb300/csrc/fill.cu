@@ -742,10 +742,71 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
     }
 }
 
+// Duffy moments of the touching kinds, once per plan (FP64). For a pair
+// sharing an endpoint, j_touch sums w [phi(gamma rho1)/rho1 + phi(gamma rho2)/rho2]
+// over the Duffy halves' nodes; with phi(x) = sum_n (-x)^n / (n + 1)! that is
+//   J = sum_n (-gamma)^n / (n + 1)! M_n,   M_n = sum_q w_q (rho1^(n-1) + rho2^(n-1)),
+// geometry only. rho <= L_a + L_b, so the series converges like that of
+// e^{|gamma| (L_a + L_b)}: 24 terms cover |gamma| (L_a + L_b) up to ~3 at FP64
+// accuracy. Warp per special entry, lane per node of a 32-point rule (more
+// than the plain form's 16 + 2 |gamma| L for the same integrals).
+constexpr int TM_Q = 32;
+
+__global__ void __launch_bounds__(128) k_touch_moments(const double* __restrict__ elec, const double* __restrict__ img,
+                                                       int m, const int2* __restrict__ ent, int nent,
+                                                       double* __restrict__ tm) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int e = blockIdx.x * 4 + warp;
+    if (e >= nent) return;
+    const int2 en = ent[e];
+    int i, k;
+    pair_index(en.x, m, i, k);
+    Seg S, R;
+    ld_seg(elec + 11LL * i, S);
+    for (int kind = 0; kind < 2; ++kind) {
+        double acc[MOM_N];
+#pragma unroll
+        for (int n = 0; n < MOM_N; ++n) acc[n] = 0.0;
+        bool ok = (en.y & (1 << kind)) != 0;
+        int ia = 0, ib = 0;
+        if (ok) {
+            ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
+            ok = touching(R, S, 1e-9 * fmax(S.len, R.len), ia, ib);
+        }
+        if (ok) {
+            double a[3], b[3];
+            for (int d = 0; d < 3; ++d) {
+                a[d] = ia == 0 ? R.b[d] - R.a[d] : R.a[d] - R.b[d];
+                b[d] = ib == 0 ? S.b[d] - S.a[d] : S.a[d] - S.b[d];
+            }
+            const double t = g_glx[gl_off(TM_Q) + lane], w = g_glw[gl_off(TM_Q) + lane];
+            const double u1[3] = {a[0] - t * b[0], a[1] - t * b[1], a[2] - t * b[2]};
+            const double u2[3] = {t * a[0] - b[0], t * a[1] - b[1], t * a[2] - b[2]};
+            const double r1 = sqrt(dot3(u1, u1)), r2 = sqrt(dot3(u2, u2));
+            double v1 = w / r1, v2 = w / r2;
+#pragma unroll
+            for (int n = 0; n < MOM_N; ++n) {
+                acc[n] = v1 + v2;
+                v1 *= r1;
+                v2 *= r2;
+            }
+        }
+#pragma unroll
+        for (int n = 0; n < MOM_N; ++n)
+            for (int o = 16; o > 0; o >>= 1) acc[n] += __shfl_xor_sync(0xffffffffu, acc[n], o);
+        if (lane == 0) {
+#pragma unroll
+            for (int n = 0; n < MOM_N; ++n) tm[((long long)e * 2 + kind) * MOM_N + n] = acc[n];
+        }
+    }
+}
+
 // The log-singular entries in FP64: for each special entry (a pair with a
-// kind that shares an endpoint, or a diagonal entry) the Duffy rule of
-// j_touch at the plain form's order (16 + 2 |gamma| L) for the touching kinds,
-// and the static closed form for the self term, added to the FP32 value
+// kind that shares an endpoint, or a diagonal entry) the touching kinds from
+// their Duffy moments (k_touch_moments) as an FP64 series in gamma, or, for a
+// warp of samples the 24-term series does not reach, the Duffy rule of
+// j_touch at the plain form's order (16 + 2 |gamma| L) directly; and the
+// static closed form for the self term, added to the FP32 value
 // the regular fill left there for the regular kinds (lower triangle, hi in Z
 // and lo in Zlo). The sum v is formed in FP64 and stored again as hi = fl(v)
 // in Z and lo = fl(v - hi) in Zlo, which the refinement's residual reads. One warp per entry and
@@ -756,7 +817,7 @@ constexpr int SPEC_WARPS = 4;
 __global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
     const double* __restrict__ elec, const double* __restrict__ img, int m, const int2* __restrict__ ent, int nent,
     const SampleCoef* __restrict__ coef, int nsamp, float2* zl0, float2* zt0, float2* zlo0, float2* ztlo0,
-    long long bstride, int* status) {
+    long long bstride, int* status, const double* __restrict__ tm, double tdmax) {
     __shared__ double2 nodes_all[SPEC_WARPS][2 * QMAX];      // (rho, w / rho)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     double2* nodes = nodes_all[warp];
@@ -773,6 +834,19 @@ __global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
     ld_seg(elec + 11LL * i, S);
     double2 dl = cz(0.0, 0.0), dt = cz(0.0, 0.0);
     bool bad = false;
+    // the moment series when every lane's sample needs at most MOM_N terms:
+    // the first n with x^n / (n + 1)! <= 1e-17 e^{-x}, x = |gamma| (L_a + L_b)
+    int ntw = 0;
+    {
+        const double xg = valid ? sqrt(cabs2(c.gamma)) * tdmax : 0.0, lim = 1e-17 * exp(-xg);
+        double term = 1.0;
+        while (ntw <= MOM_N && !(term <= lim && ntw > 4)) {
+            ++ntw;
+            term *= xg / (ntw + 1);
+        }
+        ntw = __reduce_max_sync(0xffffffffu, ntw);
+    }
+    const bool series = tm && ntw <= MOM_N;
     for (int kind = 0; kind < 2 && !bad; ++kind) {
         if (!(en.y & (1 << kind))) continue;
         ld_seg((kind == 0 ? elec : img) + 11LL * k, R);
@@ -785,6 +859,26 @@ __global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
             bad = fmax(fabs(ro[0] - so[0]), fmax(fabs(ro[1] - so[1]), fabs(ro[2] - so[2]))) <= 1e-9 * lmax;
         }
         if (bad) break;
+        if (series) {
+            // J = sum_n (-gamma)^n / (n + 1)! M_n in FP64
+            const double* M = tm + ((long long)e * 2 + kind) * MOM_N;
+            double2 J = cz(0.0, 0.0), an = cz(1.0, 0.0);
+            const double2 mg = cz(-c.gamma.x, -c.gamma.y);
+            for (int n = 0; n < ntw; ++n) {
+                const double Mn = M[n];
+                J.x = fma(an.x, Mn, J.x);
+                J.y = fma(an.y, Mn, J.y);
+                an = cscale(cmul(an, mg), 1.0 / (n + 2));
+            }
+            double cost = 0.0;
+            for (int d = 0; d < 3; ++d) cost += (S.b[d] - S.a[d]) * (R.b[d] - R.a[d]);
+            cost = fabs(cost);
+            const bool keep = kind == 0 ? !(cost < TAGS_DBL_EPSILON) : (cost > TAGS_DBL_EPSILON);
+            const double2 cL = kind == 0 ? c.cL : c.cLi, cT = kind == 0 ? c.cT : c.cTi;
+            dt = cadd(dt, cmul(cT, J));
+            if (keep) dl = cadd(dl, cscale(cmul(cL, J), cost));
+            continue;
+        }
         int q = valid ? min(QMAX, 16 + 2 * (int)ceil(sqrt(cabs2(c.gamma)) * lmax)) : 0;
         q = __reduce_max_sync(0xffffffffu, q);
         double a[3], b[3];
@@ -1319,7 +1413,7 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
                                                  d_ztlo);
     dim3 gs((unsigned)((sp.n + SPEC_WARPS - 1) / SPEC_WARPS), (unsigned)((nsamp + 31) / 32));
     k_fill_special64<<<gs, SPEC_WARPS * 32, 0, st>>>(d_elec, d_img, m, sp.ent, sp.n, d_coef, nsamp, d_zl, d_zt, d_zlo,
-                                                     d_ztlo, bstride, d_status);
+                                                     d_ztlo, bstride, d_status, sp.tm, sp.tdmax);
     const dim3 gm((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS));
     k_zmirror<<<gm, 256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
     k_zmirror<<<gm, 256, 0, st>>>(d_zlo, d_ztlo, bstride, m, 2 * nsamp);
@@ -1403,8 +1497,21 @@ int tags_mixed_special_build(void* ws, int m, int batch, SpecialEntries* sp, cud
     return 0;
 }
 
+int tags_mixed_special_moments(const double* d_elec, const double* d_img, int m, double lmax, SpecialEntries* sp,
+                               cudaStream_t st) {
+    if (sp->tm) cudaFree(sp->tm);
+    sp->tm = nullptr;
+    if (sp->n <= 0) return 0;
+    TAGS_CUDA_OK(cudaMalloc(&sp->tm, sizeof(double) * 2 * MOM_N * (size_t)sp->n));
+    k_touch_moments<<<(unsigned)((sp->n + 3) / 4), 128, 0, st>>>(d_elec, d_img, m, sp->ent, sp->n, sp->tm);
+    tags_note_launch();
+    TAGS_CUDA_OK(cudaGetLastError());
+    sp->tdmax = 2.0 * lmax;
+    return 0;
+}
+
 void tags_mixed_special_free(SpecialEntries* sp) {
-    void* ptrs[] = {sp->ent};
+    void* ptrs[] = {sp->ent, sp->tm};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     *sp = SpecialEntries{};

@@ -529,6 +529,12 @@ int tags_mixed_alloc(tags_plan_s* p) {
     if (err) return err;
     err = tags_mixed_special_build(p->d_fillws, p->m, (int)b, &p->spec, p->stream);
     if (err) return err;
+    {
+        double lmax = 0.0;
+        for (int e = 0; e < p->m; ++e) lmax = std::max(lmax, p->h_elec[11 * (size_t)e + 9]);
+        err = tags_mixed_special_moments(p->d_elec, p->d_img, p->m, lmax, &p->spec, p->stream);
+        if (err) return err;
+    }
     err = tags_moment_fill_build(p->d_elec, p->has_images ? p->d_img : p->d_elec, p->m, p->has_images,
                                  p->h_elec.data(), p->has_images ? p->h_img.data() : p->h_elec.data(), (int)b, &p->mom,
                                  p->stream);

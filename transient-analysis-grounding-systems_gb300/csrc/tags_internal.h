@@ -56,8 +56,13 @@ int tags_mixed_touch_count(void* ws, int m, cudaStream_t st, int* out);
 struct SpecialEntries {
     int n = 0;                   // entries
     int2* ent = nullptr;         // (pair index p of (k, i), k >= i; kinds mask: bit 0 direct, 1 image, 2 self)
+    double* tm = nullptr;        // FP64 Duffy moments of the touching kinds: [entry][kind][24]
+    double tdmax = 0.0;          // bound of the Duffy distances (2 x the longest segment)
 };
 int tags_mixed_special_build(void* ws, int m, int batch, SpecialEntries* sp, cudaStream_t st);
+// the Duffy moments of the special entries' touching kinds (once per plan)
+int tags_mixed_special_moments(const double* d_elec, const double* d_img, int m, double lmax, SpecialEntries* sp,
+                               cudaStream_t st);
 void tags_mixed_special_free(SpecialEntries* sp);
 // The moment expansion of the regular kinds (fill.cu): moments of every
 // (pair, kind) once per plan; per pass the samples' constants and the table
