@@ -24,6 +24,7 @@
  *   nodes_file             src/electrode.c:82-101   (decl src/electrode.h:140-141)
  *   alipio_soil            src/auxiliary.c:60-70    (decl src/auxiliary.h:101-103)
  *   smith_longmire_soil    src/auxiliary.c:72-93    (decl src/auxiliary.h:119-121)
+ *   heidler                src/auxiliary.c:331-336  (decl src/auxiliary.h:398)
  *   laplace_trans          replaces src/auxiliary.c:239-263 (decl src/auxiliary.h:320-321)
  *   inv_laplace_trans      replaces src/auxiliary.c:265-329 (decl src/auxiliary.h:366-368)
  *
@@ -117,6 +118,10 @@ int alipio_soil (tags_cdouble *sigma, tags_cdouble *epsr, double sigma0, tags_cd
 
 /* Smith-Longmire soil: conductivity and relative permittivity at s. */
 int smith_longmire_soil (tags_cdouble *sigma, tags_cdouble *epsr, double sigma0, tags_cdouble s, double erinf);
+
+/* Heidler lightning-current waveform at time t (peak imax, front and tail
+ * time constants tau1, tau2, steepness n). */
+double heidler (double t, double imax, double tau1, double tau2, double n);
 
 /* ---- nodal admittance formulation (the reference's mHEM examples) ---------- */
 

@@ -44,6 +44,13 @@ def test_soil_and_samples_match_reference(pkg, ref):
     assert np.array_equal(pkg.laplace_samples(4094, 204.7e-6), s)
 
 
+def test_heidler_matches_reference(pkg, ref):
+    for t in (0.0, 1e-7, 1.9e-6, 2e-5, 1e-4):
+        for tau1, tau2, n in ((1.8e-6, 95e-6, 2.0), (0.454e-6, 143e-6, 10.0), (1.9e-6, 485e-6, 2.0)):
+            a, b = pkg.heidler(t, 1e3, tau1, tau2, n), ref.heidler(t, 1e3, tau1, tau2, n)
+            assert abs(a - b) <= 1e-14 * max(abs(b), 1e-300)
+
+
 def test_logspace_linspace_match_reference(pkg):
     f = pkg.logspace(2, 7, 100)
     assert f[-1] == 1e7 and f[0] == 100.0 and len(f) == 100

@@ -54,7 +54,7 @@ EPS0 = 8.854187817620e-12
 EXPORTS = (
     "calculate_impedances", "impedances_images", "fill_incidence_imm", "fill_impedance_imm",
     "solve_immittance", "fill_incidence_adm", "fill_impedance_adm", "calculate_yla_ytb", "fill_impedance_adm2",
-    "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "laplace_trans",
+    "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "heidler", "laplace_trans",
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
@@ -137,6 +137,8 @@ def lib() -> ctypes.CDLL:
             L.nodes_file.argtypes = [ctypes.c_char_p, _vp, _sz]
             L.alipio_soil.argtypes = [_vp, _vp, ctypes.c_double, C, ctypes.c_double, ctypes.c_double, ctypes.c_double]
             L.smith_longmire_soil.argtypes = [_vp, _vp, ctypes.c_double, C, ctypes.c_double]
+            L.heidler.argtypes = [ctypes.c_double] * 5
+            L.heidler.restype = ctypes.c_double
             L.laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz]
             L.inv_laplace_trans.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, ctypes.c_int]
             L.tags_plan_create.argtypes = [ctypes.POINTER(_vp), _vp, _vp, _sz, _vp, _sz, ctypes.c_int, _sz]
@@ -440,6 +442,11 @@ def smith_longmire_soil(sigma0: float, s: complex, erinf: float):
     out = np.zeros(2, dtype=np.complex128)
     lib().smith_longmire_soil(_addr(out[:1]), _addr(out[1:]), float(sigma0), c_complex.of(s), float(erinf))
     return complex(out[0]), complex(out[1])
+
+
+def heidler(t: float, imax: float, tau1: float, tau2: float, n: float) -> float:
+    """Heidler lightning current at time t (src/auxiliary.c:331-336)."""
+    return lib().heidler(float(t), float(imax), float(tau1), float(tau2), float(n))
 
 
 def inv_laplace_batch(g, s, tmax: float, nt: int, filt: int = FILTER_NONE) -> np.ndarray:

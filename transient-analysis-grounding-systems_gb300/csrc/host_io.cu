@@ -4,6 +4,7 @@
 //   nodes_file           src/electrode.c:82-101 (CSV "x, y, z" per line)
 //   alipio_soil          src/auxiliary.c:60-70
 //   smith_longmire_soil  src/auxiliary.c:72-93
+//   heidler              src/auxiliary.c:331-336
 // Return codes follow the reference: -10 when the file cannot be opened, the
 // fscanf shortfall (count read - count expected) of the first bad line, or
 // populate_electrode's error for a degenerate segment.
@@ -140,4 +141,12 @@ extern "C" int smith_longmire_soil(tags_cdouble* sigma, tags_cdouble* epsr, doub
     *sigma = {sg.real(), sg.imag()};
     *epsr = {er.real(), er.imag()};
     return 0;
+}
+
+// Heidler lightning current: imax / xi (t/tau1)^n / (1 + (t/tau1)^n) e^{-t/tau2},
+// xi = e^{-(tau1/tau2) (n tau2/tau1)^(1/n)} the peak correction factor.
+extern "C" double heidler(double t, double imax, double tau1, double tau2, double n) {
+    const double xi = std::exp(-(tau1 / tau2) * std::pow(n * tau2 / tau1, 1.0 / n));
+    const double u = std::pow(t / tau1, n);
+    return imax / xi * u / (1.0 + u) * std::exp(-t / tau2);
 }
