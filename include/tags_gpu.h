@@ -271,7 +271,9 @@ typedef struct tags_plan_s *tags_plan;
 typedef struct {
     int max_iterations;        /* largest refinement iteration count (mixed) */
     int fallbacks;             /* samples re-solved in plain FP64 (mixed) */
-    double max_backward_error; /* largest normwise backward error |b - W x| / (|W| |x| + |b|) */
+    double max_backward_error; /* largest normwise backward error |b - W x| / (|W| |x|) of the last
+                                  iterate whose residual the refinement formed: the one before
+                                  the final correction (which shrinks the error further) */
     double seconds;            /* device time of the run */
     int split;                 /* split form used by the last pass (mixed; see tags_plan_set_split) */
 } tags_run_stats;
@@ -435,6 +437,13 @@ int tags_plan_set_tc_pairs (tags_plan plan, int on);
 /* No counterpart in the reference. The same switch for the diagnostic entry
  * points tags_debug_ldl and tags_debug_ldl_solve (process-wide). */
 int tags_debug_tc_pairs (int on);
+
+/* No counterpart in the reference. Test hook (process-wide, for passes and
+ * graphs built afterwards): 1 (default) runs each triangular solve of the
+ * mixed form as one CTA per sample with x in shared memory, where x fits;
+ * 0 runs it block by block (two kernels per 128-row block and sweep). Both
+ * form every sum in the same order and give identical results. */
+int tags_debug_solve_cta (int on);
 
 /* No counterpart in the reference. Caps the refinement steps of the mixed
  * form's passes (1 .. 40; 0 restores the default 40). A sample that has not

@@ -204,6 +204,8 @@ def test_mixed_fill_matches_fp64_fill(gpu_pkg, with_images):
     for b in range(len(s)):
         zl_p, zt_p = gpu_fill(pkg, e, img, s[b], kappa[b])
         for name, zm, zp in (("zl", zl_m[b], zl_p), ("zt", zt_m[b], zt_p)):
+            # both triangles hold the same float pair
+            assert np.array_equal(zm, zm.T)
             for part, mask in (("special", spec), ("regular", regular)):
                 nz = mask & (np.abs(zp) > 0)
                 assert np.all(zm[mask & (zp == 0)] == 0)

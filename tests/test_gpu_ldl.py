@@ -114,3 +114,29 @@ def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group, pairs)
     for q in range(2):
         ref = np.linalg.solve(mats[q], rhs[q])
         assert np.linalg.norm(x[q] - ref) / np.linalg.norm(ref) < 2e-5, (N, zl_m, q)
+
+
+@pytest.mark.parametrize("N,zl_m", [(517, 0), (1000, 300), (1500, 400)])
+def test_one_cta_solve_equals_block_solve(gpu_pkg, N, zl_m):
+    """The solve as one CTA per sample (x in shared memory) and block by block
+    (two kernels per 128-row block and sweep) form every sum in the same order:
+    identical results, partial last block and the zero ZL/ZT band included."""
+    fn = gpu_pkg.lib().tags_debug_ldl_solve
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                   ctypes.c_int]
+    fn.restype = ctypes.c_int
+    rng = np.random.default_rng(N + 7 * zl_m)
+    mats = np.stack([_banded_sym(rng, N, zl_m, d) for d in (4.0, 3.0)])
+    rhs = rng.standard_normal((2, N)) + 1j * rng.standard_normal((2, N))
+    out = []
+    for cta in (1, 0):
+        buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)
+        x = rhs.copy()
+        gpu_pkg.lib().tags_debug_solve_cta(cta)
+        try:
+            code = fn(buf.ctypes.data, x.ctypes.data, N, 2, 16, zl_m, 4)
+        finally:
+            gpu_pkg.lib().tags_debug_solve_cta(1)
+        assert code == 0, gpu_pkg.last_error()
+        out.append(x)
+    assert np.array_equal(out[0], out[1])

@@ -299,3 +299,29 @@ def test_two_sm_updates_match_single_sm(gpu_pkg):
             assert np.all(info == 0) and st.fallbacks == 0
             out.append(sol)
         assert rel_err(out[1], out[0]) < 1e-12
+
+
+def test_one_cta_solves_match_block_solves_in_plans(gpu_pkg):
+    """The mixed form's refinement with its triangular solves as one CTA per
+    sample (x in shared memory) and block by block: identical solutions and
+    refinement counts (config 2 grid, 40 samples in passes of 16, CUDA graphs;
+    the first solve of each pass starts at the node rows in both)."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    idx = np.linspace(0, len(gd["s"]) - 1, 40).astype(int)
+    s, kappa = gd["s"][idx], gd["kappa"][idx]
+    ie = np.zeros((len(idx), nodes.shape[0]), np.complex128)
+    ie[:, 0] = gd["inj_s"][idx]
+    out = []
+    for cta in (1, 0):
+        pkg.lib().tags_debug_solve_cta(cta)
+        try:
+            sol, info, st = pkg.hem_sweep(e, pkg.images(e), nodes, s, kappa, ie=ie, precision=pkg.MIXED,
+                                          max_batch=16)
+        finally:
+            pkg.lib().tags_debug_solve_cta(1)
+        assert np.all(info == 0) and st.fallbacks == 0
+        out.append((sol, st.max_iterations))
+    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+    assert np.max(np.abs(out[0][0][:, 0] - gd["u0"][idx]) / np.abs(gd["u0"][idx])) < 1e-6

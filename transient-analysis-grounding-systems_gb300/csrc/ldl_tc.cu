@@ -1131,17 +1131,28 @@ __global__ void __launch_bounds__(256) k_panel_planes(const float2* __restrict__
 
 // ---- solves with the factors: L D L^T x = b (one right-hand side per sample) ----------
 
+// A right-hand side whose first lead_zero rows are zero (the immittance
+// system's b = [I_E; 0; 0] in the order ZL, ZT, nodes) stays zero there
+// through the forward sweep, so the blocks that end at or before lead_zero
+// have nothing to do. Applies while *lead_step is 0 (the refinement's first
+// solve, whose right-hand side is b itself); later residuals are dense.
+TAGS_D bool lead_skip(const int* lead_step, int lead_zero, int block_end) {
+    return lead_step && block_end <= lead_zero && *lead_step == 0;
+}
+
 // z_b = Linv_b * r_b for block b (128 rows), or Linv_b^T * r_b with
 // transpose = 1, in place; one CTA of 512 threads per sample: four threads
 // per output row, each a quarter of the row, reading the stored copy whose
 // row index is contiguous across threads (the transpose of the one applied).
 __global__ void __launch_bounds__(512) k_blk_inv_apply(const float2* __restrict__ linv32, long long lstride, int blk,
                                                        int jb, float2* __restrict__ x0, long long xstride,
-                                                       int transpose, const int* __restrict__ active) {
+                                                       int transpose, const int* __restrict__ active,
+                                                       const int* __restrict__ lead_step, int lead_zero) {
     __shared__ float2 v[TB];
     __shared__ float2 part[4][TB];
     const int smp = blockIdx.x, tid = threadIdx.x, r = tid & (TB - 1), qt = tid >> 7;
     if (active && !active[smp]) return;              // the sample has finished refining
+    if (lead_skip(lead_step, lead_zero, blk * TB + jb)) return;
     float2* x = x0 + xstride * smp + (long long)blk * TB;
     // M[r][k] is at Mt[k * TB + r]: Mt = Linv^T (row-major) for z = Linv r, Linv for z = Linv^T r
     const float2* Mt = linv32 + lstride * smp + (long long)blk * 2 * TB * TB + (transpose ? 0 : TB * TB);
@@ -1169,10 +1180,12 @@ __global__ void __launch_bounds__(512) k_blk_inv_apply(const float2* __restrict_
 // a thread per row, 16 loads in flight, the block's x in shared memory
 __global__ void __launch_bounds__(128) k_blk_fwd_update(const float2* __restrict__ A0, long long ld, long long mstride,
                                                         int N, int j0, int jb, float2* __restrict__ x0,
-                                                        long long xstride, int zl_m, const int* __restrict__ active) {
+                                                        long long xstride, int zl_m, const int* __restrict__ active,
+                                                        const int* __restrict__ lead_step, int lead_zero) {
     __shared__ float2 xs[TB];
     const int smp = blockIdx.y;
     if (active && !active[smp]) return;
+    if (lead_skip(lead_step, lead_zero, j0 + jb)) return;
     float2* x = x0 + xstride * smp;
     if ((int)threadIdx.x < jb) xs[threadIdx.x] = x[j0 + threadIdx.x];
     __syncthreads();
@@ -1253,6 +1266,138 @@ __global__ void k_diag_scale(const float2* __restrict__ A0, long long ld, long l
     if (i >= N) return;
     const float2 d = A0[mstride * smp + i + ld * (long long)i];
     x0[xstride * smp + i] = fmulc(x0[xstride * smp + i], crecip_f(d));
+}
+
+// 1: solves with k_ldl_solve_cta where x fits in shared memory; 0: the
+// per-block kernels (tags_debug_solve_cta)
+static int g_solve_cta = 1;
+
+// The whole solve of one sample (forward sweep, D, backward sweep) in one CTA
+// of SOLVE_THREADS threads, x held in shared memory: one launch per solve, no
+// grid-wide step between the blocks, and each SM keeps 16 loads per thread of
+// L in flight. Every sum is formed in the same order as in the per-block
+// kernels above (k_blk_inv_apply, k_blk_fwd_update, k_diag_scale,
+// k_blk_bwd_update), so both paths give identical results. Dynamic shared
+// memory: v (TB), part (4 TB), x (N) complex values.
+constexpr int SOLVE_THREADS = 1024;
+constexpr int SOLVE_SMEM_MAX = 200 * 1024;
+
+__global__ void __launch_bounds__(SOLVE_THREADS, 1) k_ldl_solve_cta(
+    const float2* __restrict__ A0, long long ld, long long mstride, int N, const float2* __restrict__ linv32,
+    long long lstride, float2* __restrict__ x0, long long xstride, int zl_m, const int* __restrict__ active,
+    const int* __restrict__ lead_step, int lead_zero) {
+    extern __shared__ float2 solve_sm[];
+    float2* v = solve_sm;                          // the current block of x, zero beyond jb
+    float2* part = solve_sm + TB;                  // 4 x TB partial sums of the block-inverse products
+    float2* xs = solve_sm + 5 * TB;                // x
+    const int smp = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (active && !active[smp]) return;            // the sample has finished refining
+    const float2* A = A0 + mstride * smp;
+    const float2* Lv = linv32 + lstride * smp;
+    float2* x = x0 + xstride * smp;
+    const int nblk = (N + TB - 1) / TB;
+    const int b0 = lead_step && *lead_step == 0 ? lead_zero / TB : 0;
+    for (int i = tid; i < N; i += SOLVE_THREADS) xs[i] = x[i];
+    __syncthreads();
+    // z_b = M x_b for the block inverse M (M[r][k] at Mt[k TB + r]), as k_blk_inv_apply
+    auto inv_apply = [&](const float2* Mt, int j0, int jb) {
+        if (tid < TB) v[tid] = tid < jb ? xs[j0 + tid] : make_float2(0.f, 0.f);
+        __syncthreads();
+        if (tid < 4 * TB) {
+            const int r = tid & (TB - 1), qt = tid >> 7, k0 = 32 * qt;
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float2 w[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) w[q] = Mt[(long long)(k0 + 16 * h + q) * TB + r];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc = ffmac(w[q], v[k0 + 16 * h + q], acc);
+            }
+            part[qt * TB + r] = acc;
+        }
+        __syncthreads();
+        if (tid < jb) {
+            const float2 a = part[tid], b = part[TB + tid], c = part[2 * TB + tid], d = part[3 * TB + tid];
+            xs[j0 + tid] = make_float2((a.x + b.x) + (c.x + d.x), (a.y + b.y) + (c.y + d.y));
+        }
+        __syncthreads();
+    };
+    // forward: L y = b
+    for (int b = b0; b < nblk; ++b) {
+        const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
+        inv_apply(Lv + (long long)b * 2 * TB * TB + TB * TB, j0, jb);
+        // rows below the block, as k_blk_fwd_update; while the block lies in
+        // the ZL columns the ZT rows are skipped (L[ZT rows, ZL cols] = 0)
+        const int i_lo = j0 + jb;
+        const bool band = i_lo <= zl_m;
+        const int nhead = band ? zl_m - i_lo : N - i_lo;               // rows before the band (or all)
+        const int nrows = band ? nhead + (N - 2 * zl_m) : N - i_lo;
+        for (int t = tid; t < nrows; t += SOLVE_THREADS) {
+            const int i = t < nhead ? i_lo + t : 2 * zl_m + (t - nhead);
+            const float2* Ai = A + i + ld * (long long)j0;
+            float2 acc = make_float2(0.f, 0.f);
+            int k = 0;
+            for (; k + 16 <= jb; k += 16) {
+                float2 w[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) w[q] = Ai[ld * (long long)(k + q)];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc = ffmac(w[q], xs[j0 + k + q], acc);
+            }
+            for (; k < jb; ++k) acc = ffmac(Ai[ld * (long long)k], xs[j0 + k], acc);
+            xs[i] = fsub(xs[i], acc);
+        }
+        __syncthreads();
+    }
+    // x /= D, as k_diag_scale
+    for (int i = tid; i < N; i += SOLVE_THREADS) xs[i] = fmulc(xs[i], crecip_f(A[i + ld * (long long)i]));
+    __syncthreads();
+    // backward: L^T x = y
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
+        inv_apply(Lv + (long long)b * 2 * TB * TB, j0, jb);
+        if (j0 == 0) break;
+        if (tid < TB) v[tid] = tid < jb ? xs[j0 + tid] : make_float2(0.f, 0.f);
+        __syncthreads();
+        // rows above the block, as k_blk_bwd_update: a warp per 4 consecutive r
+        const bool zero_cols = j0 >= zl_m && j0 + jb <= 2 * zl_m;   // L[ZT rows, ZL cols] = 0
+        for (int r0 = 4 * warp; r0 < j0; r0 += 4 * (SOLVE_THREADS / 32)) {
+            float2 acc[4];
+            float2 w[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                acc[q] = make_float2(0.f, 0.f);
+                const int r = r0 + q;
+                const float2* col = A + ld * (long long)r + j0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int c = lane + 32 * t;
+                    w[q][t] = r < j0 && c < jb && !(zero_cols && r < zl_m) ? col[c] : make_float2(0.f, 0.f);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int t = 0; t < 4; ++t) acc[q] = ffmac(w[q][t], v[lane + 32 * t], acc[q]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc[q].x += __shfl_xor_sync(0xffffffffu, acc[q].x, o);
+                    acc[q].y += __shfl_xor_sync(0xffffffffu, acc[q].y, o);
+                }
+            if (lane < 4) {
+                const int r = r0 + lane;
+                float2 a = acc[0];
+#pragma unroll
+                for (int q = 1; q < 4; ++q)
+                    if (lane == q) a = acc[q];
+                if (r < j0 && !(zero_cols && r < zl_m)) xs[r] = fsub(xs[r], a);
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = tid; i < N; i += SOLVE_THREADS) x[i] = xs[i];
 }
 
 // ---- host side ---------------------------------------------------------------------
@@ -1386,6 +1531,9 @@ int tags_ldl_tc_prepare() {
         if (!rc && cudaFuncSetAttribute(k_ldl_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(TB * DIAG_LD * sizeof(float2))) != cudaSuccess)
             rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_ldl_diag) failed");
+        if (!rc && cudaFuncSetAttribute(k_ldl_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        SOLVE_SMEM_MAX) != cudaSuccess)
+            rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_ldl_solve_cta) failed");
         if (!rc && !encode_fn()) rc = tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
     });
     return rc;
@@ -1439,25 +1587,36 @@ static int launch_gemm(int NS, const CUtensorMap& mA, const CUtensorMap& mB, con
 }
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
-                     float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active) {
+                     float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active,
+                     const int* lead_step, int lead_zero) {
+    if (int e0 = tags_ldl_tc_prepare()) return e0;
     const float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
     const int nblk = (N + TB - 1) / TB;
     int pf = tags_prof_begin(TAGS_PROF_LDL_SOLVE, st);
+    const size_t smem = sizeof(float2) * (5 * TB + (size_t)N);
+    if (g_solve_cta && smem <= (size_t)SOLVE_SMEM_MAX) {
+        k_ldl_solve_cta<<<nb, SOLVE_THREADS, smem, st>>>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active,
+                                                         lead_step, lead_zero);
+        tags_note_launch();
+        tags_prof_end(TAGS_PROF_LDL_SOLVE, pf, st, 8.0 * N * (double)N * nb, 8.0 * N * (double)N * nb);
+        TAGS_CUDA_OK(cudaGetLastError());
+        return 0;
+    }
     for (int b = 0; b < nblk; ++b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 0, active);
+        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 0, active, lead_step, lead_zero);
         const int rest = N - j0 - jb;
         if (rest > 0)
             k_blk_fwd_update<<<dim3((rest + 127) / 128, nb), 128, 0, st>>>(A, ld, mstride, N, j0, jb, x, xstride, zl_m,
-                                                                         active);
+                                                                         active, lead_step, lead_zero);
         tags_note_launch(rest > 0 ? 2 : 1);
     }
     k_diag_scale<<<dim3((N + 255) / 256, nb), 256, 0, st>>>(A, ld, mstride, N, x, xstride, active);
     tags_note_launch();
     for (int b = nblk - 1; b >= 0; --b) {
         const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
-        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 1, active);
+        k_blk_inv_apply<<<nb, 512, 0, st>>>(L32, ls, b, jb, x, xstride, 1, active, nullptr, 0);
         if (j0 > 0)
             k_blk_bwd_update<<<dim3((j0 + 31) / 32, nb), 256, 0, st>>>(A, ld, mstride, j0, jb, x, xstride, zl_m,
                                                                      active);
@@ -1645,6 +1804,11 @@ static int g_debug_pairs = 0;     // tags_debug_ldl*: mode-0 updates on two-SM c
 
 extern "C" int tags_debug_tc_pairs(int on) {
     g_debug_pairs = on ? 1 : 0;
+    return 0;
+}
+
+extern "C" int tags_debug_solve_cta(int on) {
+    g_solve_cta = on ? 1 : 0;
     return 0;
 }
 

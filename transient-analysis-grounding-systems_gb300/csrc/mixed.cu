@@ -20,9 +20,13 @@
 //      (sparse, +-1 / 0.5) in FP64 and the impedance blocks times x in
 //      two-float arithmetic (about 2^-44 relative), the correction from the
 //      FP32 factors; a sample stops once its predicted error is below the
-//      tolerance (1e-9 |x|) or its corrections stop shrinking. The stopping decision runs on the device
-//      (k_ir_decide), so one refinement step is a fixed launch sequence that a
-//      CUDA graph repeats under a conditional while-node;
+//      tolerance (1e-9 |x|) or its corrections stop shrinking. The stopping
+//      decision runs on the device (k_ir_decide) after each correction and
+//      before the residual, which only the samples that go on then form; one
+//      refinement step is a fixed launch sequence that a CUDA graph repeats
+//      under a conditional while-node. The first step's right-hand side is b,
+//      zero in the impedance rows, and its forward sweep starts at the node
+//      rows;
 //   5. samples that do not converge are re-solved by the plain FP64 path
 //      (LU with partial pivoting).
 #include <algorithm>
@@ -140,7 +144,7 @@ __global__ void k_ir_rhs(const double2* __restrict__ r, const double* __restrict
                          float2* __restrict__ rf, double* __restrict__ norms, double* __restrict__ dots) {
     const int N = n + 2 * m;
     int ip = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
-    if (blockIdx.x == 0 && threadIdx.x < 3) norms[4 * b + threadIdx.x] = 0.0;
+    if (blockIdx.x == 0 && threadIdx.x < 2) norms[4 * b + threadIdx.x] = 0.0;
     if (blockIdx.x == 0 && threadIdx.x < 4) dots[4 * b + threadIdx.x] = 0.0;
     if (ip >= N) return;
     double2 v = r[(size_t)b * N + orig_of(ip, m, n)];
@@ -476,38 +480,53 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
     s.extr[q] = -10;
 }
 
-// After a refinement step: per sample, stop on ir_converged (the correction
-// times the measured contraction predicts an error under the tolerance), or
-// once it stops shrinking (accepted when the backward error is below 1e-12);
-// NaN goes to the fallback. One CTA. Sets the continue
-// flag and, inside a graph, the while-node condition.
-__global__ void __launch_bounds__(1024) k_ir_decide(const double* __restrict__ norms, int nb, int max_steps, IrState s,
+// After a step's correction, before its residual: per sample, stop on
+// ir_converged (the correction times the measured contraction predicts an
+// error under the tolerance), or once the corrections stop shrinking
+// (accepted when the backward error is below 1e-12); NaN goes to the
+// fallback. Samples that stop here skip the residual of their final iterate:
+// the backward error kept is that of the iterate before the final correction
+// (norms[2] / (|W| norms[3]), formed by the previous step's residual), which
+// the correction then shrinks by about the measured contraction. For samples
+// that go on, norms[2] is cleared for this step's residual and norms[3] takes
+// |x|. One CTA. Sets the continue flag and, inside a graph, the while-node
+// condition.
+__global__ void __launch_bounds__(1024) k_ir_decide(double* __restrict__ norms, int nb, int max_steps, IrState s,
                                                     cudaGraphConditionalHandle cond, int set_cond) {
     const int step = *s.step;
     int any = 0;
     for (int q = threadIdx.x; q < nb; q += blockDim.x) {
         if (!s.active[q]) continue;
         s.iters[q] = step + 1;
-        const double dx = norms[4 * q + 0], xn = norms[4 * q + 1], rn = norms[4 * q + 2];
-        const double be = rn / (s.wnorm[q] * xn + 1e-300);
+        const double dx = norms[4 * q + 0], xn = norms[4 * q + 1];
+        // step 0 starts from x = 0: no residual of an earlier iterate yet
+        const double be = step >= 1 ? norms[4 * q + 2] / (s.wnorm[q] * norms[4 * q + 3] + 1e-300) : 0.0;
         s.berr[q] = be;
         if (!(dx == dx) || !(xn == xn)) { s.active[q] = 0; continue; }
+        bool more = true;
         if (s.extr[q] == step) {
             // extrapolated in this step: x moved by more than dx; the next
             // step measures its error against the mode's contraction
             s.prev_dx[q] = -s.lam[q];
+        } else {
+            const double pdx = s.prev_dx[q];
+            if (ir_converged(step, dx, xn, pdx, s.tol)) {
+                s.active[q] = 0;
+                s.conv[q] = 1;
+                more = false;
+            } else if (step >= 2 && pdx > 0.0 && dx > 0.5 * pdx) {
+                s.conv[q] = be <= 1e-12;
+                s.active[q] = 0;
+                more = false;
+            } else {
+                s.prev_dx[q] = dx;
+            }
+        }
+        if (more) {
+            norms[4 * q + 2] = 0.0;
+            norms[4 * q + 3] = xn;
             any = 1;
-            continue;
         }
-        const double pdx = s.prev_dx[q];
-        if (ir_converged(step, dx, xn, pdx, s.tol)) { s.active[q] = 0; s.conv[q] = 1; continue; }
-        if (step >= 2 && pdx > 0.0 && dx > 0.5 * pdx) {
-            s.conv[q] = be <= 1e-12;
-            s.active[q] = 0;
-            continue;
-        }
-        s.prev_dx[q] = dx;
-        any = 1;
     }
     any = __syncthreads_or(any);
     if (threadIdx.x == 0) {
@@ -681,8 +700,9 @@ int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st) {
     return 0;
 }
 
-// One refinement step: correction from the factors, x update, residual,
-// stopping decision. A fixed launch sequence (graph-capturable).
+// One refinement step: correction from the factors, x update, stopping
+// decision, residual of the new iterate for the samples that go on. A fixed
+// launch sequence (graph-capturable).
 int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditionalHandle cond, int set_cond) {
     const int m = p->m, n = p->n, N = p->N;
     const size_t NN = (size_t)N * N;
@@ -691,12 +711,16 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     dim3 gv((N + 255) / 256, nb);
     k_ir_rhs<<<gv, 256, 0, st>>>(p->d_r, p->d_scale, m, n, p->d_rf, p->d_norms, p->d_dots);
     tags_note_launch();
-    // samples that stopped refining skip the sweeps (their x is left alone)
-    int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st, s.active);
+    // samples that stopped refining skip the sweeps (their x is left alone);
+    // the first step's right-hand side is b, zero in the 2m impedance rows
+    // that the order ZL, ZT, nodes puts first
+    int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st, s.active,
+                               s.step, 2 * m);
     if (err) return err;
     k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active, p->d_yprev, p->d_dots,
                                     s.step);
     k_ir_extrap<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, p->d_dots, s);
+    k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, std::min(p->max_steps, kMaxSteps), s, cond, set_cond);
     int pf = tags_prof_begin(TAGS_PROF_RESID, st);
     k_residual_nodes<<<dim3((n + 255) / 256, nb), 256, 0, st>>>(p->inc, m, n, d_b, p->d_x, p->d_r, p->d_norms,
                                                                 s.active);
@@ -705,7 +729,6 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
                                                                 p->d_norms, s.active);
     // 2 m^2 complex products (4 real multiply-adds each) and a read of Z in FP32
     tags_prof_end(TAGS_PROF_RESID, pf, st, 16.0 * m * (double)m * nb, 16.0 * m * (double)m * nb);
-    k_ir_decide<<<1, 1024, 0, st>>>(p->d_norms, nb, std::min(p->max_steps, kMaxSteps), s, cond, set_cond);
     tags_note_launch(5);
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;

@@ -145,8 +145,12 @@ size_t tags_ldl_tc_workspace(int N, int batch);
 int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws, int* info,
                 int* err, int zl_m, int pieces, int group_panels, cudaStream_t st, int pairs);
 // active (optional, per sample): samples whose flag is 0 are skipped.
+// lead_step (optional, device): while *lead_step is 0 the right-hand sides are
+// zero in their first lead_zero rows, and the forward sweep starts at the
+// first block that reaches past them.
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
-                     float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active = nullptr);
+                     float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active = nullptr,
+                     const int* lead_step = nullptr, int lead_zero = 0);
 
 // profile.cu: optional CUDA-event timing of kernel families
 enum {
