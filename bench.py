@@ -856,6 +856,8 @@ def main():
     ap.add_argument("--tc-pairs", type=int, default=-1,
                     help="trailing updates on two-SM clusters: 1 on, 0 off (-1 = the plan's default)")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
+    ap.add_argument("--solve-path", type=int, default=-1,
+                    help="triangular solves: 0 per block, 1 one CTA per sample, 2/4/8 clusters (-1 = default)")
     ap.add_argument("--ref-steps", type=int, default=4, help="cap on timed steps of the reference arm")
     ap.add_argument("--first-batch", type=int, default=0,
                     help="batch of samples the warm-up and timed steps start from (0 = the whole job in order)")
@@ -896,6 +898,8 @@ def main():
         plan.set_split(args.split)
     if mixed and args.tc_pairs >= 0:
         plan.set_tc_pairs(args.tc_pairs)
+    if args.solve_path != -1 and pkg.lib().tags_debug_solve_path(args.solve_path) != 0:
+        raise SystemExit(pkg.last_error())
     if P > 1:
         plan.set_pipelines(P)
     ns_total = len(s)

@@ -343,13 +343,14 @@ int tags_batch_create (tags_batch *batch, const tags_grid_job *jobs, size_t njob
 int tags_batch_run (tags_batch batch, const tags_grid_job *jobs, size_t njobs, tags_run_stats *stats);
 int tags_batch_destroy (tags_batch batch);
 
-/* Passes in flight (1 = default, or 2): with 2 the plan builds a twin of the
- * same geometry and settings (twice the device memory) and a run of several
- * passes gives every other pass to the twin, on its own stream from a second
- * host thread, so that one pass's latency-bound phases (diagonal blocks,
- * triangular sweeps, refinement steps) overlap the other's dense work. The
- * run's statistics cover both; its device time spans both streams. Going
- * back to 1 keeps the twin's memory until the plan is destroyed. */
+/* Passes in flight (1 = default, 2 or 3): with k > 1 the plan builds k - 1
+ * twins of the same geometry and settings (k times the device memory), and a
+ * run of several passes hands each pass to whichever pipeline frees up first,
+ * each twin on its own stream from its own host thread, so that one pass's
+ * latency-bound phases (diagonal blocks, triangular sweeps, refinement steps)
+ * overlap another's dense work. The run's statistics cover all of them; its
+ * device time spans all streams. Fewer pipelines later keep the twins' memory
+ * until the plan is destroyed. */
 int tags_plan_set_pipelines (tags_plan plan, int pipelines);
 
 /* Passes as CUDA graphs (default on): each pass shape (samples in the pass,
@@ -439,11 +440,15 @@ int tags_plan_set_tc_pairs (tags_plan plan, int on);
 int tags_debug_tc_pairs (int on);
 
 /* No counterpart in the reference. Test hook (process-wide, for passes and
- * graphs built afterwards): 1 (default) runs each triangular solve of the
- * mixed form as one CTA per sample with x in shared memory, where x fits;
- * 0 runs it block by block (two kernels per 128-row block and sweep). Both
- * form every sum in the same order and give identical results. */
-int tags_debug_solve_cta (int on);
+ * graphs built afterwards): how the mixed form's triangular solves run.
+ * 0: block by block (two kernels per 128-row block and sweep); 1: one CTA per
+ * sample with x in shared memory; 2, 4, 8: a cluster of that many CTAs per
+ * sample, x spread over their shared memory; -1 (default): the larger of
+ * the cluster sizes 4 and 2 with G x samples per pass <= SMs, else one CTA
+ * per sample. Paths 1..8
+ * need x in shared memory (N up to about 25000) and otherwise run block by
+ * block. All form every sum in the same order and give identical results. */
+int tags_debug_solve_path (int path);
 
 /* No counterpart in the reference. Caps the refinement steps of the mixed
  * form's passes (1 .. 40; 0 restores the default 40). A sample that has not

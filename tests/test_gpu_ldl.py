@@ -117,9 +117,10 @@ def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group, pairs)
 
 
 @pytest.mark.parametrize("N,zl_m", [(517, 0), (1000, 300), (1500, 400)])
-def test_one_cta_solve_equals_block_solve(gpu_pkg, N, zl_m):
-    """The solve as one CTA per sample (x in shared memory) and block by block
-    (two kernels per 128-row block and sweep) form every sum in the same order:
+def test_solve_paths_are_identical(gpu_pkg, N, zl_m):
+    """The solve block by block (two kernels per 128-row block and sweep), as
+    one CTA per sample, and on clusters of 2, 4 and 8 CTAs per sample (rows
+    spread over their shared memory) form every sum in the same order:
     identical results, partial last block and the zero ZL/ZT band included."""
     fn = gpu_pkg.lib().tags_debug_ldl_solve
     fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
@@ -128,15 +129,16 @@ def test_one_cta_solve_equals_block_solve(gpu_pkg, N, zl_m):
     rng = np.random.default_rng(N + 7 * zl_m)
     mats = np.stack([_banded_sym(rng, N, zl_m, d) for d in (4.0, 3.0)])
     rhs = rng.standard_normal((2, N)) + 1j * rng.standard_normal((2, N))
-    out = []
-    for cta in (1, 0):
+    out = {}
+    for path in (0, 1, 2, 4, 8):
         buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)
         x = rhs.copy()
-        gpu_pkg.lib().tags_debug_solve_cta(cta)
+        assert gpu_pkg.lib().tags_debug_solve_path(path) == 0
         try:
             code = fn(buf.ctypes.data, x.ctypes.data, N, 2, 16, zl_m, 4)
         finally:
-            gpu_pkg.lib().tags_debug_solve_cta(1)
+            gpu_pkg.lib().tags_debug_solve_path(-1)
         assert code == 0, gpu_pkg.last_error()
-        out.append(x)
-    assert np.array_equal(out[0], out[1])
+        out[path] = x
+    for path in (1, 2, 4, 8):
+        assert np.array_equal(out[path], out[0]), path

@@ -243,12 +243,14 @@ def test_batched_inverse_laplace_matches_single_series(gpu_pkg):
             assert rel_err(F[:, 0], gd[f"inv_{nt}_{filt}"]) < 4e-16 * nt * nt
 
 
+@pytest.mark.parametrize("pipes", [2, 3])
 @pytest.mark.parametrize("graphs", [True, False])
-def test_two_pipelines_match_one(gpu_pkg, graphs):
-    """A plan with two passes in flight (a twin plan takes every other pass on
-    its own stream, from a second host thread) gives the single-pipeline
-    solutions and statistics: config 2 grid, 72 samples in passes of 16 (five
-    passes, the last ragged), with graphs and kernel by kernel, host buffers."""
+def test_two_pipelines_match_one(gpu_pkg, graphs, pipes):
+    """A plan with two or three passes in flight (twin plans take passes as
+    they free up, each on its own stream from its own host thread) gives the
+    single-pipeline solutions and statistics: config 2 grid, 72 samples in
+    passes of 16 (five passes, the last ragged), with graphs and kernel by
+    kernel, host buffers."""
     pkg = gpu_pkg
     gd = golden("grid2.npz")
     e, nodes = gd["elec"], gd["nodes"]
@@ -260,9 +262,9 @@ def test_two_pipelines_match_one(gpu_pkg, graphs):
     plan = pkg.Plan(e, img, nodes, pkg.MIXED, max_batch=16, graphs=graphs)
     try:
         one, info1, st1 = plan.run(s, kappa, 1.0, ie)
-        plan.set_pipelines(2)
+        plan.set_pipelines(pipes)
         two, info2, st2 = plan.run(s, kappa, 1.0, ie)
-        plan.set_split(3)                       # settings follow to the twin
+        plan.set_split(3)                       # settings follow to the twins
         three, info3, _ = plan.run(s, kappa, 1.0, ie)
     finally:
         plan.close()
@@ -301,11 +303,12 @@ def test_two_sm_updates_match_single_sm(gpu_pkg):
         assert rel_err(out[1], out[0]) < 1e-12
 
 
-def test_one_cta_solves_match_block_solves_in_plans(gpu_pkg):
-    """The mixed form's refinement with its triangular solves as one CTA per
-    sample (x in shared memory) and block by block: identical solutions and
-    refinement counts (config 2 grid, 40 samples in passes of 16, CUDA graphs;
-    the first solve of each pass starts at the node rows in both)."""
+def test_solve_paths_match_in_plans(gpu_pkg):
+    """The mixed form's refinement with its triangular solves on clusters of
+    four CTAs per sample, one CTA per sample, and block by block: identical
+    solutions and refinement counts (config 2 grid, 40 samples in passes of
+    16, CUDA graphs; the first solve of each pass starts at the node rows in
+    all)."""
     pkg = gpu_pkg
     gd = golden("grid2.npz")
     e, nodes = gd["elec"], gd["nodes"]
@@ -314,14 +317,15 @@ def test_one_cta_solves_match_block_solves_in_plans(gpu_pkg):
     ie = np.zeros((len(idx), nodes.shape[0]), np.complex128)
     ie[:, 0] = gd["inj_s"][idx]
     out = []
-    for cta in (1, 0):
-        pkg.lib().tags_debug_solve_cta(cta)
+    for path in (4, 1, 0):
+        assert pkg.lib().tags_debug_solve_path(path) == 0
         try:
             sol, info, st = pkg.hem_sweep(e, pkg.images(e), nodes, s, kappa, ie=ie, precision=pkg.MIXED,
                                           max_batch=16)
         finally:
-            pkg.lib().tags_debug_solve_cta(1)
+            pkg.lib().tags_debug_solve_path(-1)
         assert np.all(info == 0) and st.fallbacks == 0
         out.append((sol, st.max_iterations))
-    assert np.array_equal(out[0][0], out[1][0]) and out[0][1] == out[1][1]
+    for sol, it in out[1:]:
+        assert np.array_equal(sol, out[0][0]) and it == out[0][1]
     assert np.max(np.abs(out[0][0][:, 0] - gd["u0"][idx]) / np.abs(gd["u0"][idx])) < 1e-6

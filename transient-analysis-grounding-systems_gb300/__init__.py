@@ -58,7 +58,7 @@ EXPORTS = (
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
-    "tags_debug_tc_pairs", "tags_debug_solve_cta", "tags_debug_mixed_fill", "tags_probe_fp64",
+    "tags_debug_tc_pairs", "tags_debug_solve_path", "tags_debug_mixed_fill", "tags_probe_fp64",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
     "tags_gpu_inlt", "tags_batch_create", "tags_batch_run", "tags_batch_destroy",
@@ -153,7 +153,7 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_refine_tol.argtypes = [_vp, ctypes.c_double]
             L.tags_plan_set_tc_pairs.argtypes = [_vp, ctypes.c_int]
             L.tags_debug_tc_pairs.argtypes = [ctypes.c_int]
-            L.tags_debug_solve_cta.argtypes = [ctypes.c_int]
+            L.tags_debug_solve_path.argtypes = [ctypes.c_int]
             L.tags_probe_fp64.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.tags_debug_tc_wait_limit.argtypes = [ctypes.c_longlong]
             L.tags_debug_mixed_fill.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _vp]
@@ -188,7 +188,7 @@ def lib() -> ctypes.CDLL:
                          "tags_plan_set_pipelines",
                          "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
                          "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol",
-                         "tags_plan_set_tc_pairs", "tags_debug_tc_pairs", "tags_debug_solve_cta",
+                         "tags_plan_set_tc_pairs", "tags_debug_tc_pairs", "tags_debug_solve_path",
                          "tags_debug_mixed_fill", "tags_probe_fp64",
                          "magnetic_potential", "electric_field", "tags_fields_batch", "tags_gpd_mhem_batch",
                          "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch", "tags_gpu_inlt",
@@ -693,7 +693,7 @@ class Plan:
         self.set_graphs(graphs)
 
     def set_pipelines(self, n):
-        """1 or 2 passes in flight (2: a twin plan takes every other pass)."""
+        """1, 2 or 3 passes in flight (k > 1: k - 1 twin plans take passes as they free up)."""
         _ret(lib().tags_plan_set_pipelines(self.handle, int(n)))
 
     def set_split(self, pieces):

@@ -1268,9 +1268,18 @@ __global__ void k_diag_scale(const float2* __restrict__ A0, long long ld, long l
     x0[xstride * smp + i] = fmulc(x0[xstride * smp + i], crecip_f(d));
 }
 
-// 1: solves with k_ldl_solve_cta where x fits in shared memory; 0: the
-// per-block kernels (tags_debug_solve_cta)
-static int g_solve_cta = 1;
+// How the triangular solves run (tags_debug_solve_path): 0 the per-block
+// kernels; 1 k_ldl_solve_cta (one CTA per sample); 2, 4, 8 k_ldl_solve_cl
+// (a cluster of that many CTAs per sample); -1 (default) the larger of the
+// cluster sizes 4 and 2 with G x samples <= SMs, else one CTA per sample: with
+// the SMs full, one CTA per sample already saturates HBM and clusters only add
+// barriers and waves (measured on the 1560-segment grid, 2048 samples in
+// passes of 128: solves 104 ms against 113, 134 and 209 ms for G = 2, 4, 8),
+// while a pass of few samples gets G SMs per sample (passes of 16: 51 ms with
+// one CTA, 35, 24 and 34 ms for G = 2, 4, 8; passes of 32: 39 ms, then 27, 20
+// and 41 ms). Paths 1.. need x in shared memory and fall back to the
+// per-block kernels where it does not fit.
+static int g_solve_path = -1;
 
 // The whole solve of one sample (forward sweep, D, backward sweep) in one CTA
 // of SOLVE_THREADS threads, x held in shared memory: one launch per solve, no
@@ -1400,6 +1409,165 @@ __global__ void __launch_bounds__(SOLVE_THREADS, 1) k_ldl_solve_cta(
     for (int i = tid; i < N; i += SOLVE_THREADS) x[i] = xs[i];
 }
 
+// The solve of one sample on a cluster of G CTAs (G = 2, 4 or 8): CTA g owns
+// the rows whose 32-row chunk index is g mod G, so for G = 4 it owns rows
+// 32 g .. 32 g + 31 of every 128-row block, and keeps them in its shared
+// memory. Per block and sweep: every CTA gathers the block's 128 values from
+// their owners (distributed shared memory), applies the block inverse to its
+// own rows, and after a cluster barrier gathers the new values and updates its
+// own rows outside the block. Each row's sums are formed in the order of the
+// per-block kernels (identical results); the tail steps of a refinement, with
+// few samples still active, get G SMs per sample instead of one. Shared
+// memory: v (TB), part (4 TB), x (N) complex values; the cluster barriers are
+// the hardware's (all CTAs of a cluster run the same sequence).
+template <int G>
+__global__ void __launch_bounds__(SOLVE_THREADS, 1) k_ldl_solve_cl(
+    const float2* __restrict__ A0, long long ld, long long mstride, int N, const float2* __restrict__ linv32,
+    long long lstride, float2* __restrict__ x0, long long xstride, int zl_m, const int* __restrict__ active,
+    const int* __restrict__ lead_step, int lead_zero) {
+    static_assert(G == 2 || G == 4 || G == 8, "cluster of 2, 4 or 8 CTAs");
+    extern __shared__ float2 solve_sm[];
+    float2* v = solve_sm;
+    float2* part = solve_sm + TB;
+    float2* xs = solve_sm + 5 * TB;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int g = (int)cluster_rank(), smp = blockIdx.x / G;
+    if (active && !active[smp]) return;            // the whole cluster: the sample has finished refining
+    const float2* A = A0 + mstride * smp;
+    const float2* Lv = linv32 + lstride * smp;
+    float2* x = x0 + xstride * smp;
+    const int nblk = (N + TB - 1) / TB;
+    const int b0 = lead_step && *lead_step == 0 ? lead_zero / TB : 0;
+    auto own = [&](int i) { return ((i >> 5) & (G - 1)) == g; };
+    for (int i = tid; i < N; i += SOLVE_THREADS)
+        if (own(i)) xs[i] = x[i];
+    __syncthreads();
+    // v = the block's values x[j0 ..), zero beyond jb, read from their owners
+    auto gather = [&](int j0, int jb) {
+        if (tid < TB) {
+            float2 val = make_float2(0.f, 0.f);
+            if (tid < jb) {
+                const int i = j0 + tid;
+                const uint32_t a = mapa_cta(smem_u32(xs + i), (uint32_t)((i >> 5) & (G - 1)));
+                asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(val.x), "=f"(val.y) : "r"(a) : "memory");
+            }
+            v[tid] = val;
+        }
+        __syncthreads();
+    };
+    // own rows of z_b = M v (M[r][k] at Mt[k TB + r]), as k_blk_inv_apply:
+    // four quarter sums of 32 k each per row
+    auto inv_apply = [&](const float2* Mt, int j0, int jb) {
+        for (int t = tid; t < 4 * TB; t += SOLVE_THREADS) {
+            const int r = t & (TB - 1), qt = t >> 7, k0 = 32 * qt;
+            if (!own(j0 + r)) continue;
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                float2 w[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) w[q] = Mt[(long long)(k0 + 16 * h + q) * TB + r];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc = ffmac(w[q], v[k0 + 16 * h + q], acc);
+            }
+            part[qt * TB + r] = acc;
+        }
+        __syncthreads();
+        if (tid < jb && own(j0 + tid)) {
+            const float2 a = part[tid], b = part[TB + tid], c = part[2 * TB + tid], d = part[3 * TB + tid];
+            xs[j0 + tid] = make_float2((a.x + b.x) + (c.x + d.x), (a.y + b.y) + (c.y + d.y));
+        }
+        __syncthreads();
+    };
+    // forward: L y = b
+    for (int b = b0; b < nblk; ++b) {
+        const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
+        cluster_sync_all();                        // the block's rows are updated by all earlier blocks
+        gather(j0, jb);
+        inv_apply(Lv + (long long)b * 2 * TB * TB + TB * TB, j0, jb);
+        cluster_sync_all();                        // every owner has applied the block inverse
+        gather(j0, jb);
+        // own rows below the block, as k_blk_fwd_update (ZT rows skipped while
+        // the block lies in the ZL columns)
+        const int i_lo = j0 + jb;
+        const bool band = i_lo <= zl_m;
+        int c0 = i_lo >> 5;
+        c0 += (g - (c0 & (G - 1)) + G) & (G - 1);  // first own chunk at or after i_lo's
+        for (int c = c0 + G * warp; 32 * c < N; c += G * (SOLVE_THREADS / 32)) {
+            const int i = 32 * c + lane;
+            if (i >= N || i < i_lo || (band && i >= zl_m && i < 2 * zl_m)) continue;
+            const float2* Ai = A + i + ld * (long long)j0;
+            float2 acc = make_float2(0.f, 0.f);
+            int k = 0;
+            for (; k + 16 <= jb; k += 16) {
+                float2 w[16];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) w[q] = Ai[ld * (long long)(k + q)];
+#pragma unroll
+                for (int q = 0; q < 16; ++q) acc = ffmac(w[q], v[k + q], acc);
+            }
+            for (; k < jb; ++k) acc = ffmac(Ai[ld * (long long)k], v[k], acc);
+            xs[i] = fsub(xs[i], acc);
+        }
+    }
+    __syncthreads();
+    // own rows /= D, as k_diag_scale
+    for (int i = tid; i < N; i += SOLVE_THREADS)
+        if (own(i)) xs[i] = fmulc(xs[i], crecip_f(A[i + ld * (long long)i]));
+    __syncthreads();
+    // backward: L^T x = y
+    for (int b = nblk - 1; b >= 0; --b) {
+        const int j0 = b * TB, jb = N - j0 < TB ? N - j0 : TB;
+        cluster_sync_all();                        // the block's rows are updated by all later blocks
+        gather(j0, jb);
+        inv_apply(Lv + (long long)b * 2 * TB * TB, j0, jb);
+        cluster_sync_all();
+        if (j0 == 0) break;
+        gather(j0, jb);
+        // own rows above the block, as k_blk_bwd_update: a warp per 4
+        // consecutive rows, 8 groups per own chunk
+        const bool zero_cols = j0 >= zl_m && j0 + jb <= 2 * zl_m;   // L[ZT rows, ZL cols] = 0
+        const int ngroups = 8 * ((j0 / 32 - g + G - 1) / G);        // own chunks below j0, 8 groups each
+        for (int q_idx = warp; q_idx < ngroups; q_idx += SOLVE_THREADS / 32) {
+            const int r0 = 32 * (g + G * (q_idx >> 3)) + 4 * (q_idx & 7);
+            float2 acc[4];
+            float2 w[4][4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                acc[q] = make_float2(0.f, 0.f);
+                const int r = r0 + q;
+                const float2* col = A + ld * (long long)r + j0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int c = lane + 32 * t;
+                    w[q][t] = r < j0 && c < jb && !(zero_cols && r < zl_m) ? col[c] : make_float2(0.f, 0.f);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+#pragma unroll
+                for (int t = 0; t < 4; ++t) acc[q] = ffmac(w[q][t], v[lane + 32 * t], acc[q]);
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                for (int o = 16; o > 0; o >>= 1) {
+                    acc[q].x += __shfl_xor_sync(0xffffffffu, acc[q].x, o);
+                    acc[q].y += __shfl_xor_sync(0xffffffffu, acc[q].y, o);
+                }
+            if (lane < 4) {
+                const int r = r0 + lane;
+                float2 a = acc[0];
+#pragma unroll
+                for (int q = 1; q < 4; ++q)
+                    if (lane == q) a = acc[q];
+                if (r < j0 && !(zero_cols && r < zl_m)) xs[r] = fsub(xs[r], a);
+            }
+        }
+    }
+    // the last cluster barrier followed every read of another CTA's x
+    for (int i = tid; i < N; i += SOLVE_THREADS)
+        if (own(i)) x[i] = xs[i];
+}
+
 // ---- host side ---------------------------------------------------------------------
 
 namespace {
@@ -1516,6 +1684,55 @@ static int set_gemm2_attr() {
     return 0;
 }
 
+// Cluster solves: shared-memory size and whether a cluster of G CTAs with the
+// largest shared memory fits at all (else the one-CTA solve runs).
+static bool g_solve_cl_ok[9] = {};
+
+template <int G>
+static int set_solve_cl_attr() {
+    TAGS_CUDA_OK(cudaFuncSetAttribute(k_ldl_solve_cl<G>, cudaFuncAttributeMaxDynamicSharedMemorySize, SOLVE_SMEM_MAX));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(SOLVE_THREADS);
+    cfg.dynamicSmemBytes = SOLVE_SMEM_MAX;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, (void*)k_ldl_solve_cl<G>, &cfg) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 0;
+    }
+    g_solve_cl_ok[G] = n > 0;
+    return 0;
+}
+
+template <int G>
+static int launch_solve_cl(const float2* A, long long ld, long long mstride, int N, const float2* L32, long long ls,
+                           float2* x, long long xstride, int zl_m, const int* active, const int* lead_step,
+                           int lead_zero, int nb, size_t smem, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(G * nb));
+    cfg.blockDim = dim3(SOLVE_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = G;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    TAGS_CUDA_OK(cudaLaunchKernelEx(&cfg, k_ldl_solve_cl<G>, A, ld, mstride, N, L32, ls, x, xstride, zl_m, active,
+                                    lead_step, lead_zero));
+    tags_note_launch();
+    return 0;
+}
+
 // Kernel attributes and the tensor-map encoder, set once per process before
 // any launch (and so before any graph capture).
 int tags_ldl_tc_prepare() {
@@ -1534,6 +1751,9 @@ int tags_ldl_tc_prepare() {
         if (!rc && cudaFuncSetAttribute(k_ldl_solve_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         SOLVE_SMEM_MAX) != cudaSuccess)
             rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_ldl_solve_cta) failed");
+        if (!rc) rc = set_solve_cl_attr<2>();
+        if (!rc) rc = set_solve_cl_attr<4>();
+        if (!rc) rc = set_solve_cl_attr<8>();
         if (!rc && !encode_fn()) rc = tags_fail(TAGS_E_CUDA, "cuTensorMapEncodeTiled is not available");
     });
     return rc;
@@ -1595,10 +1815,30 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     const int nblk = (N + TB - 1) / TB;
     int pf = tags_prof_begin(TAGS_PROF_LDL_SOLVE, st);
     const size_t smem = sizeof(float2) * (5 * TB + (size_t)N);
-    if (g_solve_cta && smem <= (size_t)SOLVE_SMEM_MAX) {
-        k_ldl_solve_cta<<<nb, SOLVE_THREADS, smem, st>>>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active,
-                                                         lead_step, lead_zero);
-        tags_note_launch();
+    int path = g_solve_path;
+    if (path < 0) {
+        path = 1;
+        for (int G = 4; G >= 2; G /= 2)
+            if ((long long)nb * G <= num_sms() && g_solve_cl_ok[G]) {
+                path = G;
+                break;
+            }
+    }
+    if (path >= 1 && smem <= (size_t)SOLVE_SMEM_MAX) {
+        int e = 0;
+        if (path >= 2 && g_solve_cl_ok[path]) {
+            e = path == 2   ? launch_solve_cl<2>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active, lead_step,
+                                                 lead_zero, nb, smem, st)
+                : path == 4 ? launch_solve_cl<4>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active, lead_step,
+                                                 lead_zero, nb, smem, st)
+                            : launch_solve_cl<8>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active, lead_step,
+                                                 lead_zero, nb, smem, st);
+        } else {
+            k_ldl_solve_cta<<<nb, SOLVE_THREADS, smem, st>>>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active,
+                                                             lead_step, lead_zero);
+            tags_note_launch();
+        }
+        if (e) return e;
         tags_prof_end(TAGS_PROF_LDL_SOLVE, pf, st, 8.0 * N * (double)N * nb, 8.0 * N * (double)N * nb);
         TAGS_CUDA_OK(cudaGetLastError());
         return 0;
@@ -1807,8 +2047,10 @@ extern "C" int tags_debug_tc_pairs(int on) {
     return 0;
 }
 
-extern "C" int tags_debug_solve_cta(int on) {
-    g_solve_cta = on ? 1 : 0;
+extern "C" int tags_debug_solve_path(int path) {
+    if (path != -1 && path != 0 && path != 1 && path != 2 && path != 4 && path != 8)
+        return tags_fail(TAGS_E_ARG, "tags_debug_solve_path: -1, 0, 1, 2, 4 or 8");
+    g_solve_path = path;
     return 0;
 }
 

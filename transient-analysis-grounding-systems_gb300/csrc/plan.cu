@@ -625,50 +625,56 @@ static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble*
     return 0;
 }
 
-// The twin follows the plan's settings (split, panels per update, samples per
-// pass, graphs, fill model) before it takes passes.
+// The twins (the plan's further pipelines, a chain p->twin->twin) follow the
+// plan's settings (split, panels per update, samples per pass, graphs, fill
+// model) before they take passes.
 static int sync_twin(tags_plan_s* p) {
-    tags_plan_s* t = p->twin;
-    if (t->split_pieces != p->split_pieces || t->group_panels != p->group_panels || t->pass_batch != p->pass_batch ||
-        t->max_steps != p->max_steps || t->ir_tol != p->ir_tol || t->tc_pairs != p->tc_pairs) {
-        t->split_pieces = p->split_pieces;
-        t->group_panels = p->group_panels;
-        t->pass_batch = p->pass_batch;
-        t->max_steps = p->max_steps;
-        t->ir_tol = p->ir_tol;
-        t->tc_pairs = p->tc_pairs;
-        tags_plan_drop_graphs(t);
+    for (tags_plan_s* t = p->twin; t; t = t->twin) {
+        if (t->split_pieces != p->split_pieces || t->group_panels != p->group_panels ||
+            t->pass_batch != p->pass_batch || t->max_steps != p->max_steps || t->ir_tol != p->ir_tol ||
+            t->tc_pairs != p->tc_pairs) {
+            t->split_pieces = p->split_pieces;
+            t->group_panels = p->group_panels;
+            t->pass_batch = p->pass_batch;
+            t->max_steps = p->max_steps;
+            t->ir_tol = p->ir_tol;
+            t->tc_pairs = p->tc_pairs;
+            tags_plan_drop_graphs(t);
+        }
+        t->use_graphs = p->use_graphs;
+        if (t->fill_model != p->fill_model)
+            if (int e = tags_plan_set_fill(t, p->fill_model)) return e;
     }
-    t->use_graphs = p->use_graphs;
-    if (t->fill_model != p->fill_model) return tags_plan_set_fill(t, p->fill_model);
     return 0;
 }
 
 extern "C" int tags_plan_set_pipelines(tags_plan plan, int pipelines) {
     tags_plan_s* p = plan;
     if (!p || p->twin == p) return tags_fail(TAGS_E_ARG, "tags_plan_set_pipelines: invalid plan");
-    if (pipelines != 1 && pipelines != 2) return tags_fail(TAGS_E_ARG, "tags_plan_set_pipelines: 1 or 2");
+    if (pipelines < 1 || pipelines > TAGS_MAX_PIPELINES)
+        return tags_fail(TAGS_E_ARG, "tags_plan_set_pipelines: 1, 2 or 3");
     TAGS_CUDA_OK(cudaSetDevice(p->device));
-    if (pipelines == 1) {           // the twin (if any) is kept for a later switch back
-        p->pipelines = 1;
-        return 0;
-    }
-    if (!p->twin) {
-        tags_plan t = nullptr;
-        const size_t m = (size_t)p->m, n = (size_t)p->n;
-        int err = tags_plan_create(&t, reinterpret_cast<const Electrode*>(p->h_elec.data()),
-                                   p->h_img.empty() ? nullptr : reinterpret_cast<const Electrode*>(p->h_img.data()), m,
-                                   p->h_nodes.data(), n, p->precision, (size_t)p->batch);
-        if (err) return err;
-        if (t->batch != p->batch) {
-            plan_free(t);
-            return tags_fail(TAGS_E_NOMEM, "tags_plan_set_pipelines: no room for a second pipeline of the same batch");
+    // twins beyond the count asked for are kept for a later switch back
+    tags_plan_s* last = p;
+    for (int k = 1; k < pipelines; ++k) {
+        if (!last->twin) {
+            tags_plan t = nullptr;
+            const size_t m = (size_t)p->m, n = (size_t)p->n;
+            int err = tags_plan_create(&t, reinterpret_cast<const Electrode*>(p->h_elec.data()),
+                                       p->h_img.empty() ? nullptr : reinterpret_cast<const Electrode*>(p->h_img.data()),
+                                       m, p->h_nodes.data(), n, p->precision, (size_t)p->batch);
+            if (err) return err;
+            if (t->batch != p->batch) {
+                plan_free(t);
+                return tags_fail(TAGS_E_NOMEM,
+                                 "tags_plan_set_pipelines: no room for another pipeline of the same batch");
+            }
+            last->twin = t;
         }
-        p->twin = t;
-        err = sync_twin(p);
-        if (err) return err;
+        last = last->twin;
     }
-    p->pipelines = 2;
+    if (int err = sync_twin(p)) return err;
+    p->pipelines = pipelines;
     return 0;
 }
 
@@ -688,45 +694,56 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_status, 0, sizeof(int) * 4, st));
     const size_t per_pass = p->pass_batch > 0 && p->pass_batch < p->batch ? p->pass_batch : p->batch;
     const size_t passes = (ns + per_pass - 1) / per_pass;
-    const bool two = p->twin && p->pipelines == 2 && passes >= 2;
-    if (two) {
+    // the pipelines that take passes: the plan and its first twins
+    std::vector<tags_plan_s*> pl{p};
+    for (tags_plan_s* t = p->twin; t && (int)pl.size() < p->pipelines && pl.size() < passes; t = t->twin)
+        pl.push_back(t);
+    if (pl.size() > 1) {
         if (int e = sync_twin(p)) return e;
-        TAGS_CUDA_OK(cudaMemsetAsync(p->twin->d_status, 0, sizeof(int) * 4, p->twin->stream));
+        for (size_t k = 1; k < pl.size(); ++k)
+            TAGS_CUDA_OK(cudaMemsetAsync(pl[k]->d_status, 0, sizeof(int) * 4, pl[k]->stream));
     }
     TAGS_CUDA_OK(cudaEventRecord(p->ev0, st));
     int err = 0;
     std::atomic<size_t> next{0};
-    if (two) {
-        // the twin takes passes on its own stream from a second host thread; it
-        // starts after ev0 so the run's device time spans both
-        tags_plan_s* t = p->twin;
-        TAGS_CUDA_OK(cudaStreamWaitEvent(t->stream, p->ev0, 0));
-        int err2 = 0;
-        std::thread th([&] {
-            if (cudaSetDevice(t->device) != cudaSuccess) {
-                err2 = TAGS_E_CUDA;
-                return;
-            }
-            err2 = run_passes(t, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &acc2);
-            if (!err2 && cudaEventRecord(t->ev1, t->stream) != cudaSuccess) err2 = TAGS_E_CUDA;
-        });
+    if (pl.size() > 1) {
+        // each twin takes passes on its own stream from its own host thread;
+        // they start after ev0 so the run's device time spans them all
+        std::vector<tags_run_stats> accs(pl.size());
+        std::vector<int> errs(pl.size(), 0);
+        std::vector<std::thread> th;
+        for (size_t k = 1; k < pl.size(); ++k) {
+            tags_plan_s* t = pl[k];
+            TAGS_CUDA_OK(cudaStreamWaitEvent(t->stream, p->ev0, 0));
+        }
+        for (size_t k = 1; k < pl.size(); ++k) {
+            tags_plan_s* t = pl[k];
+            th.emplace_back([&, k, t] {
+                if (cudaSetDevice(t->device) != cudaSuccess) {
+                    errs[k] = TAGS_E_CUDA;
+                    return;
+                }
+                errs[k] = run_passes(t, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &accs[k]);
+                if (!errs[k] && cudaEventRecord(t->ev1, t->stream) != cudaSuccess) errs[k] = TAGS_E_CUDA;
+            });
+        }
         err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &acc);
-        th.join();
-        if (!err) err = err2;
-        if (!err) {
-            TAGS_CUDA_OK(cudaStreamWaitEvent(st, t->ev1, 0));
-            acc.max_iterations = std::max(acc.max_iterations, acc2.max_iterations);
-            acc.max_backward_error = std::max(acc.max_backward_error, acc2.max_backward_error);
-            acc.fallbacks += acc2.fallbacks;
+        for (auto& h : th) h.join();
+        for (size_t k = 1; k < pl.size() && !err; ++k) err = errs[k];
+        for (size_t k = 1; k < pl.size() && !err; ++k) {
+            TAGS_CUDA_OK(cudaStreamWaitEvent(st, pl[k]->ev1, 0));
+            acc.max_iterations = std::max(acc.max_iterations, accs[k].max_iterations);
+            acc.max_backward_error = std::max(acc.max_backward_error, accs[k].max_backward_error);
+            acc.fallbacks += accs[k].fallbacks;
         }
     } else {
         err = run_passes(p, s, kappa, mur, ns, ie, inj_node, sol, info, flags, per_pass, &next, &acc);
     }
     if (err) return err;
     TAGS_CUDA_OK(cudaEventRecord(p->ev1, st));
-    int status[2] = {0, 0};
-    TAGS_CUDA_OK(cudaMemcpyAsync(&status[0], p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
-    if (two) TAGS_CUDA_OK(cudaMemcpyAsync(&status[1], p->twin->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    int status[TAGS_MAX_PIPELINES] = {0};
+    for (size_t k = 0; k < pl.size(); ++k)
+        TAGS_CUDA_OK(cudaMemcpyAsync(&status[k], pl[k]->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaStreamSynchronize(st));
     if (stats) {
         *stats = acc;
@@ -735,7 +752,8 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
         stats->seconds = ms * 1e-3;
         stats->split = p->precision == TAGS_PLAIN_FP64 ? 0 : p->split_pieces;
     }
-    const int stt = status[0] | status[1];
+    int stt = 0;
+    for (int k = 0; k < TAGS_MAX_PIPELINES; ++k) stt |= status[k];
     if (stt & TAGS_ST_DEGENERATE_PAIR)
         return tags_fail(TAGS_E_GEOMETRY, "coincident or overlapping segments: the pair integral diverges");
     if (stt & TAGS_ST_NONFINITE) return tags_fail(TAGS_E_NONFINITE, "non-finite value in the impedance fill");

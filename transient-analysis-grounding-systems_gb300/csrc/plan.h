@@ -38,6 +38,8 @@ struct Incidence {
     int nnz = 0;
 };
 
+constexpr int TAGS_MAX_PIPELINES = 3;     // passes in flight per plan
+
 struct tags_plan_s {
     int device = -1;
     int precision = 0;
@@ -107,10 +109,11 @@ struct tags_plan_s {
     // host copy of the geometry (11 doubles per segment; nodes 3 per node), so
     // a twin plan can be built from it
     std::vector<double> h_elec, h_img, h_nodes;
-    // second pipeline (tags_plan_set_pipelines): a plan of the same geometry
-    // and settings on its own stream; runs take every other pass
+    // further pipelines (tags_plan_set_pipelines): a chain of plans of the
+    // same geometry and settings, each on its own stream; a run's passes go to
+    // whichever pipeline frees up first
     tags_plan_s* twin = nullptr;
-    int pipelines = 1;
+    int pipelines = 1;                  // 1 .. TAGS_MAX_PIPELINES
 };
 
 int tags_plan_run_plain(tags_plan_s* p, const double2* d_s_unused, int nb, cudaStream_t st);
