@@ -303,25 +303,28 @@ def test_two_sm_updates_match_single_sm(gpu_pkg):
         assert rel_err(out[1], out[0]) < 1e-12
 
 
-def test_solve_paths_match_in_plans(gpu_pkg):
-    """The mixed form's refinement with its triangular solves on clusters of
-    four CTAs per sample, one CTA per sample, and block by block: identical
-    solutions and refinement counts (config 2 grid, 40 samples in passes of
-    16, CUDA graphs; the first solve of each pass starts at the node rows in
-    all)."""
+@pytest.mark.parametrize("count,per_pass", [(40, 16), (200, 100)])
+def test_solve_paths_match_in_plans(gpu_pkg, count, per_pass):
+    """The mixed form's refinement with its triangular solves chosen by pass
+    size (the default: clusters of four CTAs per sample for passes of 16; for
+    passes of 100 one CTA per sample, and clusters of four per sample in the
+    steps with at most SMs / 4 samples left), on clusters of four, one CTA per
+    sample, and block by block: identical solutions and refinement counts
+    (config 2 grid, CUDA graphs; the first solve of each pass starts at the
+    node rows in all)."""
     pkg = gpu_pkg
     gd = golden("grid2.npz")
     e, nodes = gd["elec"], gd["nodes"]
-    idx = np.linspace(0, len(gd["s"]) - 1, 40).astype(int)
+    idx = np.linspace(0, len(gd["s"]) - 1, count).astype(int)
     s, kappa = gd["s"][idx], gd["kappa"][idx]
     ie = np.zeros((len(idx), nodes.shape[0]), np.complex128)
     ie[:, 0] = gd["inj_s"][idx]
     out = []
-    for path in (4, 1, 0):
+    for path in (-1, 4, 1, 0):
         assert pkg.lib().tags_debug_solve_path(path) == 0
         try:
             sol, info, st = pkg.hem_sweep(e, pkg.images(e), nodes, s, kappa, ie=ie, precision=pkg.MIXED,
-                                          max_batch=16)
+                                          max_batch=per_pass)
         finally:
             pkg.lib().tags_debug_solve_path(-1)
         assert np.all(info == 0) and st.fallbacks == 0

@@ -1294,13 +1294,14 @@ constexpr int SOLVE_SMEM_MAX = 200 * 1024;
 __global__ void __launch_bounds__(SOLVE_THREADS, 1) k_ldl_solve_cta(
     const float2* __restrict__ A0, long long ld, long long mstride, int N, const float2* __restrict__ linv32,
     long long lstride, float2* __restrict__ x0, long long xstride, int zl_m, const int* __restrict__ active,
-    const int* __restrict__ lead_step, int lead_zero) {
+    const int* __restrict__ lead_step, int lead_zero, const int* __restrict__ nact, int few) {
     extern __shared__ float2 solve_sm[];
     float2* v = solve_sm;                          // the current block of x, zero beyond jb
     float2* part = solve_sm + TB;                  // 4 x TB partial sums of the block-inverse products
     float2* xs = solve_sm + 5 * TB;                // x
     const int smp = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     if (active && !active[smp]) return;            // the sample has finished refining
+    if (nact && *nact <= few) return;              // few samples left: the cluster kernel takes them
     const float2* A = A0 + mstride * smp;
     const float2* Lv = linv32 + lstride * smp;
     float2* x = x0 + xstride * smp;
@@ -1424,15 +1425,42 @@ template <int G>
 __global__ void __launch_bounds__(SOLVE_THREADS, 1) k_ldl_solve_cl(
     const float2* __restrict__ A0, long long ld, long long mstride, int N, const float2* __restrict__ linv32,
     long long lstride, float2* __restrict__ x0, long long xstride, int zl_m, const int* __restrict__ active,
-    const int* __restrict__ lead_step, int lead_zero) {
+    const int* __restrict__ lead_step, int lead_zero, const int* __restrict__ nact, int few, int nb) {
     static_assert(G == 2 || G == 4 || G == 8, "cluster of 2, 4 or 8 CTAs");
     extern __shared__ float2 solve_sm[];
+    __shared__ int s_smp;
     float2* v = solve_sm;
     float2* part = solve_sm + TB;
     float2* xs = solve_sm + 5 * TB;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int g = (int)cluster_rank(), smp = blockIdx.x / G;
-    if (active && !active[smp]) return;            // the whole cluster: the sample has finished refining
+    const int g = (int)cluster_rank();
+    int smp = blockIdx.x / G;
+    if (nact) {
+        // a step with few samples left: cluster c takes the c-th active one
+        // (every CTA of the cluster finds the same)
+        const int na = *nact;
+        if (na > few || smp >= na) return;         // the whole cluster
+        if (warp == 0) {
+            int seen = 0, found = -1;
+            for (int q0 = 0; q0 < nb && found < 0; q0 += 32) {
+                const int q = q0 + lane;
+                const unsigned msk = __ballot_sync(0xffffffffu, q < nb && active[q] != 0);
+                const int c = __popc(msk);
+                if (smp < seen + c) {
+                    unsigned mm = msk;
+                    for (int k = smp - seen; k > 0; --k) mm &= mm - 1;
+                    found = q0 + __ffs(mm) - 1;
+                }
+                seen += c;
+            }
+            if (lane == 0) s_smp = found;
+        }
+        __syncthreads();
+        smp = s_smp;
+        if (smp < 0) return;                       // the whole cluster
+    } else if (active && !active[smp]) {
+        return;                                    // the whole cluster: the sample has finished refining
+    }
     const float2* A = A0 + mstride * smp;
     const float2* Lv = linv32 + lstride * smp;
     float2* x = x0 + xstride * smp;
@@ -1711,12 +1739,15 @@ static int set_solve_cl_attr() {
     return 0;
 }
 
+// clusters: nb (one per sample), or, with nact, `few` (one per active sample
+// of a step with at most `few` of them)
 template <int G>
 static int launch_solve_cl(const float2* A, long long ld, long long mstride, int N, const float2* L32, long long ls,
                            float2* x, long long xstride, int zl_m, const int* active, const int* lead_step,
-                           int lead_zero, int nb, size_t smem, cudaStream_t st) {
+                           int lead_zero, int nb, size_t smem, cudaStream_t st, const int* nact = nullptr,
+                           int few = 0) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)(G * nb));
+    cfg.gridDim = dim3((unsigned)(G * (nact ? few : nb)));
     cfg.blockDim = dim3(SOLVE_THREADS);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
@@ -1728,7 +1759,7 @@ static int launch_solve_cl(const float2* A, long long ld, long long mstride, int
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     TAGS_CUDA_OK(cudaLaunchKernelEx(&cfg, k_ldl_solve_cl<G>, A, ld, mstride, N, L32, ls, x, xstride, zl_m, active,
-                                    lead_step, lead_zero));
+                                    lead_step, lead_zero, nact, few, nb));
     tags_note_launch();
     return 0;
 }
@@ -1808,7 +1839,7 @@ static int launch_gemm(int NS, const CUtensorMap& mA, const CUtensorMap& mB, con
 
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
                      float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active,
-                     const int* lead_step, int lead_zero) {
+                     const int* lead_step, int lead_zero, const int* nact) {
     if (int e0 = tags_ldl_tc_prepare()) return e0;
     const float2* L32 = linv32_of(ws, N, batch_cap);
     const long long ls = linv32_stride(N);
@@ -1816,6 +1847,7 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
     int pf = tags_prof_begin(TAGS_PROF_LDL_SOLVE, st);
     const size_t smem = sizeof(float2) * (5 * TB + (size_t)N);
     int path = g_solve_path;
+    bool split = false;
     if (path < 0) {
         path = 1;
         for (int G = 4; G >= 2; G /= 2)
@@ -1823,6 +1855,9 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
                 path = G;
                 break;
             }
+        // one CTA per sample, except in steps with few samples left (known
+        // on the device only): those run on clusters of four per sample
+        split = path == 1 && nact && active && g_solve_cl_ok[4];
     }
     if (path >= 1 && smem <= (size_t)SOLVE_SMEM_MAX) {
         int e = 0;
@@ -1834,9 +1869,13 @@ int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, in
                             : launch_solve_cl<8>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active, lead_step,
                                                  lead_zero, nb, smem, st);
         } else {
+            const int few = split ? num_sms() / 4 : 0;
             k_ldl_solve_cta<<<nb, SOLVE_THREADS, smem, st>>>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active,
-                                                             lead_step, lead_zero);
+                                                             lead_step, lead_zero, split ? nact : nullptr, few);
             tags_note_launch();
+            if (split)
+                e = launch_solve_cl<4>(A, ld, mstride, N, L32, ls, x, xstride, zl_m, active, lead_step, lead_zero, nb,
+                                       smem, st, nact, few);
         }
         if (e) return e;
         tags_prof_end(TAGS_PROF_LDL_SOLVE, pf, st, 8.0 * N * (double)N * nb, 8.0 * N * (double)N * nb);

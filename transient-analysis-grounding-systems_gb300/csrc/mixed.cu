@@ -372,6 +372,7 @@ struct IrState {
     int* step;       // steps done
     int* cont;       // 1 while another step is wanted
     int* extr;       // per sample: the step of its last extrapolation (k_ir_extrap)
+    int* nact;       // samples that refine in the coming step
     double* lam;     // per sample: |lambda| of that extrapolation
     double tol;      // stopping tolerance (relative error left in x)
 };
@@ -410,6 +411,7 @@ IrState ir_state(tags_plan_s* p) {
     s.step = p->d_iri + 3 * b;
     s.cont = p->d_iri + 3 * b + 1;
     s.extr = p->d_iri + 3 * b + 2;
+    s.nact = p->d_iri + 4 * b + 2;
     s.prev_dx = p->d_ird;
     s.wnorm = p->d_ird + b;
     s.berr = p->d_ird + 2 * b;
@@ -469,6 +471,7 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
     if (q == 0) {
         *s.step = 0;
         *s.cont = 1;
+        *s.nact = nb;
     }
     if (q >= nb) return;
     s.active[q] = info[q] == 0 && tc_err[0] == 0 && tc_err[1] == 0;
@@ -493,8 +496,10 @@ __global__ void k_ir_init(const double* __restrict__ norms, const int* __restric
 // condition.
 __global__ void __launch_bounds__(1024) k_ir_decide(double* __restrict__ norms, int nb, int max_steps, IrState s,
                                                     cudaGraphConditionalHandle cond, int set_cond) {
+    __shared__ int going;
     const int step = *s.step;
-    int any = 0;
+    if (threadIdx.x == 0) going = 0;
+    __syncthreads();
     for (int q = threadIdx.x; q < nb; q += blockDim.x) {
         if (!s.active[q]) continue;
         s.iters[q] = step + 1;
@@ -525,14 +530,15 @@ __global__ void __launch_bounds__(1024) k_ir_decide(double* __restrict__ norms, 
         if (more) {
             norms[4 * q + 2] = 0.0;
             norms[4 * q + 3] = xn;
-            any = 1;
+            atomicAdd(&going, 1);
         }
     }
-    any = __syncthreads_or(any);
+    __syncthreads();
     if (threadIdx.x == 0) {
-        const int c = any && step + 1 < max_steps;
+        const int c = going > 0 && step + 1 < max_steps;
         *s.step = step + 1;
         *s.cont = c;
+        *s.nact = going;
         if (set_cond) cudaGraphSetConditional(cond, c ? 1u : 0u);
     }
 }
@@ -567,7 +573,7 @@ int tags_mixed_alloc(tags_plan_s* p) {
     TAGS_CUDA_OK(cudaMalloc(&p->d_r, sizeof(double2) * 2 * N * b));      // residual + right-hand side
     TAGS_CUDA_OK(cudaMalloc(&p->d_rf, sizeof(float2) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_norms, sizeof(double) * 4 * b));
-    TAGS_CUDA_OK(cudaMalloc(&p->d_iri, sizeof(int) * (4 * b + 2)));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_iri, sizeof(int) * (4 * b + 3)));
     TAGS_CUDA_OK(cudaMalloc(&p->d_yprev, sizeof(float2) * N * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_dots, sizeof(double) * 4 * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_ird, sizeof(double) * 4 * b));
@@ -715,7 +721,7 @@ int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditi
     // the first step's right-hand side is b, zero in the 2m impedance rows
     // that the order ZL, ZT, nodes puts first
     int err = tags_ldl_solve_c(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_rf, N, m, st, s.active,
-                               s.step, 2 * m);
+                               s.step, 2 * m, s.nact);
     if (err) return err;
     k_ir_update<<<gv, 256, 0, st>>>(p->d_rf, p->d_scale, m, n, p->d_x, p->d_norms, s.active, p->d_yprev, p->d_dots,
                                     s.step);

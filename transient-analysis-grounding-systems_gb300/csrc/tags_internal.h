@@ -148,9 +148,12 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
 // lead_step (optional, device): while *lead_step is 0 the right-hand sides are
 // zero in their first lead_zero rows, and the forward sweep starts at the
 // first block that reaches past them.
+// nact (optional, device, with active): the number of active samples; where
+// the solves run one CTA per sample, a step with at most SMs / 4 of them
+// active runs on clusters of four CTAs per active sample instead.
 int tags_ldl_solve_c(const float2* A, int N, long long ld, long long mstride, int nb, int batch_cap, void* ws,
                      float2* x, long long xstride, int zl_m, cudaStream_t st, const int* active = nullptr,
-                     const int* lead_step = nullptr, int lead_zero = 0);
+                     const int* lead_step = nullptr, int lead_zero = 0, const int* nact = nullptr);
 
 // profile.cu: optional CUDA-event timing of kernel families
 enum {
