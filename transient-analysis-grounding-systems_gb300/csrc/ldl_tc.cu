@@ -980,11 +980,26 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
             a[p][q] = v;
         }
     __syncthreads();
-    // ---- LDL^T: k = 16 kq + kw; q index kq and p index kq / 2 are compile-time
+    // ---- LDL^T and X = L11^{-1} in one sweep: k = 16 kq + kw (q index kq and p
+    // index kq / 2 are compile-time). Step k scales column k (l_i = w_i / d_k)
+    // and applies one rank-1 update to the rows i > k: the columns j > k hold
+    // the trailing matrix (A[i][j] -= l_i A[j][k]), the finished columns j < k
+    // hold X, which takes the same row operation (X[i][j] -= l_i X[k][j]), and
+    // column k switches from A to X (X[i][k] = 0 - l_i, X[k][k] = 1). Each X
+    // entry sees the operations of the forward substitution in the same order.
+    // One barrier per step; the broadcast row is W: X[k][j] for j < k, 1 at k,
+    // A[j][k] for j > k.
 #pragma unroll
     for (int kq = 0; kq < 8; ++kq) {
         for (int kw = 0; kw < 16; ++kw) {
             const int k = 16 * kq + kw, buf = k & 1;
+            if (tx == (k & 31)) {                // row k of X, final since step k - 1
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int j = ty + 16 * q;
+                    if (j < k) wv[buf][j] = a[kq >> 1][q];
+                }
+            }
             if (ty == kw) {
                 const int src = k & 31;
                 float2 d;
@@ -992,6 +1007,7 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
                 d.y = __shfl_sync(0xffffffffu, a[kq >> 1][kq].y, src);
                 if (tx == 0) {
                     dsh[k] = d;
+                    wv[buf][k] = make_float2(1.f, 0.f);
                     if (!(d.x != 0.f || d.y != 0.f) && k < jb) atomicMin(&zero_at, k);
                 }
                 const float2 di = crecip_f(d);
@@ -1003,7 +1019,9 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
                         wv[buf][i] = w;
                         lv[buf][i] = l;
                         S[k * TB + i] = l;
-                        a[p][kq] = l;
+                        a[p][kq] = make_float2(0.f, 0.f);
+                    } else if (i == k) {
+                        a[p][kq] = make_float2(1.f, 0.f);
                     }
                 }
             }
@@ -1014,58 +1032,31 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
 #pragma unroll
             for (int q = 0; q < 8; ++q) W[q] = wv[buf][ty + 16 * q];
 #pragma unroll
-            for (int p = kq >> 1; p < 4; ++p)        // rows i <= k < 32 (kq / 2) need no update
+            for (int p = kq >> 1; p < 4; ++p)        // rows i <= k are final
 #pragma unroll
-                for (int q = kq; q < 8; ++q) {       // columns j < 16 kq are finished
-                    const int i = tx + 32 * p, j = ty + 16 * q;
-                    if (j > k && i >= j) a[p][q] = fsub(a[p][q], fmulc(L[p], W[q]));
+                for (int q = 0; q < 2 * p + 2; ++q) {   // columns j >= 32 p + 32 lie above the diagonal
+                    const int i = tx + 32 * p;
+                    if (i > k) a[p][q] = fsub(a[p][q], fmulc(L[p], W[q]));
                 }
         }
     }
-    // L11 (unit lower, strictly below the diagonal) and D back to A
+    // X is unit lower: clear what the updates left above the diagonal
 #pragma unroll
     for (int p = 0; p < 4; ++p)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int i = tx + 32 * p, j = ty + 16 * q;
-            if (i < jb && j < jb && i >= j) A[(long long)(j0 + i) + ld * (j0 + j)] = a[p][q];
-        }
+        for (int q = 0; q < 8; ++q)
+            if (ty + 16 * q > tx + 32 * p) a[p][q] = make_float2(0.f, 0.f);
     __syncthreads();
+    // L11 (unit lower, strictly below the diagonal, from S) and D back to A
+    for (int t = tid; t < TB * TB; t += blockDim.x) {
+        const int i = t % TB, j = t / TB;
+        if (i < jb && j < jb && i >= j) A[(long long)(j0 + i) + ld * (j0 + j)] = i == j ? dsh[i] : S[j * TB + i];
+    }
     if (tid == 0 && zero_at < jb && info[smp] == 0) info[smp] = j0 + zero_at + 1;
     if (tid < TB) {
         const float2 di = tid < jb ? crecip_f(dsh[tid]) : make_float2(0.f, 0.f);
         dinv[(long long)TB * smp + tid] = di;
         dsq[(long long)TB * smp + tid] = csqrt_f(di);
-    }
-    // ---- X = L11^{-1}: for k = 0..126, X[i, j] -= L[i, k] X[k, j] (i > k, j <= k);
-    // row k of X is final once step k - 1 is done. Reuse a[][] for X.
-#pragma unroll
-    for (int p = 0; p < 4; ++p)
-#pragma unroll
-        for (int q = 0; q < 8; ++q) a[p][q] = make_float2(tx + 32 * p == ty + 16 * q ? 1.f : 0.f, 0.f);
-#pragma unroll
-    for (int kp = 0; kp < 4; ++kp) {
-        for (int kl = 0; kl < 32; ++kl) {
-            const int k = 32 * kp + kl, buf = k & 1;
-            if (k == TB - 1) break;
-            if (tx == kl) {
-#pragma unroll
-                for (int q = 0; q < 8; ++q) wv[buf][ty + 16 * q] = a[kp][q];
-            }
-            __syncthreads();
-            float2 X[8], L[4];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) X[q] = wv[buf][ty + 16 * q];
-#pragma unroll
-            for (int p = kp; p < 4; ++p) L[p] = S[k * TB + tx + 32 * p];
-#pragma unroll
-            for (int p = kp; p < 4; ++p)             // rows i < 32 kp are finished
-#pragma unroll
-                for (int q = 0; q < 2 * kp + 2; ++q) {   // columns j > k < 32 kp + 32 stay zero
-                    const int i = tx + 32 * p, j = ty + 16 * q;
-                    if (i > k && j <= k) a[p][q] = fsub(a[p][q], fmulc(L[p], X[q]));
-                }
-        }
     }
     __syncthreads();                                    // S (L columns) is dead: stage X row-major, padded
 #pragma unroll
