@@ -1026,18 +1026,20 @@ __global__ void __launch_bounds__(512, 1) k_ldl_diag(float2* __restrict__ A0, lo
                 }
             }
             __syncthreads();
-            float2 L[4], W[8];
+            float2 nL[4], W[8];
 #pragma unroll
-            for (int p = kq >> 1; p < 4; ++p) L[p] = lv[buf][tx + 32 * p];
+            for (int p = kq >> 1; p < 4; ++p) {
+                const float2 l = lv[buf][tx + 32 * p];
+                nL[p] = make_float2(-l.x, -l.y);
+            }
 #pragma unroll
             for (int q = 0; q < 8; ++q) W[q] = wv[buf][ty + 16 * q];
+            // rows i <= k are final: only register row kq / 2 holds some
 #pragma unroll
-            for (int p = kq >> 1; p < 4; ++p)        // rows i <= k are final
+            for (int p = kq >> 1; p < 4; ++p)
 #pragma unroll
-                for (int q = 0; q < 2 * p + 2; ++q) {   // columns j >= 32 p + 32 lie above the diagonal
-                    const int i = tx + 32 * p;
-                    if (i > k) a[p][q] = fsub(a[p][q], fmulc(L[p], W[q]));
-                }
+                for (int q = 0; q < 2 * p + 2; ++q)     // columns j >= 32 p + 32 lie above the diagonal
+                    if (p > (kq >> 1) || tx + 32 * p > k) a[p][q] = ffmac(nL[p], W[q], a[p][q]);
         }
     }
     // X is unit lower: clear what the updates left above the diagonal
