@@ -713,9 +713,17 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
 // shared memory (coalesced reads and writes). A CTA moves one tile position
 // of MIRROR_MATS matrices (ZL and ZT of consecutive samples), so each CTA
 // carries enough traffic to hide its start-up.
+// With pmax / psum (the high parts' pass) it also leaves the row statistics'
+// partials: per matrix, row R and tile slot t (KB = ceil(m / 32) slots) the
+// max and the sum of |Z[R][j]| over the 32 columns of block t, from the tile
+// (R's block, t) for t below R's block, from the column below the diagonal in
+// tile (t, R's block) for t above it, and from both halves of the diagonal
+// tile at t = R's block: layout [mat][t][R]. Every sum has a fixed order.
 constexpr int MIRROR_MATS = 8;
-__global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long long bstride, int m, int nmat) {
+__global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long long bstride, int m, int nmat,
+                                                 float* __restrict__ pmax, float* __restrict__ psum) {
     __shared__ float2 tile[2][32][33];
+    __shared__ float rmx[2][8][32], rsm[2][8][32], cmx[2][32], csm[2][32];
     const long long t = blockIdx.x;
     // lower tiles by block row: row block bk holds column blocks 0 .. bk
     int bk = (int)floor((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
@@ -725,19 +733,71 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
     const int bi = (int)(t - (long long)bk * (bk + 1) / 2);
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int mat0 = blockIdx.y * MIRROR_MATS;
+    const int KB = (m + 31) / 32;
     for (int q = 0; q < MIRROR_MATS; ++q) {
         const int mat = mat0 + q;                      // 2 x sample + (0: ZL, 1: ZT)
         if (mat >= nmat) break;
         float2* Z = ((mat & 1) ? zt0 : zl0) + bstride * (mat >> 1);
         float2 (*T)[33] = tile[q & 1];                 // two buffers: one barrier per matrix
+        float rowmx = 0.f, rowsm = 0.f;                // row bk * 32 + tx over this thread's columns
         for (int j = ty; j < 32; j += 8) {
             const int r = bk * 32 + tx, cc = bi * 32 + j;
-            if (r < m && cc < m && r > cc) T[j][tx] = Z[r + (long long)m * cc];
+            float a = 0.f;
+            if (r < m && cc < m && r >= cc) {
+                const float2 z = Z[r + (long long)m * cc];
+                if (r > cc) T[j][tx] = z;
+                a = sqrtf(z.x * z.x + z.y * z.y);
+            }
+            if (pmax) {
+                rowmx = fmaxf(rowmx, a);
+                rowsm += a;
+                // column cc below the diagonal: row cc's entries in this tile
+                float cm = r > cc ? a : 0.f, cs = cm;
+                for (int o = 16; o > 0; o >>= 1) {
+                    cm = fmaxf(cm, __shfl_xor_sync(0xffffffffu, cm, o));
+                    cs += __shfl_xor_sync(0xffffffffu, cs, o);
+                }
+                if (tx == 0) {
+                    cmx[q & 1][j] = cm;
+                    csm[q & 1][j] = cs;
+                }
+            }
+        }
+        if (pmax) {
+            rmx[q & 1][ty][tx] = rowmx;
+            rsm[q & 1][ty][tx] = rowsm;
         }
         __syncthreads();
         for (int j = ty; j < 32; j += 8) {
             const int cc = bi * 32 + tx, r = bk * 32 + j;     // element (row cc, column r) of the upper triangle
             if (r < m && cc < m && r > cc) Z[cc + (long long)m * r] = T[tx][j];
+        }
+        if (pmax && ty < 2) {
+            float mx = 0.f, sm = 0.f;
+            if (ty == 0 || bk != bi) {
+                // ty 0: the rows of block bk (their columns in block bi);
+                // ty 1: the rows of block bi (their column parts), off the diagonal
+                if (ty == 0) {
+#pragma unroll
+                    for (int w = 0; w < 8; ++w) {
+                        mx = fmaxf(mx, rmx[q & 1][w][tx]);
+                        sm += rsm[q & 1][w][tx];
+                    }
+                    if (bk == bi) {
+                        mx = fmaxf(mx, cmx[q & 1][tx]);
+                        sm += csm[q & 1][tx];
+                    }
+                } else {
+                    mx = cmx[q & 1][tx];
+                    sm = csm[q & 1][tx];
+                }
+                const int row = (ty == 0 ? bk : bi) * 32 + tx, slot = ty == 0 ? bi : bk;
+                if (row < m) {
+                    const long long o = ((long long)mat * KB + slot) * m + row;
+                    pmax[o] = mx;
+                    psum[o] = sm;
+                }
+            }
         }
     }
 }
@@ -1390,7 +1450,7 @@ int tags_launch_pair_plan(const double* d_elec, const double* d_img, int m, int 
 int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
                            int nsamp, float2* d_zl, float2* d_zt, float2* d_zlo, float2* d_ztlo, long long bstride,
                            int has_img, const SpecialEntries& sp, const MomentFill& mf, int* d_status,
-                           cudaStream_t st) {
+                           cudaStream_t st, float* rowpart) {
     if (m <= 0 || nsamp <= 0) return 0;
     if (nsamp > 4096 || nsamp > mf.batch)
         return tags_fail_cuda(cudaErrorInvalidValue, "fill_mixed: batch above capacity", __FILE__, __LINE__);
@@ -1415,8 +1475,10 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
     k_fill_special64<<<gs, SPEC_WARPS * 32, 0, st>>>(d_elec, d_img, m, sp.ent, sp.n, d_coef, nsamp, d_zl, d_zt, d_zlo,
                                                      d_ztlo, bstride, d_status, sp.tm, sp.tdmax);
     const dim3 gm((unsigned)((long long)KB * (KB + 1) / 2), (unsigned)((2 * nsamp + MIRROR_MATS - 1) / MIRROR_MATS));
-    k_zmirror<<<gm, 256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp);
-    k_zmirror<<<gm, 256, 0, st>>>(d_zlo, d_ztlo, bstride, m, 2 * nsamp);
+    float* pmax = rowpart;
+    float* psum = rowpart ? rowpart + (size_t)2 * nsamp * KB * m : nullptr;
+    k_zmirror<<<gm, 256, 0, st>>>(d_zl, d_zt, bstride, m, 2 * nsamp, pmax, psum);
+    k_zmirror<<<gm, 256, 0, st>>>(d_zlo, d_ztlo, bstride, m, 2 * nsamp, nullptr, nullptr);
     tags_prof_end(TAGS_PROF_FILL_MIXED, pf, st, 0.0, 0.0);
     tags_note_launch(8);
     TAGS_CUDA_OK(cudaGetLastError());

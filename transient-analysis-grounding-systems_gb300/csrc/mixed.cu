@@ -76,6 +76,29 @@ __global__ void k_rowstats(const float2* __restrict__ Z, int m, double* __restri
     }
 }
 
+// The same statistics from the partials the fill's mirror pass leaves
+// (max and sum of |Z[R][j]| per row R and 32-column block t, [mat][t][R]):
+// the max over t, the sum over t in order. One thread per (row, block, sample).
+__global__ void k_rowstats_part(const float* __restrict__ pmax, const float* __restrict__ psum, int m,
+                                double* __restrict__ scale, double* __restrict__ rsum, float* __restrict__ scalef,
+                                int N) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, blk = blockIdx.y, b = blockIdx.z;
+    if (r >= m) return;
+    const int KB = (m + 31) / 32;
+    const long long base = (long long)(2 * b + blk) * KB * m + r;
+    float mx = 0.f, sm = 0.f;
+    for (int t = 0; t < KB; ++t) {
+        mx = fmaxf(mx, pmax[base + (long long)t * m]);
+        sm += psum[base + (long long)t * m];
+    }
+    const double inc = blk == 0 ? 1.0 : 0.5;            // incidence entries of the row
+    const int row = blk * m + r;                          // reordered index
+    const double sc = 1.0 / sqrt(fmax((double)mx, inc));
+    scale[(size_t)b * N + row] = sc;
+    scalef[(size_t)b * N + row] = (float)sc;
+    rsum[(size_t)b * N + row] = (double)sm + 2.0 * inc;
+}
+
 // Node rows: max |entry| = 1 (A) so the scale is 1; row sum = sum over
 // incident segments of (1 + 0.5).
 __global__ void k_rowstats_nodes(const int* __restrict__ node_ptr, int n, int m, double* __restrict__ scale,
@@ -567,6 +590,7 @@ int tags_mixed_alloc(tags_plan_s* p) {
     TAGS_CUDA_OK(cudaMalloc(&p->d_Zlo, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMemset(p->d_Zlo, 0, sizeof(float2) * 2 * m * m * b));
     TAGS_CUDA_OK(cudaMalloc(&p->d_Z, sizeof(float2) * 2 * m * m * b));
+    TAGS_CUDA_OK(cudaMalloc(&p->d_rowpart, sizeof(float) * 2 * 2 * b * ((m + 31) / 32) * m));
     TAGS_CUDA_OK(cudaMalloc(&p->d_A, sizeof(float2) * N * N * b));
     // scale + row sums (FP64), then an FP32 copy of the scale
     TAGS_CUDA_OK(cudaMalloc(&p->d_scale, sizeof(double) * 2 * N * b + sizeof(float) * N * b));
@@ -587,8 +611,8 @@ int tags_mixed_alloc(tags_plan_s* p) {
 }
 
 int tags_mixed_free(tags_plan_s* p) {
-    void* ptrs[] = {p->d_Z,      p->d_A,      p->d_scale, p->d_r,      p->d_rf,  p->d_norms,
-                    p->d_fillws, p->d_ldlws, p->d_ldlerr, p->d_iri, p->d_ird, p->d_yprev, p->d_dots};
+    void* ptrs[] = {p->d_Z,      p->d_A,      p->d_scale, p->d_r,      p->d_rf,  p->d_norms,   p->d_fillws,
+                    p->d_ldlws, p->d_ldlerr, p->d_iri,  p->d_ird, p->d_yprev, p->d_dots, p->d_rowpart};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     tags_mixed_special_free(&p->spec);
@@ -599,6 +623,7 @@ int tags_mixed_free(tags_plan_s* p) {
     p->d_A = nullptr;
     p->d_yprev = nullptr;
     p->d_dots = nullptr;
+    p->d_rowpart = nullptr;
     return 0;
 }
 
@@ -673,11 +698,15 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
                                            p->d_Z + (size_t)m * m, 2LL * m * m, p->d_status, st)
                   : tags_launch_fill_mixed(p->d_elec, p->d_img, m, p->d_fillws, p->d_coef, nb, p->d_Z,
                                            p->d_Z + (size_t)m * m, p->d_Zlo, p->d_Zlo + (size_t)m * m, 2LL * m * m,
-                                           p->has_images, p->spec, p->mom, p->d_status, st);
+                                           p->has_images, p->spec, p->mom, p->d_status, st, p->d_rowpart);
     if (err) return err;
     // 2. scaling
     float* d_scalef = reinterpret_cast<float*>(p->d_scale + 2 * (size_t)p->batch * N);
-    k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, d_scalef, N);
+    if (p->fill_model == TAGS_INTG_MHEM)
+        k_rowstats<<<dim3((m * 32 + 255) / 256, 2, nb), 256, 0, st>>>(p->d_Z, m, p->d_scale, d_rsum, d_scalef, N);
+    else       // from the partials of the fill's mirror pass
+        k_rowstats_part<<<dim3((m + 255) / 256, 2, nb), 256, 0, st>>>(
+            p->d_rowpart, p->d_rowpart + (size_t)2 * nb * ((m + 31) / 32) * m, m, p->d_scale, d_rsum, d_scalef, N);
     k_rowstats_nodes<<<dim3((n + 127) / 128, nb), 128, 0, st>>>(p->inc.node_ptr, n, m, p->d_scale, d_rsum, d_scalef,
                                                                 N);
     tags_note_launch(2);

@@ -71,6 +71,7 @@ struct tags_plan_s {
     SpecialEntries spec;            // entries filled in FP64 per sample (touching pairs, diagonal)
     MomentFill mom;                 // moment expansion of the regular pairs (geometry moments, per-pass tables)
     float2* d_Zlo = nullptr;        // batch x 2 x m x m: low parts of ZL, ZT (Z holds the high parts)
+    float* d_rowpart = nullptr;     // row statistics' partials of a pass (tags_launch_fill_mixed)
     void* d_ldlws = nullptr;        // tensor-core LDL^T workspace (split planes, block inverses)
     int* d_ldlerr = nullptr;        // error word of the tensor-core kernels
     int split_pieces = TAGS_SPLIT_F16;   // split form of the tensor-core products (2, 3 bf16 pieces; TAGS_SPLIT_F16)

@@ -81,11 +81,13 @@ int tags_moment_fill_build(const double* d_elec, const double* d_img, int m, int
                            const double* h_img, int batch, MomentFill* mf, cudaStream_t st);
 void tags_moment_fill_free(MomentFill* mf);
 // The mixed fill of a pass: ZL, ZT as float pairs (hi in d_zl / d_zt, lo in
-// d_zlo / d_ztlo), full symmetric.
+// d_zlo / d_ztlo), full symmetric. rowpart (optional, 2 x 2 nsamp x ceil(m/32)
+// x m floats): the row statistics' partials of the high parts, max then sum,
+// [matrix][32-column block][row] (matrix = 2 sample + 0 for ZL, 1 for ZT).
 int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, void* ws, const SampleCoef* d_coef,
                            int nsamp, float2* d_zl, float2* d_zt, float2* d_zlo, float2* d_ztlo, long long bstride,
                            int has_img, const SpecialEntries& sp, const MomentFill& mf, int* d_status,
-                           cudaStream_t st);
+                           cudaStream_t st, float* rowpart = nullptr);
 int tags_launch_fill_fp64(const double* d_elec, const double* d_img, int m, const SampleCoef* d_coef,
                           int nsamp, const FillOut& out, int mode, int itype, int tight, int* d_status,
                           cudaStream_t st);
