@@ -854,7 +854,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true", help="skip the all-sample GPR check against plain FP64")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 sub-record")
     ap.add_argument("--tc-pairs", type=int, default=-1,
-                    help="trailing updates on two-SM clusters: 1 on, 0 off (-1 = the plan's default)")
+                    help="trailing updates: 0 one SM per tile, 1 two-SM clusters, 2 two-SM real-form N=256 "
+                         "(-1 = the plan's default)")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--solve-path", type=int, default=-1,
                     help="triangular solves: 0 per block, 1 one CTA per sample, 2/4/8 clusters (-1 = default)")

@@ -428,11 +428,15 @@ int tags_solve_immittance_noalloc (tags_cdouble *d_wg, tags_cdouble *d_ie, size_
  * refinement steps. */
 int tags_plan_set_refine_tol (tags_plan plan, double tol);
 
-/* No counterpart in the reference. 1: the mixed form's trailing updates run
- * on clusters of two SMs (tcgen05.mma.cta_group::2, 256 x 128 products, each
- * SM staging its own 128 rows of A and half of B); 0 (default): one SM per
- * 128 x 128 tile. Where the device cannot host such clusters the single-SM
- * kernel runs. */
+/* No counterpart in the reference. How the mixed form's trailing updates use
+ * the tensor cores. 0 (default): one SM per 128 x 128 tile (complex products
+ * as 4 real ones). 1: clusters of two SMs (tcgen05.mma.cta_group::2, 256 x 128
+ * products, each SM staging its own 128 rows of A and half of B). 2: clusters
+ * of two SMs with the complex update as one real product of N = 256
+ * ([Re | Im] = [Ar Ai] [[Br, -Bi], [Bi, Br]]^T, each SM staging its own 128
+ * rows of A and its 128 B rows; the panel GEMM also writes the negated
+ * imaginary planes); with three bf16 pieces this falls back to 1. Where the
+ * device cannot host such clusters the single-SM kernel runs. */
 int tags_plan_set_tc_pairs (tags_plan plan, int on);
 
 /* No counterpart in the reference. The same switch for the diagnostic entry

@@ -17,7 +17,7 @@ def _sym_matrix(rng, N, dominance):
 
 
 def _ldl(pkg, mats, pieces=3, pairs=False):
-    pkg.lib().tags_debug_tc_pairs(1 if pairs else 0)
+    pkg.lib().tags_debug_tc_pairs(int(pairs))
     fn = pkg.lib().tags_debug_ldl
     fn.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     fn.restype = ctypes.c_int
@@ -28,14 +28,16 @@ def _ldl(pkg, mats, pieces=3, pairs=False):
     return code, np.transpose(buf, (0, 2, 1))
 
 
-@pytest.mark.parametrize("pairs", [False, True])
+@pytest.mark.parametrize("pairs", [0, 1, 2])
 @pytest.mark.parametrize("pieces,tol", [(2, 2e-5), (3, 2e-6), (16, 4e-6)])
 @pytest.mark.parametrize("N", [128, 300, 517])
 def test_tensor_core_ldl_reconstructs(gpu_pkg, N, pieces, tol, pairs):
     """L D L^T reproduces A to the accuracy of the split products: ~1e-5 with
     two bf16 pieces per value (three products), FP32 level with three (six),
     near FP32 level with two fp16 pieces of 2^8 x (three products); the
-    trailing updates on one SM per tile or on two-SM clusters (pairs)."""
+    trailing updates on one SM per tile, on two-SM clusters (pairs 1), or on
+    two-SM clusters with real-form products of N = 256 (pairs 2; three bf16
+    pieces fall back to 1)."""
     rng = np.random.default_rng(N)
     mats = np.stack([_sym_matrix(rng, N, 4.0), _sym_matrix(rng, N, 2.0), _sym_matrix(rng, N, 3.0)])
     code, fac = _ldl(gpu_pkg, mats, pieces, pairs)
@@ -88,7 +90,7 @@ def _banded_sym(rng, N, zl_m, dominance):
     return a
 
 
-@pytest.mark.parametrize("pairs", [False, True])
+@pytest.mark.parametrize("pairs", [0, 1, 2])
 @pytest.mark.parametrize("pieces,group", [(3, 4), (16, 4), (16, 2), (16, 1)])
 @pytest.mark.parametrize("N,zl_m", [(300, 0), (517, 0), (700, 150), (1000, 300), (1500, 400)])
 def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group, pairs):
@@ -105,7 +107,7 @@ def test_tensor_core_solve_matches_numpy(gpu_pkg, N, zl_m, pieces, group, pairs)
     rhs = rng.standard_normal((2, N)) + 1j * rng.standard_normal((2, N))
     buf = np.ascontiguousarray(np.transpose(mats, (0, 2, 1))).astype(np.complex128)
     x = rhs.copy()
-    gpu_pkg.lib().tags_debug_tc_pairs(1 if pairs else 0)
+    gpu_pkg.lib().tags_debug_tc_pairs(int(pairs))
     try:
         code = fn(buf.ctypes.data, x.ctypes.data, N, 2, pieces, zl_m, group)
     finally:

@@ -722,9 +722,11 @@ class Plan:
         if code != 0:
             raise RuntimeError(f"tags_plan_set_fill failed ({code}): {last_error()}")
 
-    def set_tc_pairs(self, on):
-        """Trailing updates on two-SM clusters (tcgen05 cta_group::2) or not."""
-        _ret(lib().tags_plan_set_tc_pairs(self.handle, 1 if on else 0))
+    def set_tc_pairs(self, mode):
+        """Trailing updates: 0 one SM per tile, 1 two-SM clusters (tcgen05
+        cta_group::2, complex products), 2 two-SM clusters with the complex
+        update as one real product of N = 256 (True means 1)."""
+        _ret(lib().tags_plan_set_tc_pairs(self.handle, int(mode)))
 
     def set_refine_tol(self, tol):
         """Refinement stopping tolerance of the mixed form (0 = default 1e-9)."""

@@ -275,6 +275,7 @@ struct GemmArgs {
     int Mn;                    // rows of the next panel's block column
     int kblocks;               // K blocks of BK (4 per panel of the group)
     int off;                   // row offset of the operand rows (tile row TB * I reads row TB * I + off)
+    int neg_planes;            // mode 1, S = 2: also the negated imaginary planes, at slots 4, 5 of the group buffer
 };
 
 TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
@@ -300,8 +301,12 @@ TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& sk
 // Row `row`, columns c0 .. c0+15 of a plane buffer [2S][R][128] (real
 // pieces, then imaginary pieces): the split of v[0..15], two columns at a
 // time with the packed conversions (one instruction per pair of values).
+// With neg (S = 2), the imaginary pieces again with their signs flipped (an
+// exact negation of both fp16 or bf16 pieces), as planes 4 and 5: the B rows
+// [-Im] of the two-SM products in real form (k_gemm_tc2 with EMB).
 template <int S>
-TAGS_D void store_planes16(uint16_t* P, int R, int ks, int row, int c0, const float2* v, bool f16, int& ovf) {
+TAGS_D void store_planes16(uint16_t* P, int R, int ks, int row, int c0, const float2* v, bool f16, int& ovf,
+                           bool neg = false) {
     __align__(16) uint32_t pl[2 * S][8];        // 8 packed pairs = 16 columns per plane
     if (S == 2 && f16) {
 #pragma unroll
@@ -340,6 +345,16 @@ TAGS_D void store_planes16(uint16_t* P, int R, int ks, int row, int c0, const fl
         uint4* d = reinterpret_cast<uint4*>(P + plane_elem(p, R, ks, row, c0));
         d[0] = make_uint4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
         d[1] = make_uint4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
+    }
+    if (S == 2 && neg) {
+        constexpr uint32_t SG = 0x80008000u;    // the sign bits of both 16-bit values
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const uint32_t* q = pl[S + p];
+            uint4* d = reinterpret_cast<uint4*>(P + plane_elem(2 * S + p, R, ks, row, c0));
+            d[0] = make_uint4(q[0] ^ SG, q[1] ^ SG, q[2] ^ SG, q[3] ^ SG);
+            d[1] = make_uint4(q[4] ^ SG, q[5] ^ SG, q[6] ^ SG, q[7] ^ SG);
+        }
     }
 }
 
@@ -490,7 +505,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
 #pragma unroll
                     for (int j = 0; j < 16; ++j) zv[j] = make_float2(0.f, 0.f);
                     for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
-                        store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, zv, f16, ovf);
+                        store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, zv, f16, ovf,
+                                          g.neg_planes != 0);
                     }
                 }
                 // no update of this tile; if it holds rows of the next panel's
@@ -571,7 +587,8 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                         vv[j] = fmulc(wv, sq[c]);
                         if (c < g.Nn) Cb[(long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + c)] = fmulc(wv, dv[c]);
                     }
-                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, vv, f16, ovf);
+                    store_planes16<S>(g.Lp + g.pstride * smp, g.R, KG, g.prow0 + gr, g.kcol0 + cc * 16, vv, f16, ovf,
+                                      g.neg_planes != 0);
                 }
             }
             tc_fence_before();
@@ -607,11 +624,17 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
 
 constexpr int PSTB = (TB / 2) * BK * 2;              // one plane of a B half in one stage: 4 KiB
 
-template <int S> struct Gemm2Cfg {
+// EMB = 1 (S = 2 only): the complex update as one real product per split
+// pair with N = 256, [Re | Im] = [Ar Ai] [[Br, -Bi], [Bi, Br]]^T: the even CTA
+// stages B rows Br (planes 0, 1) and -Bi (planes 4, 5), the odd CTA Bi
+// (planes 2, 3) and Br, each 128 rows, so an SM reads 4 KiB of A and 4 KiB of
+// its own B per 128-cycle product (64 B per cycle, half of the single-SM
+// kernel's) and the products per K step fall from 12 to 6.
+template <int S, int EMB = 0> struct Gemm2Cfg {
     static constexpr int NPL = 2 * S;
     static constexpr int ABYTES = NPL * PST;          // A planes of one stage
-    static constexpr int STAGE = NPL * (PST + PSTB);  // A planes, then the B half's planes
-    static constexpr int STAGES = S == 2 ? 4 : 3;
+    static constexpr int STAGE = EMB ? 2 * NPL * PST : NPL * (PST + PSTB);   // A planes, then the B planes
+    static constexpr int STAGES = EMB ? 3 : (S == 2 ? 4 : 3);
     static constexpr int BARS = 512;
     static constexpr int SMEM = STAGES * STAGE + 1024 + BARS;
 };
@@ -685,11 +708,15 @@ TAGS_D void mma_pair_commit_local(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-// Instruction descriptor of the pair products: M = 256, N = 128.
-TAGS_D uint32_t idesc_mma_pair(bool negate_a, bool f16) {
+// Instruction descriptor of the pair products: M = 256, N = 128 (or N = 256).
+TAGS_D uint32_t idesc_mma_pair(bool negate_a, bool f16, bool n256 = false) {
     uint32_t d = idesc_mma(negate_a, f16);
     d &= ~(31u << 24);
     d |= (uint32_t)(2 * TB >> 4) << 24;                 // M = 256
+    if (n256) {
+        d &= ~(63u << 17);
+        d |= (uint32_t)(2 * TB >> 3) << 17;             // N = 256
+    }
     return d;
 }
 
@@ -742,10 +769,11 @@ TAGS_D void skipped_tile_planes(const GemmArgs& g, int smp, int I, int J, int r,
     }
 }
 
-template <int S>
+template <int S, int EMB>
 __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc2(const __grid_constant__ CUtensorMap tmA,
                                                               const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
-    using C = Gemm2Cfg<S>;
+    static_assert(!EMB || S == 2, "the real-form products need the negated planes of S = 2");
+    using C = Gemm2Cfg<S, EMB>;
     extern __shared__ uint8_t smem_raw[];
     const uint32_t base_u32 = (smem_u32(smem_raw) + 1023u) & ~1023u;
     uint8_t* base = smem_raw + (base_u32 - smem_u32(smem_raw));
@@ -803,10 +831,21 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc2(const __grid_const
                     const uint32_t sa = base_u32 + stage * C::STAGE, sb = sa + C::ABYTES;
                     const uint32_t cfull = mapa_cta(full(stage), 0);
                     mbar_arrive_expect_tx_cluster(cfull, C::STAGE);
-                    const int ra = TB * I + g.off, rb = TB * J + g.off + (TB / 2) * (int)rank;
-                    for (int p = 0; p < C::NPL; ++p) {
-                        tma_load_5d_pair(sa + p * PST, &tmA, 0, ra, kb, p, smp, cfull);
-                        tma_load_5d_pair(sb + p * PSTB, &tmB, 0, rb, kb, p, smp, cfull);
+                    const int ra = TB * I + g.off;
+                    if (EMB) {
+                        // 128 B rows per CTA: even Br (0, 1), -Bi (4, 5); odd Bi (2, 3), Br (0, 1)
+                        const int rb = TB * J + g.off;
+                        for (int p = 0; p < C::NPL; ++p) {
+                            const int pb = rank == 0 ? (p < S ? p : 2 * S + p - S) : (p < S ? S + p : p - S);
+                            tma_load_5d_pair(sa + p * PST, &tmA, 0, ra, kb, p, smp, cfull);
+                            tma_load_5d_pair(sb + p * PST, &tmB, 0, rb, kb, pb, smp, cfull);
+                        }
+                    } else {
+                        const int rb = TB * J + g.off + (TB / 2) * (int)rank;
+                        for (int p = 0; p < C::NPL; ++p) {
+                            tma_load_5d_pair(sa + p * PST, &tmA, 0, ra, kb, p, smp, cfull);
+                            tma_load_5d_pair(sb + p * PSTB, &tmB, 0, rb, kb, p, smp, cfull);
+                        }
                     }
                     issued[stage] = 1;
                     ipar[stage] = phase;
@@ -826,6 +865,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc2(const __grid_const
         // ---- MMA issuer: one thread of the even CTA
         if (rank == 0 && lane == 0) {
             const uint32_t idp = idesc_mma_pair(false, g.f16 != 0), idn = idesc_mma_pair(true, g.f16 != 0);
+            const uint32_t id256 = idesc_mma_pair(false, g.f16 != 0, true);
             int stage = 0, acc = 0;
             uint32_t phase = 0, aphase = 0;
             bool alive = true;
@@ -848,14 +888,23 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc2(const __grid_const
                         for (int i = 0; i < S; ++i) {
                             for (int j = 0; i + j < S; ++j) {
                                 const uint64_t ar = sdesc64(sa + i * PST + off), ai = sdesc64(sa + (S + i) * PST + off);
-                                const uint64_t br = sdesc64(sbb + j * PSTB + off),
-                                               bi = sdesc64(sbb + (S + j) * PSTB + off);
-                                mma_pair(accR, ar, br, idp, firstR ? 0u : 1u);   // + Ar Br
-                                firstR = false;
-                                mma_pair(accR, ai, bi, idn, 1u);                 // - Ai Bi
-                                mma_pair(accI, ar, bi, idp, firstI ? 0u : 1u);   // + Ar Bi
-                                firstI = false;
-                                mma_pair(accI, ai, br, idp, 1u);                 // + Ai Br
+                                if (EMB) {
+                                    // [Re | Im] += Ar [Br | Bi]^T, then Ai [-Bi | Br]^T (B rows per CTA)
+                                    const uint64_t bx = sdesc64(sbb + j * PST + off),
+                                                   by = sdesc64(sbb + (S + j) * PST + off);
+                                    mma_pair(accR, ar, bx, id256, firstR ? 0u : 1u);
+                                    firstR = false;
+                                    mma_pair(accR, ai, by, id256, 1u);
+                                } else {
+                                    const uint64_t br = sdesc64(sbb + j * PSTB + off),
+                                                   bi = sdesc64(sbb + (S + j) * PSTB + off);
+                                    mma_pair(accR, ar, br, idp, firstR ? 0u : 1u);   // + Ar Br
+                                    firstR = false;
+                                    mma_pair(accR, ai, bi, idn, 1u);                 // - Ai Bi
+                                    mma_pair(accI, ar, bi, idp, firstI ? 0u : 1u);   // + Ar Bi
+                                    firstI = false;
+                                    mma_pair(accI, ai, br, idp, 1u);                 // + Ai Br
+                                }
                             }
                         }
                     }
@@ -1679,16 +1728,17 @@ static int set_gemm_attr() {
 }
 
 // Two-SM GEMM: shared-memory size and the most clusters of two that can be
-// resident at once (the persistent grid), per split form.
-static int g_pair_clusters[4] = {0, 0, 0, 0};
+// resident at once (the persistent grid), per split form and product form.
+static int g_pair_clusters[4][2] = {};
 
-template <int S>
+template <int S, int EMB>
 static int set_gemm2_attr() {
-    TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc2<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, Gemm2Cfg<S>::SMEM));
+    TAGS_CUDA_OK(cudaFuncSetAttribute(k_gemm_tc2<S, EMB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      Gemm2Cfg<S, EMB>::SMEM));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(2 * 76);
     cfg.blockDim = dim3(GEMM_THREADS);
-    cfg.dynamicSmemBytes = Gemm2Cfg<S>::SMEM;
+    cfg.dynamicSmemBytes = Gemm2Cfg<S, EMB>::SMEM;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = 2;
@@ -1697,11 +1747,11 @@ static int set_gemm2_attr() {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, (void*)k_gemm_tc2<S>, &cfg) != cudaSuccess || n <= 0) {
+    if (cudaOccupancyMaxActiveClusters(&n, (void*)k_gemm_tc2<S, EMB>, &cfg) != cudaSuccess || n <= 0) {
         cudaGetLastError();
         n = 0;                        // two-SM products unavailable: the single-SM kernel is used
     }
-    g_pair_clusters[S] = n;
+    g_pair_clusters[S][EMB] = n;
     return 0;
 }
 
@@ -1767,8 +1817,9 @@ int tags_ldl_tc_prepare() {
         if (!rc) rc = set_gemm_attr<2, 1>();
         if (!rc) rc = set_gemm_attr<3, 0>();
         if (!rc) rc = set_gemm_attr<3, 1>();
-        if (!rc) rc = set_gemm2_attr<2>();
-        if (!rc) rc = set_gemm2_attr<3>();
+        if (!rc) rc = set_gemm2_attr<2, 0>();
+        if (!rc) rc = set_gemm2_attr<3, 0>();
+        if (!rc) rc = set_gemm2_attr<2, 1>();
         if (!rc && cudaFuncSetAttribute(k_ldl_diag, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(TB * DIAG_LD * sizeof(float2))) != cudaSuccess)
             rc = tags_fail(TAGS_E_CUDA, "cudaFuncSetAttribute(k_ldl_diag) failed");
@@ -1794,17 +1845,18 @@ static int launch_gemm_m(const CUtensorMap& mA, const CUtensorMap& mB, const Gem
 }
 
 // Mode-0 update on the two-SM kernel: clusters of two CTAs walk the pair
-// tiles (mB64: the operand map with 64-row boxes, each CTA's half of B).
-template <int S>
-static int launch_gemm2_m(const CUtensorMap& mA, const CUtensorMap& mB64, const GemmArgs& g, cudaStream_t st) {
+// tiles (mB: the operand map with 64-row boxes, each CTA's half of B; with
+// EMB the 128-row map, each CTA's B rows of the real form).
+template <int S, int EMB>
+static int launch_gemm2_m(const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g, cudaStream_t st) {
     const int T = pair_rows(g);
     const long long total = (long long)pair_count(g, T) * g.nb;
     if (total <= 0) return 0;
-    const int clusters = (int)std::min<long long>(total, g_pair_clusters[S]);
+    const int clusters = (int)std::min<long long>(total, g_pair_clusters[S][EMB]);
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(2 * clusters);
     cfg.blockDim = dim3(GEMM_THREADS);
-    cfg.dynamicSmemBytes = Gemm2Cfg<S>::SMEM;
+    cfg.dynamicSmemBytes = Gemm2Cfg<S, EMB>::SMEM;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1813,15 +1865,17 @@ static int launch_gemm2_m(const CUtensorMap& mA, const CUtensorMap& mB64, const 
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    TAGS_CUDA_OK(cudaLaunchKernelEx(&cfg, k_gemm_tc2<S>, mA, mB64, g));
+    TAGS_CUDA_OK(cudaLaunchKernelEx(&cfg, k_gemm_tc2<S, EMB>, mA, mB, g));
     tags_note_launch();
     return 0;
 }
 
-static bool pair_ready(int NS) { return g_pair_clusters[NS == 3 ? 3 : 2] > 0; }
+static bool pair_ready(int NS, int emb) { return g_pair_clusters[NS == 3 ? 3 : 2][emb ? 1 : 0] > 0; }
 
-static int launch_gemm2(int NS, const CUtensorMap& mA, const CUtensorMap& mB64, const GemmArgs& g, cudaStream_t st) {
-    return NS == 3 ? launch_gemm2_m<3>(mA, mB64, g, st) : launch_gemm2_m<2>(mA, mB64, g, st);
+static int launch_gemm2(int NS, int emb, const CUtensorMap& mA, const CUtensorMap& mB, const GemmArgs& g,
+                        cudaStream_t st) {
+    if (emb) return launch_gemm2_m<2, 1>(mA, mB, g, st);
+    return NS == 3 ? launch_gemm2_m<3, 0>(mA, mB, g, st) : launch_gemm2_m<2, 0>(mA, mB, g, st);
 }
 
 // One GEMM launch: K = 32 g.kblocks from the operand maps (mA, mB).
@@ -1926,7 +1980,10 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
     if (!e) e = make_plane_map(&mLin, Lin, TB, 2 * SMAX, batch_cap);
     if (!e) e = make_plane_map(&mLg64, Lg, N, 2 * SMAX, batch_cap, KG, TB / 2);
     if (e) return e;
-    const bool use_pairs = pairs != 0 && pair_ready(NS);
+    // pairs: 0 one SM per tile; 1 two-SM tiles in complex form; 2 two-SM tiles
+    // in real form (S = 2 only, else the complex form)
+    const int emb = pairs == 2 && NS == 2 && pair_ready(NS, 1) ? 1 : 0;
+    const bool use_pairs = pairs != 0 && pair_ready(NS, emb);
     TAGS_CUDA_OK(cudaMemsetAsync(info, 0, sizeof(int) * nb, st));
     const int G = group_panels < 1 ? 1 : (group_panels > GMAX ? GMAX : group_panels);
 
@@ -1982,6 +2039,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.Lp = Lg;
         g.prow0 = jp + jb - jg;
         g.kcol0 = TB * p;
+        g.neg_planes = use_pairs && emb;
         int pf = tags_prof_begin(TAGS_PROF_LDL_PANEL, st);
         int e1 = launch_gemm(NS, mA21, mLin, g, st);
         // triangular solve: r x jb unknowns against jb x jb (r = rest minus the band), 4 r jb^2 flops
@@ -2009,7 +2067,7 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.Mn = Mn;
         g.Np = Mn > 0 ? A21p : nullptr;
         int pf = tags_prof_begin(TAGS_PROF_LDL_TRAIL, st);
-        int e1 = use_pairs ? launch_gemm2(NS, mLg, mLg64, g, st) : launch_gemm(NS, mLg, mLg, g, st);
+        int e1 = use_pairs ? launch_gemm2(NS, emb, mLg, emb ? mLg : mLg64, g, st) : launch_gemm(NS, mLg, mLg, g, st);
         // rank-K update outside the zero band: 8 K cells flops (cells: the triangle or the block column)
         const double r = M - (double)(g.zhi - g.zlo);
         const double K = g.kblocks * BK;
@@ -2075,7 +2133,8 @@ static int debug_ldl_impl(tags_cdouble* a, tags_cdouble* b, int N, int nb, int p
 static int g_debug_pairs = 0;     // tags_debug_ldl*: mode-0 updates on two-SM clusters
 
 extern "C" int tags_debug_tc_pairs(int on) {
-    g_debug_pairs = on ? 1 : 0;
+    if (on < 0 || on > 2) return tags_fail(TAGS_E_ARG, "tags_debug_tc_pairs: 0, 1 or 2");
+    g_debug_pairs = on;
     return 0;
 }
 

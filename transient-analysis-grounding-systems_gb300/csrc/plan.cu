@@ -436,7 +436,8 @@ extern "C" int tags_plan_set_refine_tol(tags_plan plan, double tol) {
 
 extern "C" int tags_plan_set_tc_pairs(tags_plan plan, int on) {
     if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_tc_pairs: invalid plan");
-    const int v = on ? 1 : 0;
+    if (on < 0 || on > 2) return tags_fail(TAGS_E_ARG, "tags_plan_set_tc_pairs: 0, 1 or 2");
+    const int v = on;
     if (plan->tc_pairs != v) {
         plan->tc_pairs = v;
         tags_plan_drop_graphs(plan);
