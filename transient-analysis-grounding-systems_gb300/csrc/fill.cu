@@ -1162,7 +1162,6 @@ struct MomCoef {
     float a[MOM_HEAD][4];      // (-gamma)^n / n!, n < MOM_HEAD: re (hi, lo), im (hi, lo)
     float2 g;                  // gamma (FP32), for the Horner tail
     float2 a8;                 // (-gamma)^MOM_HEAD / MOM_HEAD! (FP32)
-    float cT[4], cTi[4], cL[4];   // scale factors (re hi, re lo, im hi, im lo); cLi = cL (ref_l = 1)
     int nt;                    // terms this sample needs (<= MOM_N)
     int ok;                    // 1: the series reaches 1e-14 within MOM_N terms
 };
@@ -1188,15 +1187,6 @@ __global__ void k_mom_coef(const SampleCoef* __restrict__ coef, int nsamp, doubl
     }
     o.a8 = make_float2((float)an.x, (float)an.y);
     o.g = make_float2((float)c.gamma.x, (float)c.gamma.y);
-    const double2 cc[3] = {c.cT, c.cTi, c.cL};
-    float* dst[3] = {o.cT, o.cTi, o.cL};
-    for (int j = 0; j < 3; ++j) {
-        const DF r = df_of(cc[j].x), im = df_of(cc[j].y);
-        dst[j][0] = r.h;
-        dst[j][1] = r.l;
-        dst[j][2] = im.h;
-        dst[j][3] = im.l;
-    }
     const double xg = sqrt(cabs2(c.gamma)) * dmax;
     double term = 1.0;
     int nt = 0;
@@ -1211,16 +1201,23 @@ __global__ void k_mom_coef(const SampleCoef* __restrict__ coef, int nsamp, doubl
     ok[q] = o.ok;
 }
 
-// e^{-gamma b h} per bucket b and sample (FP64, stored as complex float pairs
-// [b][sample]).
+// The series' sample factors per bucket b and sample, formed in FP64 and
+// stored as complex float pairs: tab[v][b][sample] = f_v e^{-gamma b h} with
+// f_0 = cT (direct ZT), f_1 = cTi (image ZT), f_2 = cL (ZL, both kinds: ref_l
+// = 1), so each (pair, kind) multiplies its series by one table value per
+// matrix instead of by e^{-gamma b h} and then by the factor.
 __global__ void k_mom_table(const SampleCoef* __restrict__ coef, int nsamp, int nb, int bstride,
                             float4* __restrict__ tab) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
     if (q >= nsamp || b >= nb) return;
-    const double2 g = coef[q].gamma;
-    const double2 e = cexp_d(make_double2(-g.x * b * MOM_H, -g.y * b * MOM_H));
-    const DF r = df_of(e.x), im = df_of(e.y);
-    tab[(long long)b * bstride + q] = make_float4(r.h, r.l, im.h, im.l);
+    const SampleCoef c = coef[q];
+    const double2 e = cexp_d(make_double2(-c.gamma.x * b * MOM_H, -c.gamma.y * b * MOM_H));
+    const double2 f[3] = {c.cT, c.cTi, c.cL};
+    for (int v = 0; v < 3; ++v) {
+        const double2 t = cmul(f[v], e);
+        const DF r = df_of(t.x), im = df_of(t.y);
+        tab[((long long)v * nb + b) * bstride + q] = make_float4(r.h, r.l, im.h, im.l);
+    }
 }
 
 // J of one (pair, kind) for this lane's sample from the staged record and
@@ -1261,8 +1258,8 @@ struct MomWarpSmem {
 // added afterwards by k_fill_special64.
 __global__ void __launch_bounds__(MOM_WARPS * 32) k_fill_moment(
     int m, const float* __restrict__ mom, const MomRec* __restrict__ rec, const MomCoef* __restrict__ coef,
-    const float4* __restrict__ tab, int tstride, int nsamp, float2* zl0, float2* zt0, float2* zlo0, float2* ztlo0,
-    long long bstride, long long ntiles, int* status) {
+    const float4* __restrict__ tab, int tstride, int tnb, int nsamp, float2* zl0, float2* zt0, float2* zlo0,
+    float2* ztlo0, long long bstride, long long ntiles, int* status) {
     __shared__ MomWarpSmem sw_all[MOM_WARPS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     MomWarpSmem& W = sw_all[warp];
@@ -1280,9 +1277,6 @@ __global__ void __launch_bounds__(MOM_WARPS * 32) k_fill_moment(
     ntw = __reduce_max_sync(0xffffffffu, ntw);
     const long long pstart = (long long)i * (2LL * m - i + 1) / 2;
     const int k_lo = max(i, 32 * kb), k_hi = min(m, 32 * kb + 32);
-    const CDF cT{DF{c.cT[0], c.cT[1]}, DF{c.cT[2], c.cT[3]}};
-    const CDF cTi{DF{c.cTi[0], c.cTi[1]}, DF{c.cTi[2], c.cTi[3]}};
-    const CDF cL{DF{c.cL[0], c.cL[1]}, DF{c.cL[2], c.cL[3]}};
     for (int k0 = k_lo; k0 < k_hi; k0 += FILL_SUB) {
         const int kend = min(k_hi, k0 + FILL_SUB);
         for (int k = k0; k < kend; ++k) {
@@ -1298,12 +1292,15 @@ __global__ void __launch_bounds__(MOM_WARPS * 32) k_fill_moment(
                 const MomRec rc = W.rc[kind];
                 if (!rc.regular) continue;
                 const CDF S = mom_series(W.mv[kind], ntw, c);
-                const float4 t4 = valid ? tab[(long long)rc.b * tstride + smp] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const CDF J = cdf_mul(CDF{DF{t4.x, t4.y}, DF{t4.z, t4.w}}, S);
-                zt = cdf_add(zt, cdf_mul(kind == 0 ? cT : cTi, J));
+                // cT (or cTi) e^{-gamma b h} and cL e^{-gamma b h} from the table
+                const float4 tt = valid ? tab[((long long)kind * tnb + rc.b) * tstride + smp]
+                                        : make_float4(0.f, 0.f, 0.f, 0.f);
+                zt = cdf_add(zt, cdf_mul(CDF{DF{tt.x, tt.y}, DF{tt.z, tt.w}}, S));
                 const DF fl{rc.fl_hi, rc.fl_lo};
                 if (fl.h != 0.f) {
-                    const CDF lj = cdf_mul(cL, J);
+                    const float4 tl = valid ? tab[((long long)2 * tnb + rc.b) * tstride + smp]
+                                            : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const CDF lj = cdf_mul(CDF{DF{tl.x, tl.y}, DF{tl.z, tl.w}}, S);
                     zl = cdf_add(zl, CDF{df_mul(lj.re, fl), df_mul(lj.im, fl)});
                 }
             }
@@ -1464,7 +1461,7 @@ int tags_launch_fill_mixed(const double* d_elec, const double* d_img, int m, voi
     const long long ntiles = 16LL * (KB - 1) * KB + m;
     dim3 grid((unsigned)((ntiles + MOM_WARPS - 1) / MOM_WARPS), (unsigned)((nsamp + 31) / 32));
     k_fill_moment<<<grid, MOM_WARPS * 32, 0, st>>>(m, mf.mom, reinterpret_cast<const MomRec*>(mf.rec), mc, mf.tab,
-                                                   mf.batch, nsamp, d_zl, d_zt, d_zlo, d_ztlo, bstride, ntiles,
+                                                   mf.batch, mf.nb, nsamp, d_zl, d_zt, d_zlo, d_ztlo, bstride, ntiles,
                                                    d_status);
     // samples the series does not reach: FP32 quadrature (warps with none leave at once)
     dim3 gq((unsigned)((ntiles + FILL_WARPS - 1) / FILL_WARPS), (unsigned)((nsamp + 31) / 32));
@@ -1515,7 +1512,7 @@ int tags_moment_fill_build(const double* d_elec, const double* d_img, int m, int
     TAGS_CUDA_OK(cudaMalloc(&mf->rec, sizeof(MomRec) * npk));
     TAGS_CUDA_OK(cudaMalloc(&mf->coef, sizeof(MomCoef) * batch));
     TAGS_CUDA_OK(cudaMalloc(&mf->ok, sizeof(int) * batch));
-    TAGS_CUDA_OK(cudaMalloc(&mf->tab, sizeof(float4) * (size_t)mf->nb * batch));
+    TAGS_CUDA_OK(cudaMalloc(&mf->tab, sizeof(float4) * 3 * (size_t)mf->nb * batch));
     k_moments<<<(unsigned)((npk + 3) / 4), 128, 0, st>>>(d_elec, d_img, m, has_img, mf->mom,
                                                           reinterpret_cast<MomRec*>(mf->rec));
     tags_note_launch();

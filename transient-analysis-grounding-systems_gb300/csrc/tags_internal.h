@@ -72,7 +72,7 @@ struct MomentFill {
     void* rec = nullptr;         // (pair, kind) records
     void* coef = nullptr;        // per-sample constants, batch
     int* ok = nullptr;           // per sample: 1 where the series reaches FP64 accuracy (else the FP32 quadrature)
-    float4* tab = nullptr;       // e^{-gamma b h}: [bucket][sample], complex float pairs
+    float4* tab = nullptr;       // f e^{-gamma b h}, f = cT, cTi, cL: [3][bucket][sample], complex float pairs
     int nb = 0;                  // buckets
     double dmax = 0.0;           // bound of |r - R| over the pairs (m)
     int batch = 0;
