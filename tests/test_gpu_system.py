@@ -260,14 +260,26 @@ def test_two_pipelines_match_one(gpu_pkg, graphs, pipes):
     ie = np.zeros((len(idx), nodes.shape[0]), np.complex128)
     ie[:, 0] = gd["inj_s"][idx]
     plan = pkg.Plan(e, img, nodes, pkg.MIXED, max_batch=16, graphs=graphs)
+    count = pkg.lib().tags_gpu_launch_count
     try:
+        c0 = count()
         one, info1, st1 = plan.run(s, kappa, 1.0, ie)
+        c1 = count()
         plan.set_pipelines(pipes)
-        two, info2, st2 = plan.run(s, kappa, 1.0, ie)
+        two, info2, st2 = plan.run(s, kappa, 1.0, ie)      # the twins capture their graphs here
+        c2 = count()
+        again, _, _ = plan.run(s, kappa, 1.0, ie)
+        c3 = count()
         plan.set_split(3)                       # settings follow to the twins
         three, info3, _ = plan.run(s, kappa, 1.0, ie)
     finally:
         plan.close()
+    # the same passes launch the same kernels whichever pipeline runs them,
+    # and captures made on concurrent host threads are not counted (a few
+    # percent allowed for a refinement step more or less)
+    n1, n2, n3 = c1 - c0, c2 - c1, c3 - c2
+    assert n1 > 0 and abs(n2 - n1) <= 0.05 * n1 and abs(n3 - n1) <= 0.05 * n1
+    assert np.max(np.abs(again - two)) <= 1e-12 * np.max(np.abs(two))
     assert np.all(info1 == 0) and np.all(info2 == 0) and np.all(info3 == 0)
     assert st1.max_iterations == st2.max_iterations and st1.fallbacks == st2.fallbacks == 0
     assert np.max(np.abs(two - one)) <= 1e-12 * np.max(np.abs(one))

@@ -25,6 +25,7 @@ using zd = std::complex<double>;
 namespace {
 
 std::atomic<long long> g_launches{0};
+thread_local long long t_launches = 0;    // this host thread's share (graph capture subtracts its own)
 std::atomic<int> g_quiet{-1};
 thread_local std::string g_last_error;
 std::mutex g_mutex;
@@ -41,7 +42,12 @@ bool quiet() {
 
 }  // namespace
 
-void tags_note_launch(long long n) { g_launches += n; }
+void tags_note_launch(long long n) {
+    g_launches += n;
+    t_launches += n;
+}
+
+long long tags_thread_launch_count() { return t_launches; }
 
 // drop-ins in other translation units share the scratch slots, so they
 // serialise on the same lock

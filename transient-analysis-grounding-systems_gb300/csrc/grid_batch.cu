@@ -94,7 +94,7 @@ static double bytes_per_sample(int m, int n, int precision) {
 // One capture of every grid's passes (see the file comment).
 static int capture_batch(tags_batch_s* b) {
     cudaStream_t s0 = b->stream;
-    const long long l0 = tags_gpu_launch_count();
+    const long long l0 = tags_thread_launch_count();
     std::vector<Body> bodies;
     TAGS_CUDA_OK(cudaStreamBeginCapture(s0, cudaStreamCaptureModeRelaxed));
     int err = 0;
@@ -153,7 +153,7 @@ static int capture_batch(tags_batch_s* b) {
     cudaGraph_t graph = nullptr;
     ce = cudaStreamEndCapture(s0, &graph);
     if (!err && ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
-    const long long l1 = tags_gpu_launch_count();
+    const long long l1 = tags_thread_launch_count();
     // the refinement step of every while-node, captured into its body
     for (const Body& bd : bodies) {
         if (err) break;
@@ -168,7 +168,7 @@ static int capture_batch(tags_batch_s* b) {
         ce = cudaStreamEndCapture(st, &g2);
         if (!err && ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaStreamEndCapture (body)", __FILE__, __LINE__);
     }
-    const long long l2 = tags_gpu_launch_count();
+    const long long l2 = tags_thread_launch_count();
     tags_note_launch(-(l2 - l0));      // captured, not launched
     if (!err) {
         ce = cudaGraphInstantiate(&b->exec, graph, 0);

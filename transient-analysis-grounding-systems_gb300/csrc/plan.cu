@@ -340,7 +340,7 @@ int tags_plan_add_while_node(cudaStream_t st, cudaGraphConditionalHandle* cond, 
 // clears the condition. Nothing runs during the capture.
 static int capture_pass(tags_plan_s* p, int nb, double mur, int has_ie, int inj, tags_plan_s::GraphPass* gp) {
     cudaStream_t st = p->stream;
-    const long long l0 = tags_gpu_launch_count();
+    const long long l0 = tags_thread_launch_count();
     TAGS_CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     int err = tags_plan_coef(p, p->d_sin, p->d_sin + p->batch, mur, nb, st);
     if (!err) err = tags_plan_rhs(p, p->d_x, has_ie ? p->d_iein : nullptr, inj, nb, st);
@@ -358,7 +358,7 @@ static int capture_pass(tags_plan_s* p, int nb, double mur, int has_ie, int inj,
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamEndCapture(st, &g);
     if (!err && ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaStreamEndCapture", __FILE__, __LINE__);
-    const long long l1 = tags_gpu_launch_count();
+    const long long l1 = tags_thread_launch_count();
     if (!err && body) {
         ce = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
         if (ce != cudaSuccess) {
@@ -370,7 +370,7 @@ static int capture_pass(tags_plan_s* p, int nb, double mur, int has_ie, int inj,
             if (!err && ce != cudaSuccess) err = tags_fail_cuda(ce, "cudaStreamEndCapture (body)", __FILE__, __LINE__);
         }
     }
-    const long long l2 = tags_gpu_launch_count();
+    const long long l2 = tags_thread_launch_count();
     tags_note_launch(-(l2 - l0));      // captured, not launched
     if (!err) {
         ce = cudaGraphInstantiate(&gp->exec, g, 0);

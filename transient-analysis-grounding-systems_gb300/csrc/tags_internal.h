@@ -100,8 +100,12 @@ int tags_launch_path_pairs(const double* d_elec, int m, const double* d_paths, i
 // Gauss-Legendre nodes (ascending) and weights on [0, 1] (host side).
 void tags_gauss_legendre(int q, double* x, double* w);
 
-// Bookkeeping of kernel launches (reported by tags_gpu_launch_count).
+// Bookkeeping of kernel launches (reported by tags_gpu_launch_count), also
+// per host thread: a graph capture measures and removes its own launches by
+// the calling thread's count, so passes captured on other threads at the
+// same time (the pipelines' twins) do not disturb it.
 void tags_note_launch(long long n = 1);
+long long tags_thread_launch_count();
 
 // assemble.cu
 int tags_incidence_codes(const double* d_elec, int m, const double* d_nodes, int n, signed char* d_cond,
