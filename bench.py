@@ -1014,6 +1014,12 @@ def main():
         return 0
     peaks = measured_peaks()
     roof, fams = roofline(prof, peaks, split, samples_per_pass=B)
+    if roof is not None and mixed:
+        # the whole job in the dense complex LU count: (8/3) N^3 real flops per sample
+        lu = 8.0 / 3.0 * float(N) ** 3 * value / 1e12
+        roof["lu_equivalent"] = {"tflops": lu, "frac": lu / peaks["bf16_tflops"],
+                                 "note": "(8/3) N^3 real flops per sample, the dense complex LU count with its "
+                                         "structural zeros and symmetry, times the job's solves/s; same peak"}
     line = {"metric": "Laplace-sample solves/s (1560-segment grid, 2048 samples)", "value": value,
             "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dev_time / args.steps, "step_ms": measured_step_ms,
