@@ -380,15 +380,15 @@ int tags_plan_set_fill (tags_plan plan, int integration_type);
 /* Result of tags_plan_tune: the configuration kept and its measured rate. */
 typedef struct {
     int samples_per_pass;      /* samples factorised together (<= the plan's capacity) */
-    int panels_per_update;     /* 128-column panels per trailing update (1, 2 or 4; K = 128 x that) */
+    int panels_per_update;     /* 128-column panels per trailing update (1, 2, 4 or 6; K = 128 x that) */
     int split;                 /* split form kept (TAGS_MIXED; 0 for TAGS_PLAIN_FP64) */
     double solves_per_second;  /* device rate of the kept configuration on the given samples */
     int candidates;            /* configurations timed */
 } tags_tune_result;
 
 /* Autotuner: times one pass for each candidate configuration (samples per
- * pass in powers of two up to the plan's capacity; for TAGS_MIXED also 1, 2
- * or 4 panels per trailing update and the fp16 or three-piece bf16 split) on
+ * pass in powers of two up to the plan's capacity; for TAGS_MIXED also 1, 2,
+ * 4 or 6 panels per trailing update and the fp16 or three-piece bf16 split) on
  * the first samples of s / kappa (ns >= 1; unit current at inj_node; flags as
  * in tags_plan_run) and keeps the fastest in the plan. Quadrature orders are
  * not tuned: they follow the fill's error model, so accuracy does not depend
@@ -497,7 +497,7 @@ int tags_debug_ldl (tags_cdouble *a, int N, int nb, int pieces);
  * and columns zl_m .. 2 zl_m - 1 structurally zero against columns 0 ..
  * zl_m - 1 (the ZL/ZT coupling of the immittance system), which the
  * factorisation and the solves skip. group: 128-column panels per trailing
- * update (1, 2 or 4). */
+ * update (1 .. 6). */
 int tags_debug_ldl_solve (tags_cdouble *a, tags_cdouble *b, int N, int nb, int pieces, int zl_m, int group);
 
 /* No counterpart in the reference. FP64 throughput of the current device, in

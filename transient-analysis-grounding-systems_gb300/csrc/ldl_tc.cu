@@ -39,7 +39,7 @@
 namespace {
 
 constexpr int TB = 128;                 // panel width and tile edge
-constexpr int GMAX = 4;                 // most panels per trailing update (K up to 512)
+constexpr int GMAX = 6;                 // most panels per trailing update (K up to 768)
 constexpr int KG = TB * GMAX;           // K extent of a group's plane buffers
 
 // Split planes are K-block-major: plane p of a buffer with R rows and K

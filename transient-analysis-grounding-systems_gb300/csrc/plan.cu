@@ -470,14 +470,14 @@ extern "C" int tags_plan_tune(tags_plan plan, const tags_cdouble* s, const tags_
     for (int b = 16; b < cap; b *= 2) sizes.push_back(b);
     sizes.push_back(cap);
     const bool mixed = p->precision != TAGS_PLAIN_FP64;
-    const int groups[3] = {4, 2, 1};
+    const int groups[4] = {6, 4, 2, 1};
     const int splits[2] = {TAGS_SPLIT_F16, 3};
     tags_tune_result best{};
     best.solves_per_second = -1.0;
     const int saved_pass = p->pass_batch, saved_group = p->group_panels, saved_split = p->split_pieces;
     int count = 0;
     for (int b : sizes)
-        for (int ip = 0; ip < (mixed ? 3 : 1); ++ip)
+        for (int ip = 0; ip < (mixed ? 4 : 1); ++ip)
             for (int is = 0; is < (mixed ? 2 : 1); ++is) {
                 p->pass_batch = b;
                 if (mixed) {

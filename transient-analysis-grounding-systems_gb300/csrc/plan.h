@@ -78,7 +78,7 @@ struct tags_plan_s {
     int fill_model = TAGS_INTG_DOUBLE;  // TAGS_INTG_DOUBLE (double line integrals) or TAGS_INTG_MHEM
     double2* d_pot = nullptr;       // mHEM: 4 x m x m static potentials (direct ZL, ZT; images ZL, ZT)
     SampleCoef* d_coef1 = nullptr;  // unit coefficients for the potentials
-    int group_panels = 4;           // tensor-core LDL^T: panels per trailing update (1, 2 or 4; K = 128 x that)
+    int group_panels = 6;           // tensor-core LDL^T: panels per trailing update (1 .. 6; K = 128 x that)
     int max_steps = 40;             // refinement steps per pass before the FP64 fallback (1 .. 40)
     int tc_pairs = 0;               // trailing updates on two-SM clusters (tcgen05 cta_group::2)
     double ir_tol = 1e-9;           // refinement stopping tolerance (relative error left in x)
