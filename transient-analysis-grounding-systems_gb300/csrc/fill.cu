@@ -734,21 +734,32 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
     const int mat0 = blockIdx.y * MIRROR_MATS;
     const int KB = (m + 31) / 32;
+    const int r = bk * 32 + tx;                        // this thread's row of the lower tile
+    // the four lower entries of this thread in matrix mat (columns bi * 32 + ty + 8 jj),
+    // loaded one matrix ahead so that they travel while the previous one is stored
+    float2 v[4];
+    auto load = [&](int mat) {
+        const float2* Z = ((mat & 1) ? zt0 : zl0) + bstride * (mat >> 1);
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int cc = bi * 32 + ty + 8 * jj;
+            v[jj] = r < m && cc < m && r >= cc ? Z[r + (long long)m * cc] : make_float2(0.f, 0.f);
+        }
+    };
+    if (mat0 < nmat) load(mat0);
     for (int q = 0; q < MIRROR_MATS; ++q) {
         const int mat = mat0 + q;                      // 2 x sample + (0: ZL, 1: ZT)
         if (mat >= nmat) break;
         float2* Z = ((mat & 1) ? zt0 : zl0) + bstride * (mat >> 1);
         float2 (*T)[33] = tile[q & 1];                 // two buffers: one barrier per matrix
-        float rowmx = 0.f, rowsm = 0.f;                // row bk * 32 + tx over this thread's columns
-        for (int j = ty; j < 32; j += 8) {
-            const int r = bk * 32 + tx, cc = bi * 32 + j;
-            float a = 0.f;
-            if (r < m && cc < m && r >= cc) {
-                const float2 z = Z[r + (long long)m * cc];
-                if (r > cc) T[j][tx] = z;
-                a = sqrtf(z.x * z.x + z.y * z.y);
-            }
+        float rowmx = 0.f, rowsm = 0.f;                // row r over this thread's columns
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+            const int j = ty + 8 * jj, cc = bi * 32 + j;
+            if (r < m && cc < m && r > cc) T[j][tx] = v[jj];
             if (pmax) {
+                // v is zero outside the lower triangle and the matrix
+                const float a = sqrtf(v[jj].x * v[jj].x + v[jj].y * v[jj].y);
                 rowmx = fmaxf(rowmx, a);
                 rowsm += a;
                 // column cc below the diagonal: row cc's entries in this tile
@@ -767,10 +778,11 @@ __global__ void __launch_bounds__(256) k_zmirror(float2* zl0, float2* zt0, long 
             rmx[q & 1][ty][tx] = rowmx;
             rsm[q & 1][ty][tx] = rowsm;
         }
+        if (q + 1 < MIRROR_MATS && mat + 1 < nmat) load(mat + 1);
         __syncthreads();
         for (int j = ty; j < 32; j += 8) {
-            const int cc = bi * 32 + tx, r = bk * 32 + j;     // element (row cc, column r) of the upper triangle
-            if (r < m && cc < m && r > cc) Z[cc + (long long)m * r] = T[tx][j];
+            const int cc = bi * 32 + tx, rr = bk * 32 + j;     // element (row cc, column rr) of the upper triangle
+            if (rr < m && cc < m && rr > cc) Z[cc + (long long)m * rr] = T[tx][j];
         }
         if (pmax && ty < 2) {
             float mx = 0.f, sm = 0.f;
