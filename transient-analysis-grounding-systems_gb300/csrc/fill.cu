@@ -21,6 +21,15 @@
 // The scaling and the quirks follow the reference: |cos theta| of the
 // direction vectors, ZL = 0 when cos < DBL_EPSILON (direct) and image ZL only
 // when cos > DBL_EPSILON, images include k = i and accumulate.
+// The mixed form's fill (entries as float pairs hi + lo, ~1e-14 of the FP64
+// fill): regular pairs by a moment expansion about the nearest multiple of
+// 1/8 m (FP64 moments once per plan, k_moments; a per-sample series in float
+// pairs times a per-sample FP64 table, k_fill_moment), pairs sharing an
+// endpoint by the FP64 series of their Duffy moments (k_touch_moments once,
+// k_fill_special64 per sample), the self term in closed form; the upper
+// triangle and the row statistics' partials by k_zmirror. k_fill_mixed (FP32
+// quadrature) covers the samples whose series would need more than MOM_N
+// terms.
 #include <map>
 #include <vector>
 

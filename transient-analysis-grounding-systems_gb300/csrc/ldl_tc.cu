@@ -1,27 +1,39 @@
-// Tensor-core LDL^T factorisation of the mixed form's working matrix.
+// Tensor-core LDL^T factorisation of the mixed form's working matrix, and the
+// triangular solves with its factors.
 //
 // The reordered, scaled immittance matrix W'' (complex, symmetric,
 // non-Hermitian) is factorised without pivoting as W'' = L D L^T in 128-column
-// panels (right-looking, lower triangle only):
-//   1. k_ldl_diag    : 128 x 128 diagonal block -> L11 (unit lower), D1, and
-//                      the explicit inverse L11^{-1} (one CTA per sample, in
-//                      shared memory, complex FP32);
-//   2. k_panel_planes: the block column A21 below it -> bf16 split planes;
-//   3. k_gemm_tc     : W21 = A21 L11^{-T} (the triangular solve as a GEMM),
-//                      L21 = W21 D1^{-1} in FP32 (for the solves) and
-//                      V21 = W21 D1^{-1/2} = L21 D1^{1/2} as split planes;
-//   4. k_gemm_tc     : A22 -= V21 V21^T (= L21 D1 L21^T) on the lower 128 x
-//                      128 tiles: one plane set feeds both operands.
+// panels (right-looking, lower triangle only), in groups of up to six panels:
+//   1. k_gemm_tc (mode 0, narrow): panel p's block column takes the update
+//      from panels 0 .. p-1 of its group (K = 128 p) and is written on as
+//      split planes;
+//   2. k_ldl_diag: the 128 x 128 diagonal block -> L11 (unit lower), D1 and
+//      the explicit inverse L11^{-1}, both in one elimination sweep (one CTA
+//      per sample, the block in registers, complex FP32);
+//   3. k_gemm_tc (mode 1): W21 = A21 L11^{-T} (the triangular solve as a
+//      GEMM), L21 = W21 D1^{-1} in FP32 (for the solves) and V21 = W21
+//      D1^{-1/2} = L21 D1^{1/2} as split planes into the group's buffer;
+//   4. k_gemm_tc (mode 0, after each group): A22 -= V V^T (= L D L^T) over the
+//      group's panels (K = 128 x panels) on the lower 128 x 128 tiles; one
+//      plane set feeds both operands. The zero ZL/ZT band is skipped.
 // The GEMMs run on the 5th-generation tensor cores: operands are staged in
-// shared memory by TMA (128-byte swizzle), tcgen05.mma (kind::f16, bf16 in,
-// FP32 accumulate) is issued by one thread, the two accumulators (real and
-// imaginary part, 128 x 128 FP32 each) live in tensor memory and are read
-// back with tcgen05.ld. A complex product is four real products; each real
-// operand is split into bf16 hi + lo, and hi*hi + hi*lo + lo*hi keeps about
-// 16 significant bits, so twelve tcgen05.mma per K step.
-// Every mbarrier wait has an iteration limit; on expiry the kernel raises an
-// error flag, lets its copies in flight land, frees its tensor memory and
-// returns.
+// shared memory by TMA (64-byte swizzle, K-block-major planes), tcgen05.mma
+// (kind::f16, FP32 accumulate) is issued by one thread, the two accumulators
+// (real and imaginary part, 128 x 128 FP32 each) live in tensor memory,
+// double-buffered, and are read back with tcgen05.ld by eight epilogue warps.
+// A complex product is four real products; each real operand is split into
+// two fp16 pieces of 2^8 x (about 22 significant bits; three bf16 pieces when
+// a value leaves the fp16 range), and hi*hi + hi*lo + lo*hi per real product
+// makes twelve tcgen05.mma per K step of 16. k_gemm_tc2 runs the same updates
+// on clusters of two SMs (tcgen05.mma.cta_group::2; a plan option, slower
+// here).
+// The solves L D L^T x = r of the refinement run as one CTA per sample with x
+// in shared memory (k_ldl_solve_cta), on clusters of CTAs per sample for small
+// passes and for refinement steps with few samples left (k_ldl_solve_cl), or
+// block by block where x does not fit in shared memory (k_blk_*).
+// Every mbarrier wait is bounded in time (%globaltimer); on expiry the kernel
+// raises an error flag, lets its copies in flight land, frees its tensor
+// memory and returns, and the pass is re-solved in FP64.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
