@@ -524,6 +524,12 @@ const char *tags_gpu_last_error (void);
 /* 0/1: suppress the reference-style messages printed on errors. */
 void tags_gpu_set_quiet (int quiet);
 
+/* No counterpart in the reference. Caps, process-wide, the free device memory
+ * that plans and grid batches size themselves against (bytes; 0 = no cap).
+ * Plans created afterwards take fewer samples per pass, or fail with
+ * TAGS_E_NOMEM when not even one sample fits. */
+int tags_gpu_set_memory_budget (unsigned long long bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,7 @@ EXPORTS = (
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
     "tags_debug_tc_pairs", "tags_debug_solve_path", "tags_debug_mixed_fill", "tags_probe_fp64",
+    "tags_gpu_set_memory_budget",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
     "tags_gpu_inlt", "tags_batch_create", "tags_batch_run", "tags_batch_destroy",
@@ -154,6 +155,8 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_tc_pairs.argtypes = [_vp, ctypes.c_int]
             L.tags_debug_tc_pairs.argtypes = [ctypes.c_int]
             L.tags_debug_solve_path.argtypes = [ctypes.c_int]
+            L.tags_gpu_set_memory_budget.argtypes = [ctypes.c_ulonglong]
+            L.tags_gpu_set_memory_budget.restype = ctypes.c_int
             L.tags_probe_fp64.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.tags_debug_tc_wait_limit.argtypes = [ctypes.c_longlong]
             L.tags_debug_mixed_fill.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _vp]
@@ -196,6 +199,12 @@ def lib() -> ctypes.CDLL:
                 getattr(L, name).restype = ctypes.c_int
             _lib = L
         return _lib
+
+
+def set_memory_budget(nbytes: int = 0) -> None:
+    """Cap the free device memory that plans and grid batches size themselves
+    against (0 removes the cap)."""
+    _ret(lib().tags_gpu_set_memory_budget(int(nbytes)))
 
 
 def last_error() -> str:

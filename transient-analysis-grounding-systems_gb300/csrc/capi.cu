@@ -7,6 +7,7 @@
 // Calls are serialised by a process-wide mutex; each uses the library's own
 // stream on the caller's current device.
 #include <atomic>
+#include <cmath>
 #include <complex>
 #include <cstdio>
 #include <cstdlib>
@@ -462,3 +463,30 @@ extern "C" int tags_inv_laplace_batch(double* f, const tags_cdouble* g, const ta
 extern "C" long long tags_gpu_launch_count(void) { return g_launches.load(); }
 extern "C" const char* tags_gpu_last_error(void) { return g_last_error.c_str(); }
 extern "C" void tags_gpu_set_quiet(int q) { g_quiet.store(q ? 1 : 0); }
+
+namespace {
+std::atomic<unsigned long long> g_mem_budget{0};     // 0: no cap
+}
+
+extern "C" int tags_gpu_set_memory_budget(unsigned long long bytes) {
+    g_mem_budget.store(bytes);
+    return 0;
+}
+
+bool tags_all_finite(const void* v, size_t n) {
+    if (!v) return true;
+    const double* d = static_cast<const double*>(v);
+    for (size_t i = 0; i < 2 * n; ++i)
+        if (!std::isfinite(d[i])) return false;
+    return true;
+}
+
+// Free device memory as the plans and grid batches size themselves against:
+// cudaMemGetInfo's figure, capped by tags_gpu_set_memory_budget.
+cudaError_t tags_free_memory(size_t* freeb) {
+    size_t tot = 0;
+    const cudaError_t e = cudaMemGetInfo(freeb, &tot);
+    const unsigned long long cap = g_mem_budget.load();
+    if (e == cudaSuccess && cap && *freeb > cap) *freeb = (size_t)cap;
+    return e;
+}

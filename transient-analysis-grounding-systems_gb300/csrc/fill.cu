@@ -215,8 +215,9 @@ TAGS_D int order_for(double ratio, double gl, bool tight) {
     int base;
     if (tight) base = ratio >= 16.0 ? 4 : ratio >= 8.0 ? 5 : ratio >= 4.0 ? 6 : 8;
     else base = ratio >= 8.0 ? 3 : ratio >= 4.0 ? 4 : 5;
-    int extra = (int)ceil((tight ? 1.5 : 1.0) * gl);
-    int q = base + extra;
+    // clamped before the conversion: a huge (or NaN) |gamma| L gives QMAX, never an overflow
+    const int extra = (int)ceil(fmin((tight ? 1.5 : 1.0) * gl, (double)QMAX));
+    const int q = base + extra;
     return q > QMAX ? QMAX : q;
 }
 
@@ -251,8 +252,9 @@ TAGS_D double2 pair_integral(const Seg& S, const Seg& R, double2 gamma, int ityp
             raise_status(status, TAGS_ST_DEGENERATE_PAIR);
             return cz(nan(""), nan(""));
         }
-        int q = 16 + 2 * (int)ceil(gabs * lmax);
-        if (!tight) q = 10 + (int)ceil(gabs * lmax);
+        const int glen = (int)ceil(fmin(gabs * lmax, (double)QMAX));    // clamped before the conversion
+        int q = 16 + 2 * glen;
+        if (!tight) q = 10 + glen;
         if (q > QMAX) q = QMAX;
         J = j_touch(R, S, ia, ib, gamma, stat, q, gl);
     } else {
@@ -612,9 +614,9 @@ __global__ void __launch_bounds__(FILL_WARPS * 32, 5) k_fill_mixed(
                 const float4 dr = kind == 0 ? sdir[k] : idir[k];
                 const PairRec rec = recs[2 * p + kind];
                 const float lmax = fmaxf(ds.w, dr.w);
-                const int P = min(32, max(code & 63, (int)ceilf(gmax * lmax / 1.5f)));
+                const int P = min(32, max(max(code & 63, 1), (int)ceilf(fminf(gmax * lmax / 1.5f, 32.f))));
                 const int qg = (code >> 6) & 63;
-                const int qq = min(QMIX, qg + (int)ceilf(gmax * lmax / P));
+                const int qq = min(QMIX, qg + (int)ceilf(fminf(gmax * lmax / P, (float)QMIX)));
                 const float* x = sxm + gl_off(qq);
                 const float* w = swf + gl_off(qq);
                 const float h = 1.f / (float)P;
@@ -960,7 +962,7 @@ __global__ void __launch_bounds__(SPEC_WARPS * 32) k_fill_special64(
             if (keep) dl = cadd(dl, cscale(cmul(cL, J), cost));
             continue;
         }
-        int q = valid ? min(QMAX, 16 + 2 * (int)ceil(sqrt(cabs2(c.gamma)) * lmax)) : 0;
+        int q = valid ? min(QMAX, 16 + 2 * (int)ceil(fmin(sqrt(cabs2(c.gamma)) * lmax, (double)QMAX))) : 0;
         q = __reduce_max_sync(0xffffffffu, q);
         double a[3], b[3];
         for (int d = 0; d < 3; ++d) {

@@ -219,8 +219,8 @@ extern "C" int tags_batch_create(tags_batch* out, const tags_grid_job* jobs, siz
     for (auto& e : b->events) BATCH_CHECK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     // memory admission: samples resident per grid (at most max_batch, or 256),
     // halving the largest consumer until all plans fit in 60 % of free memory
-    size_t freeb = 0, totb = 0;
-    BATCH_CHECK(cudaMemGetInfo(&freeb, &totb));
+    size_t freeb = 0;
+    BATCH_CHECK(tags_free_memory(&freeb));
     double io = 0.0;
     std::vector<double> per(njobs);
     std::vector<long long> res(njobs);
@@ -298,12 +298,16 @@ extern "C" int tags_batch_run(tags_batch batch, const tags_grid_job* jobs, size_
     }
     TAGS_CUDA_OK(cudaSetDevice(b->device));
     cudaStream_t s0 = b->stream;
+    for (size_t q = 0; q < njobs; ++q)
+        if (!tags_all_finite(jobs[q].s, jobs[q].ns) || !tags_all_finite(jobs[q].kappa, jobs[q].ns))
+            return tags_fail(TAGS_E_NONFINITE, "tags_batch_run: a job's s or kappa is not finite");
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     TAGS_CUDA_OK(cudaEventCreate(&e0));
     TAGS_CUDA_OK(cudaEventCreate(&e1));
     for (size_t q = 0; q < njobs; ++q) {
         const tags_grid_job& j = jobs[q];
         GridSlot& g = b->grids[q];
+        TAGS_CUDA_OK(cudaMemsetAsync(g.plan->d_status, 0, sizeof(int) * 4, s0));
         TAGS_CUDA_OK(cudaMemcpyAsync(g.d_s, j.s, sizeof(double2) * g.ns, cudaMemcpyHostToDevice, s0));
         TAGS_CUDA_OK(cudaMemcpyAsync(g.d_k, j.kappa, sizeof(double2) * g.ns, cudaMemcpyHostToDevice, s0));
         if (g.has_ie)
@@ -321,12 +325,17 @@ extern "C" int tags_batch_run(tags_batch batch, const tags_grid_job* jobs, size_
     acc.seconds = 1e-3 * ms;
     acc.split = b->precision == TAGS_PLAIN_FP64 ? 0 : TAGS_SPLIT_F16;
     long long launched = b->launches_fixed;
-    int first_err = 0;
+    int first_err = 0, all_status = 0;
     for (size_t q = 0; q < njobs; ++q) {
         const tags_grid_job& j = jobs[q];
         GridSlot& g = b->grids[q];
         tags_plan_s* p = g.plan;
-        if (b->precision != TAGS_PLAIN_FP64) {
+        // the fill's status word: a degenerate pair or a rejected sample
+        // fails the run (no FP64 re-solves for that grid)
+        int gst = 0;
+        TAGS_CUDA_OK(cudaMemcpy(&gst, p->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+        all_status |= gst;
+        if (b->precision != TAGS_PLAIN_FP64 && !gst) {
             const int bc = p->batch;
             std::vector<int> si((size_t)g.passes * (3 * bc + 2)), se(2 * (size_t)g.passes);
             std::vector<double> sd((size_t)g.passes * 3 * bc);
@@ -379,6 +388,11 @@ extern "C" int tags_batch_run(tags_batch batch, const tags_grid_job* jobs, size_
     }
     tags_note_launch(launched);
     if (stats) *stats = acc;
+    if (all_status & TAGS_ST_DEGENERATE_PAIR)
+        return tags_fail(TAGS_E_GEOMETRY, "coincident or overlapping segments: the pair integral diverges");
+    if (all_status & TAGS_ST_NONFINITE) return tags_fail(TAGS_E_NONFINITE, "non-finite value in the impedance fill");
+    if (all_status & TAGS_ST_BAD_ARG)
+        return tags_fail(TAGS_E_ARG, "a sample's propagation constant is outside the supported range (|gamma| > 1e5 / m)");
     return first_err;
 }
 

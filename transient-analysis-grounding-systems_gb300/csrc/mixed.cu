@@ -776,10 +776,25 @@ int tags_mixed_finish(tags_plan_s* p, int nb, cudaStream_t st, int* h_iters, dou
     std::vector<int> iri(3 * b + 2);
     std::vector<double> ird(3 * b);
     int tc_errs[2] = {0, 0};
+    int status = 0;
     TAGS_CUDA_OK(cudaMemcpyAsync(iri.data(), p->d_iri, sizeof(int) * (3 * b + 2), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaMemcpyAsync(ird.data(), p->d_ird, sizeof(double) * 3 * b, cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaMemcpyAsync(tc_errs, p->d_ldlerr, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    TAGS_CUDA_OK(cudaMemcpyAsync(&status, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     TAGS_CUDA_OK(cudaStreamSynchronize(st));
+    if (status & TAGS_ST_NONFINITE) {
+        // a non-finite input reached the fill (the run reports it): no
+        // re-solve in FP64, and no switch to bf16 pieces over a NaN that only
+        // looks like a value outside the fp16 range
+        TAGS_CUDA_OK(cudaMemsetAsync(p->d_ldlerr, 0, 2 * sizeof(int), st));
+        if (h_steps) *h_steps = iri[3 * b];
+        for (int q = 0; q < nb; ++q) {
+            h_iters[q] = iri[2 * b + q];
+            h_conv[q] = iri[b + q];
+            h_berr[q] = ird[2 * b + q];
+        }
+        return 0;
+    }
     if (tc_errs[1] && !tc_errs[0]) {
         // an fp16 split value left its range: this plan uses three bf16
         // pieces from now on (its graphs are recaptured), and the pass is

@@ -30,8 +30,12 @@ TAGS_D double2 csqrt_d(double2 z) {
     return make_double2(fabs(im), z.y >= 0.0 ? re : -re);
 }
 
+// |gamma| above this (1/m) is outside any soil and frequency the model serves;
+// the quadrature orders derived from |gamma| L stay far from integer range.
+constexpr double GAMMA_MAX = 1e5;
+
 __global__ void k_coef(const double2* __restrict__ s, const double2* __restrict__ kappa, double mur, int nb,
-                       SampleCoef* __restrict__ coef) {
+                       SampleCoef* __restrict__ coef, int* __restrict__ status) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= nb) return;
     double2 sk = s[k], kp = kappa[k];
@@ -47,6 +51,15 @@ __global__ void k_coef(const double2* __restrict__ s, const double2* __restrict_
     c.cT = cT;
     c.cLi = cL;                 // ref_l = 1
     c.cTi = cmul(ref_t, cT);
+    const bool finite = isfinite(c.gamma.x) && isfinite(c.gamma.y) && isfinite(c.cL.x) && isfinite(c.cL.y) &&
+                        isfinite(c.cT.x) && isfinite(c.cT.y) && isfinite(c.cTi.x) && isfinite(c.cTi.y);
+    if (!finite || !(cabs2(c.gamma) <= GAMMA_MAX * GAMMA_MAX)) {
+        // the run reports the sample (non-finite, or out of range); the
+        // kernels that follow see finite, small coefficients
+        atomicOr(status, finite ? TAGS_ST_BAD_ARG : TAGS_ST_NONFINITE);
+        c.gamma = make_double2(1e-3, 0.0);
+        c.cL = c.cT = c.cLi = c.cTi = make_double2(1.0, 0.0);
+    }
     coef[k] = c;
 }
 
@@ -66,7 +79,7 @@ __global__ void k_rhs(double2* __restrict__ X, int N, int n, const double2* __re
 }  // namespace
 
 int tags_plan_coef(tags_plan_s* p, const double2* d_s, const double2* d_kappa, double mur, int nb, cudaStream_t st) {
-    k_coef<<<(nb + 127) / 128, 128, 0, st>>>(d_s, d_kappa, mur, nb, p->d_coef);
+    k_coef<<<(nb + 127) / 128, 128, 0, st>>>(d_s, d_kappa, mur, nb, p->d_coef, p->d_status);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
     return 0;
@@ -221,8 +234,8 @@ extern "C" int tags_plan_create(tags_plan* out, const Electrode* electrodes, con
     p->d_W = nullptr;
     if (err) { plan_free(p); return err; }
     // batch size from free device memory
-    size_t freeb = 0, totb = 0;
-    PLAN_CHECK(cudaMemGetInfo(&freeb, &totb));
+    size_t freeb = 0;
+    PLAN_CHECK(tags_free_memory(&freeb));
     const double NN = (double)N * (double)N;
     double per = precision == TAGS_PLAIN_FP64
                      ? 16.0 * NN + 40.0 * N
@@ -686,6 +699,10 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     if (!p || !s || !kappa) return tags_fail(TAGS_E_ARG, "tags_plan_run: invalid argument");
     if (!ie && inj_node >= (size_t)p->n) return tags_fail(TAGS_E_ARG, "tags_plan_run: inj_node out of range");
     if (ns == 0) return 0;
+    // host inputs are checked here; device inputs by k_coef, which reports a
+    // non-finite sample and hands the kernels finite coefficients instead
+    if (!(flags & TAGS_RUN_DEVICE_PTRS) && (!tags_all_finite(s, ns) || !tags_all_finite(kappa, ns)))
+        return tags_fail(TAGS_E_NONFINITE, "tags_plan_run: s or kappa is not finite");
     TAGS_CUDA_OK(cudaSetDevice(p->device));
     cudaStream_t st = p->stream;
     DeviceCtx* ctx = tags_ctx();
@@ -758,5 +775,7 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
     if (stt & TAGS_ST_DEGENERATE_PAIR)
         return tags_fail(TAGS_E_GEOMETRY, "coincident or overlapping segments: the pair integral diverges");
     if (stt & TAGS_ST_NONFINITE) return tags_fail(TAGS_E_NONFINITE, "non-finite value in the impedance fill");
+    if (stt & TAGS_ST_BAD_ARG)
+        return tags_fail(TAGS_E_ARG, "a sample's propagation constant is outside the supported range (|gamma| > 1e5 / m)");
     return 0;
 }

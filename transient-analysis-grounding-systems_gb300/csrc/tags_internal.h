@@ -106,6 +106,10 @@ void tags_gauss_legendre(int q, double* x, double* w);
 // same time (the pipelines' twins) do not disturb it.
 void tags_note_launch(long long n = 1);
 long long tags_thread_launch_count();
+// Free device memory for sizing plans and grid batches (tags_gpu_set_memory_budget caps it).
+cudaError_t tags_free_memory(size_t* freeb);
+// Host arrays of n complex doubles (real, imaginary): all finite (null counts as finite).
+bool tags_all_finite(const void* v, size_t n);
 
 // assemble.cu
 int tags_incidence_codes(const double* d_elec, int m, const double* d_nodes, int n, signed char* d_cond,
