@@ -262,7 +262,8 @@ enum {
 
 /* Run flags. */
 enum {
-    TAGS_RUN_DEVICE_PTRS = 1    /* s, kappa, ie and the outputs are device pointers */
+    TAGS_RUN_DEVICE_PTRS = 1,   /* s, kappa, ie and the outputs are device pointers */
+    TAGS_TUNE_REFRESH = 256     /* tags_plan_tune only: time the candidates even where the tune cache holds the shape */
 };
 
 typedef struct tags_plan_s *tags_plan;
@@ -395,6 +396,18 @@ typedef struct {
  * on the tuner. out may be NULL. */
 int tags_plan_tune (tags_plan plan, const tags_cdouble *s, const tags_cdouble *kappa, double mur, size_t ns,
                     size_t inj_node, int flags, tags_tune_result *out);
+
+/* Autotuner cache file (process-wide; NULL or "" switches it off, the
+ * default). With a cache set, tags_plan_tune first looks for the plan's key:
+ * system size N, segments m, precision, impedance model, the samples it may
+ * put in one pass (min(capacity, ns)), pipelines, pair setting, and the GPU
+ * (name, SM count, compute capability). On a hit it applies the stored
+ * configuration without timing anything (candidates = 0, solves_per_second
+ * as stored); otherwise, or with TAGS_TUNE_REFRESH in flags, it times the
+ * candidates and appends a line. The file is plain text, one line per timed
+ * tune; the last line of a key wins. Returns TAGS_E_ARG if the file cannot be
+ * opened for appending. */
+int tags_gpu_set_tune_cache (const char *path);
 
 /* ---- Part 3: solve without device allocation -------------------------------- */
 

@@ -212,13 +212,78 @@ def test_autotuner_keeps_a_valid_configuration(gpu_pkg):
     try:
         res = plan.tune(gd["s"][:64], gd["kappa"][:64], inj_node=0)
         assert res.candidates >= 12
-        assert res.samples_per_pass in (16, 32, 64) and res.panels_per_update in (1, 2, 4) and res.split in (3, 16)
+        assert res.samples_per_pass in (16, 32, 64) and res.panels_per_update in (1, 2, 4, 6) and res.split in (3, 16)
         assert res.solves_per_second > 0
         ie = np.zeros((len(gd["s"]), nodes.shape[0]), np.complex128)
         ie[:, 0] = gd["inj_s"]
         sol, info, st = plan.run(gd["s"], gd["kappa"], ie=ie)
         assert np.all(info == 0) and st.fallbacks == 0
         assert np.max(np.abs(sol[:, 0] - gd["u0"]) / np.abs(gd["u0"])) < 1e-6
+    finally:
+        plan.close()
+
+
+def test_tune_cache_applies_a_stored_configuration(gpu_pkg, tmp_path):
+    """With a tune cache the first tune of a shape times the candidates and
+    appends one line; another plan of the same shape applies that line without
+    timing and solves within 1e-6 of the reference; TAGS_TUNE_REFRESH times
+    again and appends a second line."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    s, kappa = gd["s"][:32], gd["kappa"][:32]
+    path = tmp_path / "tune.txt"
+    pkg.set_tune_cache(str(path))
+    try:
+        plan = pkg.Plan(e, pkg.images(e), nodes, pkg.MIXED, max_batch=32)
+        try:
+            first = plan.tune(s, kappa, inj_node=0)
+        finally:
+            plan.close()
+        assert first.candidates >= 8
+        lines = path.read_text().splitlines()
+        N = nodes.shape[0] + 2 * e.shape[0]
+        assert len(lines) == 1 and f" N={N} m={e.shape[0]} prec={pkg.MIXED} " in lines[0] and " cap=32 " in lines[0]
+        plan = pkg.Plan(e, pkg.images(e), nodes, pkg.MIXED, max_batch=32)
+        try:
+            hit = plan.tune(s, kappa, inj_node=0)
+            assert hit.candidates == 0
+            assert (hit.samples_per_pass, hit.panels_per_update, hit.split) == \
+                (first.samples_per_pass, first.panels_per_update, first.split)
+            ie = np.zeros((len(gd["s"]), nodes.shape[0]), np.complex128)
+            ie[:, 0] = gd["inj_s"]
+            sol, info, st = plan.run(gd["s"], gd["kappa"], ie=ie)
+            assert np.all(info == 0) and st.fallbacks == 0
+            assert np.max(np.abs(sol[:, 0] - gd["u0"]) / np.abs(gd["u0"])) < 1e-6
+            again = plan.tune(s, kappa, inj_node=0, refresh=True)
+            assert again.candidates >= 8
+        finally:
+            plan.close()
+        assert len(path.read_text().splitlines()) == 2
+    finally:
+        pkg.set_tune_cache(None)
+
+
+def test_resumable_sweep_matches_one_run(gpu_pkg, tmp_path):
+    """Plan.run_resumable over chunks of 128 samples (the injection node's
+    potential kept) equals one run of the same plan within 1e-12; called again
+    it loads every chunk and launches no kernel."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    s, kappa = gd["s"][:300], gd["kappa"][:300]
+    plan = pkg.Plan(e, pkg.images(e), nodes, pkg.MIXED, max_batch=64)
+    try:
+        whole, info, _ = plan.run(s, kappa, inj_node=0)
+        assert np.all(info == 0)
+        d = str(tmp_path / "sweep")
+        u, info_r, st = plan.run_resumable(s, kappa, d, inj_node=0, chunk=128, columns=[0])
+        assert st["chunks_run"] == 3 and st["fallbacks"] == 0 and np.all(info_r == 0)
+        assert u.shape == (300, 1)
+        assert np.max(np.abs(u[:, 0] - whole[:, 0]) / np.abs(whole[:, 0])) <= 1e-12
+        before = pkg.launch_count()
+        u2, _, st2 = plan.run_resumable(s, kappa, d, inj_node=0, chunk=128, columns=[0])
+        assert st2["chunks_run"] == 0 and pkg.launch_count() == before and np.array_equal(u2, u)
     finally:
         plan.close()
 

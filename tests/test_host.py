@@ -175,6 +175,58 @@ def test_solve_batch_rejects_bad_jobs(pkg):
     assert L.tags_gpu_solve_batch(None, 0, pkg.MIXED, 1.0, 0, 2) == 0
 
 
+def test_tune_cache_setter_checks_its_file(pkg, tmp_path):
+    """tags_gpu_set_tune_cache opens the file for appending (creating it) and
+    keeps what is there; a path that cannot be opened is TAGS_E_ARG; None
+    switches the cache off. No GPU is touched."""
+    path = tmp_path / "tune.txt"
+    pkg.set_tune_cache(str(path))
+    assert path.exists() and path.read_text() == ""
+    path.write_text("tags-tune 1 N=1 m=1 prec=1 fill=2 cap=1 pipes=1 pairs=0 gpu=x/1/sm103 | 1 6 16 1\n")
+    pkg.set_tune_cache(str(path))
+    assert path.read_text().count("\n") == 1
+    with pytest.raises(RuntimeError, match=str(pkg.E_ARG)):
+        pkg.set_tune_cache(str(tmp_path))          # a directory
+    pkg.set_tune_cache(None)
+
+
+def test_resumable_sweep_resumes_after_an_interruption(pkg, tmp_path):
+    """A sweep interrupted inside a chunk keeps the chunks finished before it;
+    the next call with the same fingerprint runs only the rest and returns the
+    whole result; a finished sweep runs nothing; another sweep's fingerprint
+    is refused."""
+    calls = []
+
+    def runner(fail_at):
+        def run_chunk(k0, k1):
+            if k0 == fail_at:
+                raise RuntimeError("interrupted")
+            calls.append(k0)
+            x = np.arange(k0, k1, dtype=np.float64)
+            return ({"sol": np.stack([x, 2.0 * x], axis=1), "info": np.zeros(k1 - k0, np.int32)},
+                    {"fallbacks": k0, "seconds": 0.5})
+        return run_chunk
+
+    d = str(tmp_path / "sweep")
+    fp = pkg.sweep_fingerprint([np.arange(10.0), 1.0, None])
+    with pytest.raises(RuntimeError, match="interrupted"):
+        pkg.resumable_sweep(runner(6), 10, d, 3, fp)
+    assert calls == [0, 3]
+    calls.clear()
+    out, stats, ran = pkg.resumable_sweep(runner(-1), 10, d, 3, fp)
+    assert calls == [6, 9] and ran == 2
+    assert [t["fallbacks"] for t in stats] == [0, 3, 6, 9]
+    assert np.array_equal(out["sol"][:, 0], np.arange(10.0)) and np.array_equal(out["sol"][:, 1], 2 * np.arange(10.0))
+    assert out["info"].shape == (10,)
+    calls.clear()
+    out2, _, ran = pkg.resumable_sweep(runner(-1), 10, d, 3, fp)
+    assert calls == [] and ran == 0 and np.array_equal(out2["sol"], out["sol"])
+    with pytest.raises(ValueError, match="another sweep"):
+        pkg.resumable_sweep(runner(-1), 10, d, 3, pkg.sweep_fingerprint([np.arange(11.0), 1.0, None]))
+    with pytest.raises(ValueError, match="another sweep"):
+        pkg.resumable_sweep(runner(-1), 10, d, 4, fp)
+
+
 def test_bench_reference_arm_contract():
     """`bench.py --impl reference` (the CPU implementation of the path on the
     host cores) prints one JSON line carrying the bench contract's keys, with

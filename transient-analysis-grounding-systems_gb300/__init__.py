@@ -27,6 +27,8 @@ column-major layout (``z[i*m + k]`` = row k, column i).
 from __future__ import annotations
 
 import ctypes
+import hashlib
+import json
 import math
 import os
 import threading
@@ -40,6 +42,7 @@ INTG_NONE, INTG_DOUBLE, INTG_SINGLE, INTG_MHEM = 1, 2, 3, 4
 FILTER_NONE, FILTER_BLACKMAN, FILTER_HANNING, FILTER_LANCZOS, FILTER_RIESZ = range(5)
 PLAIN_FP64, MIXED = 0, 1
 RUN_DEVICE_PTRS = 1
+TUNE_REFRESH = 256
 E_ARG, E_CUDA, E_NOMEM, E_GEOMETRY, E_NONFINITE = -101, -102, -103, -104, -105
 SPLIT_BF16_2, SPLIT_BF16_3, SPLIT_F16 = 2, 3, 16
 
@@ -59,7 +62,7 @@ EXPORTS = (
     "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
     "tags_debug_tc_pairs", "tags_debug_solve_path", "tags_debug_mixed_fill", "tags_probe_fp64",
-    "tags_gpu_set_memory_budget",
+    "tags_gpu_set_memory_budget", "tags_gpu_set_tune_cache",
     "electric_potential", "magnetic_potential", "electric_field", "voltage", "tags_fields_batch",
     "tags_gpd_mhem_batch", "tags_voltage_batch", "tags_fields_evaluations", "tags_gpu_solve_batch",
     "tags_gpu_inlt", "tags_batch_create", "tags_batch_run", "tags_batch_destroy",
@@ -157,6 +160,8 @@ def lib() -> ctypes.CDLL:
             L.tags_debug_solve_path.argtypes = [ctypes.c_int]
             L.tags_gpu_set_memory_budget.argtypes = [ctypes.c_ulonglong]
             L.tags_gpu_set_memory_budget.restype = ctypes.c_int
+            L.tags_gpu_set_tune_cache.argtypes = [ctypes.c_char_p]
+            L.tags_gpu_set_tune_cache.restype = ctypes.c_int
             L.tags_probe_fp64.argtypes = [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
             L.tags_debug_tc_wait_limit.argtypes = [ctypes.c_longlong]
             L.tags_debug_mixed_fill.argtypes = [_vp, _vp, _vp, ctypes.c_double, _sz, _vp, _vp]
@@ -205,6 +210,13 @@ def set_memory_budget(nbytes: int = 0) -> None:
     """Cap the free device memory that plans and grid batches size themselves
     against (0 removes the cap)."""
     _ret(lib().tags_gpu_set_memory_budget(int(nbytes)))
+
+
+def set_tune_cache(path=None) -> None:
+    """Autotuner cache file (None switches it off): Plan.tune applies a stored
+    configuration for the plan's shape and GPU instead of timing candidates,
+    and appends each timed result."""
+    _ret(lib().tags_gpu_set_tune_cache(None if path is None else os.fsencode(path)))
 
 
 def last_error() -> str:
@@ -712,14 +724,16 @@ class Plan:
         if code != 0:
             raise RuntimeError(f"tags_plan_set_split failed ({code}): {last_error()}")
 
-    def tune(self, s, kappa, mur=1.0, inj_node=0):
+    def tune(self, s, kappa, mur=1.0, inj_node=0, refresh=False):
         """Autotune samples per pass, panels per trailing update and the split
-        form on these samples (tags_plan_tune); returns the kept TuneResult."""
+        form on these samples (tags_plan_tune); returns the kept TuneResult.
+        With a tune cache set (set_tune_cache) a stored entry is applied
+        without timing unless refresh is true."""
         s = np.ascontiguousarray(s, dtype=np.complex128)
         kappa = np.ascontiguousarray(np.broadcast_to(kappa, s.shape), dtype=np.complex128)
         res = TuneResult()
-        code = lib().tags_plan_tune(self.handle, _addr(s), _addr(kappa), float(mur), s.shape[0], int(inj_node), 0,
-                                    ctypes.byref(res))
+        code = lib().tags_plan_tune(self.handle, _addr(s), _addr(kappa), float(mur), s.shape[0], int(inj_node),
+                                    TUNE_REFRESH if refresh else 0, ctypes.byref(res))
         if code != 0:
             raise RuntimeError(f"tags_plan_tune failed ({code}): {last_error()}")
         return res
@@ -788,6 +802,36 @@ class Plan:
             raise RuntimeError(f"tags_plan_run failed ({code}): {last_error()}")
         return sol, info, st
 
+    def run_resumable(self, s, kappa, directory, mur=1.0, ie=None, inj_node=0, chunk=256, columns=None):
+        """run() over chunks of `chunk` samples with each finished chunk saved
+        under `directory`, so a sweep that was interrupted resumes from its
+        last saved chunk when called again with the same arguments. columns
+        (optional indices into the N unknowns) keeps only those columns of the
+        solution. Returns (solution, info, stats) with stats summed over the
+        chunks: max_iterations, fallbacks, max_backward_error, seconds, and
+        chunks_run (the chunks this call solved)."""
+        s = np.ascontiguousarray(s, dtype=np.complex128)
+        ns = s.shape[0]
+        kappa = np.ascontiguousarray(np.broadcast_to(kappa, (ns,)), dtype=np.complex128)
+        if ie is not None:
+            ie = np.ascontiguousarray(ie, dtype=np.complex128).reshape(ns, self.n)
+        cols = None if columns is None else np.ascontiguousarray(columns, dtype=np.int64)
+        fp = sweep_fingerprint([self.elec, self.img, self.nodes, self.precision, float(mur), int(inj_node), s,
+                                kappa, ie, cols])
+
+        def run_chunk(k0, k1):
+            sol, info, st = self.run(s[k0:k1], kappa[k0:k1], mur, None if ie is None else ie[k0:k1], inj_node)
+            return ({"sol": sol if cols is None else sol[:, cols], "info": info},
+                    {"max_iterations": st.max_iterations, "fallbacks": st.fallbacks,
+                     "max_backward_error": st.max_backward_error, "seconds": st.seconds})
+
+        out, stats, ran = resumable_sweep(run_chunk, ns, directory, chunk, fp)
+        summary = {"max_iterations": int(max((t["max_iterations"] for t in stats), default=0)),
+                   "fallbacks": int(sum(t["fallbacks"] for t in stats)),
+                   "max_backward_error": max((t["max_backward_error"] for t in stats), default=0.0),
+                   "seconds": sum(t["seconds"] for t in stats), "chunks_run": ran}
+        return out["sol"], out["info"], summary
+
     def run_device(self, s_ptr, kappa_ptr, ns, mur, ie_ptr, inj_node, sol_ptr, info_ptr):
         """Same as run() on device pointers (integers); inputs stay in HBM."""
         st = RunStats()
@@ -837,6 +881,83 @@ def hem_sweep(electrodes, imgs, nodes, s, kappa, mur=1.0, ie=None, inj_node=0, p
         return plan.run(s, kappa, mur, ie, inj_node)
     finally:
         plan.close()
+
+
+def sweep_fingerprint(parts) -> str:
+    """SHA-256 over a sweep's inputs (arrays by dtype, shape and bytes; other
+    values by repr), which a saved sweep must match to be resumed."""
+    h = hashlib.sha256()
+    for x in parts:
+        if x is None:
+            h.update(b"none")
+        elif isinstance(x, np.ndarray):
+            h.update(f"{x.dtype}{x.shape}".encode())
+            h.update(np.ascontiguousarray(x).tobytes())
+        else:
+            h.update(repr(x).encode())
+        h.update(b"|")
+    return h.hexdigest()
+
+
+def _replace_atomic(path, write):
+    tmp = path + ".tmp"
+    write(tmp)
+    os.replace(tmp, path)
+
+
+def resumable_sweep(run_chunk, ns, directory, chunk, fingerprint):
+    """Samples [0, ns) in chunks: run_chunk(k0, k1) returns (arrays, stats),
+    the arrays' first axis k1 - k0, stats a dict of numbers. After each chunk
+    its arrays go to directory/chunk_<k0>.npz and the manifest
+    (directory/manifest.json: fingerprint, ns, chunk, finished chunks and their
+    stats) records it; both are written under a temporary name and renamed, so
+    an interruption leaves the last finished chunk recorded. A call on a
+    directory with a manifest resumes when fingerprint, ns and chunk agree and
+    raises ValueError otherwise. Returns (arrays concatenated over the samples,
+    stats of every chunk in order, chunks run by this call)."""
+    if ns <= 0 or chunk <= 0:
+        raise ValueError("resumable_sweep: ns and chunk must be positive")
+    os.makedirs(directory, exist_ok=True)
+    man_path = os.path.join(directory, "manifest.json")
+    man = {"version": 1, "fingerprint": fingerprint, "ns": int(ns), "chunk": int(chunk), "done": {}}
+    if os.path.exists(man_path):
+        with open(man_path) as f:
+            old = json.load(f)
+        if (old.get("version"), old.get("fingerprint"), old.get("ns"), old.get("chunk")) != \
+                (1, fingerprint, int(ns), int(chunk)):
+            raise ValueError(f"{man_path} belongs to another sweep (inputs, sample count or chunk differ)")
+        man = old
+    parts = {}
+    ran = 0
+    for k0 in range(0, ns, chunk):
+        k1 = min(ns, k0 + chunk)
+        name = os.path.join(directory, f"chunk_{k0:09d}.npz")
+        if str(k0) in man["done"] and os.path.exists(name):
+            with np.load(name) as z:
+                arrays = {k: z[k] for k in z.files}
+        else:
+            arrays, stats = run_chunk(k0, k1)
+            arrays = {k: np.asarray(v) for k, v in arrays.items()}
+            for k, v in arrays.items():
+                if v.shape[0] != k1 - k0:
+                    raise ValueError(f"resumable_sweep: output {k} has {v.shape[0]} rows for {k1 - k0} samples")
+
+            def write_npz(tmp, arrays=arrays):
+                with open(tmp, "wb") as f:
+                    np.savez(f, **arrays)
+            _replace_atomic(name, write_npz)
+            man["done"][str(k0)] = {k: float(v) for k, v in stats.items()}
+
+            def write_man(tmp):
+                with open(tmp, "w") as f:
+                    json.dump(man, f)
+            _replace_atomic(man_path, write_man)
+            ran += 1
+        for k, v in arrays.items():
+            parts.setdefault(k, []).append(v)
+    out = {k: np.concatenate(v, axis=0) for k, v in parts.items()}
+    stats = [man["done"][str(k0)] for k0 in range(0, ns, chunk)]
+    return out, stats, ran
 
 
 def uneven_grids(count: int = 64, seed: int = 0):

@@ -427,6 +427,7 @@ extern "C" int inv_laplace_trans(double* f, tags_cdouble* g, tags_cdouble* s, do
 extern "C" int tags_inv_laplace_batch(double* f, const tags_cdouble* g, const tags_cdouble* s, double tmax, size_t nt,
                                       size_t nseries, int filter, int flags) {
     std::lock_guard<std::mutex> lk(g_mutex);
+    TagsRange range("tags INLT");
     if (nt < 2 || nseries == 0 || !f || !g || !s) return tags_fail(TAGS_E_ARG, "invalid argument");
     if (nt > (size_t)1 << 26 || nseries > (size_t)1 << 26) return tags_fail(TAGS_E_ARG, "transform too large");
     DeviceCtx* c = tags_ctx();

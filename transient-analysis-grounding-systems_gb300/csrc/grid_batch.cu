@@ -287,6 +287,7 @@ extern "C" int tags_batch_create(tags_batch* out, const tags_grid_job* jobs, siz
 }
 
 extern "C" int tags_batch_run(tags_batch batch, const tags_grid_job* jobs, size_t njobs, tags_run_stats* stats) {
+    TagsRange range("tags grid batch");
     tags_batch_s* b = batch;
     if (!b || !jobs || njobs != b->grids.size()) return tags_fail(TAGS_E_ARG, "tags_batch_run: invalid argument");
     for (size_t q = 0; q < njobs; ++q) {

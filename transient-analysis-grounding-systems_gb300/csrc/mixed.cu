@@ -629,6 +629,7 @@ int tags_mixed_free(tags_plan_s* p) {
 
 // Re-solve sample `q` of the current pass in plain FP64 (partial pivoting).
 static int fallback_plain(tags_plan_s* p, int q, cudaStream_t st) {
+    TagsRange range("tags FP64 re-solve");
     const long long N = p->N, NN = N * N;
     if (!p->d_fbW) {
         if (cudaMalloc(&p->d_fbW, sizeof(double2) * NN) != cudaSuccess ||
@@ -693,6 +694,7 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_x, 0, sizeof(double2) * N * nb, st));
     // 1. impedance blocks (full symmetric, complex FP32), direct + images: double
     //    line integrals, or the mHEM rescale of the static potentials
+    TagsRange range("tags fill");
     int err = p->fill_model == TAGS_INTG_MHEM
                   ? tags_launch_mhem_mixed(m, p->has_images, p->d_pot, p->d_fillws, p->d_coef, nb, p->d_Z,
                                            p->d_Z + (size_t)m * m, 2LL * m * m, p->d_status, st)
@@ -700,6 +702,7 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
                                            p->d_Z + (size_t)m * m, p->d_Zlo, p->d_Zlo + (size_t)m * m, 2LL * m * m,
                                            p->has_images, p->spec, p->mom, p->d_status, st, p->d_rowpart);
     if (err) return err;
+    range.next("tags assemble");
     // 2. scaling
     float* d_scalef = reinterpret_cast<float*>(p->d_scale + 2 * (size_t)p->batch * N);
     if (p->fill_model == TAGS_INTG_MHEM)
@@ -717,12 +720,14 @@ int tags_mixed_factor(tags_plan_s* p, int nb, cudaStream_t st) {
     tags_prof_end(TAGS_PROF_BUILD, pf, st, 0.0, (8.0 * 0.5 * N * (N + 1.0) + 32.0 * m * m) * nb);
     tags_note_launch();
     TAGS_CUDA_OK(cudaGetLastError());
+    range.next("tags factor");
     return tags_ldl_tc(p->d_A, N, N, (long long)NN, nb, p->batch, p->d_ldlws, p->d_info, p->d_ldlerr, m,
                        p->split_pieces, p->group_panels, st, p->tc_pairs);
 }
 
 // r = b, max row sum of W per sample, refinement state
 int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st) {
+    TagsRange range("tags refine setup");
     const int N = p->N;
     double* d_rsum = p->d_scale + (size_t)p->batch * N;
     double2* d_b = p->d_r + (size_t)p->batch * N;
@@ -739,6 +744,7 @@ int tags_mixed_ir_setup(tags_plan_s* p, int nb, cudaStream_t st) {
 // decision, residual of the new iterate for the samples that go on. A fixed
 // launch sequence (graph-capturable).
 int tags_mixed_ir_step(tags_plan_s* p, int nb, cudaStream_t st, cudaGraphConditionalHandle cond, int set_cond) {
+    TagsRange range("tags refine step");
     const int m = p->m, n = p->n, N = p->N;
     const size_t NN = (size_t)N * N;
     double2* d_b = p->d_r + (size_t)p->batch * N;

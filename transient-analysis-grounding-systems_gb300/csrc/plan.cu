@@ -10,6 +10,8 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -301,6 +303,7 @@ extern "C" int tags_plan_set_fill(tags_plan plan, int integration_type) {
 // already in p->d_coef and p->d_x.
 int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st) {
     const long long N = p->N, NN = N * N;
+    TagsRange range("tags assemble");
     TAGS_CUDA_OK(cudaMemsetAsync(p->d_W, 0, sizeof(double2) * NN * nb, st));
     int err = tags_wg_incidence(p->d_W, N, NN, nb, p->d_cond, p->n, p->m, st);
     if (err) return err;
@@ -314,10 +317,13 @@ int tags_plan_run_plain(tags_plan_s* p, const double2*, int nb, cudaStream_t st)
     out.sign = -1.0;
     out.mirror = 1;
     out.accumulate = 0;
+    range.next("tags fill");
     err = tags_plan_fill_fp64(p, p->d_coef, nb, out, st);
     if (err) return err;
+    range.next("tags factor");
     err = tags_lu_z(p->d_W, (int)N, N, NN, nb, 1, p->d_ipiv, p->d_info, st);
     if (err) return err;
+    range.next("tags solve");
     return tags_lu_solve_z(p->d_W, (int)N, N, NN, nb, p->d_ipiv, p->d_x, 1, N, N, st);
 }
 
@@ -352,6 +358,7 @@ int tags_plan_add_while_node(cudaStream_t st, cudaGraphConditionalHandle* cond, 
 // set-up and a while-node repeating the refinement step until the device
 // clears the condition. Nothing runs during the capture.
 static int capture_pass(tags_plan_s* p, int nb, double mur, int has_ie, int inj, tags_plan_s::GraphPass* gp) {
+    TagsRange range("tags capture pass");
     cudaStream_t st = p->stream;
     const long long l0 = tags_thread_launch_count();
     TAGS_CUDA_OK(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
@@ -474,11 +481,113 @@ extern "C" int tags_plan_run(tags_plan plan, const tags_cdouble* s, const tags_c
                              const tags_cdouble* ie, size_t inj_node, tags_cdouble* sol, int* info, int flags,
                              tags_run_stats* stats);
 
+// ---- autotuner cache ---------------------------------------------------------------
+// A text file, one line per timed tune:
+//   tags-tune 1 N=.. m=.. prec=.. fill=.. cap=.. pipes=.. pairs=.. gpu=<name>/<SMs>/sm<cc> | <pass> <panels> <split> <rate>
+// The key holds what the candidates' timings depend on: the system's size, the
+// precision and impedance model, the samples the tuner may put in one pass,
+// the pipelines and pair setting, and the GPU. A lookup takes the last line
+// with the plan's key; a line is appended by one write to a file opened for
+// appending, so processes may share the file.
+static std::mutex g_tune_mutex;
+static std::string g_tune_path;
+
+extern "C" int tags_gpu_set_tune_cache(const char* path) {
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    if (!path || !*path) {
+        g_tune_path.clear();
+        return 0;
+    }
+    FILE* f = fopen(path, "a");
+    if (!f) return tags_fail(TAGS_E_ARG, "tags_gpu_set_tune_cache: the file cannot be opened for appending");
+    fclose(f);
+    g_tune_path = path;
+    return 0;
+}
+
+static std::string tune_key(const tags_plan_s* p, int cap) {
+    std::string gpu = "unknown";
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, p->device) == cudaSuccess) {
+        gpu = prop.name;
+        for (char& ch : gpu)
+            if (ch == ' ' || ch == '|' || ch == '\t' || ch == '\n' || ch == '\r') ch = '_';
+        gpu += "/" + std::to_string(prop.multiProcessorCount) + "/sm" + std::to_string(prop.major * 10 + prop.minor);
+    } else {
+        cudaGetLastError();
+    }
+    char buf[160];
+    snprintf(buf, sizeof buf, "tags-tune 1 N=%d m=%d prec=%d fill=%d cap=%d pipes=%d pairs=%d gpu=", p->N, p->m,
+             p->precision, p->fill_model, cap, p->pipelines, p->tc_pairs);
+    return std::string(buf) + gpu;
+}
+
+// The last entry for `key` that is valid for this plan, if any.
+static bool tune_lookup(const std::string& path, const std::string& key, const tags_plan_s* p, int cap,
+                        tags_tune_result* r) {
+    FILE* f = fopen(path.c_str(), "r");
+    if (!f) return false;
+    const bool mixed = p->precision != TAGS_PLAIN_FP64;
+    char line[1024];
+    bool hit = false;
+    while (fgets(line, sizeof line, f)) {
+        const char* bar = strstr(line, " | ");
+        if (!bar || (size_t)(bar - line) != key.size() || strncmp(line, key.c_str(), key.size()) != 0) continue;
+        tags_tune_result t{};
+        if (sscanf(bar + 3, "%d %d %d %lf", &t.samples_per_pass, &t.panels_per_update, &t.split,
+                   &t.solves_per_second) != 4)
+            continue;
+        const int g = t.panels_per_update;
+        const bool ok = t.samples_per_pass >= 1 && t.samples_per_pass <= cap &&
+                        (mixed ? (g == 1 || g == 2 || g == 4 || g == 6) && (t.split == TAGS_SPLIT_F16 || t.split == 3)
+                               : g == 0 && t.split == 0);
+        if (ok) {
+            *r = t;
+            hit = true;
+        }
+    }
+    fclose(f);
+    return hit;
+}
+
+static void tune_store(const std::string& path, const std::string& key, const tags_tune_result& r) {
+    FILE* f = fopen(path.c_str(), "a");
+    if (!f) return;
+    char line[1024];
+    const int len = snprintf(line, sizeof line, "%s | %d %d %d %.6g\n", key.c_str(), r.samples_per_pass,
+                             r.panels_per_update, r.split, r.solves_per_second);
+    if (len > 0 && len < (int)sizeof line) fwrite(line, 1, (size_t)len, f);
+    fclose(f);
+}
+
 extern "C" int tags_plan_tune(tags_plan plan, const tags_cdouble* s, const tags_cdouble* kappa, double mur, size_t ns,
                               size_t inj_node, int flags, tags_tune_result* out) {
+    TagsRange range("tags tune");
     tags_plan_s* p = plan;
     if (!p || !s || !kappa || ns == 0) return tags_fail(TAGS_E_ARG, "tags_plan_tune: invalid argument");
     const int cap = (int)std::min<size_t>(p->batch, ns);
+    const bool refresh = (flags & TAGS_TUNE_REFRESH) != 0;
+    flags &= ~TAGS_TUNE_REFRESH;
+    std::string cache;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mutex);
+        cache = g_tune_path;
+    }
+    const std::string key = cache.empty() ? std::string() : tune_key(p, cap);
+    if (!cache.empty() && !refresh) {
+        tags_tune_result hit{};
+        if (tune_lookup(cache, key, p, cap, &hit)) {
+            p->pass_batch = hit.samples_per_pass;
+            if (p->precision != TAGS_PLAIN_FP64) {
+                p->group_panels = hit.panels_per_update;
+                p->split_pieces = hit.split;
+            }
+            tags_plan_drop_graphs(p);
+            hit.candidates = 0;                 // nothing timed
+            if (out) *out = hit;
+            return 0;
+        }
+    }
     std::vector<int> sizes;
     for (int b = 16; b < cap; b *= 2) sizes.push_back(b);
     sizes.push_back(cap);
@@ -532,6 +641,7 @@ extern "C" int tags_plan_tune(tags_plan plan, const tags_cdouble* s, const tags_
     }
     tags_plan_drop_graphs(p);
     best.candidates = count;
+    if (!cache.empty()) tune_store(cache, key, best);
     if (out) *out = best;
     return 0;
 }
@@ -568,6 +678,7 @@ static int run_passes(tags_plan_s* p, const tags_cdouble* s, const tags_cdouble*
     // (if any): a pipeline takes the next pass once its last one has finished
     for (size_t k0 = next->fetch_add(1) * per_pass; k0 < ns; k0 = next->fetch_add(1) * per_pass) {
         const int nb = (int)std::min<size_t>(per_pass, ns - k0);
+        TagsRange range("tags pass");
         const double2 *ds, *dk, *die = nullptr;
         if (p->use_graphs) {
             // inputs go to the plan's staging buffers, which the graph reads

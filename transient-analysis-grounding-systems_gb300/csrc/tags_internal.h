@@ -3,7 +3,24 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
+
+// NVTX range over a host-side phase (fill, assemble, factor, refine, FP64
+// re-solve, INLT, a pass or a grid batch): pushed on construction, popped on
+// destruction. NVTX 3 is header-only; with no tool attached a push and a pop
+// cost a few nanoseconds. In graph mode a pass is one range around its launch.
+struct TagsRange {
+    explicit TagsRange(const char* name) { nvtxRangePushA(name); }
+    ~TagsRange() { nvtxRangePop(); }
+    // ends this phase and opens the next one
+    void next(const char* name) {
+        nvtxRangePop();
+        nvtxRangePushA(name);
+    }
+    TagsRange(const TagsRange&) = delete;
+    TagsRange& operator=(const TagsRange&) = delete;
+};
 
 // Integration types, numbered as the reference's Integration_type
 // (src/electrode.h:17-31).
