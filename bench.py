@@ -166,10 +166,10 @@ def read_profile(pkg):
 
 # DRAM bytes of the trailing-update family (k_gemm_tc<2, 0>), one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) of all 35 launches of
-# one 128-sample pass of this workload (groups of six panels): 78.22 GB, i.e.
-# 17.5 MB per launch per sample (profiles/k_gemm_tc_trailing_dram_grid1560_batch128.md).
+# one 128-sample pass of this workload (groups of six panels): 64.51 GB, i.e.
+# 14.4 MB per launch per sample (profiles/k_gemm_tc_trailing_dram_grid1560_batch128.md).
 # The traffic grows in proportion to the samples in the pass.
-TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 78.22e9 / 35 / 128
+TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 64.51e9 / 35 / 128
 # Pipe use of the mixed form's fill kernel (k_fill_moment), from an ncu capture
 # at 16 samples (profiles/k_fill_moment_grid1560_batch16.md).
 FILL_PIPES = {"kernel": "k_fill_moment", "issue_active": 0.775, "fma_pipe": 0.613, "alu_pipe": 0.139,
@@ -856,6 +856,7 @@ def main():
     ap.add_argument("--tc-pairs", type=int, default=-1,
                     help="trailing updates: 0 one SM per tile, 1 two-SM clusters, 2 two-SM real-form N=256 "
                          "(-1 = the plan's default)")
+    ap.add_argument("--panels", type=int, default=0, help="mixed form: panels per trailing update, 1..6 (0 = plan default)")
     ap.add_argument("--split", type=int, default=0, help="mixed-form split: 3 bf16x3, 2 bf16x2, 16 fp16x2 (0 = plan default)")
     ap.add_argument("--solve-path", type=int, default=-1,
                     help="triangular solves: 0 per block, 1 one CTA per sample, 2/4/8 clusters (-1 = default)")
@@ -897,6 +898,8 @@ def main():
     plan = pkg.Plan(elec, img, nodes, pkg.MIXED if mixed else pkg.PLAIN_FP64, max_batch=B)
     if mixed and args.split:
         plan.set_split(args.split)
+    if mixed and args.panels:
+        plan.set_panels(args.panels)
     if mixed and args.tc_pairs >= 0:
         plan.set_tc_pairs(args.tc_pairs)
     if args.solve_path != -1 and pkg.lib().tags_debug_solve_path(args.solve_path) != 0:

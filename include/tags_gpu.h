@@ -369,6 +369,13 @@ int tags_plan_set_graphs (tags_plan plan, int enable);
  * solve that pass again). Default 16. */
 int tags_plan_set_split (tags_plan plan, int pieces);
 
+/* Panels of 128 columns per trailing update of the TAGS_MIXED factorisation
+ * (1 .. 6; 0 = the default, 6): each group of that many panels updates its
+ * own block columns left-looking (K = 128 .. 128 (panels - 1)) and then the
+ * trailing matrix once with K = 128 x panels. tags_plan_tune picks among
+ * 1, 2, 4 and 6. */
+int tags_plan_set_panels (tags_plan plan, int panels);
+
 /* Impedance model of the plan's passes: 2 (the reference's INTG_DOUBLE,
  * default) fills ZL/ZT with the double line integrals of e^{-gamma r}/r;
  * 4 (INTG_MHEM) uses the reference's mHEM examples' model: static potentials

@@ -59,7 +59,7 @@ EXPORTS = (
     "solve_immittance", "fill_incidence_adm", "fill_impedance_adm", "calculate_yla_ytb", "fill_impedance_adm2",
     "solve_admittance", "electrodes_file", "nodes_file", "alipio_soil", "smith_longmire_soil", "heidler", "laplace_trans",
     "inv_laplace_trans", "tags_plan_create", "tags_plan_run",
-    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
+    "tags_plan_destroy", "tags_plan_set_graphs", "tags_plan_set_pipelines", "tags_plan_set_split", "tags_plan_set_panels", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch", "tags_gpu_launch_count", "tags_gpu_last_error",
     "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol", "tags_plan_set_tc_pairs",
     "tags_debug_tc_pairs", "tags_debug_solve_path", "tags_debug_mixed_fill", "tags_probe_fp64",
     "tags_gpu_set_memory_budget", "tags_gpu_set_tune_cache",
@@ -152,6 +152,7 @@ def lib() -> ctypes.CDLL:
             L.tags_plan_set_graphs.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_pipelines.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_split.argtypes = [_vp, ctypes.c_int]
+            L.tags_plan_set_panels.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_fill.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_max_steps.argtypes = [_vp, ctypes.c_int]
             L.tags_plan_set_refine_tol.argtypes = [_vp, ctypes.c_double]
@@ -194,7 +195,8 @@ def lib() -> ctypes.CDLL:
                          "inv_laplace_trans",
                          "tags_plan_create", "tags_plan_run", "tags_plan_destroy", "tags_plan_set_graphs",
                          "tags_plan_set_pipelines",
-                         "tags_plan_set_split", "tags_plan_tune", "tags_plan_set_fill", "tags_inv_laplace_batch",
+                         "tags_plan_set_split", "tags_plan_set_panels", "tags_plan_tune", "tags_plan_set_fill",
+                         "tags_inv_laplace_batch",
                          "tags_plan_set_max_steps", "tags_debug_tc_wait_limit", "tags_plan_set_refine_tol",
                          "tags_plan_set_tc_pairs", "tags_debug_tc_pairs", "tags_debug_solve_path",
                          "tags_debug_mixed_fill", "tags_probe_fp64",
@@ -716,6 +718,12 @@ class Plan:
     def set_pipelines(self, n):
         """1, 2 or 3 passes in flight (k > 1: k - 1 twin plans take passes as they free up)."""
         _ret(lib().tags_plan_set_pipelines(self.handle, int(n)))
+
+    def set_panels(self, panels):
+        """Panels of 128 columns per trailing update of the mixed form (1 .. 6; 0 = default 6)."""
+        code = lib().tags_plan_set_panels(self.handle, int(panels))
+        if code != 0:
+            raise RuntimeError(f"tags_plan_set_panels failed ({code}): {last_error()}")
 
     def set_split(self, pieces):
         """Split form of the mixed form's tensor-core products: SPLIT_BF16_3,

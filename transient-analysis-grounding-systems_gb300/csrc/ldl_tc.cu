@@ -288,11 +288,70 @@ struct GemmArgs {
     int kblocks;               // K blocks of BK (4 per panel of the group)
     int off;                   // row offset of the operand rows (tile row TB * I reads row TB * I + off)
     int neg_planes;            // mode 1, S = 2: also the negated imaginary planes, at slots 4, 5 of the group buffer
+    int ba, bb;                // tri, bb > ba: tile rows/columns [ba, bb) lie wholly in the zero band and are left out
+                               // of the enumeration (tri_compact_count), but for the J = 0 tiles that write Np planes
 };
+
+// Lower-triangle tiles of an update with the zero band's tile rows/columns
+// [ba, bb) taken out, in the order of the full enumeration (row by row):
+//   rows I < ba:        J = 0 .. I                      (n1 = ba (ba + 1) / 2)
+//   rows ba <= I < bb:  J = 0 only, where the next panel's planes are written
+//                       (Np; I >= 1), and as a skipped tile (n2)
+//   rows I >= bb:       the e left columns (J < ba; if ba = 0, J = 0 as a
+//                       skipped tile when Np), then J = bb .. I  (n3)
+// Every CTA then strides over tiles that do work, so the CTAs stay within a
+// sample or two of each other: with the band's empty slots in the list, a CTA
+// whose slots fall in the band ran ahead, and the CTAs in flight spread over
+// about a dozen samples, whose operand rows no longer fitted in L2.
+struct TriCompact {
+    int n1, n2, e, r2s;
+};
+TAGS_HD TriCompact tri_compact(int ba, int bb, bool planes) {
+    TriCompact c;
+    c.n1 = ba * (ba + 1) / 2;
+    c.r2s = ba >= 1 ? ba : 1;
+    c.n2 = planes && bb > c.r2s ? bb - c.r2s : 0;
+    c.e = ba >= 1 ? ba : (planes ? 1 : 0);
+    return c;
+}
+TAGS_HD int tri_compact_count(int T, int ba, int bb, bool planes) {
+    const TriCompact c = tri_compact(ba, bb, planes);
+    const int R = T > bb ? T - bb : 0;
+    return c.n1 + c.n2 + R * c.e + R * (R + 1) / 2;
+}
 
 TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
     smp = t / g.tiles;
     int l = t - smp * g.tiles;
+    if (g.tri && g.bb > g.ba) {
+        const TriCompact c = tri_compact(g.ba, g.bb, g.Np != nullptr);
+        skip = false;
+        if (l < c.n1) {
+            I = (int)((sqrtf(8.0f * l + 1.0f) - 1.0f) * 0.5f);
+            while ((I + 1) * (I + 2) / 2 <= l) ++I;
+            while (I * (I + 1) / 2 > l) --I;
+            J = l - I * (I + 1) / 2;
+        } else if (l < c.n1 + c.n2) {
+            I = c.r2s + (l - c.n1);
+            J = 0;
+            skip = true;
+        } else {
+            const int l3 = l - c.n1 - c.n2;
+            const float bq = 2.0f * c.e + 1.0f;
+            int r = (int)((sqrtf(bq * bq + 8.0f * l3) - bq) * 0.5f);
+            while ((r + 1) * c.e + (r + 1) * (r + 2) / 2 <= l3) ++r;
+            while (r > 0 && r * c.e + r * (r + 1) / 2 > l3) --r;
+            const int q = l3 - (r * c.e + r * (r + 1) / 2);
+            I = g.bb + r;
+            if (q < c.e) {
+                J = q;
+                skip = g.ba == 0;          // J = 0 inside the band: planes only
+            } else {
+                J = g.bb + (q - c.e);
+            }
+        }
+        return;
+    }
     if (g.tri) {
         I = (int)((sqrtf(8.0f * l + 1.0f) - 1.0f) * 0.5f);
         while ((I + 1) * (I + 2) / 2 <= l) ++I;
@@ -2072,6 +2131,15 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.mode = 0;
         g.tri = tri ? 1 : 0;
         g.tiles = tri ? T * (T + 1) / 2 : T;
+        if (tri && g.zhi > g.zlo) {
+            // tile rows/columns wholly inside the zero band leave the enumeration
+            const int ba = (g.zlo + TB - 1) / TB, bb = std::min(T, g.zhi / TB);
+            if (bb > ba) {
+                g.ba = ba;
+                g.bb = bb;
+                g.tiles = tri_compact_count(T, ba, bb, Mn > 0);
+            }
+        }
         g.row0 = row0;
         g.col0 = row0;
         g.off = row0 - jg;

@@ -432,6 +432,17 @@ void tags_plan_drop_graphs(tags_plan_s* p) {
     p->graphs.clear();
 }
 
+extern "C" int tags_plan_set_panels(tags_plan plan, int panels) {
+    if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_panels: invalid plan");
+    if (panels < 0 || panels > 6) return tags_fail(TAGS_E_ARG, "tags_plan_set_panels: panels must be 0 .. 6");
+    const int v = panels == 0 ? 6 : panels;
+    if (plan->group_panels != v) {
+        plan->group_panels = v;
+        tags_plan_drop_graphs(plan);
+    }
+    return 0;
+}
+
 extern "C" int tags_plan_set_split(tags_plan plan, int pieces) {
     if (!plan) return tags_fail(TAGS_E_ARG, "tags_plan_set_split: invalid plan");
     if (pieces != 2 && pieces != 3 && pieces != TAGS_SPLIT_F16)
