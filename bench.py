@@ -166,10 +166,10 @@ def read_profile(pkg):
 
 # DRAM bytes of the trailing-update family (k_gemm_tc<2, 0>), one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) of all 35 launches of
-# one 128-sample pass of this workload (groups of six panels): 64.51 GB, i.e.
-# 14.4 MB per launch per sample (profiles/k_gemm_tc_trailing_dram_grid1560_batch128.md).
+# one 128-sample pass of this workload (groups of six panels): 63.15 GB, i.e.
+# 14.1 MB per launch per sample (profiles/k_gemm_tc_trailing_dram_grid1560_batch128.md).
 # The traffic grows in proportion to the samples in the pass.
-TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 64.51e9 / 35 / 128
+TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 63.15e9 / 35 / 128
 # Pipe use of the mixed form's fill kernel (k_fill_moment), from an ncu capture
 # at 16 samples (profiles/k_fill_moment_grid1560_batch16.md).
 FILL_PIPES = {"kernel": "k_fill_moment", "issue_active": 0.775, "fma_pipe": 0.613, "alu_pipe": 0.139,

@@ -290,13 +290,25 @@ struct GemmArgs {
     int neg_planes;            // mode 1, S = 2: also the negated imaginary planes, at slots 4, 5 of the group buffer
     int ba, bb;                // tri, bb > ba: tile rows/columns [ba, bb) lie wholly in the zero band and are left out
                                // of the enumeration (tri_compact_count), but for the J = 0 tiles that write Np planes
+    int np_band;               // mode 0 with Np: also write the planes of the band's rows (the next panel's GEMM reads
+                               // them only when its columns reach past the ZL block; before that its band rows are zero
+                               // and skipped)
 };
+
+// Mode 0: a skipped tile whose rows hold the next panel's block column writes
+// their planes (the current values), unless its rows lie in the band and the
+// next panel's GEMM skips them.
+TAGS_D bool skipped_writes_planes(const GemmArgs& g, int I, int J) {
+    if (!(g.Np && J == 0 && I >= 1)) return false;
+    if (g.np_band) return true;
+    return !(g.zhi > g.zlo && TB * I >= g.zlo && TB * I + TB <= g.zhi);
+}
 
 // Lower-triangle tiles of an update with the zero band's tile rows/columns
 // [ba, bb) taken out, in the order of the full enumeration (row by row):
 //   rows I < ba:        J = 0 .. I                      (n1 = ba (ba + 1) / 2)
 //   rows ba <= I < bb:  J = 0 only, where the next panel's planes are written
-//                       (Np; I >= 1), and as a skipped tile (n2)
+//                       there (Np and np_band; I >= 1), as a skipped tile (n2)
 //   rows I >= bb:       the e left columns (J < ba; if ba = 0, J = 0 as a
 //                       skipped tile when Np), then J = bb .. I  (n3)
 // Every CTA then strides over tiles that do work, so the CTAs stay within a
@@ -306,16 +318,16 @@ struct GemmArgs {
 struct TriCompact {
     int n1, n2, e, r2s;
 };
-TAGS_HD TriCompact tri_compact(int ba, int bb, bool planes) {
+TAGS_HD TriCompact tri_compact(int ba, int bb, bool planes, bool planes_band) {
     TriCompact c;
     c.n1 = ba * (ba + 1) / 2;
     c.r2s = ba >= 1 ? ba : 1;
-    c.n2 = planes && bb > c.r2s ? bb - c.r2s : 0;
+    c.n2 = planes && planes_band && bb > c.r2s ? bb - c.r2s : 0;
     c.e = ba >= 1 ? ba : (planes ? 1 : 0);
     return c;
 }
-TAGS_HD int tri_compact_count(int T, int ba, int bb, bool planes) {
-    const TriCompact c = tri_compact(ba, bb, planes);
+TAGS_HD int tri_compact_count(int T, int ba, int bb, bool planes, bool planes_band) {
+    const TriCompact c = tri_compact(ba, bb, planes, planes_band);
     const int R = T > bb ? T - bb : 0;
     return c.n1 + c.n2 + R * c.e + R * (R + 1) / 2;
 }
@@ -324,7 +336,7 @@ TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& sk
     smp = t / g.tiles;
     int l = t - smp * g.tiles;
     if (g.tri && g.bb > g.ba) {
-        const TriCompact c = tri_compact(g.ba, g.bb, g.Np != nullptr);
+        const TriCompact c = tri_compact(g.ba, g.bb, g.Np != nullptr, g.np_band != 0);
         skip = false;
         if (l < c.n1) {
             I = (int)((sqrtf(8.0f * l + 1.0f) - 1.0f) * 0.5f);
@@ -582,7 +594,7 @@ __global__ void __launch_bounds__(GEMM_THREADS, 1) k_gemm_tc(const __grid_consta
                 }
                 // no update of this tile; if it holds rows of the next panel's
                 // block column, their planes are the current values
-                if (MODE == 0 && g.Np && J == 0 && I >= 1 && gr < g.M && gr - TB < g.Mn) {
+                if (MODE == 0 && skipped_writes_planes(g, I, J) && gr < g.M && gr - TB < g.Mn) {
                     const float2* Cb = g.Amat + g.mstride * smp;
                     for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
                         const float2* base_p = Cb + (long long)(g.row0 + gr) + g.ld * (long long)(g.col0 + cc * 16);
@@ -828,7 +840,7 @@ TAGS_D void pair_of(const GemmArgs& g, int T, int l, int& I0, int& J) {
 template <int S>
 TAGS_D void skipped_tile_planes(const GemmArgs& g, int smp, int I, int J, int r, int half, int& ovf) {
     const int gr = TB * I + r;
-    if (!(g.Np && J == 0 && I >= 1 && gr < g.M && gr - TB < g.Mn)) return;
+    if (!(skipped_writes_planes(g, I, J) && gr < g.M && gr - TB < g.Mn)) return;
     const bool f16 = S == 2 && g.f16 != 0;
     const float2* Cb = g.Amat + g.mstride * smp;
     for (int cc = half * 4; cc < half * 4 + 4; ++cc) {
@@ -2131,13 +2143,17 @@ int tags_ldl_tc(float2* A, int N, long long ld, long long mstride, int nb, int b
         g.mode = 0;
         g.tri = tri ? 1 : 0;
         g.tiles = tri ? T * (T + 1) / 2 : T;
+        // the next panel (columns row0 ..) skips the band's rows while its
+        // columns stay inside the ZL block: their planes are not written then
+        const int jbn = std::min(TB, N - row0);
+        g.np_band = zl_m > 0 && row0 + jbn <= zl_m ? 0 : 1;
         if (tri && g.zhi > g.zlo) {
             // tile rows/columns wholly inside the zero band leave the enumeration
             const int ba = (g.zlo + TB - 1) / TB, bb = std::min(T, g.zhi / TB);
             if (bb > ba) {
                 g.ba = ba;
                 g.bb = bb;
-                g.tiles = tri_compact_count(T, ba, bb, Mn > 0);
+                g.tiles = tri_compact_count(T, ba, bb, Mn > 0, g.np_band != 0);
             }
         }
         g.row0 = row0;
