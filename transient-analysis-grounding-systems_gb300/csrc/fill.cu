@@ -1300,15 +1300,30 @@ __global__ void __launch_bounds__(MOM_WARPS * 32) k_fill_moment(
     ntw = __reduce_max_sync(0xffffffffu, ntw);
     const long long pstart = (long long)i * (2LL * m - i + 1) / 2;
     const int k_lo = max(i, 32 * kb), k_hi = min(m, 32 * kb + 32);
+    // the rows' moments and records are read one row ahead into registers,
+    // so their latency overlaps the series of the row before
+    float nm0 = 0.f, nm1 = 0.f;
+    MomRec nrc{0, 0, 0.f, 0.f};
+    if (k_lo < k_hi) {
+        const long long p = pstart + (k_lo - i);
+        nm0 = mom[(2 * p) * MOM_FLOATS + lane];
+        nm1 = mom[(2 * p + 1) * MOM_FLOATS + lane];
+        if (lane < 2) nrc = rec[2 * p + lane];
+    }
     for (int k0 = k_lo; k0 < k_hi; k0 += FILL_SUB) {
         const int kend = min(k_hi, k0 + FILL_SUB);
         for (int k = k0; k < kend; ++k) {
             const long long p = pstart + (k - i);
             __syncwarp();
-            W.mv[0][lane] = mom[(2 * p) * MOM_FLOATS + lane];
-            W.mv[1][lane] = mom[(2 * p + 1) * MOM_FLOATS + lane];
-            if (lane < 2) W.rc[lane] = rec[2 * p + lane];
+            W.mv[0][lane] = nm0;
+            W.mv[1][lane] = nm1;
+            if (lane < 2) W.rc[lane] = nrc;
             __syncwarp();
+            if (k + 1 < k_hi) {
+                nm0 = mom[(2 * p + 2) * MOM_FLOATS + lane];
+                nm1 = mom[(2 * p + 3) * MOM_FLOATS + lane];
+                if (lane < 2) nrc = rec[2 * p + 2 + lane];
+            }
             CDF zt{DF{0.f, 0.f}, DF{0.f, 0.f}}, zl = zt;
 #pragma unroll
             for (int kind = 0; kind < 2; ++kind) {
