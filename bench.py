@@ -166,15 +166,16 @@ def read_profile(pkg):
 
 # DRAM bytes of the trailing-update family (k_gemm_tc<2, 0>), one ncu capture
 # (dram__bytes_read.sum + dram__bytes_write.sum, 1 pass) of all 35 launches of
-# one 128-sample pass of this workload (groups of six panels): 63.15 GB, i.e.
-# 14.1 MB per launch per sample (profiles/k_gemm_tc_trailing_dram_grid1560_batch128.md).
-# The traffic grows in proportion to the samples in the pass.
+# one 128-sample pass of this workload (groups of six panels, bench.py --steps 1
+# --warmup 1 --pipelines 1 --no-graphs --batch 128, launches -k k_gemm_tc<2, 0>
+# -c 35): 63.15 GB, i.e. 14.1 MB per launch per sample. The traffic grows in
+# proportion to the samples in the pass.
 TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 63.15e9 / 35 / 128
-# Pipe use of the mixed form's fill kernel (k_fill_moment), from an ncu capture
-# at 16 samples (profiles/k_fill_moment_grid1560_batch16.md).
+# Pipe use of the mixed form's fill kernel (k_fill_moment), from an ncu
+# --set full capture of its first launch in a 16-sample bench run.
 FILL_PIPES = {"kernel": "k_fill_moment", "issue_active": 0.775, "fma_pipe": 0.613, "alu_pipe": 0.139,
               "fp64_pipe": 0.023, "xu_pipe": 0.014, "dram_frac": 0.106,
-              "source": "ncu --set full, 16 samples (profiles/k_fill_moment_grid1560_batch16.md)",
+              "source": "ncu --set full, first k_fill_moment launch of a 16-sample pass (profiles/)",
               "note": "FP32 ALU-bound (float-pair series); the log-singular entries run on the FP64 pipe in "
                       "k_fill_special64 (82.5 % of its pipe)"}
 
