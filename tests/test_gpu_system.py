@@ -223,6 +223,34 @@ def test_autotuner_keeps_a_valid_configuration(gpu_pkg):
         plan.close()
 
 
+def test_panels_per_update_give_the_same_solution(gpu_pkg):
+    """tags_plan_set_panels: 1, 3, 5 and 6 panels per trailing update solve the
+    config-2 grid's samples within 1e-6 of the reference and within 1e-9 of
+    each other (refinement to the same FP64 tolerance); 7 is an argument
+    error."""
+    pkg = gpu_pkg
+    gd = golden("grid2.npz")
+    e, nodes = gd["elec"], gd["nodes"]
+    s, kappa = gd["s"][::16], gd["kappa"][::16]
+    ie = np.zeros((len(s), nodes.shape[0]), np.complex128)
+    ie[:, 0] = gd["inj_s"][::16]
+    plan = pkg.Plan(e, pkg.images(e), nodes, pkg.MIXED, max_batch=64)
+    try:
+        with pytest.raises(RuntimeError, match=f"failed \\({pkg.E_ARG}\\)"):
+            plan.set_panels(7)
+        u = {}
+        for panels in (1, 3, 5, 6):
+            plan.set_panels(panels)
+            sol, info, st = plan.run(s, kappa, ie=ie)
+            assert np.all(info == 0) and st.fallbacks == 0
+            u[panels] = sol[:, 0]
+            assert np.max(np.abs(u[panels] - gd["u0"][::16]) / np.abs(gd["u0"][::16])) < 1e-6
+        for panels in (1, 3, 5):
+            assert np.max(np.abs(u[panels] - u[6]) / np.abs(u[6])) < 1e-9
+    finally:
+        plan.close()
+
+
 def test_tune_cache_applies_a_stored_configuration(gpu_pkg, tmp_path):
     """With a tune cache the first tune of a shape times the candidates and
     appends one line; another plan of the same shape applies that line without
