@@ -173,11 +173,11 @@ def read_profile(pkg):
 TRAILING_DRAM_BYTES_PER_LAUNCH_SAMPLE = 63.15e9 / 35 / 128
 # Pipe use of the mixed form's fill kernel (k_fill_moment), from an ncu
 # --set full capture of its first launch in a 16-sample bench run.
-FILL_PIPES = {"kernel": "k_fill_moment", "issue_active": 0.775, "fma_pipe": 0.613, "alu_pipe": 0.139,
-              "fp64_pipe": 0.023, "xu_pipe": 0.014, "dram_frac": 0.106,
+FILL_PIPES = {"kernel": "k_fill_moment", "issue_active": 0.818, "fma_pipe": 0.627, "alu_pipe": 0.184,
+              "fp64_pipe": 0.025, "xu_pipe": 0.016, "dram_frac": 0.117,
               "source": "ncu --set full, first k_fill_moment launch of a 16-sample pass (profiles/)",
               "note": "FP32 ALU-bound (float-pair series); the log-singular entries run on the FP64 pipe in "
-                      "k_fill_special64 (82.5 % of its pipe)"}
+                      "k_fill_special64 (84 % of its pipe)"}
 
 
 def roofline(prof, peaks, pieces=3, fp64=None, samples_per_pass=None):
