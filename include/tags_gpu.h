@@ -463,6 +463,16 @@ int tags_plan_set_tc_pairs (tags_plan plan, int on);
  * points tags_debug_ldl and tags_debug_ldl_solve (process-wide). */
 int tags_debug_tc_pairs (int on);
 
+/* No counterpart in the reference. The tile list of a trailing update of M
+ * rows (lower triangle of 128 x 128 tiles) whose rows and columns zlo .. zhi
+ * are structurally zero: the tiles that do work, row by row, plus (planes)
+ * the first-column tiles that only write the next panel's split planes, in
+ * the band's rows too when planes_band; when no tile lies wholly in the band,
+ * the full triangle, which the kernel walks then. Writes (I, J, planes only)
+ * triples into out (up to cap) and returns the count. Host code, no device
+ * work. */
+int tags_debug_tri_tiles (int M, int zlo, int zhi, int planes, int planes_band, int *out, int cap);
+
 /* No counterpart in the reference. Test hook (process-wide, for passes and
  * graphs built afterwards): how the mixed form's triangular solves run.
  * 0: block by block (two kernels per 128-row block and sweep); 1: one CTA per

@@ -227,6 +227,54 @@ def test_resumable_sweep_resumes_after_an_interruption(pkg, tmp_path):
         pkg.resumable_sweep(runner(-1), 10, d, 4, fp)
 
 
+def _tri_tiles_full(M, zlo, zhi, planes, planes_band):
+    """The lower-triangle tiles of an update of M rows, row by row, that do
+    work or only write the next panel's planes: tiles wholly inside the zero
+    band's rows (or columns) are skipped, and a skipped first-column tile below
+    the first writes planes when planes is set (in the band's rows only with
+    planes_band)."""
+    T = -(-M // 128)
+    out = []
+    for I in range(T):
+        for J in range(I + 1):
+            rz = zhi > zlo and 128 * I >= zlo and 128 * I + 128 <= zhi
+            cz = zhi > zlo and 128 * J >= zlo and 128 * J + 128 <= zhi
+            if not (rz or cz):
+                out.append((I, J, 0))
+            elif planes and J == 0 and I >= 1 and (planes_band or not rz):
+                out.append((I, J, 1))
+    return out
+
+
+def test_trailing_tile_list_leaves_out_the_zero_band(pkg):
+    """The persistent GEMM's tile list of a trailing update (the closed form
+    the kernel uses for the compacted list, run on the host) equals the full
+    triangle filtered to the tiles that do work, in the same order, for update
+    sizes and zero bands of every alignment, with and without the next panel's
+    planes (and their band rows)."""
+    fn = pkg.lib().tags_debug_tri_tiles
+    fn.argtypes = [ctypes.c_int] * 5 + [ctypes.c_void_p, ctypes.c_int]
+    fn.restype = ctypes.c_int
+    cases = 0
+    for M in [1, 100, 128, 129, 700, 1500, 3769, 2977, 4537 - 128, 17875 - 768]:
+        for zlo in sorted({0, 1, 24, 127, 128, 129, 300, 792, M // 3, M // 2}):
+            for width in (0, 100, 128, 256, 1559, 1560, 1561, 3000):
+                zhi = zlo + width
+                if zhi > M:
+                    continue
+                for planes, planes_band in ((0, 0), (1, 1), (1, 0), (0, 1)):
+                    want = _tri_tiles_full(M, zlo, zhi, planes, planes_band)
+                    n = fn(M, zlo, zhi, planes, planes_band, None, 0)
+                    assert n >= 0
+                    out = np.zeros(3 * max(n, 1), np.int32)
+                    assert fn(M, zlo, zhi, planes, planes_band, out.ctypes.data, n) == n
+                    got = [tuple(int(v) for v in out[3 * l:3 * l + 3]) for l in range(n)]
+                    assert got == want, (M, zlo, zhi, planes, planes_band)
+                    cases += 1
+    assert cases > 200
+    assert fn(-1, 0, 0, 0, 0, None, 0) == pkg.E_ARG
+
+
 def test_bench_reference_arm_contract():
     """`bench.py --impl reference` (the CPU implementation of the path on the
     host cores) prints one JSON line carrying the bench contract's keys, with

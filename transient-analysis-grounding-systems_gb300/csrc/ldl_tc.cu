@@ -332,36 +332,42 @@ TAGS_HD int tri_compact_count(int T, int ba, int bb, bool planes, bool planes_ba
     return c.n1 + c.n2 + R * c.e + R * (R + 1) / 2;
 }
 
+// Tile l of the compacted list (row I, column J; skip: a tile that only
+// writes planes).
+TAGS_HD void tri_compact_tile(int l, int ba, int bb, bool planes, bool planes_band, int& I, int& J, bool& skip) {
+    const TriCompact c = tri_compact(ba, bb, planes, planes_band);
+    skip = false;
+    if (l < c.n1) {
+        I = (int)((sqrtf(8.0f * l + 1.0f) - 1.0f) * 0.5f);
+        while ((I + 1) * (I + 2) / 2 <= l) ++I;
+        while (I * (I + 1) / 2 > l) --I;
+        J = l - I * (I + 1) / 2;
+    } else if (l < c.n1 + c.n2) {
+        I = c.r2s + (l - c.n1);
+        J = 0;
+        skip = true;
+    } else {
+        const int l3 = l - c.n1 - c.n2;
+        const float bq = 2.0f * c.e + 1.0f;
+        int r = (int)((sqrtf(bq * bq + 8.0f * l3) - bq) * 0.5f);
+        while ((r + 1) * c.e + (r + 1) * (r + 2) / 2 <= l3) ++r;
+        while (r > 0 && r * c.e + r * (r + 1) / 2 > l3) --r;
+        const int q = l3 - (r * c.e + r * (r + 1) / 2);
+        I = bb + r;
+        if (q < c.e) {
+            J = q;
+            skip = ba == 0;                // J = 0 inside the band: planes only
+        } else {
+            J = bb + (q - c.e);
+        }
+    }
+}
+
 TAGS_D void tile_of(const GemmArgs& g, int t, int& smp, int& I, int& J, bool& skip) {
     smp = t / g.tiles;
     int l = t - smp * g.tiles;
     if (g.tri && g.bb > g.ba) {
-        const TriCompact c = tri_compact(g.ba, g.bb, g.Np != nullptr, g.np_band != 0);
-        skip = false;
-        if (l < c.n1) {
-            I = (int)((sqrtf(8.0f * l + 1.0f) - 1.0f) * 0.5f);
-            while ((I + 1) * (I + 2) / 2 <= l) ++I;
-            while (I * (I + 1) / 2 > l) --I;
-            J = l - I * (I + 1) / 2;
-        } else if (l < c.n1 + c.n2) {
-            I = c.r2s + (l - c.n1);
-            J = 0;
-            skip = true;
-        } else {
-            const int l3 = l - c.n1 - c.n2;
-            const float bq = 2.0f * c.e + 1.0f;
-            int r = (int)((sqrtf(bq * bq + 8.0f * l3) - bq) * 0.5f);
-            while ((r + 1) * c.e + (r + 1) * (r + 2) / 2 <= l3) ++r;
-            while (r > 0 && r * c.e + r * (r + 1) / 2 > l3) --r;
-            const int q = l3 - (r * c.e + r * (r + 1) / 2);
-            I = g.bb + r;
-            if (q < c.e) {
-                J = q;
-                skip = g.ba == 0;          // J = 0 inside the band: planes only
-            } else {
-                J = g.bb + (q - c.e);
-            }
-        }
+        tri_compact_tile(l, g.ba, g.bb, g.Np != nullptr, g.np_band != 0, I, J, skip);
         return;
     }
     if (g.tri) {
@@ -2232,6 +2238,35 @@ extern "C" int tags_debug_tc_pairs(int on) {
     if (on < 0 || on > 2) return tags_fail(TAGS_E_ARG, "tags_debug_tc_pairs: 0, 1 or 2");
     g_debug_pairs = on;
     return 0;
+}
+
+extern "C" int tags_debug_tri_tiles(int M, int zlo, int zhi, int planes, int planes_band, int* out, int cap) {
+    if (M <= 0 || zlo < 0 || zhi < zlo || cap < 0 || (cap > 0 && !out))
+        return tags_fail(TAGS_E_ARG, "tags_debug_tri_tiles: invalid argument");
+    const int T = (M + TB - 1) / TB;
+    const int ba = (zlo + TB - 1) / TB, bb = std::min(T, zhi / TB);
+    if (zhi <= zlo || bb <= ba) {
+        // no tile wholly inside a band: the kernel walks the full triangle
+        const int n = T * (T + 1) / 2;
+        for (int l = 0, I = 0; I < T; ++I)
+            for (int J = 0; J <= I; ++J, ++l)
+                if (l < cap) {
+                    out[3 * l] = I;
+                    out[3 * l + 1] = J;
+                    out[3 * l + 2] = 0;
+                }
+        return n;
+    }
+    const int n = tri_compact_count(T, ba, bb, planes != 0, planes_band != 0);
+    for (int l = 0; l < n && l < cap; ++l) {
+        int I, J;
+        bool skip;
+        tri_compact_tile(l, ba, bb, planes != 0, planes_band != 0, I, J, skip);
+        out[3 * l] = I;
+        out[3 * l + 1] = J;
+        out[3 * l + 2] = skip ? 1 : 0;
+    }
+    return n;
 }
 
 extern "C" int tags_debug_solve_path(int path) {
